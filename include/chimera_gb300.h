@@ -1,0 +1,365 @@
+/*
+ * chimera_gb300.h -- C ABI of libchimera_gb300.so, the GB300 (sm_103a)
+ * implementation of CHIMERA's per-step particle-in-cell hot path.
+ *
+ * Every entry point replaces one subroutine of the reference's f2py module
+ * `chimera.moduls.fimera` (built from f90/*.f90, Makefile:6-11,32-34); the
+ * comment above each declaration cites the Fortran routine it replaces.  The
+ * argument meaning follows the Fortran; the dimensions that f2py hides are
+ * explicit.
+ *
+ * Conventions
+ *   - All array arguments are DEVICE pointers (cudaMalloc'd or owned by any
+ *     allocator, e.g. torch), except where a comment says "host".
+ *   - Grid and spectral arrays are column-major (Fortran order) and dense:
+ *       spatial  grid  (nx, nr, nm[, ncomp]) complex128
+ *       spectral grid  (nx, nkr, nm[, ncomp]) complex128
+ *     with nr counting the ghost row at r = -dr/2 (index 0), nm the stored
+ *     azimuthal modes (0..M-1, or -K..K for the envelope "env" solver).
+ *   - complex128 = interleaved {re, im} doubles (chm_c128).
+ *   - Particle arrays (3,np) / (6,np) / (np) are strided: element (c, i) is
+ *     at ptr[c * comp_stride + i * part_stride].  The reference's F-ordered
+ *     (3,np) arrays have comp_stride = 1, part_stride = 3; the structure-of-
+ *     arrays buffers used by chimera_gb300 have part_stride = 1.
+ *   - `stream` is a cudaStream_t; every call is asynchronous on it.
+ *   - Return value: CHM_OK or an error code; chm_last_error() gives the text.
+ *   - No entry point allocates device memory.  Scratch space is passed in by
+ *     the caller (`ws`, `ws_bytes`), sized with the matching *_ws_bytes query.
+ */
+#ifndef CHIMERA_GB300_H
+#define CHIMERA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  double re, im;
+} chm_c128;
+
+enum {
+  CHM_OK = 0,
+  CHM_ERR_ARG = 1,      /* bad shape / stride / pointer */
+  CHM_ERR_CUDA = 2,     /* a CUDA launch or runtime call failed */
+  CHM_ERR_WS = 3,       /* workspace too small */
+  CHM_ERR_CAPACITY = 4, /* particle capacity exceeded */
+  CHM_ERR_RANGE = 5     /* a value is out of the supported range */
+};
+
+/* Text of the last error reported by this thread's last failing call. */
+const char *chm_last_error(void);
+/* Library version string. */
+const char *chm_version(void);
+
+/* ======================================================================== */
+/* Particle push                                                             */
+/* ======================================================================== */
+
+/* particle_tools.f90:18-56 push_velocs(momenta, Fld, dt): Boris rotation. */
+int chm_push_velocs(double *momenta, int64_t p_cs, int64_t p_ps,
+                    const double *fld, int64_t f_cs, int64_t f_ps, double dt,
+                    int64_t np, void *stream);
+
+/* particle_tools.f90:58-82 push_coords(coord, momenta, coord_cntr, dt). */
+int chm_push_coords(double *coord, int64_t x_cs, int64_t x_ps,
+                    const double *momenta, int64_t p_cs, int64_t p_ps,
+                    double *coord_cntr, int64_t h_cs, int64_t h_ps, double dt,
+                    int64_t np, void *stream);
+
+/* ======================================================================== */
+/* Field gather                                                              */
+/* ======================================================================== */
+
+/* grid_deps.f90:149-217 proj_fld(coord, wghts, Fld, Fld_tot, leftX, Rgrid,
+ * dx_inv, dr_inv): Fld_tot(6,np) += Re(sum_m S e^{i m theta} Fld_m).
+ * rgrid: device array of nr doubles. */
+int chm_proj_fld(const double *coord, int64_t x_cs, int64_t x_ps,
+                 const double *wghts, int64_t w_ps, const chm_c128 *fld,
+                 double *fld_tot, int64_t f_cs, int64_t f_ps, double leftX,
+                 const double *rgrid, double dx_inv, double dr_inv, int64_t np,
+                 int64_t nx, int64_t nr, int64_t nm, void *stream);
+
+/* grid_deps_env.f90:164-238 proj_fld_env(..., kx0): modes -K..K, carrier
+ * e^{+i kx0 x}, on-axis phase 1. */
+int chm_proj_fld_env(const double *coord, int64_t x_cs, int64_t x_ps,
+                     const double *wghts, int64_t w_ps, const chm_c128 *fld,
+                     double *fld_tot, int64_t f_cs, int64_t f_ps, double leftX,
+                     const double *rgrid, double dx_inv, double dr_inv,
+                     double kx0, int64_t np, int64_t nx, int64_t nr,
+                     int64_t nm, void *stream);
+
+/* grid_deps.f90:219-266 eb_correction(eb_spc) and grid_deps_env.f90:240-283
+ * eb_correction_env(eb_spc): mode normalisation + ghost row. */
+int chm_eb_correction(chm_c128 *eb, int64_t nx, int64_t nr, int64_t nm,
+                      void *stream);
+int chm_eb_correction_env(chm_c128 *eb, int64_t nx, int64_t nr, int64_t nm,
+                          void *stream);
+
+/* ======================================================================== */
+/* External fields ("devices"), devices.f90                                  */
+/* ======================================================================== */
+
+/* devices.f90:162-203 undul_analytic(coord, Fld, t, params[4]); params is a
+ * HOST array (a0, lambda_u, X0, Lx). */
+int chm_undul_analytic(const double *coord, int64_t x_cs, int64_t x_ps,
+                       double *fld, int64_t f_cs, int64_t f_ps, double t,
+                       const double *params, int64_t np, void *stream);
+/* devices.f90:117-160 undul_analytic_taper(coord, Fld, t, params[5]) */
+int chm_undul_analytic_taper(const double *coord, int64_t x_cs, int64_t x_ps,
+                             double *fld, int64_t f_cs, int64_t f_ps, double t,
+                             const double *params, int64_t np, void *stream);
+/* devices.f90:18-62 undul_mapped(coord, Fld, t, a0(2,nmap), params[3]) and
+ * devices.f90:64-115 undul_mapped_tap(..., params[5]); a0 is a device array,
+ * params a host array. */
+int chm_undul_mapped(const double *coord, int64_t x_cs, int64_t x_ps,
+                     double *fld, int64_t f_cs, int64_t f_ps, double t,
+                     const double *a0, int64_t nmap, const double *params,
+                     int64_t np, void *stream);
+int chm_undul_mapped_tap(const double *coord, int64_t x_cs, int64_t x_ps,
+                         double *fld, int64_t f_cs, int64_t f_ps, double t,
+                         const double *a0, int64_t nmap, const double *params,
+                         int64_t np, void *stream);
+/* devices.f90:205-252 planewave(coord, Fld, t, params[7]) */
+int chm_planewave(const double *coord, int64_t x_cs, int64_t x_ps, double *fld,
+                  int64_t f_cs, int64_t f_ps, double t, const double *params,
+                  int64_t np, void *stream);
+/* devices.f90:254-297 gaussbeam(coord, Fld, time, a0, params[8]) */
+int chm_gaussbeam(const double *coord, int64_t x_cs, int64_t x_ps, double *fld,
+                  int64_t f_cs, int64_t f_ps, double time, double a0,
+                  const double *params, int64_t np, void *stream);
+
+/* ======================================================================== */
+/* Grid deposition (deterministic: 64-bit fixed-point accumulation, no float */
+/* atomics; results are bitwise reproducible run to run)                     */
+/* ======================================================================== */
+
+/* Workspace for any deposit onto a grid of nx*nr*nm*ncomp complex values. */
+int64_t chm_dep_ws_bytes(int64_t nx, int64_t nr, int64_t nm, int64_t ncomp,
+                         int64_t np);
+
+/* grid_deps.f90:18-87 dep_curr(coord, momenta, wghts, curr, leftX, Rgrid,
+ * dx_inv, dr_inv): curr(nx,nr,nm,3) += w v/gamma S e^{-i m theta}; ghost
+ * fold.  coord are the half-step coordinates. */
+int chm_dep_curr(const double *coord, int64_t x_cs, int64_t x_ps,
+                 const double *momenta, int64_t p_cs, int64_t p_ps,
+                 const double *wghts, int64_t w_ps, chm_c128 *curr,
+                 double leftX, const double *rgrid, double dx_inv,
+                 double dr_inv, int64_t np, int64_t nx, int64_t nr, int64_t nm,
+                 void *ws, int64_t ws_bytes, void *stream);
+/* grid_deps.f90:89-147 dep_dens(coord, wghts, dens, leftX, Rgrid, dx_inv,
+ * dr_inv) */
+int chm_dep_dens(const double *coord, int64_t x_cs, int64_t x_ps,
+                 const double *wghts, int64_t w_ps, chm_c128 *dens,
+                 double leftX, const double *rgrid, double dx_inv,
+                 double dr_inv, int64_t np, int64_t nx, int64_t nr, int64_t nm,
+                 void *ws, int64_t ws_bytes, void *stream);
+/* grid_deps_env.f90:18-95 dep_curr_env(..., kx0) (third component only) */
+int chm_dep_curr_env(const double *coord, int64_t x_cs, int64_t x_ps,
+                     const double *momenta, int64_t p_cs, int64_t p_ps,
+                     const double *wghts, int64_t w_ps, chm_c128 *curr,
+                     double leftX, const double *rgrid, double dx_inv,
+                     double dr_inv, double kx0, int64_t np, int64_t nx,
+                     int64_t nr, int64_t nm, void *ws, int64_t ws_bytes,
+                     void *stream);
+/* grid_deps_env.f90:97-162 dep_dens_env(..., kx0) (weight applied twice) */
+int chm_dep_dens_env(const double *coord, int64_t x_cs, int64_t x_ps,
+                     const double *wghts, int64_t w_ps, chm_c128 *dens,
+                     double leftX, const double *rgrid, double dx_inv,
+                     double dr_inv, double kx0, int64_t np, int64_t nx,
+                     int64_t nr, int64_t nm, void *ws, int64_t ws_bytes,
+                     void *stream);
+/* grid_deps_chnk.f90:18-130 dep_curr_chnk(coord, momenta, wghts, curr,
+ * IndInChunk, guards, leftX, Rgrid, dx_inv, dr_inv); ind_in_chunk is a
+ * device int32 array of nchnk+1 offsets.  Same guard-buffer semantics as
+ * the Fortran: chunk 0 drops its contributions to x-node 0. */
+int chm_dep_curr_chnk(const double *coord, int64_t x_cs, int64_t x_ps,
+                      const double *momenta, int64_t p_cs, int64_t p_ps,
+                      const double *wghts, int64_t w_ps, chm_c128 *curr,
+                      const int32_t *ind_in_chunk, int64_t nchnk,
+                      int64_t guards, double leftX, const double *rgrid,
+                      double dx_inv, double dr_inv, int64_t np, int64_t nx,
+                      int64_t nr, int64_t nm, void *ws, int64_t ws_bytes,
+                      void *stream);
+/* grid_deps_chnk.f90:132-234 dep_dens_chnk(...) */
+int chm_dep_dens_chnk(const double *coord, int64_t x_cs, int64_t x_ps,
+                      const double *wghts, int64_t w_ps, chm_c128 *dens,
+                      const int32_t *ind_in_chunk, int64_t nchnk,
+                      int64_t guards, double leftX, const double *rgrid,
+                      double dx_inv, double dr_inv, int64_t np, int64_t nx,
+                      int64_t nr, int64_t nm, void *ws, int64_t ws_bytes,
+                      void *stream);
+/* grid_deps_env_chnk.f90:18-145 dep_curr_env_chnk(..., kx0) */
+int chm_dep_curr_env_chnk(const double *coord, int64_t x_cs, int64_t x_ps,
+                          const double *momenta, int64_t p_cs, int64_t p_ps,
+                          const double *wghts, int64_t w_ps, chm_c128 *curr,
+                          const int32_t *ind_in_chunk, int64_t nchnk,
+                          int64_t guards, double leftX, const double *rgrid,
+                          double dx_inv, double dr_inv, double kx0, int64_t np,
+                          int64_t nx, int64_t nr, int64_t nm, void *ws,
+                          int64_t ws_bytes, void *stream);
+/* grid_deps_env_chnk.f90:147-261 dep_dens_env_chnk(..., kx0) */
+int chm_dep_dens_env_chnk(const double *coord, int64_t x_cs, int64_t x_ps,
+                          const double *wghts, int64_t w_ps, chm_c128 *dens,
+                          const int32_t *ind_in_chunk, int64_t nchnk,
+                          int64_t guards, double leftX, const double *rgrid,
+                          double dx_inv, double dr_inv, double kx0, int64_t np,
+                          int64_t nx, int64_t nr, int64_t nm, void *ws,
+                          int64_t ws_bytes, void *stream);
+
+/* ======================================================================== */
+/* Fourier-Bessel transforms, fb_io.f90                                      */
+/* ======================================================================== */
+
+/* Workspace for the FB transforms of ncomp components. */
+int64_t chm_fb_ws_bytes(int64_t nx, int64_t nr, int64_t nkr, int64_t nm,
+                        int64_t ncomp);
+
+/* fb_io.f90:18-59 fb_vec_in(vec_fb, vec, leftX, kx, In) and fb_io.f90:61-98
+ * fb_scl_in (ncomp = 1).  vec (nx,nr,nm,ncomp), In (nr-1,nkr,nm) real,
+ * kx (nx) real, out vec_fb (nx,nkr,nm,ncomp).  If `fact` is not NULL the
+ * result is also multiplied by the real (nx,nkr,nm) array fact (this fuses
+ * the omp_mult_vec(J_fb, DepFact) that follows every call in
+ * solvers.py:417-420). */
+int chm_fb_in(chm_c128 *vec_fb, const chm_c128 *vec, double leftX,
+              const double *kx, const double *In, const double *fact,
+              int64_t nx, int64_t nr, int64_t nkr, int64_t nm, int64_t ncomp,
+              void *ws, int64_t ws_bytes, void *stream);
+
+/* fb_io.f90:100-180 fb_vec_out / fb_scl_out: vec(nx,nr,nm,ncomp) = IFFT_x(
+ * e^{+i kx leftX} sum_k Out(k,r,m) vec_fb); Out (nkr,nr-1,nm); row 0 = 0.
+ * eb_mode: 0 = plain output, 1 = apply eb_correction, 2 = eb_correction_env
+ * (fuses grid_deps.f90:219-266 into the transform). */
+int chm_fb_out(chm_c128 *vec, const chm_c128 *vec_fb, double leftX,
+               const double *kx, const double *Out, int64_t nx, int64_t nr,
+               int64_t nkr, int64_t nm, int64_t ncomp, int eb_mode, void *ws,
+               int64_t ws_bytes, void *stream);
+
+/* fb_io.f90:182-228 fb_eb_out(eb_spc, e_fb, b_fb, leftX, kx, Out): the 6
+ * components of eb_spc from e_fb(:,:,:,1:3) and b_fb(:,:,:,1:3).  e_fb and
+ * b_fb point to the first component of 3 contiguous component planes. */
+int chm_fb_eb_out(chm_c128 *eb, const chm_c128 *e_fb, const chm_c128 *b_fb,
+                  double leftX, const double *kx, const double *Out,
+                  int64_t nx, int64_t nr, int64_t nkr, int64_t nm, int eb_mode,
+                  void *ws, int64_t ws_bytes, void *stream);
+
+/* fb_io.f90:230-308 fb_filtr(vec, leftX, kx, filtr, modefilt): absorbing
+ * layer applied in x-space to vec (nx,nkr,nm,ncomp). filtr: device array. */
+int chm_fb_filtr(chm_c128 *vec, double leftX, const double *kx,
+                 const double *filtr, int64_t nxfilt, int modefilt, int64_t nx,
+                 int64_t nkr, int64_t nm, int64_t ncomp, void *ws,
+                 int64_t ws_bytes, void *stream);
+
+/* ======================================================================== */
+/* Spectral differential operators, fb_math.f90 / fb_math_env.f90            */
+/* Dp, Dm: (nkr, nkr, nm+1) plain / (nkr, nkr, nm+2) env, real.              */
+/* ======================================================================== */
+
+int64_t chm_fbmath_ws_bytes(int64_t nx, int64_t nkr, int64_t nm);
+
+/* fb_math.f90:18-94 fb_rot(vec_fb_loc, vec_fb, DpS2S, DmS2S, kx) */
+int chm_fb_rot(chm_c128 *out, const chm_c128 *vec, const double *Dp,
+               const double *Dm, const double *kx, int64_t nx, int64_t nkr,
+               int64_t nm, int env, void *ws, int64_t ws_bytes, void *stream);
+/* fb_math.f90:96-149 fb_grad(vec_fb_loc, scl_fb, DpS2S, DmS2S, kx) */
+int chm_fb_grad(chm_c128 *out, const chm_c128 *scl, const double *Dp,
+                const double *Dm, const double *kx, int64_t nx, int64_t nkr,
+                int64_t nm, int env, void *ws, int64_t ws_bytes, void *stream);
+/* fb_math.f90:151-199 fb_div(scl_fb_loc, vec_fb, DpS2S, DmS2S, kx) */
+int chm_fb_div(chm_c128 *out, const chm_c128 *vec, const double *Dp,
+               const double *Dm, const double *kx, int64_t nx, int64_t nkr,
+               int64_t nm, int env, void *ws, int64_t ws_bytes, void *stream);
+/* fb_math.f90:201-293 fb_graddiv(vec_fb, DpS2S, DmS2S, kx), in place */
+int chm_fb_graddiv(chm_c128 *vec, const double *Dp, const double *Dm,
+                   const double *kx, int64_t nx, int64_t nkr, int64_t nm,
+                   int env, void *ws, int64_t ws_bytes, void *stream);
+
+/* ======================================================================== */
+/* PSATD update and spectral elementwise ops, maxwell_solvers.f90            */
+/* ======================================================================== */
+
+/* maxwell_solvers.f90:18-60 maxwell_push_with_spchrg(EG_fb, j_fb,
+ * grad_rho_n_fb, grad_rho_np1_fb, C1, C2); C1, C2 real (nx,nkr,nm,5). */
+int chm_maxwell_push_with_spchrg(chm_c128 *eg, const chm_c128 *j,
+                                 const chm_c128 *gn, const chm_c128 *gnp1,
+                                 const double *c1, const double *c2,
+                                 int64_t nx, int64_t nkr, int64_t nm,
+                                 void *stream);
+/* maxwell_solvers.f90:62-96 maxwell_push_wo_spchrg(EG_fb, j_fb, C1, C2);
+ * C1, C2 complex (nx,nkr,nm,3). */
+int chm_maxwell_push_wo_spchrg(chm_c128 *eg, const chm_c128 *j,
+                               const chm_c128 *c1, const chm_c128 *c2,
+                               int64_t nx, int64_t nkr, int64_t nm,
+                               void *stream);
+/* maxwell_solvers.f90:98-129 maxwell_init_push(EG_fb, j_fb, grad_rho_n_fb,
+ * C1, C2); C1, C2 complex (nx,nkr,nm,2). */
+int chm_maxwell_init_push(chm_c128 *eg, const chm_c128 *j, const chm_c128 *gn,
+                          const chm_c128 *c1, const chm_c128 *c2, int64_t nx,
+                          int64_t nkr, int64_t nm, void *stream);
+/* maxwell_solvers.f90:131-164 poiss_corr(j_fb, grad_div_j_fb,
+ * grad_rho_n_fb, grad_rho_np1_fb, dt_inv, w2_inv) */
+int chm_poiss_corr(chm_c128 *j, const chm_c128 *gdj, const chm_c128 *gn,
+                   const chm_c128 *gnp1, double dt_inv, const double *w2_inv,
+                   int64_t nx, int64_t nkr, int64_t nm, void *stream);
+/* maxwell_solvers.f90:166-197 poiss_corr_stat(j_fb, grad_div_j_fb,
+ * grad_rho_n_fb, DT, w2_inv); DT complex (nx). */
+int chm_poiss_corr_stat(chm_c128 *j, const chm_c128 *gdj, const chm_c128 *gn,
+                        const chm_c128 *DT, const double *w2_inv, int64_t nx,
+                        int64_t nkr, int64_t nm, void *stream);
+/* maxwell_solvers.f90:199-226 field_drift(EG_fb, kx, beta0, dt) */
+int chm_field_drift(chm_c128 *eg, const double *kx, double beta0, double dt,
+                    int64_t nx, int64_t nkr, int64_t nm, void *stream);
+/* maxwell_solvers.f90:228-272 omp_mult_vec / omp_mult_scl: v(P,ncomp) *= A(P)
+ * with P = nx*nkr*nm. */
+int chm_omp_mult(chm_c128 *v, const double *A, int64_t P, int64_t ncomp,
+                 void *stream);
+/* maxwell_solvers.f90:274-318 omp_add_vec / omp_add_scl: v(n) += A(n) */
+int chm_omp_add(chm_c128 *v, const chm_c128 *A, int64_t n, void *stream);
+
+/* ======================================================================== */
+/* Particle bookkeeping, particle_tools.f90                                  */
+/* ======================================================================== */
+
+/* particle_tools.f90:130-153 sortpartsout(coord, lims): indx2stay (device,
+ * int64, np) gets the 0-based indices of particles inside
+ * lims = (xmin, xmax, r2min, r2max) (host array) in increasing order;
+ * *num2stay (host) their number.  Synchronises the stream. */
+int64_t chm_sortpartsout_ws_bytes(int64_t np);
+int chm_sortpartsout(int64_t *indx2stay, int64_t *num2stay,
+                     const double *coord, int64_t x_cs, int64_t x_ps,
+                     const double *lims, int64_t np, void *ws,
+                     int64_t ws_bytes, void *stream);
+
+/* particle_tools.f90:155-208 chunk_coords_boundaries(coord, lims, Xgrid,
+ * nchnk): chunked_indx (device int8, np), ind_in_chnk (device int32,
+ * nchnk+1) and *go_out (host).  xgrid0, xgridc are Xgrid(0) and
+ * Xgrid((nx+1)/nchnk) (or Xgrid(nx) for one chunk).  Synchronises. */
+int chm_chunk_coords_boundaries(int8_t *chunked_indx, int32_t *ind_in_chnk,
+                                int64_t *go_out, const double *coord,
+                                int64_t x_cs, int64_t x_ps, const double *lims,
+                                double xgrid0, double xgridc, int64_t nchnk,
+                                int64_t np, void *ws, int64_t ws_bytes,
+                                void *stream);
+
+/* Stable order of the particles by chunk id, dropping ids outside
+ * [0, nchnk): the permutation index2stay.argsort()[go_out:] of
+ * species.py:379-383 (the reference's argsort is numpy's default, unstable
+ * quicksort; this one keeps the particles' relative order inside a chunk).
+ * idx_out (device int64) receives *n_kept (host) indices.  Synchronises. */
+int64_t chm_chunk_order_ws_bytes(int64_t np, int64_t nchnk);
+int chm_chunk_order(int64_t *idx_out, int64_t *n_kept, const int8_t *chunked_indx,
+                    int64_t nchnk, int64_t np, void *ws, int64_t ws_bytes,
+                    void *stream);
+
+/* particle_tools.f90:270-324 align_data_vec / align_data_scl(dat, idx):
+ * dst(:, i) = src(:, idx(i)) for i < n (idx device int64).  src and dst must
+ * not overlap (the Fortran's temporary copy). */
+int chm_align_data(double *dst, int64_t d_cs, int64_t d_ps, const double *src,
+                   int64_t s_cs, int64_t s_ps, int64_t ncomp,
+                   const int64_t *idx, int64_t n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CHIMERA_GB300_H */

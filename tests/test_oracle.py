@@ -1,0 +1,193 @@
+"""The CPU oracle against numpy and the reference's own mathematics
+(known-answer tests; the reference ships no golden kernel outputs)."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+
+@pytest.mark.parametrize("n", [1, 2, 12, 64, 131, 524, 1408, 2048])
+def test_fft_matches_numpy(orc, n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    assert rel_l2(orc.fft(x, -1), np.fft.fft(x)) < 1e-14
+    assert rel_l2(orc.fft(x, +1), np.fft.ifft(x) * n) < 1e-14
+
+
+def _ops(golden, name):
+    g = {k.split("/")[-1]: golden[k] for k in golden.files if k.startswith(f"op/{name}/Args/")}
+    return g
+
+
+def test_fb_round_trip(orc, golden):
+    """In = inv(Out) (solvers.py:743): fb_scl_in followed by fb_scl_out is Nx
+    times the identity on rows 1..Nr-1."""
+    g = _ops(golden, "lpa_m2")
+    nx, nr, nm = int(g["Nx"]), int(g["Nr"]), int(g["Mtot"])
+    rng = np.random.default_rng(0)
+    v = np.asfortranarray(rng.standard_normal((nx, nr, nm)) + 1j * rng.standard_normal((nx, nr, nm)))
+    v[:, 0] = 0
+    vfb = np.zeros((nx, int(g["Nkr"]), nm), complex, order="F")
+    vfb = orc.fb_scl_in(vfb, v, float(g["leftX"]), g["kx"], g["In"])
+    back = orc.fb_scl_out(vfb, float(g["leftX"]), g["kx"], g["Out"])
+    assert rel_l2(back[:, 1:], nx * v[:, 1:]) < 1e-12
+
+
+def _rand_fb(shape, seed):
+    rng = np.random.default_rng(seed)
+    return np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+
+
+def _np_grad(s, Dp, Dm, kx, env):
+    """numpy restatement of fb_grad (fb_math.f90:96-149 / fb_math_env.f90:18-61)."""
+    nx, nk, nm = s.shape
+    out = np.zeros((nx, nk, nm, 3), complex)
+    K = (nm - 1) // 2
+    for mi in range(nm):
+        md = mi + 1 if env else mi
+        out[:, :, mi, 0] = 1j * kx[:, None] * s[:, :, mi]
+        lo = None
+        if env:
+            if mi > 0:
+                lo = s[:, :, mi - 1]
+        else:
+            lo = s[:, :, mi - 1] if mi > 0 else (-np.conj(s[(-np.arange(nx)) % nx, :, 1]) if nm > 1 else 0 * s[:, :, 0])
+        if lo is not None:
+            sl = lo @ Dm[:, :, md]
+            out[:, :, mi, 1] -= sl
+            out[:, :, mi, 2] += 1j * sl
+        if mi < nm - 1:
+            sl = s[:, :, mi + 1] @ Dp[:, :, md]
+            out[:, :, mi, 1] += sl
+            out[:, :, mi, 2] += 1j * sl
+    return out
+
+
+@pytest.mark.parametrize("name,env", [("lpa_m2", False), ("lpa_m3_chunked", False),
+                                      ("fel_env_k1", True)])
+def test_fb_grad_vs_numpy(orc, golden, name, env):
+    g = _ops(golden, name)
+    nx, nk, nm = int(g["Nx"]), int(g["Nkr"]), int(g["Mtot"])
+    s = _rand_fb((nx, nk, nm), 1)
+    out = np.zeros((nx, nk, nm, 3), complex, order="F")
+    f = orc.fb_grad_env if env else orc.fb_grad
+    got = f(out, s, g["DpS2S"], g["DmS2S"], g["kx"])
+    ref = _np_grad(s, g["DpS2S"], g["DmS2S"], g["kx"], env)
+    assert rel_l2(got, ref) < 1e-13
+
+
+def test_graddiv_equals_grad_of_div_interior(orc, golden):
+    """fb_graddiv builds the divergence on one extra mode; for the m=0..M-2
+    outputs it equals grad(div v) formed with fb_div and fb_grad."""
+    g = _ops(golden, "lpa_m3_chunked")
+    nx, nk, nm = int(g["Nx"]), int(g["Nkr"]), int(g["Mtot"])
+    v = _rand_fb((nx, nk, nm, 3), 2)
+    gd = orc.fb_graddiv(v.copy(order="F"), g["DpS2S"], g["DmS2S"], g["kx"])
+    d = orc.fb_div(np.zeros((nx, nk, nm), complex, order="F"), v, g["DpS2S"], g["DmS2S"], g["kx"])
+    gg = orc.fb_grad(np.zeros((nx, nk, nm, 3), complex, order="F"), d, g["DpS2S"], g["DmS2S"], g["kx"])
+    assert rel_l2(gd[:, :, : nm - 2], gg[:, :, : nm - 2]) < 1e-12
+
+
+def test_boris_uniform_b_gyration(orc):
+    """particle_tools.f90:18-56 in a uniform B: |p| is conserved and the
+    rotation angle per step is 2 atan(dt B / (2 gamma))."""
+    n = 64
+    rng = np.random.default_rng(3)
+    p = np.asfortranarray(rng.standard_normal((3, n)))
+    p[2] = 0.0
+    F = np.zeros((6, n), order="F")
+    B = 0.7
+    F[5] = B
+    dt = 0.3
+    p0 = p.copy()
+    orc.push_velocs(p, F, dt)
+    g = np.sqrt(1 + (p0 ** 2).sum(0))
+    assert np.allclose(np.linalg.norm(p, axis=0), np.linalg.norm(p0, axis=0), rtol=1e-14)
+    ang = np.arctan2(p0[0] * p[1] - p0[1] * p[0], (p0[:2] * p[:2]).sum(0))
+    assert np.allclose(-ang, 2 * np.arctan(dt * B / (2 * g)), rtol=1e-12)
+
+
+def test_push_coords_half_step(orc):
+    x = np.asfortranarray(np.random.default_rng(4).standard_normal((3, 10)))
+    p = np.asfortranarray(np.random.default_rng(5).standard_normal((3, 10)))
+    xc = np.zeros_like(x, order="F")
+    x0 = x.copy()
+    orc.push_coords(x, p, xc, 0.2)
+    v = p / np.sqrt(1 + (p ** 2).sum(0))
+    assert np.allclose(x, x0 + 0.2 * v, rtol=0, atol=1e-15)
+    assert np.allclose(xc, 0.5 * (x0 + x), rtol=0, atol=1e-15)
+
+
+def _particles(n, seed, x0=-2.0, x1=1.0, rmin=0.3, rmax=2.5):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(x0, x1, n)
+    r = rng.uniform(rmin, rmax, n)
+    th = rng.uniform(0, 2 * np.pi, n)
+    c = np.asfortranarray(np.vstack([x, r * np.cos(th), r * np.sin(th)]))
+    p = np.asfortranarray(rng.standard_normal((3, n)))
+    w = rng.uniform(0.5, 1.5, n)
+    return c, p, w
+
+
+def test_dep_dens_conserves_charge(orc):
+    """grid_deps.f90:89-147: linear weights sum to one, so with particles off
+    the axis row the m=0 density sums to the total weight."""
+    c, p, w = _particles(500, 6)
+    rg = 0.25 * (np.arange(13) - 0.5)
+    dens = np.zeros((64, 13, 2), complex, order="F")
+    dens = orc.dep_dens(c, w, dens, -2.5, rg, 1 / 0.1, 1 / 0.25)
+    assert abs(dens[:, :, 0].sum() - w.sum()) < 1e-12 * w.sum()
+
+
+def test_chunked_deposit_matches_serial(orc):
+    """grid_deps_chnk.f90: same grid as the serial deposit when chunk 0 holds
+    no particle next to x-node 0."""
+    c, p, w = _particles(4000, 7, -2.3, 3.5)
+    rg = 0.25 * (np.arange(13) - 0.5)
+    leftX, nx, nch = -2.5, 64, 4
+    xg = leftX + 0.1 * np.arange(nx)
+    ids, ind, go = orc.chunk_coords_boundaries(c, np.array([leftX, xg[-1], 0, 100.0]), xg, nch)
+    order = np.argsort(ids, kind="stable")[go:]
+    c2, p2, w2 = (np.asfortranarray(a[..., order]) for a in (c, p, w))
+    ser = orc.dep_curr(c2, p2, w2, np.zeros((nx, 13, 2, 3), complex, order="F"), leftX, rg, 10.0, 4.0)
+    chk = orc.dep_curr_chnk(c2, p2, w2, np.zeros((nx, 13, 2, 3), complex, order="F"), ind, 3,
+                            leftX, rg, 10.0, 4.0)
+    assert rel_l2(chk, ser) < 1e-13
+
+
+def test_undulator_closed_form(orc):
+    """devices.f90:162-203 inside the flat part of the undulator."""
+    n = 200
+    rng = np.random.default_rng(8)
+    c = np.asfortranarray(np.vstack([rng.uniform(2.0, 8.0, n), rng.uniform(-0.1, 0.1, n),
+                                     np.zeros(n)]))
+    F = np.zeros((6, n), order="F")
+    a0, lam, X0, Lx = 1.3, 1.0, 0.5, 10.0
+    orc.undul_analytic(c, F, 0.0, np.array([a0, lam, X0, Lx]))
+    ku = 2 * np.pi / lam
+    assert np.allclose(F[4], a0 * np.sin(ku * (c[0] - X0)) * np.cosh(ku * c[1]), atol=1e-14)
+    assert np.allclose(F[3], a0 * np.cos(ku * (c[0] - X0)) * np.sinh(ku * c[1]), atol=1e-14)
+
+
+def test_psatd_vacuum_matches_analytic(orc, golden):
+    """maxwell_solvers.f90:62-96 with J = 0 rotates (E, G) by exp(i w dt):
+    N steps equal one step of N dt."""
+    g = _ops(golden, "plain_m1_vacuum")
+    nx, nk, nm = int(g["Nx"]), int(g["Nkr"]), int(g["Mtot"])
+    w = g["w"]
+    dt = 0.1
+    def coeffs(t):
+        C1 = np.zeros(w.shape + (3,), order="F")
+        C2 = np.zeros(w.shape + (3,), order="F")
+        C1[..., 0], C1[..., 1], C1[..., 2] = np.cos(t * w), np.sin(t * w) / w, -np.sin(t * w) / w
+        C2[..., 0], C2[..., 1], C2[..., 2] = -w * np.sin(t * w), np.cos(t * w), 1 - np.cos(t * w)
+        return C1, C2
+    eg = _rand_fb((nx, nk, nm, 6), 9)
+    j = np.zeros((nx, nk, nm, 3), complex, order="F")
+    a = eg.copy(order="F")
+    C1, C2 = coeffs(dt)
+    for _ in range(5):
+        a = orc.maxwell_push_wo_spchrg(a, j, C1, C2)
+    C1, C2 = coeffs(5 * dt)
+    b = orc.maxwell_push_wo_spchrg(eg.copy(order="F"), j, C1, C2)
+    assert rel_l2(a, b) < 1e-12
