@@ -1,0 +1,416 @@
+"""Benchmark of the CHIMERA PIC step on GB300: particle*steps/s.
+
+Workload (the laser-wakefield configuration the headline metric is quoted
+on): Nx = 2048 (dx = 0.04), Nr = 256 (dr = 0.4), azimuthal modes m = 0, 1,
+FixedCell (2, 2, 8) electrons filling the box (~16.7M) over still ions
+(SpaceCharge + StillAsBackground), density 0.003 n_c with a 20 lambda0
+linear up-ramp, Gaussian laser a0 = 2, w0 = 12, FWHM 10 lambda0/c, moving
+window at c, x-chunked deposition (16 chunks, 10 guard cells).  Inputs are
+synthetic (seeded numpy), of this shape.
+
+  value  particle*steps/s of ChimeraRun.make_step with all state resident on
+         the GPU (moving species only, as the metric counts them)
+  e2e    the same through the public API with the window's host-generated
+         plasma injection (AddPlasma + AbsorbLayer + IonsOnTop, as in the
+         reference's lpa-testrun.py) copied host->device every step and the
+         laser a0 read back every step
+  roofline / cpu_baseline / clocks
+
+--impl reference runs the oracle's CPU step driver (the reference's step
+loop over the C restatement of its Fortran kernels, OpenMP on every host
+core) on the same configuration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle*steps/s"
+WORKLOAD_SIZE = "cfg2"
+WORKLOAD = "lwfa_nx2048_nr256_m2_ppc2x2x8"
+
+
+SIZES = {  # name: (nx, nkr, ppc)
+    "cfg2": (2048, 256, (2, 2, 8)),
+    "small": (512, 64, (2, 2, 4)),
+}
+
+
+def workload_config(nchunks=16):
+    nx, nkr, ppc = SIZES[WORKLOAD_SIZE]
+    dx, dr = 0.04, 0.4
+    xmin = -80.0 if nx == 2048 else -(nx * dx) + 1.92
+    xmax = xmin + nx * dx
+    grid = (xmin, xmax, nkr * dr, dx, dr)
+    ramp = 20.0
+
+    def prof(x):
+        return np.interp(x, [xmin, xmin + ramp, 1e9], [0.0, 1.0, 1.0])
+
+    fwhm = 10.0
+    Lx = fwhm / (2 * np.sqrt(np.log(2) / 2))
+    return dict(
+        solver={"Grid": grid, "TimeStep": dx, "MaxAzimuthMode": 1,
+                "Xchunked": (nchunks, 10), "Features": ("SpaceCharge", "StillAsBackground")},
+        laser={"a0": 2.0, "k0": 1.0, "x0": -30.0, "x_foc": -30.0 + 20.0, "Lx": Lx, "LR": 12.0},
+        electrons={"Grid": grid, "TimeStep": dx, "Density": 0.003, "FixedCell": ppc,
+                   "Xchunked": (nchunks, 10), "Features": ("NoSorting",)},
+        domain=(xmin + 1.5 * dx, xmax, 0.0, nkr * dr),  # Xgrid starts at xmin + dx
+        profile=prof, dx=dx)
+
+
+def build_run(device_kind, window, seed=1002):
+    """Solver + electrons + still ions + ChimeraRun (GPU) or CpuRun (oracle)."""
+    from copy import deepcopy
+
+    from chimera_gb300.messages import msg
+    msg.quiet = True
+    cfg = workload_config()
+    np.random.seed(seed)
+    if device_kind == "gpu":
+        from chimera_gb300 import ChimeraRun, Solver, Specie
+        solver = Solver(deepcopy(cfg["solver"]))
+        solver.add_gauss_beam(cfg["laser"])
+        dev = None
+    else:
+        from chimera_gb300.solvers import Solver
+        from chimera_gb300.species import Specie
+        solver = Solver(deepcopy(cfg["solver"]), device="cpu")
+        dev = "cpu"
+    el_in = deepcopy(cfg["electrons"])
+    io_in = deepcopy(cfg["electrons"])
+    io_in["Charge"], io_in["Mass"], io_in["Features"] = 1.0, 1836.0, ("Still", "NoSorting")
+    kw = {} if dev is None else {"device": dev}
+    el, io = Specie(el_in, **kw), Specie(io_in, **kw)
+    parts = el.gen_parts(Domain=cfg["domain"], ProfileFunc=cfg["profile"])
+    el.add_particles(*parts)
+    parts[-1] = parts[-1] * -1
+    io.add_particles(*parts)
+    wind = {"TimeStep": cfg["dx"], "Steps": 1, "Velocity": 1.0}
+    if window == "inject":
+        wind.update({"AbsorbLayer": 64, "AddPlasma": cfg["profile"], "Features": ("IonsOnTop",)})
+    if device_kind == "gpu":
+        run = ChimeraRun({"Solvers": (solver,), "Particles": (el, io), "MovingFrames": (wind,)})
+        return run, solver, el
+    return solver, el, io, wind
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        rows = self.rows
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(r[0]) for r in rows if num(r[0]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": num(rows[0][1]), "reasons": reasons, "samples": len(rows)}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return p, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# FP64 FMA throughput of this machine's GB300 (measured with a dependent-FMA
+# probe: 1.20 TFLOP/s); the plain FP64 form's GEMMs are bound by it.
+FP64_PEAK_TFLOPS = 1.20
+
+
+def dist_setup():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(local)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_step_time(nsteps, warmup=0, window="none"):
+    """Wall time per step of the oracle's CPU step driver on this workload."""
+    from oracle.step import CpuRun, CpuSpecies
+    import torch
+    solver, el, io, wind = build_run("cpu", window)
+    # the reference initialises the laser in spectral space with the same
+    # kernels; the CPU arm takes the initial field from the same operators
+    # (zero field costs the same per step)
+    solver.Data["EG_fb"] = torch.zeros(tuple(solver.Data["EG_fb"].shape), dtype=torch.complex128)
+    run = CpuRun(solver, [CpuSpecies(el), CpuSpecies(io)], wind)
+    for i in range(1, warmup + 1):
+        run.make_step(i)
+    n_moving = run.Particles[0].n()
+    t0 = time.perf_counter()
+    for i in range(warmup + 1, warmup + nsteps + 1):
+        run.make_step(i)
+    dt = (time.perf_counter() - t0) / nsteps
+    return dt, n_moving
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cores = len(os.sched_getaffinity(0))
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    steps = max(1, min(args.steps, args.ref_max_steps))
+    warm = min(args.warmup, 1)
+    t_step, n = cpu_step_time(steps, warm)
+    value = n / t_step
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * t_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "particles": n, "cpu_threads": cores},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                         "sample": f"{steps} full steps of the workload (after {warm} warm-up) "
+                                   "with the oracle's C/OpenMP restatement of the reference "
+                                   "kernels and its step loop (oracle/step.py)"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import torch
+
+    from chimera_gb300 import _lib, fimera
+
+    world, rank, local = dist_setup()
+    lib = _lib.load()
+    run, solver, el = build_run("gpu", "none", seed=1002 + rank)
+    n_moving = el.num_particles
+    stream = torch.cuda.current_stream()
+    for i in range(1, args.warmup + 1):
+        run.make_step(i)
+    torch.cuda.synchronize()
+    # L2: the particle state (~1.9 GB for the electrons alone) is far larger
+    # than the 129 MB L2, so every step streams from HBM.
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = lib.chm_launch_count()
+    flops0 = lib.chm_gemm_flops()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    t0 = time.perf_counter()
+    psteps = 0
+    for i in range(args.warmup + 1, args.warmup + args.steps + 1):
+        run.make_step(i)
+        psteps += el.num_particles
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    barrier(world)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms_max = max_over_ranks(world, ms)
+    launches = lib.chm_launch_count() - launches0
+    gemm_flops = lib.chm_gemm_flops() - flops0
+    value = world * (psteps / args.steps) * args.steps / (ms_max / 1e3)
+
+    # stage profile of a few more steps (events around every C-ABI call)
+    _lib.profile_begin()
+    nprof = max(2, min(3, args.steps))
+    f0 = lib.chm_gemm_flops()
+    base = args.warmup + args.steps
+    for i in range(base + 1, base + nprof + 1):
+        run.make_step(i)
+    prof = _lib.profile_end()
+    prof_flops = lib.chm_gemm_flops() - f0
+    tot = sum(v[1] for v in prof.values())
+    stages = {k.replace("chm_", ""): {"calls": c / nprof, "ms_per_step": t / nprof,
+                                      "share": t / tot if tot else None}
+              for k, (c, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+    gemm_ms = sum(t for k, (c, t) in prof.items()
+                  if k in ("chm_fb_graddiv", "chm_fb_rot", "chm_fb_grad", "chm_fb_div", "chm_fb_in",
+                           "chm_fb_out", "chm_fb_eb_out"))
+    peaks, peak_kind = load_peaks()
+    achieved = prof_flops / (gemm_ms / 1e3) / 1e12 if gemm_ms else None
+    roofline = {
+        "kernel": "dgemm_kernel (DHT + fb_math dense products, FP64 SIMT)",
+        "bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+        "frac": achieved / FP64_PEAK_TFLOPS if achieved else None,
+        "traffic": None,
+        "note": "plain FP64 form: the dense products run on GB300's FP64 pipe "
+                f"({FP64_PEAK_TFLOPS} TFLOP/s measured with an FMA probe); achieved = "
+                "algorithmic 4*nx*N*K FLOPs per product over the device time of the FB "
+                "transform / operator calls that issue them",
+        "algorithmic_gflop_per_step": gemm_flops / args.steps / 1e9,
+    }
+
+    # end to end through the public API with per-step host I/O
+    e2e = None
+    if not args.no_e2e:
+        run2, solver2, el2 = build_run("gpu", "inject", seed=2002 + rank)
+        for i in range(1, args.warmup + 1):
+            run2.make_step(i)
+        torch.cuda.synchronize()
+        h0, d0 = fimera.io_bytes["h2d"], fimera.io_bytes["d2h"]
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ps2 = 0
+        a0 = 0.0
+        for i in range(args.warmup + 1, args.warmup + args.steps + 1):
+            run2.make_step(i)
+            ps2 += el2.num_particles
+            # the laser amplitude diagnostic of the demos (max Re Ey on axis)
+            a0 = float(solver2.Data["EB"][:, 1, 0, 2].real.max().item())
+        torch.cuda.synchronize()
+        t_e2e = max_over_ranks(world, time.perf_counter() - t0)
+        h2d = (fimera.io_bytes["h2d"] - h0) / args.steps
+        d2h = (fimera.io_bytes["d2h"] - d0) / args.steps + 8
+        e2e = {"value": world * ps2 / t_e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "laser_a0_last": a0,
+               "what": "ChimeraRun.make_step with AddPlasma+AbsorbLayer window (host-generated "
+                       "plasma copied H2D each step) and a laser-a0 read back each step"}
+        del run2, solver2, el2
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores = len(os.sched_getaffinity(0))
+        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+        t_cpu, n_cpu = cpu_step_time(args.cpu_steps, 0)
+        cpu = {"value": n_cpu / t_cpu, "unit": METRIC, "cores": cores, "kind": "port",
+               "sample": f"{args.cpu_steps} full step(s) of the same workload with the oracle's "
+                         "C/OpenMP restatement of the reference kernels and step loop"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "plain_fp64", "particles_moving": n_moving,
+                   "particles_still": n_moving, "nx": SIZES[WORKLOAD_SIZE][0],
+                   "nr": SIZES[WORKLOAD_SIZE][1] + 1, "modes": 2,
+                   "parallelism": f"replicas{world}" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (particle state ~1.9 GB per species)"},
+        "wall_s_timed": wall,
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "stages": stages,
+        "clocks": clk,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "peaks": {"source": peak_kind, "hbm_gbs": peaks.get("hbm_gbs"),
+                  "bf16_tflops": peaks.get("bf16_tflops")},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--ref-max-steps", type=int, default=5)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--size", default="cfg2", choices=sorted(SIZES),
+                    help="cfg2 = the benchmark workload; small = a reduced case for profiling")
+    args = ap.parse_args()
+    global WORKLOAD_SIZE, WORKLOAD
+    WORKLOAD_SIZE = args.size
+    if args.size != "cfg2":
+        nx, nkr, ppc = SIZES[args.size]
+        WORKLOAD = f"lwfa_nx{nx}_nr{nkr}_m2_ppc{ppc[0]}x{ppc[1]}x{ppc[2]}"
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -23,7 +23,7 @@ def _parse_header(path: str) -> dict[str, tuple[str, str]]:
     text = open(path).read()
     text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
     out = {}
-    for ret, name, args in re.findall(r"(int64_t|int|const char \*)\s*(chm_\w+)\s*\(([^;]*?)\)\s*;", text):
+    for ret, name, args in re.findall(r"(int64_t|int|double|const char \*)\s*(chm_\w+)\s*\(([^;]*?)\)\s*;", text):
         kinds = ""
         if args.strip() != "void":
             for a in args.split(","):
@@ -38,7 +38,7 @@ def _parse_header(path: str) -> dict[str, tuple[str, str]]:
                     kinds += N
                 else:
                     raise ValueError(f"unparsed argument {a!r} of {name}")
-        out[name] = ({"int": "n", "int64_t": "i"}.get(ret, "s"), kinds)
+        out[name] = ({"int": "n", "int64_t": "i", "double": "d"}.get(ret, "s"), kinds)
     return out
 
 
@@ -70,7 +70,7 @@ def load(build_if_missing: bool = True):
         for name, (ret, kinds) in _SIG.items():
             fn = getattr(lib, name)
             fn.argtypes = [_KIND[k] for k in kinds]
-            fn.restype = {"n": C.c_int, "i": C.c_int64, "s": C.c_char_p}[ret]
+            fn.restype = {"n": C.c_int, "i": C.c_int64, "d": C.c_double, "s": C.c_char_p}[ret]
         _lib = lib
         return lib
 
@@ -80,10 +80,37 @@ def exported_symbols() -> list[str]:
     return list(_SIG)
 
 
+_prof = None  # name -> list of (start, end) CUDA events while profiling
+
+
+def profile_begin():
+    """Record CUDA events around every C-ABI call on the current stream."""
+    global _prof
+    _prof = {}
+
+
+def profile_end() -> dict:
+    """Stop recording; returns name -> (calls, total device ms)."""
+    global _prof
+    import torch
+    prof, _prof = _prof, None
+    torch.cuda.synchronize()
+    return {k: (len(v), sum(a.elapsed_time(b) for a, b in v)) for k, v in (prof or {}).items()}
+
+
 def call(name: str, *args):
     """Call a status-returning entry point; raise ChimeraError on failure."""
     lib = load()
-    rc = getattr(lib, name)(*args)
+    if _prof is not None:
+        import torch
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        rc = getattr(lib, name)(*args)
+        b.record()
+        _prof.setdefault(name, []).append((a, b))
+    else:
+        rc = getattr(lib, name)(*args)
     if rc != 0:
         msg = lib.chm_last_error().decode(errors="replace")
         raise ChimeraError(f"{name} failed with status {rc}: {msg}")

@@ -11,6 +11,9 @@ namespace chm {
 
 // Last error text for chm_last_error(); set by the entry points.
 void set_error(const char *fmt, ...);
+// Host-side counters read by chm_launch_count() / chm_gemm_flops().
+void count_launch();
+void count_gemm_flops(double flops);
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 

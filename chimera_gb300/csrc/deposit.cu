@@ -340,8 +340,8 @@ int deposit_common(int kind, const double *coord, i64 x_cs, i64 x_ps, const doub
   if (np > 0) {
     CHM_REQUIRE(coord && wghts && (ncomp == 1 || momenta), "deposit: null particle array");
     wsum_partial_kernel<<<kRedBlocks, kDepThreads, 0, st>>>(wghts, w_ps, np, kind == DENS_ENV,
-                                                            partial);
-    wsum_final_kernel<<<1, 256, 0, st>>>(partial, kRedBlocks, scale);
+                                                            partial); chm::count_launch();
+    wsum_final_kernel<<<1, 256, 0, st>>>(partial, kRedBlocks, scale); chm::count_launch();
     DepArgs A;
     A.x = coord;
     A.x_cs = x_cs;
@@ -372,7 +372,7 @@ int deposit_common(int kind, const double *coord, i64 x_cs, i64 x_ps, const doub
   case K:                                                                                 \
     cudaFuncSetAttribute(deposit_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                          kBoxBytes);                                                      \
-    deposit_kernel<K><<<blocks, kDepThreads, kBoxBytes, st>>>(A);                         \
+    deposit_kernel<K><<<blocks, kDepThreads, kBoxBytes, st>>>(A); chm::count_launch();                         \
     break;
       LAUNCH(CURR)
       LAUNCH(DENS)
@@ -383,12 +383,12 @@ int deposit_common(int kind, const double *coord, i64 x_cs, i64 x_ps, const doub
     CHM_CHECK_LAUNCH();
   } else {
     // nothing deposited: only the fold of the existing content
-    set_one_kernel<<<1, 1, 0, st>>>(scale);
+    set_one_kernel<<<1, 1, 0, st>>>(scale); chm::count_launch();
   }
   const i64 nml = nm * ncomp;
   finalize_kernel<<<grid_for(nx * nr * nml, 256), 256, 0, st>>>(
       reinterpret_cast<double2 *>(grid), reinterpret_cast<const long long *>(acc), scale, nx,
-      nr, nml);
+      nr, nml); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }

@@ -183,11 +183,11 @@ int fft_launch(const FftLines &L, int n, i64 nlines, double2 *tw, cudaStream_t s
     return CHM_ERR_RANGE;
   }
   if (nlines <= 0) return CHM_OK;
-  fft_twiddle_kernel<<<(n + 255) / 256, 256, 0, st>>>(tw, n);
+  fft_twiddle_kernel<<<(n + 255) / 256, 256, 0, st>>>(tw, n); chm::count_launch();
   const size_t smem = 2 * (size_t)n * sizeof(double2);
   cudaFuncSetAttribute(fft_lines_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int threads = n >= 1024 ? 512 : (n >= 256 ? 256 : 128);
-  fft_lines_kernel<<<(unsigned)nlines, threads, smem, st>>>(plan, tw, L);
+  fft_lines_kernel<<<(unsigned)nlines, threads, smem, st>>>(plan, tw, L); chm::count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error("fft: %s", cudaGetErrorString(e));

@@ -292,7 +292,7 @@ int chm_push_velocs(double *momenta, int64_t p_cs, int64_t p_ps, const double *f
   if (np == 0) return CHM_OK;
   CHM_REQUIRE(momenta && fld, "push_velocs: null pointer");
   push_velocs_kernel<<<grid_for(np, kThreads), kThreads, 0, as_stream(stream)>>>(
-      momenta, p_cs, p_ps, fld, f_cs, f_ps, dt, np);
+      momenta, p_cs, p_ps, fld, f_cs, f_ps, dt, np); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -304,7 +304,7 @@ int chm_push_coords(double *coord, int64_t x_cs, int64_t x_ps, const double *mom
   if (np == 0) return CHM_OK;
   CHM_REQUIRE(coord && momenta && coord_cntr, "push_coords: null pointer");
   push_coords_kernel<<<grid_for(np, kThreads), kThreads, 0, as_stream(stream)>>>(
-      coord, x_cs, x_ps, momenta, p_cs, p_ps, coord_cntr, h_cs, h_ps, dt, np);
+      coord, x_cs, x_ps, momenta, p_cs, p_ps, coord_cntr, h_cs, h_ps, dt, np); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -321,7 +321,7 @@ static int proj_common(bool env, const double *coord, int64_t x_cs, int64_t x_ps
   auto k = env ? proj_fld_kernel<true> : proj_fld_kernel<false>;
   k<<<grid_for(np, kThreads), kThreads, 0, as_stream(stream)>>>(
       coord, x_cs, x_ps, wghts, w_ps, reinterpret_cast<const double2 *>(fld), fld_tot, f_cs,
-      f_ps, leftX, rgrid, dx_inv, dr_inv, kx0, np, nx, nr, (int)nm);
+      f_ps, leftX, rgrid, dx_inv, dr_inv, kx0, np, nx, nr, (int)nm); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -347,7 +347,7 @@ int chm_eb_correction(chm_c128 *eb, int64_t nx, int64_t nr, int64_t nm, void *st
   CHM_REQUIRE(eb && nx > 0 && nr > 1 && nm >= 1, "eb_correction: bad args");
   i64 n = nx * (nr - 1) * nm * 6;
   eb_correction_kernel<false><<<grid_for(n, kThreads), kThreads, 0, as_stream(stream)>>>(
-      reinterpret_cast<double2 *>(eb), nx, nr, (int)nm);
+      reinterpret_cast<double2 *>(eb), nx, nr, (int)nm); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -356,7 +356,7 @@ int chm_eb_correction_env(chm_c128 *eb, int64_t nx, int64_t nr, int64_t nm, void
   CHM_REQUIRE(eb && nx > 0 && nr > 1 && nm >= 1, "eb_correction_env: bad args");
   i64 n = nx * (nr - 1) * nm * 6;
   eb_correction_kernel<true><<<grid_for(n, kThreads), kThreads, 0, as_stream(stream)>>>(
-      reinterpret_cast<double2 *>(eb), nx, nr, (int)nm);
+      reinterpret_cast<double2 *>(eb), nx, nr, (int)nm); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -368,7 +368,7 @@ int chm_undul_analytic(const double *coord, int64_t x_cs, int64_t x_ps, double *
   if (np == 0) return CHM_OK;
   CHM_REQUIRE(params[1] != 0.0, "undul_analytic: lambda_u is zero");
   undul_analytic_kernel<false><<<grid_for(np, kThreads), kThreads, 0, as_stream(stream)>>>(
-      coord, x_cs, x_ps, fld, f_cs, f_ps, load_params(params, 4), np);
+      coord, x_cs, x_ps, fld, f_cs, f_ps, load_params(params, 4), np); chm::count_launch();
   (void)t;
   CHM_CHECK_LAUNCH();
   return CHM_OK;
@@ -380,7 +380,7 @@ int chm_undul_analytic_taper(const double *coord, int64_t x_cs, int64_t x_ps, do
   CHM_REQUIRE(params, "undul_analytic_taper: params (host) is null");
   if (np == 0) return CHM_OK;
   undul_analytic_kernel<true><<<grid_for(np, kThreads), kThreads, 0, as_stream(stream)>>>(
-      coord, x_cs, x_ps, fld, f_cs, f_ps, load_params(params, 5), np);
+      coord, x_cs, x_ps, fld, f_cs, f_ps, load_params(params, 5), np); chm::count_launch();
   (void)t;
   CHM_CHECK_LAUNCH();
   return CHM_OK;
@@ -392,7 +392,7 @@ int chm_undul_mapped(const double *coord, int64_t x_cs, int64_t x_ps, double *fl
   CHM_REQUIRE(params && a0 && nmap > 0, "undul_mapped: bad args");
   if (np == 0) return CHM_OK;
   undul_mapped_kernel<false><<<grid_for(np, kThreads), kThreads, 0, as_stream(stream)>>>(
-      coord, x_cs, x_ps, fld, f_cs, f_ps, a0, nmap, load_params(params, 3), np);
+      coord, x_cs, x_ps, fld, f_cs, f_ps, a0, nmap, load_params(params, 3), np); chm::count_launch();
   (void)t;
   CHM_CHECK_LAUNCH();
   return CHM_OK;
@@ -404,7 +404,7 @@ int chm_undul_mapped_tap(const double *coord, int64_t x_cs, int64_t x_ps, double
   CHM_REQUIRE(params && a0 && nmap > 0, "undul_mapped_tap: bad args");
   if (np == 0) return CHM_OK;
   undul_mapped_kernel<true><<<grid_for(np, kThreads), kThreads, 0, as_stream(stream)>>>(
-      coord, x_cs, x_ps, fld, f_cs, f_ps, a0, nmap, load_params(params, 5), np);
+      coord, x_cs, x_ps, fld, f_cs, f_ps, a0, nmap, load_params(params, 5), np); chm::count_launch();
   (void)t;
   CHM_CHECK_LAUNCH();
   return CHM_OK;
@@ -415,7 +415,7 @@ int chm_planewave(const double *coord, int64_t x_cs, int64_t x_ps, double *fld, 
   CHM_REQUIRE(params, "planewave: params (host) is null");
   if (np == 0) return CHM_OK;
   planewave_kernel<<<grid_for(np, kThreads), kThreads, 0, as_stream(stream)>>>(
-      coord, x_cs, x_ps, fld, f_cs, f_ps, t, load_params(params, 7), np);
+      coord, x_cs, x_ps, fld, f_cs, f_ps, t, load_params(params, 7), np); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -426,7 +426,7 @@ int chm_gaussbeam(const double *coord, int64_t x_cs, int64_t x_ps, double *fld, 
   CHM_REQUIRE(params, "gaussbeam: params (host) is null");
   if (np == 0) return CHM_OK;
   gaussbeam_kernel<<<grid_for(np, kThreads), kThreads, 0, as_stream(stream)>>>(
-      coord, x_cs, x_ps, fld, f_cs, f_ps, time, a0, load_params(params, 8), np);
+      coord, x_cs, x_ps, fld, f_cs, f_ps, time, a0, load_params(params, 8), np); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }

@@ -183,9 +183,9 @@ int stable_bucket_order(const BucketSrc &B, i64 n, int nb, int keep, i64 *idx_ou
   }
   int *hist = reinterpret_cast<int *>(ws);
   int *total = hist + ntiles * nb;
-  hist_kernel<<<(unsigned)ntiles, kSortThreads, 0, st>>>(B, n, nb, ntiles, hist);
-  scan_kernel<<<1, 1024, 0, st>>>(hist, ntiles * nb, total);
-  scatter_kernel<<<(unsigned)ntiles, kSortThreads, 0, st>>>(B, n, nb, ntiles, hist, idx_out, keep);
+  hist_kernel<<<(unsigned)ntiles, kSortThreads, 0, st>>>(B, n, nb, ntiles, hist); chm::count_launch();
+  scan_kernel<<<1, 1024, 0, st>>>(hist, ntiles * nb, total); chm::count_launch();
+  scatter_kernel<<<(unsigned)ntiles, kSortThreads, 0, st>>>(B, n, nb, ntiles, hist, idx_out, keep); chm::count_launch();
   CHM_CHECK_LAUNCH();
   // kept = offset of bucket `keep` (first dropped bucket) = sum of kept buckets
   if (kept) {
@@ -248,9 +248,9 @@ int chm_chunk_coords_boundaries(int8_t *chunked_indx, int32_t *ind_in_chnk, int6
     for (int i = 0; i < 4; ++i) L.v[i] = lims[i];
     chunk_ids_kernel<<<grid_for(np, 256), 256, 0, st>>>(coord, x_cs, x_ps, L, xgrid0,
                                                         1.0 / (xgridc - xgrid0), (int)nchnk, np,
-                                                        chunked_indx, counts);
+                                                        chunked_indx, counts); chm::count_launch();
   }
-  offsets_kernel<<<1, 32, 0, st>>>(counts, (int)nchnk, ind_in_chnk);
+  offsets_kernel<<<1, 32, 0, st>>>(counts, (int)nchnk, ind_in_chnk); chm::count_launch();
   CHM_CHECK_LAUNCH();
   int go = 0;
   cudaMemcpyAsync(&go, counts + nchnk, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -291,7 +291,7 @@ int chm_align_data(double *dst, int64_t d_cs, int64_t d_ps, const double *src, i
   if (n == 0) return CHM_OK;
   CHM_REQUIRE(dst && src && idx && dst != src, "align_data: null or aliased pointers");
   gather_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(dst, d_cs, d_ps, src, s_cs, s_ps,
-                                                                 (int)ncomp, idx, n);
+                                                                 (int)ncomp, idx, n); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }

@@ -108,6 +108,7 @@ int gemm_launch(int epi, const GemmBatch &b, int M, int N, int K, i64 lda, i64 l
     dgemm_kernel<EPI_STORE><<<grid, kGemmThreads, 0, st>>>(b, M, N, K, lda, ldb, ldc, shift);
   else
     dgemm_kernel<EPI_SHIFT><<<grid, kGemmThreads, 0, st>>>(b, M, N, K, lda, ldb, ldc, shift);
+  chm::count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error("gemm: %s", cudaGetErrorString(e));
@@ -127,6 +128,7 @@ struct GemmList {
   int err = CHM_OK;
   void add(const double *A, const double *B, double *C, const double *fac = nullptr) {
     if (err) return;
+    count_gemm_flops(2.0 * M * N * K);  // algorithmic: 4 nx N K per complex x real product
     b.p[b.count++] = GemmProblem{A, B, C, fac};
     if (b.count == kMaxProblems) flush();
   }
@@ -207,7 +209,7 @@ int chm_fb_in(chm_c128 *vec_fb, const chm_c128 *vec, double leftX, const double 
   double2 *shift = c.take<double2>(nx);
   const i64 nrr = nr - 1;
   double2 *tmp = c.take<double2>(nx * nrr * nm * ncomp);
-  shift_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, -1, nx);
+  shift_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, -1, nx); chm::count_launch();
   // 1) forward FFT of rows 1..nr-1 of every (mode, component) plane
   FftLines L{};
   L.in = reinterpret_cast<const double2 *>(vec);
@@ -259,7 +261,7 @@ int chm_fb_out(chm_c128 *vec, const chm_c128 *vec_fb, double leftX, const double
   double2 *shift = c.take<double2>(nx);
   const i64 nrr = nr - 1;
   double2 *tmp = c.take<double2>(nx * nrr * nm * ncomp);
-  shift_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx);
+  shift_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx); chm::count_launch();
   // 1) inverse DHT with the shift epilogue: tmp(x, r) = shift(x) sum_k vfb(x,k) Out(k,r)
   GemmList g;
   g.epi = EPI_SHIFT;
@@ -323,7 +325,7 @@ int chm_fb_filtr(chm_c128 *vec, double leftX, const double *kx, const double *fi
   WsCursor c{reinterpret_cast<char *>(ws), ws_bytes};
   double2 *tw = c.take<double2>(nx);
   double2 *shift = c.take<double2>(nx);
-  shift_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx);
+  shift_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx); chm::count_launch();
   FftLines L{};
   L.in = reinterpret_cast<const double2 *>(vec);
   L.out = reinterpret_cast<double2 *>(vec);
@@ -604,8 +606,8 @@ int chm_fb_grad(chm_c128 *out, const chm_c128 *scl, const double *Dp, const doub
   double2 *ext = F.c.take<double2>(plane);
   const double2 *refl[3] = {ext, nullptr, nullptr};
   if (!env) {
-    if (nm > 1) reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext, s + plane, nx, nkr);
-    else zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext, plane);
+    if (nm > 1) { reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext, s + plane, nx, nkr); chm::count_launch(); }
+    else { zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext, plane); chm::count_launch(); }
   }
   unsigned char lo[64], hi[64];
   // plain: D mode md = m; env: md = m + 1 (D covers -K-1..K+1)
@@ -626,7 +628,7 @@ int chm_fb_grad(chm_c128 *out, const chm_c128 *scl, const double *Dp, const doub
   A.up[0] = up[0];
   A.lo_valid_from = env ? 1 : 0;
   A.hi_valid_to = (int)nm - 1;
-  combine_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A);
+  combine_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -646,11 +648,11 @@ int chm_fb_div(chm_c128 *out, const chm_c128 *vec, const double *Dp, const doubl
   const double2 *refl[3] = {nullptr, ext2, ext3};
   if (!env) {
     if (nm > 1) {
-      reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext2, v + cs + plane, nx, nkr);
-      reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext3, v + 2 * cs + plane, nx, nkr);
+      reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext2, v + cs + plane, nx, nkr); chm::count_launch();
+      reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext3, v + 2 * cs + plane, nx, nkr); chm::count_launch();
     } else {
-      zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext2, plane);
-      zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext3, plane);
+      zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext2, plane); chm::count_launch();
+      zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext3, plane); chm::count_launch();
     }
   }
   // only components 2, 3 are coupled: shift the base by one component
@@ -675,7 +677,7 @@ int chm_fb_div(chm_c128 *out, const chm_c128 *vec, const double *Dp, const doubl
   A.up[2] = up[2];
   A.lo_valid_from = env ? 1 : 0;
   A.hi_valid_to = (int)nm - 1;
-  combine_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A);
+  combine_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -699,8 +701,8 @@ int chm_fb_rot(chm_c128 *out, const chm_c128 *vec, const double *Dp, const doubl
   const double2 *refl[3] = {ext[0], ext[1], ext[2]};
   if (!env) {
     for (int c = 0; c < 3; ++c) {
-      if (nm > 1) reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[c], v + c * cs + plane, nx, nkr);
-      else zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[c], plane);
+      if (nm > 1) { reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[c], v + c * cs + plane, nx, nkr); chm::count_launch(); }
+      else { zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[c], plane); chm::count_launch(); }
     }
   }
   unsigned char lo[64], hi[64];
@@ -729,7 +731,7 @@ int chm_fb_rot(chm_c128 *out, const chm_c128 *vec, const double *Dp, const doubl
   }
   A.lo_valid_from = env ? 1 : 0;
   A.hi_valid_to = (int)nm - 1;
-  combine_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A);
+  combine_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -756,11 +758,11 @@ int chm_fb_graddiv(chm_c128 *vec, const double *Dp, const double *Dm, const doub
   // --- divergence on ns modes (fb_math.f90:222-252 / fb_math_env.f90:180-206)
   if (!env) {
     if (nm > 1) {
-      reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[1], v + cs + plane, nx, nkr);
-      reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[2], v + 2 * cs + plane, nx, nkr);
+      reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[1], v + cs + plane, nx, nkr); chm::count_launch();
+      reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[2], v + 2 * cs + plane, nx, nkr); chm::count_launch();
     } else {
-      zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[1], plane);
-      zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[2], plane);
+      zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[1], plane); chm::count_launch();
+      zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[2], plane); chm::count_launch();
     }
   }
   ModeFlags fl{};
@@ -800,14 +802,14 @@ int chm_fb_graddiv(chm_c128 *vec, const double *Dp, const double *Dm, const doub
       D.um[c] = um[c];
       D.up[c] = up[c];
     }
-    div_ext_kernel<<<grid_for(plane * ns, 256), 256, 0, F.st>>>(D, fl);
+    div_ext_kernel<<<grid_for(plane * ns, 256), 256, 0, F.st>>>(D, fl); chm::count_launch();
     CHM_CHECK_LAUNCH();
   }
   // --- gradient of the extended scalar back onto nm modes (in place)
   {
     if (!env) {
-      if (nm > 1) reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[0], scl + plane, nx, nkr);
-      else zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[0], plane);
+      if (nm > 1) { reflect_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[0], scl + plane, nx, nkr); chm::count_launch(); }
+      else { zero_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[0], plane); chm::count_launch(); }
     }
     GemmList g = make_gemm(F);
     for (int m = 0; m < nm; ++m) {
@@ -822,7 +824,7 @@ int chm_fb_graddiv(chm_c128 *vec, const double *Dp, const double *Dm, const doub
     g.flush();
     if (g.err) return g.err;
     grad_ext_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(nx, nkr, (int)nm, off, scl, um[0],
-                                                                 up[0], v, cs, kx);
+                                                                 up[0], v, cs, kx); chm::count_launch();
     CHM_CHECK_LAUNCH();
   }
   return CHM_OK;
@@ -947,7 +949,7 @@ int chm_maxwell_push_with_spchrg(chm_c128 *eg, const chm_c128 *j, const chm_c128
   CHM_REQUIRE(eg && j && gn && gnp1 && c1 && c2, "maxwell_push_with_spchrg: null pointer");
   const i64 P = nx * nkr * nm;
   psatd_spchrg_kernel<<<grid_for(P, 256), 256, 0, as_stream(stream)>>>(
-      (double2 *)eg, (const double2 *)j, (const double2 *)gn, (const double2 *)gnp1, c1, c2, P);
+      (double2 *)eg, (const double2 *)j, (const double2 *)gn, (const double2 *)gnp1, c1, c2, P); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -958,7 +960,7 @@ int chm_maxwell_push_wo_spchrg(chm_c128 *eg, const chm_c128 *j, const chm_c128 *
   CHM_REQUIRE(eg && j && c1 && c2, "maxwell_push_wo_spchrg: null pointer");
   const i64 P = nx * nkr * nm;
   psatd_wo_kernel<<<grid_for(P, 256), 256, 0, as_stream(stream)>>>(
-      (double2 *)eg, (const double2 *)j, (const double2 *)c1, (const double2 *)c2, P);
+      (double2 *)eg, (const double2 *)j, (const double2 *)c1, (const double2 *)c2, P); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -969,7 +971,7 @@ int chm_maxwell_init_push(chm_c128 *eg, const chm_c128 *j, const chm_c128 *gn, c
   const i64 P = nx * nkr * nm;
   init_push_kernel<<<grid_for(P, 256), 256, 0, as_stream(stream)>>>(
       (double2 *)eg, (const double2 *)j, (const double2 *)gn, (const double2 *)c1,
-      (const double2 *)c2, P);
+      (const double2 *)c2, P); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -981,7 +983,7 @@ int chm_poiss_corr(chm_c128 *j, const chm_c128 *gdj, const chm_c128 *gn, const c
   const i64 P = nx * nkr * nm;
   poiss_corr_kernel<<<grid_for(P, 256), 256, 0, as_stream(stream)>>>(
       (double2 *)j, (const double2 *)gdj, (const double2 *)gn, (const double2 *)gnp1, dt_inv,
-      w2_inv, P);
+      w2_inv, P); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -991,7 +993,7 @@ int chm_poiss_corr_stat(chm_c128 *j, const chm_c128 *gdj, const chm_c128 *gn, co
   CHM_REQUIRE(j && gdj && gn && DT && w2_inv, "poiss_corr_stat: null pointer");
   const i64 P = nx * nkr * nm;
   poiss_corr_stat_kernel<<<grid_for(P, 256), 256, 0, as_stream(stream)>>>(
-      (double2 *)j, (const double2 *)gdj, (const double2 *)gn, (const double2 *)DT, w2_inv, P, nx);
+      (double2 *)j, (const double2 *)gdj, (const double2 *)gn, (const double2 *)DT, w2_inv, P, nx); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -1001,7 +1003,7 @@ int chm_field_drift(chm_c128 *eg, const double *kx, double beta0, double dt, int
   CHM_REQUIRE(eg && kx, "field_drift: null pointer");
   const i64 P = nx * nkr * nm;
   field_drift_kernel<<<grid_for(6 * P, 256), 256, 0, as_stream(stream)>>>((double2 *)eg, kx, beta0,
-                                                                           dt, P, nx);
+                                                                           dt, P, nx); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -1009,7 +1011,7 @@ int chm_field_drift(chm_c128 *eg, const double *kx, double beta0, double dt, int
 int chm_omp_mult(chm_c128 *v, const double *A, int64_t P, int64_t ncomp, void *stream) {
   CHM_REQUIRE(v && A && P >= 0 && ncomp > 0, "omp_mult: bad args");
   if (P == 0) return CHM_OK;
-  mult_kernel<<<grid_for(P, 256), 256, 0, as_stream(stream)>>>((double2 *)v, A, P, ncomp);
+  mult_kernel<<<grid_for(P, 256), 256, 0, as_stream(stream)>>>((double2 *)v, A, P, ncomp); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -1017,7 +1019,7 @@ int chm_omp_mult(chm_c128 *v, const double *A, int64_t P, int64_t ncomp, void *s
 int chm_omp_add(chm_c128 *v, const chm_c128 *A, int64_t n, void *stream) {
   CHM_REQUIRE(v && A && n >= 0, "omp_add: bad args");
   if (n == 0) return CHM_OK;
-  add_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>((double2 *)v, (const double2 *)A, n);
+  add_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>((double2 *)v, (const double2 *)A, n); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }

@@ -128,6 +128,10 @@ def _stream():
 
 _ws_cache: dict = {}
 
+# host<->device bytes moved by the shim and the drop-in classes (particle
+# injection, particle counts read back); the benchmark reports them.
+io_bytes = {"h2d": 0, "d2h": 0}
+
 
 def workspace(nbytes: int, device=None) -> torch.Tensor:
     """Scratch buffer for the C ABI (grown on demand, reused across calls)."""
@@ -177,6 +181,7 @@ def sortpartsout(coord, lims):
     ws = workspace(_lib.query("chm_sortpartsout_ws_bytes", n))
     _lib.call("chm_sortpartsout", idx.data_ptr(), C.addressof(num), x, xcs, xps,
               limsh.ctypes.data, n, ws.data_ptr(), ws.numel(), _stream())
+    io_bytes["d2h"] += 4
     return idx, int(num.value)
 
 
@@ -195,6 +200,7 @@ def chunk_coords_boundaries(coord, lims, Xgrid, nchnk):
     _lib.call("chm_chunk_coords_boundaries", ids.data_ptr(), ind.data_ptr(), C.addressof(go), x,
               xcs, xps, limsh.ctypes.data, float(xg[0]), float(xgc), nchnk, n, ws.data_ptr(),
               ws.numel(), _stream())
+    io_bytes["d2h"] += 4
     return ids, ind, int(go.value)
 
 
@@ -207,6 +213,7 @@ def chunk_order(chunked_indx, nchnk):
     ws = workspace(_lib.query("chm_chunk_order_ws_bytes", n, int(nchnk)))
     _lib.call("chm_chunk_order", idx.data_ptr(), C.addressof(kept), chunked_indx.data_ptr(),
               int(nchnk), n, ws.data_ptr(), ws.numel(), _stream())
+    io_bytes["d2h"] += 4
     return idx[: kept.value]
 
 

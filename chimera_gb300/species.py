@@ -67,8 +67,12 @@ class ParticleStore:
             self.reserve(max(self.n + m, int(1.5 * self.cap) + 1024))
         for k, nc in self.names.items():
             a = arrays[k]
-            t = a if isinstance(a, torch.Tensor) else torch.from_numpy(
-                np.ascontiguousarray(np.asarray(a, dtype=np.float64)))
+            if isinstance(a, torch.Tensor):
+                t = a
+            else:
+                t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64)))
+                if self.device.type == "cuda":
+                    chimera.io_bytes["h2d"] += t.numel() * 8
             t = t.to(self.device, torch.float64).reshape(nc, m)
             self.buf[k][:, self.n: self.n + m].copy_(t)
         self.n += m

@@ -52,6 +52,12 @@ enum {
 const char *chm_last_error(void);
 /* Library version string. */
 const char *chm_version(void);
+/* Diagnostics (no reference counterpart): number of kernels this library has
+ * launched since it was loaded, and the algorithmic FLOPs of the dense
+ * DHT / mode-coupling products it has issued (4 nx N K per complex plane
+ * times real matrix product). */
+int64_t chm_launch_count(void);
+double chm_gemm_flops(void);
 
 /* ======================================================================== */
 /* Particle push                                                             */
