@@ -261,7 +261,16 @@ def run_gb300(args):
     world, rank, local = dist_setup()
     lib = _lib.load()
     run, solver, el = build_run("gpu", "none", seed=1002 + rank)
-    n_moving = el.num_particles
+    if args.form == "split":
+        from chimera_gb300.split import SplitRun
+        run = SplitRun(None, fp64_run=run)
+
+        def nmov():
+            return run.num_moving
+    else:
+        def nmov():
+            return el.num_particles
+    n_moving = nmov()
     stream = torch.cuda.current_stream()
     for i in range(1, args.warmup + 1):
         run.make_step(i)
@@ -281,7 +290,7 @@ def run_gb300(args):
     psteps = 0
     for i in range(args.warmup + 1, args.warmup + args.steps + 1):
         run.make_step(i)
-        psteps += el.num_particles
+        psteps += nmov()
     ev1.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -327,6 +336,13 @@ def run_gb300(args):
     e2e = None
     if not args.no_e2e:
         run2, solver2, el2 = build_run("gpu", "inject", seed=2002 + rank)
+        eb2 = lambda: solver2.Data["EB"]  # noqa: E731
+        cnt2 = lambda: el2.num_particles  # noqa: E731
+        if args.form == "split":
+            from chimera_gb300.split import SplitRun
+            run2 = SplitRun(None, fp64_run=run2)
+            eb2 = lambda: run2.EB  # noqa: E731
+            cnt2 = lambda: run2.num_moving  # noqa: E731
         for i in range(1, args.warmup + 1):
             run2.make_step(i)
         torch.cuda.synchronize()
@@ -338,9 +354,9 @@ def run_gb300(args):
         a0 = 0.0
         for i in range(args.warmup + 1, args.warmup + args.steps + 1):
             run2.make_step(i)
-            ps2 += el2.num_particles
+            ps2 += cnt2()
             # the laser amplitude diagnostic of the demos (max Re Ey on axis)
-            a0 = float(solver2.Data["EB"][:, 1, 0, 2].real.max().item())
+            a0 = float(eb2()[:, 1, 0, 2].real.max().item())
         torch.cuda.synchronize()
         t_e2e = max_over_ranks(world, time.perf_counter() - t0)
         h2d = (fimera.io_bytes["h2d"] - h0) / args.steps
@@ -364,7 +380,7 @@ def run_gb300(args):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": "plain_fp64", "particles_moving": n_moving,
+        "config": {"workload": WORKLOAD, "form": args.form, "particles_moving": n_moving,
                    "particles_still": n_moving, "nx": SIZES[WORKLOAD_SIZE][0],
                    "nr": SIZES[WORKLOAD_SIZE][1] + 1, "modes": 2,
                    "parallelism": f"replicas{world}" if world > 1 else "single",
@@ -397,6 +413,8 @@ def main():
     ap.add_argument("--ref-max-steps", type=int, default=5)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--form", default="fp64", choices=["fp64", "split"],
+                    help="fp64 = plain FP64 form; split = split-precision form")
     ap.add_argument("--size", default="cfg2", choices=sorted(SIZES),
                     help="cfg2 = the benchmark workload; small = a reduced case for profiling")
     args = ap.parse_args()

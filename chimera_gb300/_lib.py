@@ -34,6 +34,8 @@ def _parse_header(path: str) -> dict[str, tuple[str, str]]:
                     kinds += I
                 elif a.startswith("double"):
                     kinds += D
+                elif a.startswith("float"):
+                    kinds += "f"
                 elif a.startswith("int"):
                     kinds += N
                 else:
@@ -44,7 +46,7 @@ def _parse_header(path: str) -> dict[str, tuple[str, str]]:
 
 _SIG = _parse_header(_HEADER)
 
-_KIND = {P: C.c_void_p, I: C.c_int64, D: C.c_double, N: C.c_int}
+_KIND = {P: C.c_void_p, I: C.c_int64, D: C.c_double, N: C.c_int, "f": C.c_float}
 
 
 class ChimeraError(RuntimeError):

@@ -1,0 +1,829 @@
+// Spectral stage of the split-precision form: complex64 fields, FP32 FFT
+// along x, dense DHT / mode-coupling products on the tensor cores (see
+// tc_gemm.cu) and fused FP32 epilogues.
+//
+// Differences from the FP64 path that keep memory traffic down:
+//  - the forward transforms read the 64-bit deposit accumulators directly
+//    (scale, ghost-row fold and the background density are applied on load);
+//  - the gradient of the Poisson correction updates J in place
+//    (maxwell_solvers.f90:131-164 fused into fb_graddiv's epilogue);
+//  - the curl that turns G into B applies PoissFact in its epilogue;
+//  - eb_correction is applied by the inverse FFT (as in the FP64 path).
+#include <math.h>
+
+#include "common.cuh"
+#include "tc_gemm.cuh"
+
+using namespace chm;
+
+namespace {
+
+constexpr int kMaxN = 4096;
+constexpr double kPi = 3.14159265358979323846;
+
+__device__ __forceinline__ float2 fadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 fsub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 fmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 fscl(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 fmi(float2 a) { return make_float2(-a.y, a.x); }  // i a
+
+struct Plan {
+  int n, ns;
+  int radix[24];
+};
+
+bool make_plan(int n, Plan *p) {
+  if (n < 1 || n > kMaxN) return false;
+  p->n = n;
+  p->ns = 0;
+  int m = n;
+  while (m % 4 == 0) {
+    p->radix[p->ns++] = 4;
+    m /= 4;
+  }
+  const int small[4] = {2, 3, 5, 7};
+  for (int s = 0; s < 4; ++s)
+    while (m % small[s] == 0 && p->ns < 24) {
+      p->radix[p->ns++] = small[s];
+      m /= small[s];
+    }
+  for (int f = 11; m > 1 && p->ns < 24;) {
+    if ((i64)f * f > m) f = m;
+    if (m % f == 0) {
+      p->radix[p->ns++] = f;
+      m /= f;
+    } else {
+      f += 2;
+    }
+  }
+  return m == 1;
+}
+
+// exp(-2 pi i t / n) in FP32 from an FP64 evaluation
+__global__ void twiddle32_kernel(float2 *tw, int n) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)t / (double)n, &s, &c);
+    tw[t] = make_float2((float)c, (float)-s);
+  }
+}
+
+// exp(sign i kx leftX) evaluated in FP64 (the argument can be large), stored FP32
+__global__ void shift32_kernel(float2 *shift, const double *kx, double leftX, int sign, i64 nx) {
+  for (i64 x = blockIdx.x * (i64)blockDim.x + threadIdx.x; x < nx; x += (i64)gridDim.x * blockDim.x) {
+    double s, c;
+    sincos(leftX * kx[x], &s, &c);
+    shift[x] = make_float2((float)c, (float)(sign * s));
+  }
+}
+
+__device__ __forceinline__ float2 tw32(const float2 *tw, int t, int sign) {
+  float2 w = tw[t];
+  if (sign > 0) w.y = -w.y;
+  return w;
+}
+
+__device__ void pass32(const float2 *__restrict__ src, float2 *__restrict__ dst, int n, int R, int Ns,
+                       const float2 *__restrict__ tw, int sign) {
+  const int nb = n / R;
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+    const int k = j % Ns;
+    const int tstep = (n / (Ns * R)) * k;
+    const int base = (j / Ns) * Ns * R + k;
+    if (R == 4) {
+      float2 v[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        float2 a = src[j + r * nb];
+        if (r > 0 && k > 0) a = fmul(a, tw32(tw, (r * tstep) % n, sign));
+        v[r] = a;
+      }
+      float2 a0 = fadd(v[0], v[2]), a1 = fsub(v[0], v[2]);
+      float2 a2 = fadd(v[1], v[3]), a3 = fsub(v[1], v[3]);
+      float2 a3r = sign < 0 ? make_float2(a3.y, -a3.x) : make_float2(-a3.y, a3.x);
+      dst[base] = fadd(a0, a2);
+      dst[base + Ns] = fadd(a1, a3r);
+      dst[base + 2 * Ns] = fsub(a0, a2);
+      dst[base + 3 * Ns] = fsub(a1, a3r);
+    } else if (R == 2) {
+      float2 a = src[j], b = src[j + nb];
+      if (k > 0) b = fmul(b, tw32(tw, tstep % n, sign));
+      dst[base] = fadd(a, b);
+      dst[base + Ns] = fsub(a, b);
+    } else {
+      const int step = n / R;
+      for (int q = 0; q < R; ++q) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int r = 0; r < R; ++r) {
+          float2 a = src[j + r * nb];
+          if (r > 0 && k > 0) a = fmul(a, tw32(tw, (r * tstep) % n, sign));
+          acc = fadd(acc, fmul(a, tw32(tw, ((r * q) % R) * step, sign)));
+        }
+        dst[base + q * Ns] = acc;
+      }
+    }
+  }
+}
+
+__device__ float2 *run32(const Plan &P, float2 *a, float2 *b, const float2 *tw, int sign) {
+  int Ns = 1;
+  for (int s = 0; s < P.ns; ++s) {
+    __syncthreads();
+    pass32(a, b, P.n, P.radix[s], Ns, tw, sign);
+    Ns *= P.radix[s];
+    float2 *t = a;
+    a = b;
+    b = t;
+  }
+  __syncthreads();
+  return a;
+}
+
+// Line sources/sinks of the FP32 FFT.
+struct Lines32 {
+  // input: either complex64 rows or a 64-bit deposit accumulator
+  const float2 *in;
+  const long long *acc;   // (n, rows_tot, planes) x {re, im}, or null
+  const double *acc_scale;
+  const long long *acc2;  // optional second accumulator (background density)
+  const double *acc2_scale;
+  int in_rows, in_rows_tot, in_row_off;
+  float2 *out;
+  int out_rows, out_rows_tot, out_row_off;
+  int nm, eb_mode, sign;
+  const float2 *pre_shift;  // multiply inputs (filter path)
+  int filt_mode, nxfilt;
+  const float *filtr;
+};
+
+__global__ void lines32_kernel(Plan P, const float2 *__restrict__ tw, Lines32 L) {
+  extern __shared__ __align__(16) float2 sm32[];
+  const int n = P.n;
+  float2 *a = sm32, *b = sm32 + n;
+  const i64 line = blockIdx.x;
+  const i64 ib = line / L.in_rows, ir = line % L.in_rows;
+  const i64 row = ib * L.in_rows_tot + ir + L.in_row_off;
+  if (L.acc) {
+    // deposit accumulator: value / scale with the ghost fold row1 -= row0
+    const double inv = 1.0 / L.acc_scale[0];
+    const double inv2 = L.acc2 ? 1.0 / L.acc2_scale[0] : 0.0;
+    const bool fold = (ir + L.in_row_off) == 1;
+    const i64 row0 = ib * L.in_rows_tot;
+    for (int x = threadIdx.x; x < n; x += blockDim.x) {
+      const i64 e = row * n + x;
+      double re = (double)L.acc[2 * e] * inv, im = (double)L.acc[2 * e + 1] * inv;
+      if (L.acc2) {
+        re += (double)L.acc2[2 * e] * inv2;
+        im += (double)L.acc2[2 * e + 1] * inv2;
+      }
+      if (fold) {
+        const i64 e0 = row0 * n + x;
+        re -= (double)L.acc[2 * e0] * inv;
+        im -= (double)L.acc[2 * e0 + 1] * inv;
+        if (L.acc2) {
+          re -= (double)L.acc2[2 * e0] * inv2;
+          im -= (double)L.acc2[2 * e0 + 1] * inv2;
+        }
+      }
+      a[x] = make_float2((float)re, (float)im);
+    }
+  } else {
+    const float2 *src = L.in + row * (i64)n;
+    for (int x = threadIdx.x; x < n; x += blockDim.x) {
+      float2 v = src[x];
+      if (L.pre_shift) v = fmul(v, L.pre_shift[x]);
+      a[x] = v;
+    }
+  }
+  float2 *res = run32(P, a, b, tw, L.sign);
+  if (L.filt_mode >= 0) {
+    for (int x = threadIdx.x; x < L.nxfilt; x += blockDim.x)
+      if (L.filt_mode == 0 || L.filt_mode == 2) res[x] = fscl(res[x], L.filtr[x]);
+    __syncthreads();
+    for (int x = threadIdx.x; x < L.nxfilt; x += blockDim.x)
+      if (L.filt_mode == 1 || L.filt_mode == 2) res[n - 1 - x] = fscl(res[n - 1 - x], L.filtr[x]);
+    float2 *other = (res == a) ? b : a;
+    res = run32(P, res, other, tw, -1);
+  }
+  const i64 ob = line / L.out_rows, orow = line % L.out_rows;
+  float2 *dst = L.out + (ob * L.out_rows_tot + orow + L.out_row_off) * (i64)n;
+  float fac = 1.0f, sg = 1.0f;
+  if (L.eb_mode) {
+    const int m = (int)(ob % L.nm);
+    fac = (float)((m == 0) ? 0.5 / kPi : 1.0 / kPi);
+    sg = (m == 0) ? 1.0f : -1.0f;
+  }
+  const bool ghost = L.eb_mode && orow == 0;
+  float2 *gdst = L.out + (ob * L.out_rows_tot) * (i64)n;
+  for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    float2 v = res[x];
+    if (L.filt_mode >= 0) {
+      float2 s = L.pre_shift[x];
+      float inv = 1.0f / ((float)n * (s.x * s.x + s.y * s.y));
+      v = fmul(v, make_float2(s.x * inv, -s.y * inv));
+    }
+    if (L.eb_mode) v = fscl(v, fac);
+    dst[x] = v;
+    if (ghost) gdst[x] = fscl(v, sg);
+  }
+}
+
+int lines32_launch(const Lines32 &L, int n, i64 nlines, float2 *tw, cudaStream_t st) {
+  Plan P;
+  if (!make_plan(n, &P)) {
+    set_error("split fft: unsupported length %d", n);
+    return CHM_ERR_RANGE;
+  }
+  if (nlines <= 0) return CHM_OK;
+  twiddle32_kernel<<<(n + 255) / 256, 256, 0, st>>>(tw, n); chm::count_launch();
+  const size_t smem = 2 * (size_t)n * sizeof(float2);
+  cudaFuncSetAttribute(lines32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int threads = n >= 1024 ? 512 : (n >= 256 ? 256 : 128);
+  lines32_kernel<<<(unsigned)nlines, threads, smem, st>>>(P, tw, L); chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+// -------------------------------------------------------------------------
+// Workspace
+// -------------------------------------------------------------------------
+struct Ws {
+  char *p;
+  i64 left;
+  template <typename T>
+  T *take(i64 n) {
+    i64 bytes = (n * (i64)sizeof(T) + 255) / 256 * 256;
+    if (bytes > left) return nullptr;
+    T *r = reinterpret_cast<T *>(p);
+    p += bytes;
+    left -= bytes;
+    return r;
+  }
+};
+
+inline i64 r256(i64 b) { return (b + 255) / 256 * 256; }
+
+// -------------------------------------------------------------------------
+// Elementwise / combine kernels
+// -------------------------------------------------------------------------
+__global__ void reflect32_kernel(float2 *__restrict__ dst, const float2 *__restrict__ src, i64 nx, i64 nk) {
+  const i64 n = nx * nk;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x) {
+    i64 x = t % nx, k = t / nx;
+    i64 xs = x == 0 ? 0 : nx - x;
+    float2 v = src[xs + k * nx];
+    dst[t] = make_float2(-v.x, v.y);
+  }
+}
+
+__global__ void zero32_kernel(float2 *p, i64 n) {
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x)
+    p[t] = make_float2(0.f, 0.f);
+}
+
+// grad of a scalar: out1 = i kx s, out2 = up - lo, out3 = i (lo + up)
+// (fb_math.f90:96-149); with `poiss` the result updates J in place:
+// J += (grad + (gnxt - gprv) dt_inv) * PF (maxwell_solvers.f90:131-164), or
+// J += grad * PF without space charge (solvers.py:328-331).
+struct GradArgs {
+  i64 nx, nk;
+  int nm, off;  // scalar index of output mode 0
+  const float2 *scl;
+  const float2 *lo, *up;  // products per output mode
+  const float *kx;
+  float2 *out;            // vector (nx, nk, nm, 3)
+  i64 cs;                 // component stride of out
+  int poiss;              // 0: store; 1: J update with charge; 2: J update, no charge
+  const float2 *gprv, *gnxt;
+  const float *pf;
+  float dt_inv;
+  int up_from;            // modes m < up_to have an upper product
+  int up_to;
+};
+
+__global__ void grad32_kernel(GradArgs A) {
+  const i64 plane = A.nx * A.nk;
+  const i64 n = plane * A.nm;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x) {
+    const i64 x = t % A.nx;
+    const int m = (int)(t / plane);
+    const i64 e = t - (i64)m * plane;
+    const float2 s = A.scl[e + plane * (m + A.off)];
+    const float2 lo = A.lo[t];
+    const float2 up = (m < A.up_to) ? A.up[t] : make_float2(0.f, 0.f);
+    float2 g[3];
+    g[0] = fscl(fmi(s), A.kx[x]);
+    g[1] = fsub(up, lo);
+    g[2] = fmi(fadd(lo, up));
+    if (A.poiss == 0) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) A.out[t + c * A.cs] = g[c];
+    } else {
+      const float f = A.pf[t];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        float2 v = g[c];
+        if (A.poiss == 1) {
+          float2 d = fsub(A.gnxt[t + c * A.cs], A.gprv[t + c * A.cs]);
+          v = fadd(v, fscl(d, A.dt_inv));
+        }
+        A.out[t + c * A.cs] = fadd(A.out[t + c * A.cs], fscl(v, f));
+      }
+    }
+  }
+}
+
+// divergence on ns scalar modes (fb_math.f90:222-252)
+struct DivArgs {
+  i64 nx, nk;
+  int ns, nm;
+  const float2 *v;  // (nx, nk, nm, 3)
+  i64 cs;
+  const float2 *lo2, *lo3, *up2, *up3;  // per scalar mode
+  const float *kx;
+  float2 *scl;
+  unsigned char lo_ok[16], up_ok[16];
+};
+
+__global__ void div32_kernel(DivArgs A) {
+  const i64 plane = A.nx * A.nk;
+  const i64 n = plane * A.ns;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x) {
+    const i64 x = t % A.nx;
+    const int ms = (int)(t / plane);
+    const i64 e = t - (i64)ms * plane;
+    float2 r = make_float2(0.f, 0.f);
+    if (ms < A.nm) r = fscl(fmi(A.v[e + plane * ms]), A.kx[x]);
+    if (A.lo_ok[ms]) r = fadd(r, fsub(fmi(A.lo3[t]), A.lo2[t]));
+    if (A.up_ok[ms]) r = fadd(r, fadd(fmi(A.up3[t]), A.up2[t]));
+    A.scl[t] = r;
+  }
+}
+
+// curl of G with PoissFact: B = rot(G) * PF (fb_math.f90:18-94, solvers.py:536-553)
+struct RotArgs {
+  i64 nx, nk;
+  int nm;
+  const float2 *v;
+  i64 cs;
+  const float2 *lo[3], *up[3];
+  const float *kx, *pf;
+  float2 *out;
+};
+
+__global__ void rot32_kernel(RotArgs A) {
+  const i64 plane = A.nx * A.nk;
+  const i64 n = plane * A.nm;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x) {
+    const i64 x = t % A.nx;
+    const int m = (int)(t / plane);
+    const float kxv = A.kx[x];
+    const float2 v2 = A.v[t + A.cs], v3 = A.v[t + 2 * A.cs];
+    const bool hi = m < A.nm - 1;
+    const float2 z = make_float2(0.f, 0.f);
+    const float2 p1 = hi ? A.up[0][t] : z, p2 = hi ? A.up[1][t] : z, p3 = hi ? A.up[2][t] : z;
+    const float2 m1 = A.lo[0][t], m2 = A.lo[1][t], m3 = A.lo[2][t];
+    float2 o1 = fsub(make_float2(0.f, 0.f), fsub(fmi(p2), p3));
+    o1 = fsub(o1, fadd(fmi(m2), m3));
+    float2 o2 = fadd(fscl(fmi(v3), -kxv), fadd(fmi(p1), fmi(m1)));
+    float2 o3 = fadd(fscl(fmi(v2), kxv), fsub(m1, p1));
+    const float f = A.pf[t];
+    A.out[t] = fscl(o1, f);
+    A.out[t + A.cs] = fscl(o2, f);
+    A.out[t + 2 * A.cs] = fscl(o3, f);
+  }
+}
+
+// PSATD (maxwell_solvers.f90:18-96), FP32 real coefficients, 3 or 5 terms
+__global__ void psatd32_kernel(float2 *__restrict__ eg, const float2 *__restrict__ j,
+                               const float2 *__restrict__ ga, const float2 *__restrict__ gb,
+                               const float *__restrict__ c1, const float *__restrict__ c2, int nterm,
+                               i64 P) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < P; i += (i64)gridDim.x * blockDim.x) {
+    float a[5], b[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      a[k] = k < nterm ? c1[i + k * P] : 0.f;
+      b[k] = k < nterm ? c2[i + k * P] : 0.f;
+    }
+#pragma unroll
+    for (int l = 0; l < 3; ++l) {
+      const float2 e = eg[i + P * l], g = eg[i + P * (3 + l)], jj = j[i + P * l];
+      float2 en = fadd(fadd(fscl(e, a[0]), fscl(g, a[1])), fscl(jj, a[2]));
+      float2 gn = fadd(fadd(fscl(e, b[0]), fscl(g, b[1])), fscl(jj, b[2]));
+      if (nterm == 5) {
+        const float2 x = ga[i + P * l], y = gb[i + P * l];
+        en = fadd(en, fadd(fscl(x, a[3]), fscl(y, a[4])));
+        gn = fadd(gn, fadd(fscl(x, b[3]), fscl(y, b[4])));
+      }
+      eg[i + P * (3 + l)] = gn;
+      eg[i + P * l] = en;
+    }
+  }
+}
+
+// -------------------------------------------------------------------------
+// dense products C(2nx, N) = A(2nx, K) * B(K, N) for a batch of planes
+// -------------------------------------------------------------------------
+struct Batch32 {
+  TcProblem p[64];
+  int count;
+};
+
+// scratch of the tensor-core path, set per call from the workspace
+struct Scr {
+  void *p;
+  i64 bytes;
+};
+thread_local Scr g_scr{nullptr, 0};
+
+int gemm32(const Batch32 &b, int M, int N, int K, const TcOperand &bop, int epi,
+           const float2 *shift, cudaStream_t st) {
+  if (b.count == 0) return CHM_OK;
+  return tc_gemm_launch(b.p, b.count, M, N, K, bop, epi, shift, g_scr.p, g_scr.bytes, st);
+}
+
+// carves the tensor-core scratch (up to 6 planes of M x K) from a workspace
+bool take_scratch(Ws &W, i64 M, i64 K) {
+  const i64 b = tc_scratch_bytes(M, K, 6);
+  g_scr.p = W.take<char>(b);
+  g_scr.bytes = g_scr.p ? b : 0;
+  return g_scr.p != nullptr;
+}
+
+struct Fb32 {
+  i64 nx, nk, nm;
+  TcMatrices Dp, Dm;  // per-mode operands (split for the tensor cores)
+  const float *kx;
+  cudaStream_t st;
+  Ws ws;
+};
+
+}  // namespace
+
+// =========================================================================
+// C ABI of the split-form spectral stage
+// =========================================================================
+extern "C" {
+
+int64_t chm_sp_fb_ws_bytes(int64_t nx, int64_t nr, int64_t nkr, int64_t nm) {
+  const i64 rows = nr - 1 > nkr ? nr - 1 : nkr;
+  const i64 plane = 8 * nx * (rows > nkr ? rows : nkr);
+  return 4 * r256(8 * nx) + r256(plane * nm * 6) + 8 * r256(plane * (nm + 2)) +
+         r256(tc_scratch_bytes(2 * nx, rows, 6)) + 8192;
+}
+
+// fb_vec_in / fb_scl_in of a deposit accumulator (ncomp 3 or 1), with
+// DepFact: out = shift * fact * DHT(FFT(acc / scale [+ acc2 / scale2]))
+int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, const int64_t *acc2,
+                     const double *scale2, double leftX, const double *kx, const void *In_ops,
+                     const float *fact, int64_t nx, int64_t nr, int64_t nkr, int64_t nm,
+                     int64_t ncomp, void *ws, int64_t ws_bytes, void *stream) {
+  CHM_REQUIRE(out_c64 && acc && scale && kx && In_ops && fact, "sp_fb_in_acc: null pointer");
+  CHM_REQUIRE(ws && ws_bytes >= chm_sp_fb_ws_bytes(nx, nr, nkr, nm), "sp_fb_in_acc: workspace");
+  cudaStream_t st = as_stream(stream);
+  Ws W{(char *)ws, ws_bytes};
+  float2 *tw = W.take<float2>(nx);
+  float2 *shift = W.take<float2>(nx);
+  const i64 nrr = nr - 1;
+  float2 *tmp = W.take<float2>(nx * nrr * nm * ncomp);
+  if (!tmp || !take_scratch(W, 2 * nx, nrr)) {
+    set_error("sp_fb_in_acc: workspace exhausted");
+    return CHM_ERR_WS;
+  }
+  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, -1, nx); chm::count_launch();
+  Lines32 L{};
+  L.acc = reinterpret_cast<const long long *>(acc);
+  L.acc_scale = scale;
+  L.acc2 = reinterpret_cast<const long long *>(acc2);
+  L.acc2_scale = scale2;
+  L.in_rows = (int)nrr;
+  L.in_rows_tot = (int)nr;
+  L.in_row_off = 1;
+  L.out = tmp;
+  L.out_rows = L.out_rows_tot = (int)nrr;
+  L.nm = (int)nm;
+  L.sign = -1;
+  L.filt_mode = -1;
+  int rc = lines32_launch(L, (int)nx, nrr * nm * ncomp, tw, st);
+  if (rc) return rc;
+  const TcMatrices In = tc_matrices(reinterpret_cast<const chm_sp_ops *>(In_ops));
+  for (i64 m = 0; m < nm; ++m) {
+    Batch32 b{};
+    for (i64 l = 0; l < ncomp; ++l)
+      b.p[b.count++] = TcProblem{reinterpret_cast<const float *>(tmp + nx * nrr * (m + nm * l)),
+                                 reinterpret_cast<float *>(out_c64) + 2 * nx * nkr * (m + nm * l),
+                                 fact + nx * nkr * m};
+    rc = gemm32(b, (int)(2 * nx), (int)nkr, (int)nrr, In.mode[m], TC_EPI_SHIFT_FAC, shift, st);
+    if (rc) return rc;
+  }
+  return CHM_OK;
+}
+
+// fb_eb_out + eb_correction (fb_io.f90:182-228, grid_deps.f90:219-266)
+int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double leftX,
+                     const double *kx, const void *Out_ops, int64_t nx, int64_t nr, int64_t nkr,
+                     int64_t nm, void *ws, int64_t ws_bytes, void *stream) {
+  CHM_REQUIRE(eb_c64 && e_c64 && b_c64 && kx && Out_ops, "sp_fb_eb_out: null pointer");
+  CHM_REQUIRE(ws && ws_bytes >= chm_sp_fb_ws_bytes(nx, nr, nkr, nm), "sp_fb_eb_out: workspace");
+  cudaStream_t st = as_stream(stream);
+  Ws W{(char *)ws, ws_bytes};
+  float2 *tw = W.take<float2>(nx);
+  float2 *shift = W.take<float2>(nx);
+  const i64 nrr = nr - 1;
+  float2 *tmp = W.take<float2>(nx * nrr * nm * 6);
+  if (!tmp || !take_scratch(W, 2 * nx, nkr)) {
+    set_error("sp_fb_eb_out: workspace exhausted");
+    return CHM_ERR_WS;
+  }
+  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx); chm::count_launch();
+  const TcMatrices Out = tc_matrices(reinterpret_cast<const chm_sp_ops *>(Out_ops));
+  for (i64 m = 0; m < nm; ++m) {
+    Batch32 b{};
+    for (int l = 0; l < 6; ++l) {
+      const float2 *src = (l < 3 ? reinterpret_cast<const float2 *>(e_c64) + nx * nkr * (m + nm * l)
+                                 : reinterpret_cast<const float2 *>(b_c64) + nx * nkr * (m + nm * (l - 3)));
+      b.p[b.count++] = TcProblem{reinterpret_cast<const float *>(src),
+                                 reinterpret_cast<float *>(tmp + nx * nrr * (m + nm * l)), nullptr};
+    }
+    int rc = gemm32(b, (int)(2 * nx), (int)nrr, (int)nkr, Out.mode[m], TC_EPI_SHIFT, shift, st);
+    if (rc) return rc;
+  }
+  Lines32 L{};
+  L.in = tmp;
+  L.in_rows = L.in_rows_tot = (int)nrr;
+  L.out = reinterpret_cast<float2 *>(eb_c64);
+  L.out_rows = (int)nrr;
+  L.out_rows_tot = (int)nr;
+  L.out_row_off = 1;
+  L.nm = (int)nm;
+  L.eb_mode = 1;
+  L.sign = +1;
+  L.filt_mode = -1;
+  return lines32_launch(L, (int)nx, nrr * nm * 6, tw, st);
+}
+
+// fb_filtr on complex64 planes (fb_io.f90:230-308)
+int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx, const float *filtr,
+                    int64_t nxfilt, int modefilt, int64_t nx, int64_t nkr, int64_t nm,
+                    int64_t ncomp, void *ws, int64_t ws_bytes, void *stream) {
+  CHM_REQUIRE(vec_c64 && kx && (nxfilt == 0 || filtr) && modefilt >= 0 && modefilt <= 2,
+              "sp_fb_filtr: bad args");
+  CHM_REQUIRE(ws && ws_bytes >= 2 * r256(8 * nx), "sp_fb_filtr: workspace");
+  cudaStream_t st = as_stream(stream);
+  Ws W{(char *)ws, ws_bytes};
+  float2 *tw = W.take<float2>(nx);
+  float2 *shift = W.take<float2>(nx);
+  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx); chm::count_launch();
+  Lines32 L{};
+  L.in = reinterpret_cast<const float2 *>(vec_c64);
+  L.out = reinterpret_cast<float2 *>(vec_c64);
+  L.in_rows = L.in_rows_tot = L.out_rows = L.out_rows_tot = (int)nkr;
+  L.nm = (int)nm;
+  L.sign = +1;
+  L.pre_shift = shift;
+  L.filt_mode = modefilt;
+  L.filtr = filtr;
+  L.nxfilt = (int)nxfilt;
+  return lines32_launch(L, (int)nx, nkr * nm * ncomp, tw, st);
+}
+
+}  // extern "C"
+
+namespace {
+
+// lower / upper neighbour products of `ncomp` components for output modes
+// 0..nout-1 (input mode m-1+shift / m+1+shift, D mode m); the lower
+// neighbour of input mode -1 is the reflected m = 1 plane `refl[c]`.
+int neighbours32(Fb32 &F, const float2 *in, i64 cs, int ncomp, int nin, int nout, int shift,
+                 const float2 *const *refl, float2 *lo[3], float2 *up[3], unsigned char *lo_ok,
+                 unsigned char *up_ok) {
+  const i64 plane = F.nx * F.nk;
+  for (int m = 0; m < nout; ++m) {
+    const int mlo = m - 1 + shift, mhi = m + 1 + shift;
+    Batch32 bl{}, bu{};
+    lo_ok[m] = up_ok[m] = 0;
+    for (int c = 0; c < ncomp; ++c) {
+      const float2 *src = nullptr;
+      if (mlo >= 0 && mlo < nin) src = in + c * cs + plane * mlo;
+      else if (mlo == -1 && refl) src = refl[c];
+      if (src) {
+        bl.p[bl.count++] = TcProblem{reinterpret_cast<const float *>(src),
+                                     reinterpret_cast<float *>(lo[c] + plane * m), nullptr};
+        lo_ok[m] = 1;
+      }
+      if (mhi >= 0 && mhi < nin) {
+        bu.p[bu.count++] = TcProblem{reinterpret_cast<const float *>(in + c * cs + plane * mhi),
+                                     reinterpret_cast<float *>(up[c] + plane * m), nullptr};
+        up_ok[m] = 1;
+      }
+    }
+    int rc = gemm32(bl, (int)(2 * F.nx), (int)F.nk, (int)F.nk, F.Dm.mode[m], TC_EPI_STORE, nullptr, F.st);
+    if (rc) return rc;
+    rc = gemm32(bu, (int)(2 * F.nx), (int)F.nk, (int)F.nk, F.Dp.mode[m], TC_EPI_STORE, nullptr, F.st);
+    if (rc) return rc;
+  }
+  return CHM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// fb_grad (fb_math.f90:96-149) on complex64
+int chm_sp_fb_grad(void *out_c64, const void *scl_c64, const void *Dp_ops, const void *Dm_ops,
+                   const float *kx, int64_t nx, int64_t nkr, int64_t nm, void *ws,
+                   int64_t ws_bytes, void *stream) {
+  CHM_REQUIRE(out_c64 && scl_c64 && Dp_ops && Dm_ops && kx && nm <= 14, "sp_fb_grad: bad args");
+  CHM_REQUIRE(ws && ws_bytes >= chm_sp_fb_ws_bytes(nx, nkr + 1, nkr, nm), "sp_fb_grad: workspace");
+  Fb32 F{nx, nkr, nm, tc_matrices(reinterpret_cast<const chm_sp_ops *>(Dp_ops)),
+         tc_matrices(reinterpret_cast<const chm_sp_ops *>(Dm_ops)), kx, as_stream(stream), Ws{(char *)ws, ws_bytes}};
+  const i64 plane = nx * nkr;
+  const float2 *s = reinterpret_cast<const float2 *>(scl_c64);
+  float2 *lo[3] = {F.ws.take<float2>(plane * nm), nullptr, nullptr};
+  float2 *up[3] = {F.ws.take<float2>(plane * nm), nullptr, nullptr};
+  float2 *ext = F.ws.take<float2>(plane);
+  if (!ext || !take_scratch(F.ws, 2 * nx, nkr)) {
+    set_error("sp_fb_grad: workspace exhausted");
+    return CHM_ERR_WS;
+  }
+  if (nm > 1) { reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext, s + plane, nx, nkr); chm::count_launch(); }
+  else { zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext, plane); chm::count_launch(); }
+  const float2 *refl[3] = {ext, nullptr, nullptr};
+  unsigned char lok[16], uok[16];
+  int rc = neighbours32(F, s, 0, 1, (int)nm, (int)nm, 0, refl, lo, up, lok, uok);
+  if (rc) return rc;
+  GradArgs A{};
+  A.nx = nx;
+  A.nk = nkr;
+  A.nm = (int)nm;
+  A.off = 0;
+  A.scl = s;
+  A.lo = lo[0];
+  A.up = up[0];
+  A.kx = kx;
+  A.out = reinterpret_cast<float2 *>(out_c64);
+  A.cs = plane * nm;
+  A.up_to = (int)nm - 1;
+  grad32_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A); chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+// The Poisson correction of solvers.py:301-331 on complex64: `iters` times
+//   v = grad(div(J)) (fb_graddiv, fb_math.f90:201-293)
+//   J += (v + (gnxt - gprv) dt_inv) PF      (space charge)
+//   J += v PF                               (otherwise)
+int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, const float *pf,
+                   float dt_inv, const void *Dp_ops, const void *Dm_ops, const float *kx,
+                   int64_t nx, int64_t nkr, int64_t nm, int iters, int space_charge, void *ws,
+                   int64_t ws_bytes, void *stream) {
+  CHM_REQUIRE(J_c64 && pf && Dp_ops && Dm_ops && kx && nm <= 14, "sp_poisson: bad args");
+  CHM_REQUIRE(!space_charge || (gprv_c64 && gnxt_c64), "sp_poisson: missing charge gradients");
+  CHM_REQUIRE(ws && ws_bytes >= chm_sp_fb_ws_bytes(nx, nkr + 1, nkr, nm), "sp_poisson: workspace");
+  Fb32 F{nx, nkr, nm, tc_matrices(reinterpret_cast<const chm_sp_ops *>(Dp_ops)),
+         tc_matrices(reinterpret_cast<const chm_sp_ops *>(Dm_ops)), kx, as_stream(stream), Ws{(char *)ws, ws_bytes}};
+  const i64 plane = nx * nkr;
+  const i64 cs = plane * nm;
+  const int ns = (int)nm + 1;
+  float2 *J = reinterpret_cast<float2 *>(J_c64);
+  float2 *scl = F.ws.take<float2>(plane * ns);
+  float2 *lo[3], *up[3];
+  for (int c = 0; c < 3; ++c) {
+    lo[c] = F.ws.take<float2>(plane * ns);
+    up[c] = F.ws.take<float2>(plane * ns);
+  }
+  float2 *ext[3];
+  for (int c = 0; c < 3; ++c) ext[c] = F.ws.take<float2>(plane);
+  if (!ext[2] || !take_scratch(F.ws, 2 * nx, nkr)) {
+    set_error("sp_poisson: workspace exhausted");
+    return CHM_ERR_WS;
+  }
+  for (int it = 0; it < iters; ++it) {
+    // divergence on nm + 1 modes
+    if (nm > 1) {
+      reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[1], J + cs + plane, nx, nkr); chm::count_launch();
+      reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[2], J + 2 * cs + plane, nx, nkr); chm::count_launch();
+    } else {
+      zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[1], plane); chm::count_launch();
+      zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[2], plane); chm::count_launch();
+    }
+    const float2 *refl23[3] = {ext[1], ext[2], nullptr};
+    float2 *lo23[3] = {lo[1], lo[2], nullptr}, *up23[3] = {up[1], up[2], nullptr};
+    DivArgs D{};
+    int rc = neighbours32(F, J + cs, cs, 2, (int)nm, ns, 0, refl23, lo23, up23, D.lo_ok, D.up_ok);
+    if (rc) return rc;
+    for (int ms = 0; ms < ns; ++ms)
+      if (!(ms < (int)nm - 1)) D.up_ok[ms] = 0;
+    D.nx = nx;
+    D.nk = nkr;
+    D.ns = ns;
+    D.nm = (int)nm;
+    D.v = J;
+    D.cs = cs;
+    D.lo2 = lo[1];
+    D.lo3 = lo[2];
+    D.up2 = up[1];
+    D.up3 = up[2];
+    D.kx = kx;
+    D.scl = scl;
+    div32_kernel<<<grid_for(plane * ns, 256), 256, 0, F.st>>>(D); chm::count_launch();
+    // gradient back onto nm modes, fused with the J update
+    if (nm > 1) { reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[0], scl + plane, nx, nkr); chm::count_launch(); }
+    else { zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[0], plane); chm::count_launch(); }
+    for (int m = 0; m < (int)nm; ++m) {
+      Batch32 bl{}, bu{};
+      const float2 *lsrc = (m - 1 >= 0) ? scl + plane * (m - 1) : ext[0];
+      bl.p[bl.count++] = TcProblem{reinterpret_cast<const float *>(lsrc),
+                                   reinterpret_cast<float *>(lo[0] + plane * m), nullptr};
+      bu.p[bu.count++] = TcProblem{reinterpret_cast<const float *>(scl + plane * (m + 1)),
+                                   reinterpret_cast<float *>(up[0] + plane * m), nullptr};
+      rc = gemm32(bl, (int)(2 * nx), (int)nkr, (int)nkr, F.Dm.mode[m], TC_EPI_STORE, nullptr, F.st);
+      if (rc) return rc;
+      rc = gemm32(bu, (int)(2 * nx), (int)nkr, (int)nkr, F.Dp.mode[m], TC_EPI_STORE, nullptr, F.st);
+      if (rc) return rc;
+    }
+    GradArgs A{};
+    A.nx = nx;
+    A.nk = nkr;
+    A.nm = (int)nm;
+    A.off = 0;
+    A.scl = scl;
+    A.lo = lo[0];
+    A.up = up[0];
+    A.kx = kx;
+    A.out = J;
+    A.cs = cs;
+    A.poiss = space_charge ? 1 : 2;
+    A.gprv = reinterpret_cast<const float2 *>(gprv_c64);
+    A.gnxt = reinterpret_cast<const float2 *>(gnxt_c64);
+    A.pf = pf;
+    A.dt_inv = dt_inv;
+    A.up_to = (int)nm;
+    grad32_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A); chm::count_launch();
+  }
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+// B = rot(G) * PoissFact (solvers.py:536-553)
+int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf, const void *Dp_ops,
+                 const void *Dm_ops, const float *kx, int64_t nx, int64_t nkr, int64_t nm, void *ws,
+                 int64_t ws_bytes, void *stream) {
+  CHM_REQUIRE(B_c64 && G_c64 && pf && Dp_ops && Dm_ops && kx && nm <= 14, "sp_rot_b: bad args");
+  CHM_REQUIRE(ws && ws_bytes >= chm_sp_fb_ws_bytes(nx, nkr + 1, nkr, nm), "sp_rot_b: workspace");
+  Fb32 F{nx, nkr, nm, tc_matrices(reinterpret_cast<const chm_sp_ops *>(Dp_ops)),
+         tc_matrices(reinterpret_cast<const chm_sp_ops *>(Dm_ops)), kx, as_stream(stream), Ws{(char *)ws, ws_bytes}};
+  const i64 plane = nx * nkr;
+  const i64 cs = plane * nm;
+  const float2 *G = reinterpret_cast<const float2 *>(G_c64);
+  float2 *lo[3], *up[3], *ext[3];
+  for (int c = 0; c < 3; ++c) {
+    lo[c] = F.ws.take<float2>(plane * nm);
+    up[c] = F.ws.take<float2>(plane * nm);
+  }
+  if (!take_scratch(F.ws, 2 * nx, nkr)) {
+    set_error("sp_rot_b: workspace exhausted");
+    return CHM_ERR_WS;
+  }
+  for (int c = 0; c < 3; ++c) {
+    ext[c] = F.ws.take<float2>(plane);
+    if (nm > 1) { reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[c], G + c * cs + plane, nx, nkr); chm::count_launch(); }
+    else { zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[c], plane); chm::count_launch(); }
+  }
+  const float2 *refl[3] = {ext[0], ext[1], ext[2]};
+  unsigned char lok[16], uok[16];
+  int rc = neighbours32(F, G, cs, 3, (int)nm, (int)nm, 0, refl, lo, up, lok, uok);
+  if (rc) return rc;
+  RotArgs A{};
+  A.nx = nx;
+  A.nk = nkr;
+  A.nm = (int)nm;
+  A.v = G;
+  A.cs = cs;
+  for (int c = 0; c < 3; ++c) {
+    A.lo[c] = lo[c];
+    A.up[c] = up[c];
+  }
+  A.kx = kx;
+  A.pf = pf;
+  A.out = reinterpret_cast<float2 *>(B_c64);
+  rot32_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A); chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+int chm_sp_psatd(void *eg_c64, const void *j_c64, const void *gprv_c64, const void *gnxt_c64,
+                 const float *c1, const float *c2, int nterm, int64_t P, void *stream) {
+  CHM_REQUIRE(eg_c64 && j_c64 && c1 && c2 && (nterm == 3 || nterm == 5), "sp_psatd: bad args");
+  CHM_REQUIRE(nterm == 3 || (gprv_c64 && gnxt_c64), "sp_psatd: missing charge gradients");
+  psatd32_kernel<<<grid_for(P, 256), 256, 0, as_stream(stream)>>>(
+      (float2 *)eg_c64, (const float2 *)j_c64, (const float2 *)gprv_c64, (const float2 *)gnxt_c64,
+      c1, c2, nterm, P); chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,38 @@
+// Dense products of the split-precision form:
+//   C(M, N) = A(M, K) * B(K, N), A = a complex64 plane viewed as real
+//   (M = 2 nx rows), B = a per-mode real DHT / coupling matrix.
+#pragma once
+#include "common.cuh"
+
+namespace chm {
+
+// One mode's B operand: FP32 copy and the 3-term BF16 split
+// (b = b0 + b1 + b2 exactly to ~2^-24) in the tensor-core operand layout.
+struct TcOperand {
+  const float *f32;        // (K, N) column-major
+  const uint16_t *bf[3];   // split terms, see tc_gemm.cu
+  int K, N;
+};
+
+struct TcMatrices {
+  TcOperand mode[16];
+};
+
+struct TcProblem {
+  const float *A;    // (M, K) column-major, ld = M
+  float *C;          // (M, N) column-major, ld = M
+  const float *fac;  // optional (M/2, N) real factor
+};
+
+enum { TC_EPI_STORE = 0, TC_EPI_SHIFT = 1, TC_EPI_SHIFT_FAC = 2 };
+
+// scratch: caller-provided device memory for the split A operand,
+// tc_scratch_bytes(M, K, count) bytes
+int tc_gemm_launch(const TcProblem *p, int count, int M, int N, int K, const TcOperand &B, int epi,
+                   const float2 *shift, void *scratch, int64_t scratch_bytes, cudaStream_t st);
+int64_t tc_scratch_bytes(int64_t M, int64_t K, int64_t count);
+
+// Host view of a prepared operator set (chm_sp_ops) as per-mode operands.
+TcMatrices tc_matrices(const chm_sp_ops *ops);
+
+}  // namespace chm

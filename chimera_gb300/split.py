@@ -1,0 +1,430 @@
+"""Split-precision form of the PIC step (``SplitRun``).
+
+The precision pattern of the GB300 build: particles in FP32 with the x
+position stored as an int32 cell index plus an FP32 offset, complex64
+fields, the DHT / mode-coupling products on the tcgen05 tensor cores as
+3-term split-BF16 products with FP32 accumulation.  FP64 is kept for the
+operator build (Bessel-zero DHT matrices, PSATD coefficients), for the
+running window origin ``leftX`` and for the initial half step.
+
+``SplitRun(SimComps)`` takes the same components as ``ChimeraRun``; it first
+builds the FP64 ``ChimeraRun`` (which performs the reference's initial half
+step), converts its state, and then advances every ``make_step(istep)`` with
+the split kernels.  ``to_fp64()`` writes the state back into the solver's and
+species' FP64 ``Data`` for diagnostics.
+
+Supported: plain (non-envelope) solver, SpaceCharge, StillAsBackground,
+NoPoissonCorrection, Still species, moving window with AbsorbLayer /
+AddPlasma / IonsOnTop / Staged.  Not in this form (raises): the envelope
+(KxShift) solver, devices, StaticKick.  Deposits follow the serial
+``dep_curr`` / ``dep_dens`` semantics (the chunked variants only differ by
+the dropped x-node-0 contributions of chunk 0 and by summation order).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import fimera as chimera
+from .chimera_main import ChimeraRun
+
+
+class SpOps(C.Structure):
+    _fields_ = [("K", C.c_int32), ("N", C.c_int32), ("nmodes", C.c_int32), ("pad", C.c_int32),
+                ("f32", C.c_void_p), ("bf16", C.c_void_p * 3)]
+
+
+def _prepare_ops(mats: np.ndarray, device) -> tuple:
+    """FP64 (K, N, nmodes) Fortran-ordered matrices -> prepared operator set."""
+    K, N, nm = mats.shape
+    d = torch.from_numpy(np.asfortranarray(mats, dtype=np.float64)).to(device)
+    buf = torch.empty(_lib.query("chm_sp_ops_bytes", K, N, nm), dtype=torch.uint8, device=device)
+    ops = SpOps()
+    _lib.call("chm_sp_prepare_ops", C.addressof(ops), d.data_ptr(), K, N, nm, buf.data_ptr(),
+              buf.numel(), torch.cuda.current_stream().cuda_stream)
+    return ops, buf, d
+
+
+def _c64(t: torch.Tensor) -> torch.Tensor:
+    """complex128 Fortran tensor -> complex64 Fortran tensor."""
+    out = chimera.fortran_empty(tuple(t.shape), dtype=torch.complex64, device=t.device)
+    out.copy_(t)
+    return out
+
+
+def _f32(a, device) -> torch.Tensor:
+    arr = np.asfortranarray(np.asarray(a), dtype=np.float32)
+    return torch.from_numpy(arr).to(device)
+
+
+class _SpParticles:
+    """Split-layout SoA buffers of one species (capacity-allocated)."""
+
+    NAMES = ("ix", "fx", "y", "z", "px", "py", "pz", "w")
+
+    def __init__(self, device, cap):
+        self.device = device
+        self.cap = 0
+        self.n = 0
+        self.buf = {}
+        self.reserve(cap)
+
+    def reserve(self, cap):
+        cap = int(max(cap, 1024))
+        if cap <= self.cap:
+            return
+        new = {k: torch.zeros(cap, dtype=torch.int32 if k == "ix" else torch.float32,
+                              device=self.device) for k in self.NAMES}
+        for k in self.NAMES:
+            if self.n:
+                new[k][: self.n].copy_(self.buf[k][: self.n])
+        self.buf, self.cap = new, cap
+
+    def ptrs(self):
+        return [self.buf[k].data_ptr() for k in self.NAMES]
+
+    def append_f64(self, coords, momenta, weights, X0, dx):
+        m = int(coords.shape[-1])
+        if m == 0:
+            return
+        if self.n + m > self.cap:
+            self.reserve(max(self.n + m, int(1.5 * self.cap)))
+        dev = self.device
+        tx = coords if isinstance(coords, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(coords, dtype=np.float64))
+        tp = momenta if isinstance(momenta, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(momenta, dtype=np.float64))
+        tw = weights if isinstance(weights, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(weights, dtype=np.float64))
+        if tx.device.type != "cuda":
+            chimera.io_bytes["h2d"] += (tx.numel() + tp.numel() + tw.numel()) * 8
+        tx, tp, tw = (t.to(dev, torch.float64) for t in (tx, tp, tw))
+        _lib.call("chm_sp_from_f64", *self.ptrs(), self.n, tx.data_ptr(), tx.stride(0),
+                  tx.stride(1), tp.data_ptr(), tp.stride(0), tp.stride(1), tw.data_ptr(),
+                  tw.stride(0), float(X0), float(dx), m, _stream())
+        self.n += m
+
+    def keep(self, flags: torch.Tensor):
+        """Stable compaction to the particles with flag 1."""
+        idx = torch.nonzero(flags[: self.n], as_tuple=False).flatten()
+        n = int(idx.numel())
+        chimera.io_bytes["d2h"] += 8
+        for k in self.NAMES:
+            self.buf[k][:n] = self.buf[k][: self.n][idx]
+        self.n = n
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+class SplitRun:
+    """Precision form of ``ChimeraRun`` (same SimComps, same make_step)."""
+
+    def __init__(self, SimComps, fp64_run: ChimeraRun | None = None):
+        self.fp = fp64_run if fp64_run is not None else ChimeraRun(SimComps)
+        if len(self.fp.Solvers) != 1:
+            raise NotImplementedError("the split form runs one solver")
+        self.solver = S = self.fp.Solvers[0]
+        A = S.Args
+        feats = A["Features"]
+        if "KxShift" in A or "StaticKick" in feats:
+            raise NotImplementedError("the split form covers the plain (non-envelope) solver")
+        for sp in self.fp.Particles:
+            if sp.Devices:
+                raise NotImplementedError("external-field devices are not in the split form")
+        dev = self.device = S.device
+        self.space_charge = "SpaceCharge" in feats
+        self.poisson = "NoPoissonCorrection" not in feats
+        self.nx, self.nr, self.nkr, self.nm = A["Nx"], A["Nr"], A["Nkr"], A["Mtot"]
+        self.dx, self.dt = A["dx"], A["TimeStep"]
+        self.X0 = float(A["Xgrid"][0])  # fixed origin of the particle cell index
+        # operators (FP64 host build -> FP32 copy + split BF16)
+        self._keep = []
+        self.ops = {}
+        for name, key in (("InCurr", "InCurr"), ("Out", "Out"), ("Dp", "DpS2S"), ("Dm", "DmS2S")):
+            ops, buf, d = _prepare_ops(A[key], dev)
+            self.ops[name] = ops
+            self._keep += [buf, d]
+        self.kx64 = S.dev["kx"]
+        self.kx32 = self.kx64.to(torch.float32)
+        self.depfact = _f32(A["DepFact"], dev)
+        self.pf = _f32(A["PoissFact"], dev)
+        CE, CG = S.Data["PSATD_E"], S.Data["PSATD_G"]
+        if CE.is_complex():
+            raise NotImplementedError("complex PSATD coefficients (envelope solver)")
+        self.nterm = CE.shape[-1]
+        self.c1 = CE.to(torch.float32)
+        self.c2 = CG.to(torch.float32)
+        if not chimera.is_fortran(self.c1):
+            self.c1 = chimera.fortran_empty(tuple(CE.shape), torch.float32, dev)
+            self.c1.copy_(CE)
+            self.c2 = chimera.fortran_empty(tuple(CG.shape), torch.float32, dev)
+            self.c2.copy_(CG)
+        # fields
+        D = S.Data
+        fb = (self.nx, self.nkr, self.nm)
+        sp = (self.nx, self.nr, self.nm)
+        z = lambda shape: chimera.fortran_zeros(shape, torch.complex64, dev)  # noqa: E731
+        self.EG = _c64(D["EG_fb"])
+        self.Jfb = z(fb + (3,))
+        self.Bfb = z(fb + (3,))
+        self.EB = z(sp + (6,))
+        if self.space_charge:
+            self.Rfb = z(fb)
+            self.gprv = _c64(D["gradRho_fb_prv"])
+            self.gnxt = _c64(D["gradRho_fb_nxt"])
+        n_grid = self.nx * self.nr * self.nm
+        self.accJ = torch.zeros(n_grid * 3 * 2, dtype=torch.int64, device=dev)
+        self.accR = torch.zeros(n_grid * 2, dtype=torch.int64, device=dev)
+        self.accBG = torch.zeros(n_grid * 2, dtype=torch.int64, device=dev)
+        self.ws = torch.empty(_lib.query("chm_sp_fb_ws_bytes", self.nx, self.nr, self.nkr, self.nm),
+                              dtype=torch.uint8, device=dev)
+        self.scale_ws = torch.empty(_lib.query("chm_sp_scale_ws_bytes"), dtype=torch.uint8,
+                                    device=dev)
+        # particles
+        self.parts = []
+        for spc in self.fp.Particles:
+            P = _SpParticles(dev, spc.num_particles)
+            d = spc.Data
+            P.append_f64(d["coords"], d["momenta"], d["weights"], self.X0, self.dx)
+            self.parts.append(P)
+        self.scaleJ = torch.zeros(2, dtype=torch.float64, device=dev)
+        self.scaleR = torch.zeros(2, dtype=torch.float64, device=dev)
+        self.scaleBG = torch.zeros(2, dtype=torch.float64, device=dev)
+        self._scales_valid = False
+        # the background density is deposited on window moves
+        # (chimera_main.py:277-284); it starts empty, as the reference's
+        self.have_bg = False
+
+    # ------------------------------------------------------------------
+    def _moving(self):
+        return [(spc, P) for spc, P in zip(self.fp.Particles, self.parts)
+                if "Still" not in spc.Args["Features"]]
+
+    def _still(self):
+        return [(spc, P) for spc, P in zip(self.fp.Particles, self.parts)
+                if "Still" in spc.Args["Features"]]
+
+    def _win(self):
+        """Window origin leftX = X0 + (k + f) dx, in FP64 on the host."""
+        s = (float(self.solver.Args["leftX"]) - self.X0) / self.dx
+        k = int(np.floor(s))
+        return k, float(s - k)
+
+    def _refresh_scales(self):
+        """Global deposit scales from sum |w| (recomputed when particles change)."""
+        st = _stream()
+        mov = self._moving()
+        # one species deposits into each accumulator in the benchmark; with
+        # several, the largest bound times the species count is used
+        for target, group in ((self.scaleJ, mov), (self.scaleR, mov), (self.scaleBG, self._still())):
+            if not group:
+                target.fill_(1.0)
+                continue
+            vals = []
+            for spc, P in group:
+                tmp = torch.empty(2, dtype=torch.float64, device=self.device)
+                _lib.call("chm_sp_weight_scale", tmp.data_ptr(), P.buf["w"].data_ptr(), P.n,
+                          self.scale_ws.data_ptr(), self.scale_ws.numel(), st)
+                vals.append(tmp)
+            if len(vals) == 1:
+                target.copy_(vals[0])
+            else:
+                B = torch.stack([v[1] for v in vals]).sum()
+                e = torch.ceil(torch.log2(B))
+                target[0] = torch.pow(2.0, 61.0 - e)
+                target[1] = B
+        self._scales_valid = True
+
+    def _deposit(self, P, push, accJ, accR, scaleJ, scaleR):
+        k, f = self._win()
+        _lib.call("chm_sp_push_deposit", *P.ptrs(), P.n, k, f, 1.0 / self.dx,
+                  float(self.solver.Args["dr_inv"]), float(self.dt), self.nx, self.nr, self.nm,
+                  int(push), accJ.data_ptr() if accJ is not None else None,
+                  scaleJ.data_ptr() if scaleJ is not None else None,
+                  accR.data_ptr() if accR is not None else None,
+                  scaleR.data_ptr() if scaleR is not None else None, _stream())
+
+    def _deposit_background(self):
+        if not self._scales_valid:
+            self._refresh_scales()
+        self.accBG.zero_()
+        for spc, P in self._still():
+            self._deposit(P, False, None, self.accBG, None, self.scaleBG)
+        self.have_bg = bool(self._still())
+
+    def _fb_in(self, out, acc, scale, acc2, scale2, ncomp):
+        A = self.solver.Args
+        _lib.call("chm_sp_fb_in_acc", out.data_ptr(), acc.data_ptr(), scale.data_ptr(),
+                  acc2.data_ptr() if acc2 is not None else None,
+                  scale2.data_ptr() if scale2 is not None else None, float(A["leftX"]),
+                  self.kx64.data_ptr(), C.addressof(self.ops["InCurr"]), self.depfact.data_ptr(),
+                  self.nx, self.nr, self.nkr, self.nm, ncomp, self.ws.data_ptr(), self.ws.numel(),
+                  _stream())
+
+    # ------------------------------------------------------------------
+    def make_step(self, istep):
+        """chimera_main.py:82-92 in the split precision."""
+        fp = self.fp
+        A = self.solver.Args
+        st = _stream()
+        ws, wsb = self.ws.data_ptr(), self.ws.numel()
+        staged_move = False
+        # window, stage 1 (chimera_main.py:292-302)
+        for wind in fp.MovingFrames:
+            if istep < wind["TimeActive"][0] or istep > wind["TimeActive"][1]:
+                continue
+            if np.mod(istep - wind["TimeActive"][0], wind["Steps"]) != 0:
+                continue
+            if "Staged" in wind["Features"]:
+                staged_move = True
+            if wind.get("AbsorbLayer", 0) > 0:
+                prof = A.get("_damp32")
+                if prof is None:
+                    prof = A["_damp32"] = _f32(A["damp_profile"].cpu().numpy()
+                                               if isinstance(A["damp_profile"], torch.Tensor)
+                                               else A["damp_profile"], self.device)
+                _lib.call("chm_sp_fb_filtr", self.EG.data_ptr(), float(A["leftX"]),
+                          self.kx64.data_ptr(), prof.data_ptr(), prof.numel(), 0, self.nx,
+                          self.nkr, self.nm, 6, ws, wsb, st)
+            fp.move_frame(wind)
+            if "AddPlasma" in wind:
+                self._add_plasma(wind)
+            if "AbsorbLayer" in wind:
+                self._absorb(wind)
+            if self.space_charge and "BckGrndRho" in self.solver.Data:
+                self._deposit_background()
+            # the reference's dep_dens here (postframe_corr) is overwritten by
+            # project_density before any use; it is not repeated
+        if not self._scales_valid:
+            self._refresh_scales()
+        # push_coords + J (half step) [+ rho (new position), fused unless a
+        # staged frame moves between the two deposits]
+        self.accJ.zero_()
+        fuse_rho = self.space_charge and not staged_move
+        if self.space_charge:
+            self.accR.zero_()
+        for spc, P in self._moving():
+            self._deposit(P, True, self.accJ, self.accR if fuse_rho else None, self.scaleJ,
+                          self.scaleR if fuse_rho else None)
+        if "NoCurrent" in A["Features"]:
+            self.Jfb.zero_()
+        else:
+            self._fb_in(self.Jfb, self.accJ, self.scaleJ, None, None, 3)
+        # window, stage 2
+        for wind in fp.MovingFrames:
+            if istep < wind["TimeActive"][0] or istep > wind["TimeActive"][1]:
+                continue
+            if np.mod(istep - wind["TimeActive"][0], wind["Steps"]) != 0:
+                continue
+            if "Staged" in wind["Features"]:
+                fp.move_frame(wind)
+        # density
+        if self.space_charge:
+            if not fuse_rho:
+                for spc, P in self._moving():
+                    self._deposit(P, False, None, self.accR, None, self.scaleR)
+            self.gprv, self.gnxt = self.gnxt, self.gprv
+            bg = self.accBG if self.have_bg else None
+            self._fb_in(self.Rfb, self.accR, self.scaleR, bg, self.scaleBG if bg is not None else None,
+                        1)
+            _lib.call("chm_sp_fb_grad", self.gnxt.data_ptr(), self.Rfb.data_ptr(),
+                      C.addressof(self.ops["Dp"]), C.addressof(self.ops["Dm"]),
+                      self.kx32.data_ptr(), self.nx, self.nkr, self.nm, ws, wsb, st)
+        # fields
+        if self.poisson:
+            _lib.call("chm_sp_poisson", self.Jfb.data_ptr(),
+                      self.gprv.data_ptr() if self.space_charge else None,
+                      self.gnxt.data_ptr() if self.space_charge else None, self.pf.data_ptr(),
+                      float(A["dt_inv"]), C.addressof(self.ops["Dp"]), C.addressof(self.ops["Dm"]),
+                      self.kx32.data_ptr(), self.nx, self.nkr, self.nm, 3, int(self.space_charge),
+                      ws, wsb, st)
+        P_ = self.nx * self.nkr * self.nm
+        _lib.call("chm_sp_psatd", self.EG.data_ptr(), self.Jfb.data_ptr(),
+                  self.gprv.data_ptr() if self.space_charge else None,
+                  self.gnxt.data_ptr() if self.space_charge else None, self.c1.data_ptr(),
+                  self.c2.data_ptr(), int(self.nterm), P_, st)
+        self._project_fields_and_push()
+
+    def _project_fields_and_push(self):
+        A = self.solver.Args
+        st = _stream()
+        ws, wsb = self.ws.data_ptr(), self.ws.numel()
+        if "NoPush" in A["Features"]:
+            self.EB.zero_()
+            return
+        G = self.EG[:, :, :, 3:]
+        _lib.call("chm_sp_rot_b", self.Bfb.data_ptr(), G.data_ptr(), self.pf.data_ptr(),
+                  C.addressof(self.ops["Dp"]), C.addressof(self.ops["Dm"]), self.kx32.data_ptr(),
+                  self.nx, self.nkr, self.nm, ws, wsb, st)
+        _lib.call("chm_sp_fb_eb_out", self.EB.data_ptr(), self.EG.data_ptr(), self.Bfb.data_ptr(),
+                  float(A["leftX"]), self.kx64.data_ptr(), C.addressof(self.ops["Out"]), self.nx,
+                  self.nr, self.nkr, self.nm, ws, wsb, st)
+        k, f = self._win()
+        for spc, P in self._moving():
+            dtq = spc.Args["push_fact"] * spc.Args["TimeStep"]
+            _lib.call("chm_sp_gather_push", *P.ptrs(), P.n, k, f, float(A["dr_inv"]),
+                      self.EB.data_ptr(), self.nx, self.nr, self.nm, float(dtq), st)
+
+    def _add_plasma(self, wind):
+        fp = self.fp
+        xsteps = int(wind["shiftX"] / wind["TimeStep"]) + 1
+        idx = {id(s): i for i, s in enumerate(fp.Particles)}
+        if "IonsOnTop" in wind["Features"]:
+            s1, s2 = fp.Particles[:2]
+            parts = s1.gen_parts(Xsteps=xsteps, ProfileFunc=wind["AddPlasma"])
+            self.parts[idx[id(s1)]].append_f64(*parts, self.X0, self.dx)
+            parts[-1] = parts[-1] * -1
+            self.parts[idx[id(s2)]].append_f64(*parts, self.X0, self.dx)
+        else:
+            for s in fp.Particles:
+                self.parts[idx[id(s)]].append_f64(
+                    *s.gen_parts(Xsteps=xsteps, ProfileFunc=wind["AddPlasma"]), self.X0, self.dx)
+        self._scales_valid = False
+
+    def _absorb(self, wind):
+        """species.py:351-398 absorption (SimDom test) on the split layout."""
+        for spc, P in zip(self.fp.Particles, self.parts):
+            if P.n == 0:
+                continue
+            a = spc.Args
+            k, f = self._win()
+            # species grid box in window cells
+            xmin = (a["leftX"] + wind["AbsorbLayer"] * a["dx"] - self.solver.Args["leftX"]) / self.dx
+            xmax = (a["rightX"] - self.solver.Args["leftX"]) / self.dx
+            flags = torch.empty(P.n, dtype=torch.int32, device=self.device)
+            _lib.call("chm_sp_keep_flags", P.buf["ix"].data_ptr(), P.buf["fx"].data_ptr(),
+                      P.buf["y"].data_ptr(), P.buf["z"].data_ptr(), P.n, k, f, float(xmin),
+                      float(xmax), float(a["upperR"] ** 2), flags.data_ptr(), _stream())
+            P.keep(flags)
+        self._scales_valid = False
+
+    # ------------------------------------------------------------------
+    @property
+    def num_moving(self) -> int:
+        return sum(P.n for _, P in self._moving())
+
+    def to_fp64(self):
+        """Write the split state into the FP64 Data of the solver and species."""
+        D = self.solver.Data
+        D["EG_fb"].copy_(self.EG)
+        D["EB"].copy_(self.EB)
+        D["J_fb"].copy_(self.Jfb)
+        D["B_fb"].copy_(self.Bfb)
+        if self.space_charge:
+            D["Rho_fb"].copy_(self.Rfb)
+            D["gradRho_fb_nxt"].copy_(self.gnxt)
+            D["gradRho_fb_prv"].copy_(self.gprv)
+        for spc, P in zip(self.fp.Particles, self.parts):
+            spc.store.resize(P.n)
+            spc._sync()
+            d = spc.Data
+            _lib.call("chm_sp_to_f64", *P.ptrs(), P.n, d["coords"].data_ptr(), d["coords"].stride(0),
+                      d["coords"].stride(1), d["momenta"].data_ptr(), d["momenta"].stride(0),
+                      d["momenta"].stride(1), d["weights"].data_ptr(), d["weights"].stride(0),
+                      self.X0, self.dx, _stream())
+        return self

@@ -365,6 +365,114 @@ int chm_align_data(double *dst, int64_t d_cs, int64_t d_ps, const double *src,
                    int64_t s_cs, int64_t s_ps, int64_t ncomp,
                    const int64_t *idx, int64_t n, void *stream);
 
+/* ======================================================================== */
+/* Split-precision form (spec precision pattern; no counterpart entry  */
+/* point in the reference): FP32 particles stored as int32 cell index +      */
+/* FP32 offset, complex64 fields, DHT / coupling products on the tensor      */
+/* cores as 3-term split-BF16 with FP32 accumulation.  FP64 stays in the     */
+/* operator build and the window origin.                                     */
+/* ======================================================================== */
+
+/* A prepared per-mode operator set (DHT In/Out or DpS2S/DmS2S): FP32 copy
+ * and split-BF16 terms in device memory owned by the caller. */
+typedef struct {
+  int32_t K, N, nmodes, pad;
+  const float *f32;       /* (K, N, nmodes) column-major */
+  const void *bf16[3];    /* split terms, tensor-core operand layout */
+} chm_sp_ops;
+
+/* Bytes of device memory chm_sp_prepare_ops needs for (K, N, nmodes). */
+int64_t chm_sp_ops_bytes(int64_t K, int64_t N, int64_t nmodes);
+/* Convert FP64 matrices mats(K, N, nmodes) (device) into `buf`, filling
+ * *ops (host struct).  Used once per run (solvers.py:717-759 operators). */
+int chm_sp_prepare_ops(chm_sp_ops *ops, const double *mats, int64_t K, int64_t N,
+                       int64_t nmodes, void *buf, int64_t buf_bytes, void *stream);
+
+/* Deterministic global deposit scale: scale2[0] = 2^(61 - ceil(log2 B)),
+ * scale2[1] = B = sum |w| (device doubles). */
+int64_t chm_sp_scale_ws_bytes(void);
+int chm_sp_weight_scale(double *scale2, const float *w, int64_t n, void *ws,
+                        int64_t ws_bytes, void *stream);
+
+/* push_coords + current deposit at the half step + charge deposit at the
+ * new position, fused (particle_tools.f90:58-82, grid_deps.f90:18-147).
+ * Particles: ix, fx, y, z, px, py, pz, w (n).  accJ (nx,nr,nm,3) and accR
+ * (nx,nr,nm) are int64 {re, im} accumulators (either may be NULL) at the
+ * scales scaleJ / scaleR.  win_k, win_f: window origin in cells.  push=0
+ * deposits charge without moving (Still species). */
+int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px,
+                        float *py, float *pz, float *w, int64_t n, int win_k,
+                        float win_f, float dx_inv, float dr_inv, float dt,
+                        int nx, int nr, int nm, int push, uint64_t *accJ,
+                        const double *scaleJ, uint64_t *accR,
+                        const double *scaleR, void *stream);
+
+/* proj_fld + push_velocs fused (grid_deps.f90:149-217,
+ * particle_tools.f90:18-56): gather from the complex64 EB grid and Boris. */
+int chm_sp_gather_push(int32_t *ix, float *fx, float *y, float *z, float *px,
+                       float *py, float *pz, float *w, int64_t n, int win_k,
+                       float win_f, float dr_inv, const void *eb_c64, int nx,
+                       int nr, int nm, float dtq, void *stream);
+
+/* FP64 (3,n)/(n) particle arrays <-> split layout (offset = first slot). */
+int chm_sp_from_f64(int32_t *ix, float *fx, float *y, float *z, float *px,
+                    float *py, float *pz, float *w, int64_t offset,
+                    const double *coord, int64_t x_cs, int64_t x_ps,
+                    const double *momenta, int64_t p_cs, int64_t p_ps,
+                    const double *wghts, int64_t w_ps, double X0, double dx,
+                    int64_t n, void *stream);
+int chm_sp_to_f64(const int32_t *ix, const float *fx, const float *y,
+                  const float *z, const float *px, const float *py,
+                  const float *pz, const float *w, int64_t n, double *coord,
+                  int64_t x_cs, int64_t x_ps, double *momenta, int64_t p_cs,
+                  int64_t p_ps, double *wghts, int64_t w_ps, double X0,
+                  double dx, void *stream);
+/* keep flags of the absorbing boundary (species.py:351-398 SimDom test). */
+int chm_sp_keep_flags(const int32_t *ix, const float *fx, const float *y,
+                      const float *z, int64_t n, int win_k, float win_f,
+                      float xmin_cells, float xmax_cells, float r2max,
+                      int32_t *flag, void *stream);
+
+/* Spectral stage on complex64 (nx, nkr, nm, comps) planes. */
+int64_t chm_sp_fb_ws_bytes(int64_t nx, int64_t nr, int64_t nkr, int64_t nm);
+int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale,
+                     const int64_t *acc2, const double *scale2, double leftX,
+                     const double *kx, const void *In_ops, const float *fact,
+                     int64_t nx, int64_t nr, int64_t nkr, int64_t nm,
+                     int64_t ncomp, void *ws, int64_t ws_bytes, void *stream);
+int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64,
+                     double leftX, const double *kx, const void *Out_ops,
+                     int64_t nx, int64_t nr, int64_t nkr, int64_t nm, void *ws,
+                     int64_t ws_bytes, void *stream);
+int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx,
+                    const float *filtr, int64_t nxfilt, int modefilt,
+                    int64_t nx, int64_t nkr, int64_t nm, int64_t ncomp,
+                    void *ws, int64_t ws_bytes, void *stream);
+int chm_sp_fb_grad(void *out_c64, const void *scl_c64, const void *Dp_ops,
+                   const void *Dm_ops, const float *kx, int64_t nx,
+                   int64_t nkr, int64_t nm, void *ws, int64_t ws_bytes,
+                   void *stream);
+int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64,
+                   const float *pf, float dt_inv, const void *Dp_ops,
+                   const void *Dm_ops, const float *kx, int64_t nx,
+                   int64_t nkr, int64_t nm, int iters, int space_charge,
+                   void *ws, int64_t ws_bytes, void *stream);
+int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf,
+                 const void *Dp_ops, const void *Dm_ops, const float *kx,
+                 int64_t nx, int64_t nkr, int64_t nm, void *ws,
+                 int64_t ws_bytes, void *stream);
+int chm_sp_psatd(void *eg_c64, const void *j_c64, const void *gprv_c64,
+                 const void *gnxt_c64, const float *c1, const float *c2,
+                 int nterm, int64_t P, void *stream);
+/* Dense product C(M,N) = A(M,K) B(K,N) with B a prepared operator mode, on
+ * the tensor cores (tcgen05, split-BF16) or, with engine = 0, on the FP32
+ * SIMT path; for tests and tuning. */
+int64_t chm_sp_gemm_ws_bytes(int64_t M, int64_t K, int64_t count);
+int chm_sp_gemm(float *C, const float *A, const chm_sp_ops *ops, int64_t mode,
+                int64_t M, int engine, void *ws, int64_t ws_bytes, void *stream);
+/* Nonzero if a tensor-core GEMM CTA hit a wait limit since load. */
+int chm_sp_umma_status(void);
+
 #ifdef __cplusplus
 }
 #endif
