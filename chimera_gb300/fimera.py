@@ -409,10 +409,13 @@ def _fb_in(vec_fb, vec, leftX, kx, In, ncomp, fact=None):
     if tuple(out.shape[:3]) != (nx, nkr, nm) or In_.shape[0] != nr - 1:
         raise ChimeraError("fb_in: inconsistent shapes")
     kx_ = to_device(kx, torch.float64, v.device)
-    fac = to_device(fact, torch.float64, v.device).data_ptr() if fact is not None else None
+    # device copies stay bound until the call is enqueued (a freed temporary
+    # could be handed to the workspace allocation below)
+    fac_t = to_device(fact, torch.float64, v.device) if fact is not None else None
     ws = workspace(_lib.query("chm_fb_ws_bytes", nx, nr, nkr, nm, ncomp))
     _lib.call("chm_fb_in", out.data_ptr(), v.data_ptr(), float(leftX), kx_.data_ptr(),
-              In_.data_ptr(), fac, nx, nr, nkr, nm, ncomp, ws.data_ptr(), ws.numel(), _stream())
+              In_.data_ptr(), fac_t.data_ptr() if fac_t is not None else None, nx, nr, nkr, nm,
+              ncomp, ws.data_ptr(), ws.numel(), _stream())
     return vec_fb
 
 

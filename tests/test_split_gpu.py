@@ -82,9 +82,12 @@ def test_split_spectral_operators_match_fp64(mods, lpa):
     pf = g["PoissFact"]
     pf32 = _c(pf.astype(np.float32), torch)
     # fb_grad
+    # (every device input is bound to a name: a temporary's memory could be
+    # handed to the next allocation before the asynchronous kernel reads it)
     s = _rand((nx, nkr, nm), 1).astype(np.complex64)
+    sd = _c(s, torch)
     out = fm.fortran_zeros((nx, nkr, nm, 3), torch.complex64)
-    _lib.call("chm_sp_fb_grad", out.data_ptr(), _c(s, torch).data_ptr(), C.addressof(o["Dp"][0]),
+    _lib.call("chm_sp_fb_grad", out.data_ptr(), sd.data_ptr(), C.addressof(o["Dp"][0]),
               C.addressof(o["Dm"][0]), kx32.data_ptr(), nx, nkr, nm, ws.data_ptr(), ws.numel(), st)
     ref = fm.fb_grad(fm.fortran_zeros((nx, nkr, nm, 3)), _c(s.astype(np.complex128), torch),
                      g["DpS2S"], g["DmS2S"], g["kx"])
@@ -94,7 +97,8 @@ def test_split_spectral_operators_match_fp64(mods, lpa):
     gp = (0.1 * _rand((nx, nkr, nm, 3), 3)).astype(np.complex64)
     gn = (0.1 * _rand((nx, nkr, nm, 3), 4)).astype(np.complex64)
     Js = _c(J, torch)
-    _lib.call("chm_sp_poisson", Js.data_ptr(), _c(gp, torch).data_ptr(), _c(gn, torch).data_ptr(),
+    gpd, gnd = _c(gp, torch), _c(gn, torch)
+    _lib.call("chm_sp_poisson", Js.data_ptr(), gpd.data_ptr(), gnd.data_ptr(),
               pf32.data_ptr(), 10.0, C.addressof(o["Dp"][0]), C.addressof(o["Dm"][0]),
               kx32.data_ptr(), nx, nkr, nm, 3, 1, ws.data_ptr(), ws.numel(), st)
     Jd = _c(J.astype(np.complex128), torch)
@@ -107,7 +111,8 @@ def test_split_spectral_operators_match_fp64(mods, lpa):
     # B = rot(G) PoissFact
     G = _rand((nx, nkr, nm, 3), 5).astype(np.complex64)
     Bs = fm.fortran_zeros((nx, nkr, nm, 3), torch.complex64)
-    _lib.call("chm_sp_rot_b", Bs.data_ptr(), _c(G, torch).data_ptr(), pf32.data_ptr(),
+    Gd = _c(G, torch)
+    _lib.call("chm_sp_rot_b", Bs.data_ptr(), Gd.data_ptr(), pf32.data_ptr(),
               C.addressof(o["Dp"][0]), C.addressof(o["Dm"][0]), kx32.data_ptr(), nx, nkr, nm,
               ws.data_ptr(), ws.numel(), st)
     Bd = fm.fb_rot(fm.fortran_zeros((nx, nkr, nm, 3)), _c(G.astype(np.complex128), torch),
@@ -119,7 +124,8 @@ def test_split_spectral_operators_match_fp64(mods, lpa):
     Bq = _rand((nx, nkr, nm, 3), 7).astype(np.complex64)
     EBs = fm.fortran_zeros((nx, nr, nm, 6), torch.complex64)
     leftX = float(g["leftX"]) + 3.3
-    _lib.call("chm_sp_fb_eb_out", EBs.data_ptr(), _c(E, torch).data_ptr(), _c(Bq, torch).data_ptr(),
+    Ed, Bqd = _c(E, torch), _c(Bq, torch)
+    _lib.call("chm_sp_fb_eb_out", EBs.data_ptr(), Ed.data_ptr(), Bqd.data_ptr(),
               leftX, kx64.data_ptr(), C.addressof(o["Out"][0]), nx, nr, nkr, nm, ws.data_ptr(),
               ws.numel(), st)
     EBd = fm.fb_eb_out(fm.fortran_zeros((nx, nr, nm, 6)), _c(E.astype(np.complex128), torch),
