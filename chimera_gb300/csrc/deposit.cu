@@ -485,3 +485,76 @@ int chm_dep_dens_env_chnk(const double *coord, int64_t x_cs, int64_t x_ps, const
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free current deposit
+//
+// Some callers of this library cannot allocate device memory: a host code
+// that reaches the GPU only through this C ABI (an FFI binding with no CUDA
+// allocator of its own), or a loop whose device memory budget is fixed at
+// start-up and that may not call cudaMalloc mid-run (cudaMalloc can
+// synchronise the device and stall other streams).  For them,
+// chm_dep_curr_noalloc runs the same deposit as chm_dep_curr with its scratch
+// (the 64-bit accumulator, the weight partial sums and the scale) in the
+// static device array below instead of a caller-provided workspace.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr int64_t kNoAllocScratchBytes = 16LL << 20;  // 16 MiB, held per GPU until exit
+static __device__ __align__(256) unsigned char g_dep_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[128] = {};  // device address of g_dep_scratch, per device
+
+// Resolves (once per device, with that device current) the device address of
+// the static scratch; host code cannot pass g_dep_scratch itself, whose name
+// on the host is only a stand-in for the symbol.
+int noalloc_scratch(void **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 128) {
+    set_error("dep_curr_noalloc: cudaGetDevice failed (%s)", cudaGetErrorString(e));
+    return CHM_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_dep_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("dep_curr_noalloc: cudaGetSymbolAddress failed (%s)", cudaGetErrorString(e));
+      return CHM_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return CHM_OK;
+}
+
+}  // namespace
+
+extern "C" int64_t chm_dep_noalloc_max_bytes(void) { return kNoAllocScratchBytes; }
+
+extern "C" int chm_dep_curr_noalloc(const double *coord, int64_t x_cs, int64_t x_ps,
+                                    const double *momenta, int64_t p_cs, int64_t p_ps,
+                                    const double *wghts, int64_t w_ps, chm_c128 *curr,
+                                    double leftX, const double *rgrid, double dx_inv,
+                                    double dr_inv, int64_t np, int64_t nx, int64_t nr, int64_t nm,
+                                    void *stream) {
+  const int64_t need = chm_dep_ws_bytes(nx, nr, nm, 3, np);
+  if (need > kNoAllocScratchBytes || nx <= 0 || nr <= 0 || nm <= 0) {
+    set_error("dep_curr_noalloc: a (%lld, %lld, %lld, 3) grid needs %lld bytes of scratch, more "
+              "than the %lld-byte static array; use chm_dep_curr with a workspace",
+              (long long)nx, (long long)nr, (long long)nm, (long long)need,
+              (long long)kNoAllocScratchBytes);
+    return CHM_ERR_RANGE;
+  }
+  void *scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  // deposit_common zeroes the accumulator at the start of every call
+  return deposit_common(CURR, coord, x_cs, x_ps, momenta, p_cs, p_ps, wghts, w_ps, curr, nullptr, 0,
+                        0, leftX, rgrid, dx_inv, dr_inv, 0.0, np, nx, nr, nm, scratch,
+                        kNoAllocScratchBytes, stream);
+}

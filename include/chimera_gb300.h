@@ -154,6 +154,26 @@ int chm_dep_curr(const double *coord, int64_t x_cs, int64_t x_ps,
                  double leftX, const double *rgrid, double dx_inv,
                  double dr_inv, int64_t np, int64_t nx, int64_t nr, int64_t nm,
                  void *ws, int64_t ws_bytes, void *stream);
+/* No counterpart in the reference.  The current deposit of chm_dep_curr for
+ * callers that cannot allocate device memory (an FFI host with no CUDA
+ * allocator of its own, or a loop with a device memory budget fixed at
+ * start-up that may not call cudaMalloc mid-run).  Same arguments minus the
+ * workspace: the scratch lives in a 16 MiB static device array that every
+ * GPU loading the library keeps until exit (chm_dep_noalloc_max_bytes()).
+ * Grids needing more scratch than that are rejected with CHM_ERR_RANGE.  The
+ * first call on a device resolves the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the one array, which keeps the last call's contents (the
+ * accumulator is cleared at the start of each call): calls that overlap on
+ * the GPU (concurrent streams or host threads) race on it. */
+int64_t chm_dep_noalloc_max_bytes(void);
+int chm_dep_curr_noalloc(const double *coord, int64_t x_cs, int64_t x_ps,
+                         const double *momenta, int64_t p_cs, int64_t p_ps,
+                         const double *wghts, int64_t w_ps, chm_c128 *curr,
+                         double leftX, const double *rgrid, double dx_inv,
+                         double dr_inv, int64_t np, int64_t nx, int64_t nr,
+                         int64_t nm, void *stream);
+
 /* grid_deps.f90:89-147 dep_dens(coord, wghts, dens, leftX, Rgrid, dx_inv,
  * dr_inv) */
 int chm_dep_dens(const double *coord, int64_t x_cs, int64_t x_ps,
