@@ -177,6 +177,69 @@ def load_peaks():
 FP64_PEAK_TFLOPS = 1.20
 
 
+def still_count(run, form):
+    parts = run.fp.Particles if form == "split" else run.Particles
+    return sum(p.num_particles for p in parts if "Still" in p.Args["Features"])
+
+
+# algorithmic HBM bytes per particle of the particle stages
+SPLIT_BYTES = {"push_electrons": 32 + 16,  # read ix,fx,y,z,p,w; write ix,fx,y,z
+               "deposit_still": 20,       # read ix,fx,y,z,w
+               "gather_push": 32 + 12}    # read ix,fx,y,z,p,w; write p
+FP64_BYTES = {"push_velocs": 48 + 48 + 24, "push_coords": 24 + 24 + 24 + 24,
+              "dep_curr": 24 + 24 + 8, "dep_dens": 24 + 8, "proj_fld": 24 + 8 + 48 + 48}
+GEMM_STAGES = ("chm_fb_graddiv", "chm_fb_rot", "chm_fb_grad", "chm_fb_div", "chm_fb_in",
+               "chm_fb_out", "chm_fb_eb_out", "chm_sp_poisson", "chm_sp_fb_in_acc",
+               "chm_sp_fb_eb_out", "chm_sp_rot_b", "chm_sp_fb_grad")
+
+
+def stage_roofline(form, prof, nprof, n_e, n_i, peaks, peak_kind):
+    """Roofline of the dominant stage: algorithmic work over its live
+    CUDA-event time, against the measured peak of its bound."""
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    bf16 = float(peaks.get("bf16_tflops", 1900.0))
+    rows = []
+    for name, (calls, ms, flops) in prof.items():
+        t = ms / nprof / 1e3  # seconds per step
+        if t <= 0:
+            continue
+        if name in GEMM_STAGES and flops > 0:
+            alg = flops / nprof / t / 1e12
+            if form == "split":
+                rows.append({"stage": name, "bound": "tensor", "achieved": alg, "unit": "TFLOP/s",
+                             "peak": bf16, "frac": alg / bf16, "executed_tflops": 6 * alg,
+                             "executed_frac": 6 * alg / bf16, "ms_per_step": t * 1e3})
+            else:
+                rows.append({"stage": name, "bound": "fp64", "achieved": alg, "unit": "TFLOP/s",
+                             "peak": FP64_PEAK_TFLOPS, "frac": alg / FP64_PEAK_TFLOPS,
+                             "ms_per_step": t * 1e3})
+            continue
+        nb = None
+        if name == "chm_sp_push_deposit":
+            nb = n_e * SPLIT_BYTES["push_electrons"] + n_i * SPLIT_BYTES["deposit_still"]
+        elif name == "chm_sp_gather_push":
+            nb = n_e * SPLIT_BYTES["gather_push"]
+        elif name in ("chm_push_velocs", "chm_push_coords", "chm_proj_fld"):
+            nb = n_e * FP64_BYTES[name[4:]]
+        elif name == "chm_dep_curr_chnk":
+            nb = n_e * FP64_BYTES["dep_curr"]
+        elif name == "chm_dep_dens_chnk":
+            nb = (2 * n_e + n_i) * FP64_BYTES["dep_dens"]
+        if nb is not None:
+            ach = nb / t / 1e9
+            rows.append({"stage": name, "bound": "hbm", "achieved": ach, "unit": "GB/s",
+                         "peak": hbm, "frac": ach / hbm, "ms_per_step": t * 1e3,
+                         "algorithmic_bytes_per_step": nb})
+    rows.sort(key=lambda r: -r["ms_per_step"])
+    top = dict(rows[0]) if rows else {"stage": None}
+    top["kernel"] = top.pop("stage")
+    top["traffic"] = None
+    top["peak_source"] = f"MEASURED_PEAKS.json ({peak_kind})" if top.get("bound") != "fp64" else \
+        "FP64 FMA probe on this pool (1.20 TFLOP/s)"
+    top["stages"] = rows
+    return top
+
+
 def dist_setup():
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -208,23 +271,24 @@ def max_over_ranks(world, v):
 
 
 def cpu_step_time(nsteps, warmup=0, window="none"):
-    """Wall time per step of the oracle's CPU step driver on this workload."""
+    """Wall time per step and moving particles per step of the oracle's CPU
+    step driver on this workload."""
     from oracle.step import CpuRun, CpuSpecies
     import torch
     solver, el, io, wind = build_run("cpu", window)
     # the reference initialises the laser in spectral space with the same
-    # kernels; the CPU arm takes the initial field from the same operators
-    # (zero field costs the same per step)
+    # kernels; the CPU arm starts from a zero field (same cost per step)
     solver.Data["EG_fb"] = torch.zeros(tuple(solver.Data["EG_fb"].shape), dtype=torch.complex128)
     run = CpuRun(solver, [CpuSpecies(el), CpuSpecies(io)], wind)
     for i in range(1, warmup + 1):
         run.make_step(i)
-    n_moving = run.Particles[0].n()
+    psteps = 0
     t0 = time.perf_counter()
     for i in range(warmup + 1, warmup + nsteps + 1):
         run.make_step(i)
+        psteps += run.Particles[0].n()
     dt = (time.perf_counter() - t0) / nsteps
-    return dt, n_moving
+    return dt, psteps / nsteps
 
 
 def run_reference(args):
@@ -236,13 +300,15 @@ def run_reference(args):
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     steps = max(1, min(args.steps, args.ref_max_steps))
     warm = min(args.warmup, 1)
-    t_step, n = cpu_step_time(steps, warm)
+    t_step, n = cpu_step_time(steps, warm, window="inject")
     value = n / t_step
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * t_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "particles": n, "cpu_threads": cores},
+        "config": {"workload": WORKLOAD + "_window_inject", "particles": n, "cpu_threads": cores,
+                   "window": "AbsorbLayer=64, AddPlasma, IonsOnTop, moving at c (the e2e "
+                             "workload of the gb300 arm)"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
                          "sample": f"{steps} full steps of the workload (after {warm} warm-up) "
                                    "with the oracle's C/OpenMP restatement of the reference "
@@ -305,32 +371,19 @@ def run_gb300(args):
     # stage profile of a few more steps (events around every C-ABI call)
     _lib.profile_begin()
     nprof = max(2, min(3, args.steps))
-    f0 = lib.chm_gemm_flops()
     base = args.warmup + args.steps
     for i in range(base + 1, base + nprof + 1):
         run.make_step(i)
     prof = _lib.profile_end()
-    prof_flops = lib.chm_gemm_flops() - f0
     tot = sum(v[1] for v in prof.values())
     stages = {k.replace("chm_", ""): {"calls": c / nprof, "ms_per_step": t / nprof,
-                                      "share": t / tot if tot else None}
-              for k, (c, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
-    gemm_ms = sum(t for k, (c, t) in prof.items()
-                  if k in ("chm_fb_graddiv", "chm_fb_rot", "chm_fb_grad", "chm_fb_div", "chm_fb_in",
-                           "chm_fb_out", "chm_fb_eb_out"))
+                                      "share": t / tot if tot else None,
+                                      "gemm_gflop_per_step": f / nprof / 1e9}
+              for k, (c, t, f) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
     peaks, peak_kind = load_peaks()
-    achieved = prof_flops / (gemm_ms / 1e3) / 1e12 if gemm_ms else None
-    roofline = {
-        "kernel": "dgemm_kernel (DHT + fb_math dense products, FP64 SIMT)",
-        "bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-        "frac": achieved / FP64_PEAK_TFLOPS if achieved else None,
-        "traffic": None,
-        "note": "plain FP64 form: the dense products run on GB300's FP64 pipe "
-                f"({FP64_PEAK_TFLOPS} TFLOP/s measured with an FMA probe); achieved = "
-                "algorithmic 4*nx*N*K FLOPs per product over the device time of the FB "
-                "transform / operator calls that issue them",
-        "algorithmic_gflop_per_step": gemm_flops / args.steps / 1e9,
-    }
+    roofline = stage_roofline(args.form, prof, nprof, n_moving, still_count(run, args.form),
+                              peaks, peak_kind)
+    roofline["algorithmic_gemm_gflop_per_step"] = gemm_flops / args.steps / 1e9
 
     # end to end through the public API with per-step host I/O
     e2e = None
@@ -371,15 +424,18 @@ def run_gb300(args):
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
         os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-        t_cpu, n_cpu = cpu_step_time(args.cpu_steps, 0)
+        t_cpu, n_cpu = cpu_step_time(args.cpu_steps, 0, window="inject")
         cpu = {"value": n_cpu / t_cpu, "unit": METRIC, "cores": cores, "kind": "port",
-               "sample": f"{args.cpu_steps} full step(s) of the same workload with the oracle's "
-                         "C/OpenMP restatement of the reference kernels and step loop"}
+               "sample": f"{args.cpu_steps} full step(s) of the e2e workload (window with "
+                         "injection and absorption) with the oracle's C/OpenMP restatement of "
+                         "the reference kernels and step loop"}
 
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.form == "fp64" else "f32 (bf16x3 split tensor-core GEMMs)",
+        "data": "synthetic",
         "config": {"workload": WORKLOAD, "form": args.form, "particles_moving": n_moving,
                    "particles_still": n_moving, "nx": SIZES[WORKLOAD_SIZE][0],
                    "nr": SIZES[WORKLOAD_SIZE][1] + 1, "modes": 2,
@@ -413,7 +469,7 @@ def main():
     ap.add_argument("--ref-max-steps", type=int, default=5)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--form", default="fp64", choices=["fp64", "split"],
+    ap.add_argument("--form", default="split", choices=["fp64", "split"],
                     help="fp64 = plain FP64 form; split = split-precision form")
     ap.add_argument("--size", default="cfg2", choices=sorted(SIZES),
                     help="cfg2 = the benchmark workload; small = a reduced case for profiling")

@@ -92,12 +92,14 @@ def profile_begin():
 
 
 def profile_end() -> dict:
-    """Stop recording; returns name -> (calls, total device ms)."""
+    """Stop recording; returns name -> (calls, total device ms, dense-product
+    FLOPs issued by those calls)."""
     global _prof
     import torch
     prof, _prof = _prof, None
     torch.cuda.synchronize()
-    return {k: (len(v), sum(a.elapsed_time(b) for a, b in v)) for k, v in (prof or {}).items()}
+    return {k: (len(v), sum(a.elapsed_time(b) for a, b, _ in v), sum(f for _, _, f in v))
+            for k, v in (prof or {}).items()}
 
 
 def call(name: str, *args):
@@ -107,10 +109,11 @@ def call(name: str, *args):
         import torch
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
+        f0 = lib.chm_gemm_flops()
         a.record()
         rc = getattr(lib, name)(*args)
         b.record()
-        _prof.setdefault(name, []).append((a, b))
+        _prof.setdefault(name, []).append((a, b, lib.chm_gemm_flops() - f0))
     else:
         rc = getattr(lib, name)(*args)
     if rc != 0:
