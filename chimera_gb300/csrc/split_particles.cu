@@ -10,13 +10,15 @@
 // the host and enters as (k, f): leftX = X0 + (k + f) dx, k integer, f in
 // [0, 1); the grid-relative position is (ix - k) + (fx - f).
 //
-// Deposition stays deterministic without float atomics: each block
-// accumulates its particles' contributions in 32-bit fixed point in shared
-// memory (scale 2^e_l from the block's own sum |w|), then adds the block box
-// into the global 64-bit accumulator after an exact power-of-two rescale to
-// the global scale 2^e_g.  Integer sums are order-independent, so the result
-// depends only on which particles share a block, which is fixed.
+// Deposition stays deterministic without float atomics: values are rounded
+// to the global 64-bit fixed-point quantum 2^-e (2^e = 2^(61 - ceil(log2
+// sum |w|))) and added as integers, first into a shared-memory box of the
+// block's nodes, then into the global accumulator.  Integer sums are
+// order-independent; the cell-run kernel sums the particles of a run in FP32
+// before rounding, which depends only on the (fixed) particle order.
 #include <climits>
+#include <cstdlib>
+#include <cstring>
 #include <math.h>
 
 #include "common.cuh"
@@ -28,7 +30,7 @@ namespace {
 constexpr int kSpThreads = 256;
 constexpr int kSpPerThread = 8;
 constexpr int kSpPerBlock = kSpThreads * kSpPerThread;
-constexpr int kSpBoxBytes = 64 * 1024;
+constexpr int kSpBoxBytes = 96 * 1024;  // 12288 int64 values
 
 struct SpParts {
   int32_t *ix;
@@ -63,20 +65,17 @@ __device__ __forceinline__ Loc locate(int ix, float fx, float y, float z, const 
   float fl = floorf(d);
   L.cx = ix - G.win_k + (int)fl;
   L.sx1 = d - fl;
-  float r = sqrtf(y * y + z * z);
+  // r and 1/r from one reciprocal square root (a few ulp, FP32)
+  const float r2 = y * y + z * z;
+  const float ri = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
+  const float r = r2 * ri;
   float s = r * G.dr_inv + 0.5f;
   float sf = floorf(s);
   L.cr = (int)sf;
   L.sr1 = s - sf;
   L.ok = (L.cr >= 0 && L.cr <= G.nr - 2);
-  if (r > 0.0f) {
-    float ri = 1.0f / r;
-    L.phr = y * ri;
-    L.phi = z * ri;
-  } else {
-    L.phr = 0.0f;
-    L.phi = 0.0f;
-  }
+  L.phr = y * ri;  // 0 on the axis
+  L.phi = z * ri;
   return L;
 }
 
@@ -123,8 +122,54 @@ struct PushDepArgs {
   int dep_rho;     // deposit rho at the new position
   unsigned long long *accJ;  // (nx, nr, nm, 3) x {re, im}
   unsigned long long *accR;  // (nx, nr, nm) x {re, im}
-  const double *scaleJ, *scaleR;  // global scales 2^e_g
+  const double *scaleJ, *scaleR;  // global scales 2^e
 };
+
+// Block box: 64-bit fixed-point values at the global scales, planes (J: 3 nm,
+// then rho: nm) of bnr x bnx nodes starting at (br0, bx0), {re, im}
+// interleaved.
+struct BoxGeo {
+  unsigned long long *box;
+  long long bx0, br0, bnx, bnr;
+  float sJ, sR;                  // 2^eJ, 2^eR
+  unsigned long long *gJ, *gR;   // global accumulators
+  int nx, nr, nmj;               // grid; the nmj = 3 nm J planes precede rho
+};
+
+// Adds v at node (r, x) of a plane, part im, to the box; a node outside the
+// box (the plan bounds every deposit location, so this is a guard only) goes
+// to the global accumulator directly -- both hold the same scale.
+__device__ __forceinline__ void box_put(const BoxGeo &B, long long plane, int r, int x, int im,
+                                        long long v) {
+  const long long rr = r - B.br0, xx = x - B.bx0;
+  if (rr >= 0 && rr < B.bnr && xx >= 0 && xx < B.bnx) {
+    atomicAdd(&B.box[((plane * B.bnr + rr) * B.bnx + xx) * 2 + im], (unsigned long long)v);
+    return;
+  }
+  const bool isj = plane < B.nmj;
+  const long long pl = isj ? plane : plane - B.nmj;
+  unsigned long long *acc = isj ? B.gJ : B.gR;
+  atomicAdd(&acc[2 * ((pl * B.nr + r) * B.nx + x) + im], (unsigned long long)v);
+}
+
+// Adds the block box into the global accumulators.
+__device__ void flush_box(const BoxGeo &B, long long nvals) {
+  for (long long t = threadIdx.x; t < nvals; t += blockDim.x) {
+    const unsigned long long v = B.box[t];
+    if (v == 0) continue;
+    const long long c2 = t & 1;
+    const long long b = t >> 1;
+    const long long bx = b % B.bnx;
+    const long long rest = b / B.bnx;
+    const long long br = rest % B.bnr;
+    const long long plane = rest / B.bnr;
+    const bool isj = plane < B.nmj;
+    const long long pl = isj ? plane : plane - B.nmj;
+    const i64 e = (pl * B.nr + (br + B.br0)) * B.nx + (bx + B.bx0);
+    unsigned long long *acc = isj ? B.gJ : B.gR;
+    atomicAdd(&acc[2 * e + c2], v);
+  }
+}
 
 // Particle update of push_coords (particle_tools.f90:58-82) in cell units:
 // half-step and new positions.
@@ -134,14 +179,11 @@ struct Pushed {
   float vj[3];
 };
 
-__device__ __forceinline__ Pushed push_one(const PushDepArgs &A, i64 i) {
-  const SpParts &P = A.P;
+__device__ __forceinline__ Pushed push_vals(const PushDepArgs &A, int ix, float fx, float y, float z,
+                                            float px, float py, float pz, float w) {
   Pushed o;
-  const int ix = P.ix[i];
-  const float fx = P.fx[i], y = P.y[i], z = P.z[i];
-  const float px = P.px[i], py = P.py[i], pz = P.pz[i], w = P.w[i];
-  const float g = sqrtf(1.0f + (px * px + py * py + pz * pz));
-  const float dtg = A.push ? A.dt / g : 0.0f;
+  const float ig = rsqrtf(1.0f + (px * px + py * py + pz * pz));  // 1 / gamma
+  const float dtg = A.push ? A.dt * ig : 0.0f;
   const float dxc = px * dtg * A.dx_inv;  // displacement in cells
   float xh = fx + 0.5f * dxc, xn = fx + dxc;
   float flh = floorf(xh), fln = floorf(xn);
@@ -155,121 +197,150 @@ __device__ __forceinline__ Pushed push_one(const PushDepArgs &A, i64 i) {
   o.zn = z + pz * dtg;
   // grid_deps.f90:42: particles at rest deposit no current
   const bool moving = (fabsf(px) + fabsf(py) + fabsf(pz)) != 0.0f;
-  const float wg = moving ? w / g : 0.0f;
+  const float wg = moving ? w * ig : 0.0f;
   o.vj[0] = px * wg;
   o.vj[1] = py * wg;
   o.vj[2] = pz * wg;
   return o;
 }
 
-__global__ void __launch_bounds__(kSpThreads) push_deposit_kernel(PushDepArgs A) {
-  extern __shared__ __align__(16) int box[];
-  __shared__ long long bb[4];
-  __shared__ double wred[kSpThreads / 32];
-  const i64 p0 = (i64)blockIdx.x * kSpPerBlock, p1 = min(A.P.n, p0 + (i64)kSpPerBlock);
+__device__ __forceinline__ Pushed push_one(const PushDepArgs &A, i64 i) {
+  const SpParts &P = A.P;
+  return push_vals(A, P.ix[i], P.fx[i], P.y[i], P.z[i], P.px[i], P.py[i], P.pz[i], P.w[i]);
+}
+
+// Block plan shared by both deposit kernels: the box of nodes the block's
+// deposits can touch.  Thread t reads the run p0 + 8t .. p0 + 8t + 7.  The
+// box is bounded without pushing: a particle moves less than c dt, so its
+// deposit cells lie within ceil(dt/dx) cells of its x cell and within dt of
+// its radius.
+struct BlockPlan {
+  long long bx0, br0, bnx, bnr, nvals;
+  bool use_box;
+  float sJ, sR;  // global scales 2^eJ, 2^eR
+};
+
+__device__ __forceinline__ void bound_one(int ix, float y, float z, float w, int &xlo, int &xhi,
+                                          float &r2lo, float &r2hi) {
+  if (w == 0.0f) return;
+  xlo = min(xlo, ix);
+  xhi = max(xhi, ix);
+  const float r2 = y * y + z * z;
+  r2lo = fminf(r2lo, r2);
+  r2hi = fmaxf(r2hi, r2);
+}
+
+__device__ BlockPlan plan_block(const PushDepArgs &A, i64 p0, i64 p1, bool vec, int *bb) {
   if (threadIdx.x == 0) {
-    bb[0] = LLONG_MAX;
-    bb[1] = LLONG_MIN;
-    bb[2] = LLONG_MAX;
-    bb[3] = LLONG_MIN;
+    bb[0] = INT_MAX;
+    bb[1] = INT_MIN;
+    bb[2] = INT_MAX;
+    bb[3] = INT_MIN;
   }
   __syncthreads();
-  // pass 1: box of every deposit location and the block's sum |w|
-  long long x0 = LLONG_MAX, x1 = LLONG_MIN, r0 = LLONG_MAX, r1 = LLONG_MIN;
-  double wsum = 0.0;
-  for (i64 i = p0 + threadIdx.x; i < p1; i += kSpThreads) {
-    const float w = A.P.w[i];
-    if (w == 0.0f) continue;
-    Pushed q = push_one(A, i);
-    wsum += fabs((double)w);
-    if (A.dep_j) {
-      Loc L = locate(q.ixh, q.fxh, q.yh, q.zh, A.G);
-      if (L.ok) {
-        x0 = min(x0, (long long)L.cx);
-        x1 = max(x1, (long long)L.cx + 1);
-        r0 = min(r0, (long long)L.cr);
-        r1 = max(r1, (long long)L.cr + 1);
-      }
+  const i64 r0i = p0 + (i64)threadIdx.x * (kSpPerBlock / kSpThreads);
+  const i64 r1i = min(p1, r0i + (i64)(kSpPerBlock / kSpThreads));
+  int xlo = INT_MAX, xhi = INT_MIN;
+  float r2lo = INFINITY, r2hi = -INFINITY;
+  if (vec && r1i - r0i == kSpPerBlock / kSpThreads) {
+#pragma unroll
+    for (int h = 0; h < kSpPerBlock / kSpThreads; h += 4) {
+      const int4 a = *reinterpret_cast<const int4 *>(A.P.ix + r0i + h);
+      const float4 y = *reinterpret_cast<const float4 *>(A.P.y + r0i + h);
+      const float4 z = *reinterpret_cast<const float4 *>(A.P.z + r0i + h);
+      const float4 w = *reinterpret_cast<const float4 *>(A.P.w + r0i + h);
+      bound_one(a.x, y.x, z.x, w.x, xlo, xhi, r2lo, r2hi);
+      bound_one(a.y, y.y, z.y, w.y, xlo, xhi, r2lo, r2hi);
+      bound_one(a.z, y.z, z.z, w.z, xlo, xhi, r2lo, r2hi);
+      bound_one(a.w, y.w, z.w, w.w, xlo, xhi, r2lo, r2hi);
     }
-    if (A.dep_rho) {
-      Loc L = locate(q.ixn, q.fxn, q.yn, q.zn, A.G);
-      if (L.ok) {
-        x0 = min(x0, (long long)L.cx);
-        x1 = max(x1, (long long)L.cx + 1);
-        r0 = min(r0, (long long)L.cr);
-        r1 = max(r1, (long long)L.cr + 1);
-      }
-    }
+  } else {
+    for (i64 i = r0i; i < r1i; ++i)
+      bound_one(A.P.ix[i], A.P.y[i], A.P.z[i], A.P.w[i], xlo, xhi, r2lo, r2hi);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    x0 = min(x0, __shfl_xor_sync(0xffffffffu, x0, o));
-    x1 = max(x1, __shfl_xor_sync(0xffffffffu, x1, o));
-    r0 = min(r0, __shfl_xor_sync(0xffffffffu, r0, o));
-    r1 = max(r1, __shfl_xor_sync(0xffffffffu, r1, o));
-    wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+  int x0 = INT_MAX, x1 = INT_MIN, r0 = INT_MAX, r1 = INT_MIN;
+  if (xlo <= xhi) {
+    const int D = A.push ? (int)ceilf(A.dt * A.dx_inv) : 0;
+    const float drc = A.push ? A.dt : 0.0f;
+    x0 = xlo - A.G.win_k - 1 - D;
+    x1 = xhi - A.G.win_k + 1 + D;
+    r0 = max(0, (int)floorf((sqrtf(r2lo) - drc) * A.G.dr_inv + 0.5f) - 1);
+    r1 = (int)floorf((sqrtf(r2hi) + drc) * A.G.dr_inv + 0.5f) + 2;
   }
+  x0 = __reduce_min_sync(0xffffffffu, x0);
+  x1 = __reduce_max_sync(0xffffffffu, x1);
+  r0 = __reduce_min_sync(0xffffffffu, r0);
+  r1 = __reduce_max_sync(0xffffffffu, r1);
   if ((threadIdx.x & 31) == 0) {
     atomicMin(&bb[0], x0);
     atomicMax(&bb[1], x1);
     atomicMin(&bb[2], r0);
     atomicMax(&bb[3], r1);
-    wred[threadIdx.x >> 5] = wsum;
   }
   __syncthreads();
-  double Bl = 0.0;
-  for (int k = 0; k < kSpThreads / 32; ++k) Bl += wred[k];  // fixed order
-  const long long bx0 = max(bb[0], 0LL), bx1 = min(bb[1], (long long)A.G.nx - 1);
-  const long long br0 = max(bb[2], 0LL), br1 = min(bb[3], (long long)A.G.nr - 1);
-  const long long bnx = bx1 - bx0 + 1, bnr = br1 - br0 + 1;
+  BlockPlan P;
+  P.bx0 = max(bb[0], 0);
+  P.br0 = max(bb[2], 0);
+  const long long bx1 = min(bb[1], A.G.nx - 1), br1 = min(bb[3], A.G.nr - 1);
+  P.bnx = bx1 - P.bx0 + 1;
+  P.bnr = br1 - P.br0 + 1;
   const int nplanes = A.G.nm * 4;  // J: 3 nm planes, rho: nm planes
-  const long long nvals = (bnx > 0 && bnr > 0) ? bnx * bnr * nplanes * 2 : 0;
-  const bool use_box = nvals > 0 && nvals * 4 <= kSpBoxBytes && Bl > 0.0;
-  const int el = use_box ? 29 - ceil_log2(Bl) : 0;
-  const float lscale = ldexpf(1.0f, el);
-  const int eJ = ilogb(A.scaleJ ? A.scaleJ[0] : 1.0);
-  const int eR = ilogb(A.scaleR ? A.scaleR[0] : 1.0);
-  if (use_box)
-    for (long long t = threadIdx.x; t < nvals; t += kSpThreads) box[t] = 0;
+  P.nvals = (bb[0] <= bb[1] && P.bnx > 0 && P.bnr > 0) ? P.bnx * P.bnr * nplanes * 2 : 0;
+  P.use_box = P.nvals > 0 && P.nvals * 8 <= kSpBoxBytes;
+  P.sJ = A.scaleJ ? (float)A.scaleJ[0] : 1.0f;
+  P.sR = A.scaleR ? (float)A.scaleR[0] : 1.0f;
+  return P;
+}
+
+__device__ __forceinline__ BoxGeo make_geo(unsigned long long *box, const BlockPlan &P,
+                                           const PushDepArgs &A) {
+  return BoxGeo{box, P.bx0, P.br0, P.bnx, P.bnr, P.sJ, P.sR, A.accJ, A.accR,
+                A.G.nx, A.G.nr, 3 * A.G.nm};
+}
+
+// Generic push + deposit (any nm): one particle per thread and iteration,
+// each value rounded to the global quantum and added to the box.
+__global__ void __launch_bounds__(kSpThreads) push_deposit_kernel(PushDepArgs A) {
+  extern __shared__ __align__(16) unsigned long long box[];
+  __shared__ int bb[4];
+  const i64 p0 = (i64)blockIdx.x * kSpPerBlock, p1 = min(A.P.n, p0 + (i64)kSpPerBlock);
+  const BlockPlan Pl = plan_block(A, p0, p1, false, bb);
+  if (Pl.use_box)
+    for (long long t = threadIdx.x; t < Pl.nvals; t += kSpThreads) box[t] = 0;
   __syncthreads();
-  // pass 2: push, deposit, store
+  const BoxGeo geo = make_geo(box, Pl, A);
   for (i64 i = p0 + threadIdx.x; i < p1; i += kSpThreads) {
     const float w = A.P.w[i];
-    Pushed q = push_one(A, i);
+    const Pushed q = push_one(A, i);
     if (w != 0.0f) {
-      auto to_box = [&](int plane, int r, int x, float re, float im) {
-        const long long b = (((long long)plane * bnr + (r - br0)) * bnx + (x - bx0)) * 2;
-        const int qr = __float2int_rn(re * lscale), qi = __float2int_rn(im * lscale);
-        if (qr) atomicAdd(&box[b], qr);
-        if (qi) atomicAdd(&box[b + 1], qi);
-      };
       if (A.dep_j) {
-        Loc L = locate(q.ixh, q.fxh, q.yh, q.zh, A.G);
-        if (use_box) {
-          deposit_at(L, q.vj, 3, 0, A.G, to_box);
-        } else {
-          const float sc = ldexpf(1.0f, eJ);
-          deposit_at(L, q.vj, 3, 0, A.G, [&](int plane, int r, int x, float re, float im) {
+        const Loc L = locate(q.ixh, q.fxh, q.yh, q.zh, A.G);
+        deposit_at(L, q.vj, 3, 0, A.G, [&](int plane, int r, int x, float re, float im) {
+          const long long qr = __float2ll_rn(re * geo.sJ), qi = __float2ll_rn(im * geo.sJ);
+          if (Pl.use_box) {
+            if (qr) box_put(geo, plane, r, x, 0, qr);
+            if (qi) box_put(geo, plane, r, x, 1, qi);
+          } else {
             const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
-            long long qr = __double2ll_rn((double)re * sc), qi = __double2ll_rn((double)im * sc);
             if (qr) atomicAdd(&A.accJ[2 * e], (unsigned long long)qr);
             if (qi) atomicAdd(&A.accJ[2 * e + 1], (unsigned long long)qi);
-          });
-        }
+          }
+        });
       }
       if (A.dep_rho) {
-        Loc L = locate(q.ixn, q.fxn, q.yn, q.zn, A.G);
+        const Loc L = locate(q.ixn, q.fxn, q.yn, q.zn, A.G);
         const float wv[1] = {w};
-        if (use_box) {
-          deposit_at(L, wv, 1, 3 * A.G.nm, A.G, to_box);
-        } else {
-          const float sc = ldexpf(1.0f, eR);
-          deposit_at(L, wv, 1, 0, A.G, [&](int plane, int r, int x, float re, float im) {
-            const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
-            long long qr = __double2ll_rn((double)re * sc), qi = __double2ll_rn((double)im * sc);
+        deposit_at(L, wv, 1, 3 * A.G.nm, A.G, [&](int plane, int r, int x, float re, float im) {
+          const long long qr = __float2ll_rn(re * geo.sR), qi = __float2ll_rn(im * geo.sR);
+          if (Pl.use_box) {
+            if (qr) box_put(geo, plane, r, x, 0, qr);
+            if (qi) box_put(geo, plane, r, x, 1, qi);
+          } else {
+            const i64 e = ((i64)(plane - 3 * A.G.nm) * A.G.nr + r) * A.G.nx + x;
             if (qr) atomicAdd(&A.accR[2 * e], (unsigned long long)qr);
             if (qi) atomicAdd(&A.accR[2 * e + 1], (unsigned long long)qi);
-          });
-        }
+          }
+        });
       }
     }
     if (A.push) {
@@ -279,40 +350,272 @@ __global__ void __launch_bounds__(kSpThreads) push_deposit_kernel(PushDepArgs A)
       A.P.z[i] = q.zn;
     }
   }
-  if (!use_box) return;
+  if (!Pl.use_box) return;
   __syncthreads();
-  // flush: local 2^el -> global 2^eg is an exact shift (el >= eg)
-  for (long long t = threadIdx.x; t < nvals; t += kSpThreads) {
-    const int v = box[t];
-    if (v == 0) continue;
-    const long long c2 = t & 1;
-    const long long b = t >> 1;
-    const long long bx = b % bnx;
-    const long long rest = b / bnx;
-    const long long br = rest % bnr;
-    const long long plane = rest / bnr;
-    const bool isj = plane < 3 * A.G.nm;
-    const int eg = isj ? eJ : eR;
-    const long long pl = isj ? plane : plane - 3 * A.G.nm;
-    // local quantum 2^-el -> global quantum 2^-eg: an exact left shift when
-    // eg >= el (the usual case: the block holds a small share of the total
-    // weight), otherwise a right shift rounded half away from zero
-    const int s = el - eg;
-    const long long q = (long long)v;
-    long long qq;
-    if (s <= 0) {
-      qq = q << (-s);
-    } else if (s >= 62) {
-      qq = 0;
-    } else {
-      const long long h = 1LL << (s - 1);
-      qq = (q >= 0) ? ((q + h) >> s) : -((-q + h) >> s);
-    }
-    if (qq == 0) continue;
-    const i64 e = (pl * A.G.nr + (br + br0)) * A.G.nx + (bx + bx0);
-    unsigned long long *acc = isj ? A.accJ : A.accR;
-    atomicAdd(&acc[2 * e + c2], (unsigned long long)qq);
+  flush_box(geo, Pl.nvals);
+}
+
+// ----------------------------------------------------------------------
+// Cell-run form of push + deposit for nm = 1, 2.  Particles generated cell
+// by cell (and the x-chunk sort) leave runs of consecutive particles in one
+// deposit cell, so each thread takes kRun consecutive particles, sums their
+// node values (already at the global scale) in FP32 registers while the
+// cell stays the same, and adds the sums, rounded to the global quantum, to
+// the block box when the cell changes.
+// ----------------------------------------------------------------------
+constexpr int kRun = 8;  // consecutive particles per thread (kSpThreads * kRun = kSpPerBlock)
+static_assert(kSpThreads * kRun == kSpPerBlock, "block = threads x run");
+
+template <int V>
+struct RunV {
+  int ix[V];
+  float fx[V], y[V], z[V], px[V], py[V], pz[V], w[V];
+};
+
+template <int V>
+struct VecT;
+template <>
+struct VecT<4> {
+  typedef int4 I;
+  typedef float4 F;
+};
+template <>
+struct VecT<2> {
+  typedef int2 I;
+  typedef float2 F;
+};
+
+template <int V, typename T, typename S>
+__device__ __forceinline__ void unpack(const T &t, S *o) {
+  o[0] = t.x;
+  o[1] = t.y;
+  if constexpr (V == 4) {
+    o[2] = t.z;
+    o[3] = t.w;
   }
+}
+
+// particles i0 .. i0+V-1 (cnt of them valid); vec: V-wide vector loads allowed
+template <int V>
+__device__ __forceinline__ void load_run(const SpParts &P, i64 i0, int cnt, bool vec, RunV<V> &q) {
+  typedef typename VecT<V>::I VI;
+  typedef typename VecT<V>::F VF;
+  if (vec && cnt == V) {
+    unpack<V>(*reinterpret_cast<const VI *>(P.ix + i0), q.ix);
+    unpack<V>(*reinterpret_cast<const VF *>(P.fx + i0), q.fx);
+    unpack<V>(*reinterpret_cast<const VF *>(P.y + i0), q.y);
+    unpack<V>(*reinterpret_cast<const VF *>(P.z + i0), q.z);
+    unpack<V>(*reinterpret_cast<const VF *>(P.px + i0), q.px);
+    unpack<V>(*reinterpret_cast<const VF *>(P.py + i0), q.py);
+    unpack<V>(*reinterpret_cast<const VF *>(P.pz + i0), q.pz);
+    unpack<V>(*reinterpret_cast<const VF *>(P.w + i0), q.w);
+  } else {
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+      const bool ok = j < cnt;
+      const i64 i = ok ? i0 + j : i0;
+      q.ix[j] = P.ix[i];
+      q.fx[j] = P.fx[i];
+      q.y[j] = P.y[i];
+      q.z[j] = P.z[i];
+      q.px[j] = P.px[i];
+      q.py[j] = P.py[i];
+      q.pz[j] = P.pz[i];
+      q.w[j] = ok ? P.w[i] : 0.0f;
+    }
+  }
+}
+
+template <int V>
+__device__ __forceinline__ void store_pos(const SpParts &P, i64 i0, int cnt, bool vec,
+                                          const int *oix, const float *ofx, const float *oy,
+                                          const float *oz) {
+  if (vec && cnt == V) {
+    if constexpr (V == 4) {
+      *reinterpret_cast<int4 *>(P.ix + i0) = make_int4(oix[0], oix[1], oix[2], oix[3]);
+      *reinterpret_cast<float4 *>(P.fx + i0) = make_float4(ofx[0], ofx[1], ofx[2], ofx[3]);
+      *reinterpret_cast<float4 *>(P.y + i0) = make_float4(oy[0], oy[1], oy[2], oy[3]);
+      *reinterpret_cast<float4 *>(P.z + i0) = make_float4(oz[0], oz[1], oz[2], oz[3]);
+    } else {
+      *reinterpret_cast<int2 *>(P.ix + i0) = make_int2(oix[0], oix[1]);
+      *reinterpret_cast<float2 *>(P.fx + i0) = make_float2(ofx[0], ofx[1]);
+      *reinterpret_cast<float2 *>(P.y + i0) = make_float2(oy[0], oy[1]);
+      *reinterpret_cast<float2 *>(P.z + i0) = make_float2(oz[0], oz[1]);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < V; ++j)
+      if (j < cnt) {
+        P.ix[i0 + j] = oix[j];
+        P.fx[i0 + j] = ofx[j];
+        P.y[i0 + j] = oy[j];
+        P.z[i0 + j] = oz[j];
+      }
+  }
+}
+
+// node sums of one deposit cell at the global scale (FP32, summed over the
+// particles of a run): v[comp][part][node], part 0 = mode 0 re, then
+// (re, im) of modes 1 .. NM-1; node = 2 j + k (r + j, x + k)
+template <int NM, int NC>
+struct CellAcc {
+  int cx, cr;
+  bool live;
+  float v[NC][2 * NM - 1][4];
+};
+
+template <int NM, int NC>
+__device__ __forceinline__ void acc_flush(CellAcc<NM, NC> &c, int plane0, const SpGrid &G,
+                                          const BoxGeo &B) {
+  if (!c.live) return;
+#pragma unroll
+  for (int l = 0; l < NC; ++l)
+#pragma unroll
+    for (int p = 0; p < 2 * NM - 1; ++p) {
+      const int m = (p + 1) >> 1;
+      const int im = (p > 0 && (p & 1) == 0) ? 1 : 0;
+      const long long plane = plane0 + m + (long long)G.nm * l;
+#pragma unroll
+      for (int nd = 0; nd < 4; ++nd) {
+        const long long v = __float2ll_rn(c.v[l][p][nd]);
+        const int j = nd >> 1, k = nd & 1;
+        const int gx = c.cx + k;
+        if (v == 0 || gx < 0 || gx >= G.nx) continue;
+        box_put(B, plane, c.cr + j, gx, im, v);
+      }
+    }
+  c.live = false;
+}
+
+// val: the particle's values already multiplied by the global scale
+template <int NM, int NC>
+__device__ __forceinline__ void acc_add(CellAcc<NM, NC> &c, const Loc &L, const float *val,
+                                        int plane0, const SpGrid &G, const BoxGeo &B) {
+  if (!L.ok) return;
+  if (!c.live || c.cx != L.cx || c.cr != L.cr) {
+    acc_flush(c, plane0, G, B);
+    c.cx = L.cx;
+    c.cr = L.cr;
+    c.live = true;
+#pragma unroll
+    for (int l = 0; l < NC; ++l)
+#pragma unroll
+      for (int p = 0; p < 2 * NM - 1; ++p)
+#pragma unroll
+        for (int nd = 0; nd < 4; ++nd) c.v[l][p][nd] = 0.0f;
+  }
+  const float sx[2] = {1.0f - L.sx1, L.sx1};
+  const float sr[2] = {1.0f - L.sr1, L.sr1};
+  float pr = 1.0f, pi = 0.0f;  // e^{-i m theta}
+#pragma unroll
+  for (int m = 0; m < NM; ++m) {
+    if (m > 0) {
+      float nr_ = pr * L.phr + pi * L.phi;
+      float ni_ = pi * L.phr - pr * L.phi;
+      pr = nr_;
+      pi = ni_;
+    }
+#pragma unroll
+    for (int l = 0; l < NC; ++l) {
+      const float vr = pr * val[l], vi = pi * val[l];
+#pragma unroll
+      for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const float s = sx[k] * sr[j];
+          const int nd = 2 * j + k;
+          if (m == 0) {
+            c.v[l][0][nd] += vr * s;
+          } else {
+            c.v[l][2 * m - 1][nd] += vr * s;
+            c.v[l][2 * m][nd] += vi * s;
+          }
+        }
+    }
+  }
+}
+
+template <int NM, bool PUSH, bool DJ, bool DR>
+__global__ void __launch_bounds__(kSpThreads, 2) push_deposit_run_kernel(PushDepArgs A, int vec) {
+  extern __shared__ __align__(16) unsigned long long box[];
+  __shared__ int bb[4];
+  const i64 p0 = (i64)blockIdx.x * kSpPerBlock, p1 = min(A.P.n, p0 + (i64)kSpPerBlock);
+  const BlockPlan Pl = plan_block(A, p0, p1, vec != 0, bb);
+  if (Pl.use_box)
+    for (long long t = threadIdx.x; t < Pl.nvals; t += kSpThreads) box[t] = 0;
+  __syncthreads();
+  const i64 r0i = p0 + (i64)threadIdx.x * kRun;  // this thread's run
+  const int rcnt = (int)max((i64)0, min((i64)kRun, p1 - r0i));
+  const BoxGeo geo = make_geo(box, Pl, A);
+  CellAcc<NM, 3> cj;
+  CellAcc<NM, 1> cr;
+  cj.live = false;
+  cr.live = false;
+  // vector width: the fused moving-species kernel at nm = 2 holds the most
+  // accumulators and loads two particles at a time
+  constexpr int V = (NM == 2 && PUSH && DJ && DR) ? 2 : 4;
+  for (int h = 0; h < kRun / V; ++h) {
+    const int cnt = rcnt - V * h;
+    if (cnt <= 0) break;
+    const i64 i0 = r0i + V * h;
+    RunV<V> q;
+    load_run<V>(A.P, i0, cnt, vec != 0, q);
+    int oix[V];
+    float ofx[V], oy[V], oz[V];
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+      Pushed u;
+      if (PUSH || DJ) {
+        u = push_vals(A, q.ix[j], q.fx[j], q.y[j], q.z[j], q.px[j], q.py[j], q.pz[j], q.w[j]);
+      } else {
+        u.ixh = u.ixn = q.ix[j];
+        u.fxh = u.fxn = q.fx[j];
+        u.yh = u.yn = q.y[j];
+        u.zh = u.zn = q.z[j];
+      }
+      if (PUSH) {
+        oix[j] = u.ixn;
+        ofx[j] = u.fxn;
+        oy[j] = u.yn;
+        oz[j] = u.zn;
+      }
+      if (q.w[j] == 0.0f) continue;
+      if (DJ) {
+        const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, A.G);
+        const float vs[3] = {u.vj[0] * Pl.sJ, u.vj[1] * Pl.sJ, u.vj[2] * Pl.sJ};
+        if (Pl.use_box) {
+          acc_add(cj, L, vs, 0, A.G, geo);
+        } else {
+          deposit_at(L, vs, 3, 0, A.G, [&](int plane, int r, int x, float re, float im) {
+            const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
+            const long long qr = __float2ll_rn(re), qi = __float2ll_rn(im);
+            if (qr) atomicAdd(&A.accJ[2 * e], (unsigned long long)qr);
+            if (qi) atomicAdd(&A.accJ[2 * e + 1], (unsigned long long)qi);
+          });
+        }
+      }
+      if (DR) {
+        const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, A.G);
+        const float ws[1] = {q.w[j] * Pl.sR};
+        if (Pl.use_box) {
+          acc_add(cr, L, ws, 3 * NM, A.G, geo);
+        } else {
+          deposit_at(L, ws, 1, 0, A.G, [&](int plane, int r, int x, float re, float im) {
+            const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
+            const long long qr = __float2ll_rn(re), qi = __float2ll_rn(im);
+            if (qr) atomicAdd(&A.accR[2 * e], (unsigned long long)qr);
+            if (qi) atomicAdd(&A.accR[2 * e + 1], (unsigned long long)qi);
+          });
+        }
+      }
+    }
+    if (PUSH) store_pos<V>(A.P, i0, cnt, vec != 0, oix, ofx, oy, oz);
+  }
+  if (!Pl.use_box) return;
+  if (DJ) acc_flush(cj, 0, A.G, geo);
+  if (DR) acc_flush(cr, 3 * NM, A.G, geo);
+  __syncthreads();
+  flush_box(geo, Pl.nvals);
 }
 
 // Global scale 2^(61 - ceil(log2 B)), B = sum |w| (deterministic order).
@@ -336,9 +639,25 @@ __global__ void sp_scale_kernel(const double *__restrict__ partial, int np, doub
     double B = 0.0;
     for (int i = 0; i < np; ++i) B += partial[i];
     if (!(B > 0.0) || !isfinite(B)) B = 1.0;
-    out[0] = ldexp(1.0, 61 - ceil_log2(B));
+    // the exponent stays inside the FP32 range the deposit kernels use
+    out[0] = ldexp(1.0, min(61 - ceil_log2(B), 120));
     out[1] = B;
   }
+}
+
+// Boris rotation (particle_tools.f90:18-56) of one momentum in FP32: 1/gamma
+// from a reciprocal square root, one division for 2/(1 + t^2)
+__device__ __forceinline__ void boris(float &px, float &py, float &pz, const float *F, float hh) {
+  const float um0 = px + hh * F[0], um1 = py + hh * F[1], um2 = pz + hh * F[2];
+  const float ig = rsqrtf(1.0f + (um0 * um0 + um1 * um1 + um2 * um2));
+  const float t0 = hh * F[3] * ig, t1 = hh * F[4] * ig, t2 = hh * F[5] * ig;
+  const float f = 2.0f / (1.0f + (t0 * t0 + t1 * t1 + t2 * t2));
+  const float s0 = t0 * f, s1 = t1 * f, s2 = t2 * f;
+  const float u0 = um0 + um1 * t2 - um2 * t1, u1 = um1 - um0 * t2 + um2 * t0,
+              u2 = um2 + um0 * t1 - um1 * t0;
+  px = um0 + u1 * s2 - u2 * s1 + hh * F[0];
+  py = um1 - u0 * s2 + u2 * s0 + hh * F[1];
+  pz = um2 + u0 * s1 - u1 * s0 + hh * F[2];
 }
 
 // gather (proj_fld) + Boris (push_velocs), FP32
@@ -389,18 +708,110 @@ __global__ void __launch_bounds__(256) gather_push_kernel(GatherArgs A) {
         }
       }
     }
-    // Boris rotation (particle_tools.f90:18-56)
-    const float h = 0.5f * A.dtq;
-    float um[3] = {A.P.px[i] + h * F[0], A.P.py[i] + h * F[1], A.P.pz[i] + h * F[2]};
-    const float g = sqrtf(1.0f + (um[0] * um[0] + um[1] * um[1] + um[2] * um[2]));
-    float t[3] = {h * F[3] / g, h * F[4] / g, h * F[5] / g};
-    const float t2 = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
-    float s[3] = {2 * t[0] / (1 + t2), 2 * t[1] / (1 + t2), 2 * t[2] / (1 + t2)};
-    float u0[3] = {um[0] + um[1] * t[2] - um[2] * t[1], um[1] - um[0] * t[2] + um[2] * t[0],
-                   um[2] + um[0] * t[1] - um[1] * t[0]};
-    A.P.px[i] = um[0] + u0[1] * s[2] - u0[2] * s[1] + h * F[0];
-    A.P.py[i] = um[1] - u0[0] * s[2] + u0[2] * s[0] + h * F[1];
-    A.P.pz[i] = um[2] + u0[0] * s[1] - u0[1] * s[0] + h * F[2];
+    float px = A.P.px[i], py = A.P.py[i], pz = A.P.pz[i];
+    boris(px, py, pz, F, 0.5f * A.dtq);
+    A.P.px[i] = px;
+    A.P.py[i] = py;
+    A.P.pz[i] = pz;
+  }
+}
+
+// Cell-run gather + Boris for nm = 1, 2: a thread takes kRun consecutive
+// particles and keeps the fields of the 4 nodes of the current cell in
+// registers (mode 0: real parts; modes >= 1: complex), reloading them only
+// when the cell changes.  Same interpolation and rotation as
+// gather_push_kernel.
+template <int NM>
+__global__ void __launch_bounds__(256, 2) gather_push_run_kernel(GatherArgs A, int vec) {
+  constexpr int V = 2;
+  const SpGrid &G = A.G;
+  const i64 plane = (i64)G.nx * G.nr;
+  const i64 r0i = ((i64)blockIdx.x * blockDim.x + threadIdx.x) * kRun;
+  if (r0i >= A.P.n) return;
+  const int rcnt = (int)min((i64)kRun, A.P.n - r0i);
+  int ccx = INT_MIN, ccr = INT_MIN;
+  float f0[6][4];
+  float2 f1[NM > 1 ? NM - 1 : 1][6][4];
+  for (int h = 0; h < kRun / V; ++h) {
+    const int cnt = rcnt - V * h;
+    if (cnt <= 0) break;
+    const i64 i0 = r0i + V * h;
+    RunV<V> q;
+    load_run<V>(A.P, i0, cnt, vec != 0, q);
+    float opx[V], opy[V], opz[V];
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+      float F[6] = {0, 0, 0, 0, 0, 0};
+      if (q.w[j] != 0.0f) {
+        const Loc L = locate(q.ix[j], q.fx[j], q.y[j], q.z[j], G);
+        if (L.ok) {
+          if (L.cx != ccx || L.cr != ccr) {
+            ccx = L.cx;
+            ccr = L.cr;
+#pragma unroll
+            for (int nd = 0; nd < 4; ++nd) {
+              const int gx = L.cx + (nd & 1), gr = L.cr + (nd >> 1);
+              const bool okx = gx >= 0 && gx < G.nx;
+#pragma unroll
+              for (int l = 0; l < 6; ++l) {
+                const float2 *b = A.eb + (i64)(G.nm * l) * plane + (i64)gr * G.nx + gx;
+                f0[l][nd] = okx ? b[0].x : 0.0f;
+#pragma unroll
+                for (int m = 1; m < NM; ++m)
+                  f1[m - 1][l][nd] = okx ? b[(i64)m * plane] : make_float2(0.0f, 0.0f);
+              }
+            }
+          }
+          const float sx[2] = {1.0f - L.sx1, L.sx1};
+          const float sr[2] = {1.0f - L.sr1, L.sr1};
+#pragma unroll
+          for (int l = 0; l < 6; ++l) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int jj = 0; jj < 2; ++jj) {
+              acc += sr[jj] * sx[0] * f0[l][2 * jj];
+              acc += sr[jj] * sx[1] * f0[l][2 * jj + 1];
+            }
+            F[l] += acc;
+          }
+          float pr = 1.0f, pi = 0.0f;  // e^{+i m theta}
+#pragma unroll
+          for (int m = 1; m < NM; ++m) {
+            const float a = pr * L.phr - pi * L.phi, b2 = pr * L.phi + pi * L.phr;
+            pr = a;
+            pi = b2;
+#pragma unroll
+            for (int l = 0; l < 6; ++l) {
+              float acc = 0.0f;
+#pragma unroll
+              for (int jj = 0; jj < 2; ++jj) {
+                const float2 u0 = f1[m - 1][l][2 * jj], u1 = f1[m - 1][l][2 * jj + 1];
+                acc += sr[jj] * sx[0] * (pr * u0.x - pi * u0.y);
+                acc += sr[jj] * sx[1] * (pr * u1.x - pi * u1.y);
+              }
+              F[l] += acc;
+            }
+          }
+        }
+      }
+      opx[j] = q.px[j];
+      opy[j] = q.py[j];
+      opz[j] = q.pz[j];
+      boris(opx[j], opy[j], opz[j], F, 0.5f * A.dtq);
+    }
+    if (vec && cnt == V) {
+      *reinterpret_cast<float2 *>(A.P.px + i0) = make_float2(opx[0], opx[1]);
+      *reinterpret_cast<float2 *>(A.P.py + i0) = make_float2(opy[0], opy[1]);
+      *reinterpret_cast<float2 *>(A.P.pz + i0) = make_float2(opz[0], opz[1]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < V; ++j)
+        if (j < cnt) {
+          A.P.px[i0 + j] = opx[j];
+          A.P.py[i0 + j] = opy[j];
+          A.P.pz[i0 + j] = opz[j];
+        }
+    }
   }
 }
 
@@ -443,14 +854,115 @@ __global__ void to_f64_kernel(SpParts P, double *__restrict__ x, i64 x_cs, i64 x
   }
 }
 
-// absorption flags: inside the box xmin <= x and r^2 <= r2max (x in the
-// window-relative cell units of the same (k, f) convention)
-__global__ void keep_flags_kernel(SpParts P, int win_k, float win_f, float xmin_cells,
-                                  float xmax_cells, float r2max, int *__restrict__ flag) {
+// Absorbing boundary (species.py:351-398, SimDom test) in place: a live
+// particle outside xmin <= x <= xmax, r^2 <= r2max (window-relative cell
+// units of the (k, f) convention) is marked dead and its weight zeroed, so
+// that it deposits nothing until a compaction drops it.  counters[0] counts
+// the dead particles.
+__global__ void __launch_bounds__(256) absorb_kernel(SpParts P, uint8_t *__restrict__ dead,
+                                                     int win_k, float win_f, float xmin_cells,
+                                                     float xmax_cells, float r2max,
+                                                     unsigned long long *counters) {
+  unsigned cnt = 0;
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < P.n; i += (i64)gridDim.x * blockDim.x) {
+    if (dead[i]) continue;
     const float xc = (float)(P.ix[i] - win_k) + (P.fx[i] - win_f);
     const float r2 = P.y[i] * P.y[i] + P.z[i] * P.z[i];
-    flag[i] = (xc >= xmin_cells && xc <= xmax_cells && r2 <= r2max) ? 1 : 0;
+    if (!(xc >= xmin_cells && xc <= xmax_cells && r2 <= r2max)) {
+      dead[i] = 1;
+      P.w[i] = 0.0f;
+      ++cnt;
+    }
+  }
+  cnt = __reduce_add_sync(0xffffffffu, cnt);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&counters[0], (unsigned long long)cnt);
+}
+
+// counters[1] += n - counters[0]: live particles of this step
+__global__ void live_steps_kernel(unsigned long long *counters, i64 n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) counters[1] += (unsigned long long)n - counters[0];
+}
+
+// Stable compaction of the live particles: tile counts, one scan, scatter.
+constexpr int kCmpThreads = 256;
+constexpr int kCmpTile = 4096;  // particles per tile
+
+__global__ void __launch_bounds__(kCmpThreads) compact_count_kernel(const uint8_t *__restrict__ dead,
+                                                                    i64 n, int *__restrict__ cnt) {
+  const i64 t0 = (i64)blockIdx.x * kCmpTile, t1 = min(n, t0 + kCmpTile);
+  int c = 0;
+  for (i64 i = t0 + threadIdx.x; i < t1; i += kCmpThreads) c += dead[i] ? 0 : 1;
+  c = __reduce_add_sync(0xffffffffu, c);
+  __shared__ int ws[kCmpThreads / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int k = 0; k < kCmpThreads / 32; ++k) s += ws[k];
+    cnt[blockIdx.x] = s;
+  }
+}
+
+// exclusive scan of the tile counts in place (one block), total -> n_out
+__global__ void __launch_bounds__(1024) compact_scan_kernel(int *__restrict__ cnt, int ntiles,
+                                                            int64_t *__restrict__ n_out) {
+  __shared__ long long part[1024];
+  const int per = (ntiles + 1023) / 1024;
+  const int a = threadIdx.x * per, b = min(ntiles, a + per);
+  long long s = 0;
+  for (int i = a; i < b; ++i) s += cnt[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan
+    const long long v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  long long run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+  for (int i = a; i < b; ++i) {
+    const int c = cnt[i];
+    cnt[i] = (int)run;  // tile offsets stay below 2^31 tiles x 4096: checked on the host
+    run += c;
+  }
+  if (threadIdx.x == 1023) *n_out = part[1023];
+}
+
+__global__ void __launch_bounds__(kCmpThreads) compact_scatter_kernel(SpParts S, SpParts D,
+                                                                      const uint8_t *__restrict__ dead,
+                                                                      const int *__restrict__ off) {
+  const i64 t0 = (i64)blockIdx.x * kCmpTile, t1 = min(S.n, t0 + kCmpTile);
+  __shared__ int wsum[kCmpThreads / 32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = off[blockIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (i64 c0 = t0; c0 < t1; c0 += kCmpThreads) {
+    const i64 i = c0 + threadIdx.x;
+    const bool live = i < t1 && !dead[i];
+    const unsigned m = __ballot_sync(0xffffffffu, live);
+    if (lane == 0) wsum[warp] = __popc(m);
+    __syncthreads();
+    int before = carry;
+    for (int k = 0; k < warp; ++k) before += wsum[k];
+    if (live) {
+      const i64 j = (i64)before + __popc(m & ((1u << lane) - 1u));
+      D.ix[j] = S.ix[i];
+      D.fx[j] = S.fx[i];
+      D.y[j] = S.y[i];
+      D.z[j] = S.z[i];
+      D.px[j] = S.px[i];
+      D.py[j] = S.py[i];
+      D.pz[j] = S.pz[i];
+      D.w[j] = S.w[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int k = 0; k < kCmpThreads / 32; ++k) t += wsum[k];
+      carry += t;
+    }
+    __syncthreads();
   }
 }
 
@@ -502,10 +1014,40 @@ int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, f
   A.accR = reinterpret_cast<unsigned long long *>(accR);
   A.scaleJ = scaleJ;
   A.scaleR = scaleR;
-  cudaFuncSetAttribute(push_deposit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       kSpBoxBytes);
   const unsigned blocks = (unsigned)((n + kSpPerBlock - 1) / kSpPerBlock);
-  push_deposit_kernel<<<blocks, kSpThreads, kSpBoxBytes, as_stream(stream)>>>(A); chm::count_launch();
+  // 16-byte vector access when every array starts on a 16-byte boundary
+  const uintptr_t al = reinterpret_cast<uintptr_t>(ix) | reinterpret_cast<uintptr_t>(fx) |
+                       reinterpret_cast<uintptr_t>(y) | reinterpret_cast<uintptr_t>(z) |
+                       reinterpret_cast<uintptr_t>(px) | reinterpret_cast<uintptr_t>(py) |
+                       reinterpret_cast<uintptr_t>(pz) | reinterpret_cast<uintptr_t>(w);
+  const int vec = (al & 15u) == 0;
+  cudaStream_t st = as_stream(stream);
+  // CHIMERA_GB300_DEPOSIT=generic selects the per-particle kernels of the
+  // deposit and the gather for every nm (the deposit kernels produce
+  // identical accumulators)
+  const char *var = getenv("CHIMERA_GB300_DEPOSIT");
+  const bool generic = var && strcmp(var, "generic") == 0;
+  // cell-run kernels for nm 1, 2 and the three uses: moving species (push,
+  // J, rho), moving species without the fused rho, still species (rho)
+  void (*kern)(PushDepArgs, int) = nullptr;
+  if (!generic && (nm == 1 || nm == 2)) {
+    const int mode = (push ? 4 : 0) | (A.dep_j ? 2 : 0) | (A.dep_rho ? 1 : 0);
+    if (mode == 7) kern = nm == 1 ? push_deposit_run_kernel<1, true, true, true>
+                                  : push_deposit_run_kernel<2, true, true, true>;
+    if (mode == 6) kern = nm == 1 ? push_deposit_run_kernel<1, true, true, false>
+                                  : push_deposit_run_kernel<2, true, true, false>;
+    if (mode == 1) kern = nm == 1 ? push_deposit_run_kernel<1, false, false, true>
+                                  : push_deposit_run_kernel<2, false, false, true>;
+  }
+  if (kern) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpBoxBytes);
+    kern<<<blocks, kSpThreads, kSpBoxBytes, st>>>(A, vec);
+  } else {
+    cudaFuncSetAttribute(push_deposit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kSpBoxBytes);
+    push_deposit_kernel<<<blocks, kSpThreads, kSpBoxBytes, st>>>(A);
+  }
+  chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -521,7 +1063,25 @@ int chm_sp_gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, fl
   A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
   A.eb = reinterpret_cast<const float2 *>(eb_c64);
   A.dtq = dtq;
-  gather_push_kernel<<<grid_for(n, 256, 16), 256, 0, as_stream(stream)>>>(A); chm::count_launch();
+  const uintptr_t al = reinterpret_cast<uintptr_t>(ix) | reinterpret_cast<uintptr_t>(fx) |
+                       reinterpret_cast<uintptr_t>(y) | reinterpret_cast<uintptr_t>(z) |
+                       reinterpret_cast<uintptr_t>(px) | reinterpret_cast<uintptr_t>(py) |
+                       reinterpret_cast<uintptr_t>(pz) | reinterpret_cast<uintptr_t>(w);
+  const int vec = (al & 7u) == 0;  // 8-byte (two-particle) vector access
+  const char *var = getenv("CHIMERA_GB300_DEPOSIT");
+  const bool generic = var && strcmp(var, "generic") == 0;
+  cudaStream_t st = as_stream(stream);
+  if (!generic && (nm == 1 || nm == 2)) {
+    const i64 threads = (n + kRun - 1) / kRun;
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    if (nm == 1)
+      gather_push_run_kernel<1><<<blocks, 256, 0, st>>>(A, vec);
+    else
+      gather_push_run_kernel<2><<<blocks, 256, 0, st>>>(A, vec);
+  } else {
+    gather_push_kernel<<<grid_for(n, 256, 16), 256, 0, st>>>(A);
+  }
+  chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -554,15 +1114,62 @@ int chm_sp_to_f64(const int32_t *ix, const float *fx, const float *y, const floa
   return CHM_OK;
 }
 
-int chm_sp_keep_flags(const int32_t *ix, const float *fx, const float *y, const float *z,
-                      int64_t n, int win_k, float win_f, float xmin_cells, float xmax_cells,
-                      float r2max, int32_t *flag, void *stream) {
-  CHM_REQUIRE(n >= 0, "sp_keep_flags: bad args");
+int chm_sp_absorb(const int32_t *ix, const float *fx, const float *y, const float *z, float *w,
+                  uint8_t *dead, int64_t n, int win_k, float win_f, float xmin_cells,
+                  float xmax_cells, float r2max, uint64_t *counters, void *stream) {
+  CHM_REQUIRE(n >= 0 && counters, "sp_absorb: bad args");
   if (n == 0) return CHM_OK;
+  CHM_REQUIRE(ix && fx && y && z && w && dead, "sp_absorb: null pointer");
   SpParts P{const_cast<int32_t *>(ix), const_cast<float *>(fx), const_cast<float *>(y),
-            const_cast<float *>(z), nullptr, nullptr, nullptr, nullptr, n};
-  keep_flags_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(P, win_k, win_f, xmin_cells,
-                                                                     xmax_cells, r2max, flag); chm::count_launch();
+            const_cast<float *>(z), nullptr, nullptr, nullptr, w, n};
+  absorb_kernel<<<grid_for(n, 256, 8), 256, 0, as_stream(stream)>>>(
+      P, dead, win_k, win_f, xmin_cells, xmax_cells, r2max,
+      reinterpret_cast<unsigned long long *>(counters));
+  chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+int chm_sp_count_live(uint64_t *counters, int64_t n, void *stream) {
+  CHM_REQUIRE(counters && n >= 0, "sp_count_live: bad args");
+  live_steps_kernel<<<1, 32, 0, as_stream(stream)>>>(reinterpret_cast<unsigned long long *>(counters), n);
+  chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+int64_t chm_sp_compact_ws_bytes(int64_t n) {
+  return ((n + kCmpTile - 1) / kCmpTile) * 4 + 256;
+}
+
+int chm_sp_compact(const int32_t *ix, const float *fx, const float *y, const float *z,
+                   const float *px, const float *py, const float *pz, const float *w,
+                   const uint8_t *dead, int64_t n, int32_t *ix_out, float *fx_out, float *y_out,
+                   float *z_out, float *px_out, float *py_out, float *pz_out, float *w_out,
+                   int64_t *n_out, void *ws, int64_t ws_bytes, void *stream) {
+  CHM_REQUIRE(n >= 0 && n_out, "sp_compact: bad args");
+  CHM_REQUIRE(n < ((int64_t)1 << 31), "sp_compact: more than 2^31 - 1 particles");
+  CHM_REQUIRE(ws && ws_bytes >= chm_sp_compact_ws_bytes(n), "sp_compact: workspace too small");
+  cudaStream_t st = as_stream(stream);
+  if (n == 0) {
+    cudaMemsetAsync(n_out, 0, sizeof(int64_t), st);
+    return CHM_OK;
+  }
+  CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && dead && ix_out && fx_out && y_out &&
+                  z_out && px_out && py_out && pz_out && w_out,
+              "sp_compact: null pointer");
+  const int ntiles = (int)((n + kCmpTile - 1) / kCmpTile);
+  int *cnt = reinterpret_cast<int *>(ws);
+  SpParts S{const_cast<int32_t *>(ix), const_cast<float *>(fx), const_cast<float *>(y),
+            const_cast<float *>(z), const_cast<float *>(px), const_cast<float *>(py),
+            const_cast<float *>(pz), const_cast<float *>(w), n};
+  SpParts D{ix_out, fx_out, y_out, z_out, px_out, py_out, pz_out, w_out, n};
+  compact_count_kernel<<<ntiles, kCmpThreads, 0, st>>>(dead, n, cnt);
+  chm::count_launch();
+  compact_scan_kernel<<<1, 1024, 0, st>>>(cnt, ntiles, n_out);
+  chm::count_launch();
+  compact_scatter_kernel<<<ntiles, kCmpThreads, 0, st>>>(S, D, dead, cnt);
+  chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }

@@ -61,7 +61,11 @@ def _f32(a, device) -> torch.Tensor:
 
 
 class _SpParticles:
-    """Split-layout SoA buffers of one species (capacity-allocated)."""
+    """Split-layout SoA buffers of one species (capacity-allocated).
+
+    Absorbed particles stay in place, marked in ``dead`` with zero weight,
+    until ``compact`` drops them; ``counters`` (device) holds the number of
+    dead particles and the running sum of live particles over steps."""
 
     NAMES = ("ix", "fx", "y", "z", "px", "py", "pz", "w")
 
@@ -70,21 +74,32 @@ class _SpParticles:
         self.cap = 0
         self.n = 0
         self.buf = {}
+        self.spare = None
+        self.dead = None
+        self.counters = torch.zeros(2, dtype=torch.int64, device=device)
+        self.moves = 0  # window moves since the last compaction
         self.reserve(cap)
+
+    def _alloc(self, cap):
+        return {k: torch.zeros(cap, dtype=torch.int32 if k == "ix" else torch.float32,
+                               device=self.device) for k in self.NAMES}
 
     def reserve(self, cap):
         cap = int(max(cap, 1024))
         if cap <= self.cap:
             return
-        new = {k: torch.zeros(cap, dtype=torch.int32 if k == "ix" else torch.float32,
-                              device=self.device) for k in self.NAMES}
-        for k in self.NAMES:
-            if self.n:
+        new = self._alloc(cap)
+        dead = torch.zeros(cap, dtype=torch.uint8, device=self.device)
+        if self.n:
+            for k in self.NAMES:
                 new[k][: self.n].copy_(self.buf[k][: self.n])
-        self.buf, self.cap = new, cap
+            dead[: self.n].copy_(self.dead[: self.n])
+        self.buf, self.dead, self.cap = new, dead, cap
+        self.spare = None
 
-    def ptrs(self):
-        return [self.buf[k].data_ptr() for k in self.NAMES]
+    def ptrs(self, buf=None):
+        b = self.buf if buf is None else buf
+        return [b[k].data_ptr() for k in self.NAMES]
 
     def append_f64(self, coords, momenta, weights, X0, dx):
         m = int(coords.shape[-1])
@@ -105,16 +120,26 @@ class _SpParticles:
         _lib.call("chm_sp_from_f64", *self.ptrs(), self.n, tx.data_ptr(), tx.stride(0),
                   tx.stride(1), tp.data_ptr(), tp.stride(0), tp.stride(1), tw.data_ptr(),
                   tw.stride(0), float(X0), float(dx), m, _stream())
+        self.dead[self.n: self.n + m].zero_()
         self.n += m
 
-    def keep(self, flags: torch.Tensor):
-        """Stable compaction to the particles with flag 1."""
-        idx = torch.nonzero(flags[: self.n], as_tuple=False).flatten()
-        n = int(idx.numel())
+    def compact(self):
+        """Drop the dead particles (stable order); one device->host read."""
+        if self.n == 0:
+            return
+        if self.spare is None:
+            self.spare = self._alloc(self.cap)
+        ws = chimera.workspace(_lib.query("chm_sp_compact_ws_bytes", self.n), self.device)
+        n_out = torch.empty(1, dtype=torch.int64, device=self.device)
+        _lib.call("chm_sp_compact", *self.ptrs(), self.dead.data_ptr(), self.n,
+                  *self.ptrs(self.spare), n_out.data_ptr(), ws.data_ptr(), ws.numel(), _stream())
+        n = int(n_out.item())
         chimera.io_bytes["d2h"] += 8
-        for k in self.NAMES:
-            self.buf[k][:n] = self.buf[k][: self.n][idx]
+        self.buf, self.spare = self.spare, self.buf
         self.n = n
+        self.dead[:n].zero_()
+        self.counters[0].zero_()
+        self.moves = 0
 
 
 def _stream():
@@ -196,6 +221,9 @@ class SplitRun:
         self.scaleR = torch.zeros(2, dtype=torch.float64, device=dev)
         self.scaleBG = torch.zeros(2, dtype=torch.float64, device=dev)
         self._scales_valid = False
+        # absorbed particles are dropped from the arrays every this many
+        # window moves (they are marked dead, with zero weight, meanwhile)
+        self.compact_every = 32
         # the background density is deposited on window moves
         # (chimera_main.py:277-284); it starts empty, as the reference's
         self.have_bg = False
@@ -349,6 +377,8 @@ class SplitRun:
                   self.gnxt.data_ptr() if self.space_charge else None, self.c1.data_ptr(),
                   self.c2.data_ptr(), int(self.nterm), P_, st)
         self._project_fields_and_push()
+        for spc, P in self._moving():
+            _lib.call("chm_sp_count_live", P.counters.data_ptr(), P.n, st)
 
     def _project_fields_and_push(self):
         A = self.solver.Args
@@ -387,7 +417,8 @@ class SplitRun:
         self._scales_valid = False
 
     def _absorb(self, wind):
-        """species.py:351-398 absorption (SimDom test) on the split layout."""
+        """species.py:351-398 absorption (SimDom test) on the split layout:
+        marks in place, compacts every ``compact_every`` window moves."""
         for spc, P in zip(self.fp.Particles, self.parts):
             if P.n == 0:
                 continue
@@ -396,17 +427,27 @@ class SplitRun:
             # species grid box in window cells
             xmin = (a["leftX"] + wind["AbsorbLayer"] * a["dx"] - self.solver.Args["leftX"]) / self.dx
             xmax = (a["rightX"] - self.solver.Args["leftX"]) / self.dx
-            flags = torch.empty(P.n, dtype=torch.int32, device=self.device)
-            _lib.call("chm_sp_keep_flags", P.buf["ix"].data_ptr(), P.buf["fx"].data_ptr(),
-                      P.buf["y"].data_ptr(), P.buf["z"].data_ptr(), P.n, k, f, float(xmin),
-                      float(xmax), float(a["upperR"] ** 2), flags.data_ptr(), _stream())
-            P.keep(flags)
+            b = P.buf
+            _lib.call("chm_sp_absorb", b["ix"].data_ptr(), b["fx"].data_ptr(), b["y"].data_ptr(),
+                      b["z"].data_ptr(), b["w"].data_ptr(), P.dead.data_ptr(), P.n, k, f,
+                      float(xmin), float(xmax), float(a["upperR"] ** 2),
+                      P.counters.data_ptr(), _stream())
+            P.moves += 1
+            if P.moves >= self.compact_every:
+                P.compact()
         self._scales_valid = False
 
     # ------------------------------------------------------------------
     @property
     def num_moving(self) -> int:
+        """Particles held by the moving species, dead ones not yet compacted
+        included (an upper bound of the live count)."""
         return sum(P.n for _, P in self._moving())
+
+    def live_particle_steps(self) -> int:
+        """Sum over the steps made of the live moving particles after each
+        step (one device->host read)."""
+        return int(sum(int(P.counters[1].item()) for _, P in self._moving()))
 
     def to_fp64(self):
         """Write the split state into the FP64 Data of the solver and species."""
@@ -420,6 +461,7 @@ class SplitRun:
             D["gradRho_fb_nxt"].copy_(self.gnxt)
             D["gradRho_fb_prv"].copy_(self.gprv)
         for spc, P in zip(self.fp.Particles, self.parts):
+            P.compact()
             spc.store.resize(P.n)
             spc._sync()
             d = spc.Data

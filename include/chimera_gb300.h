@@ -408,8 +408,8 @@ int64_t chm_sp_ops_bytes(int64_t K, int64_t N, int64_t nmodes);
 int chm_sp_prepare_ops(chm_sp_ops *ops, const double *mats, int64_t K, int64_t N,
                        int64_t nmodes, void *buf, int64_t buf_bytes, void *stream);
 
-/* Deterministic global deposit scale: scale2[0] = 2^(61 - ceil(log2 B)),
- * scale2[1] = B = sum |w| (device doubles). */
+/* Deterministic global deposit scale: scale2[0] = 2^min(61 - ceil(log2 B),
+ * 120), scale2[1] = B = sum |w| (device doubles). */
 int64_t chm_sp_scale_ws_bytes(void);
 int chm_sp_weight_scale(double *scale2, const float *w, int64_t n, void *ws,
                         int64_t ws_bytes, void *stream);
@@ -447,11 +447,26 @@ int chm_sp_to_f64(const int32_t *ix, const float *fx, const float *y,
                   int64_t x_cs, int64_t x_ps, double *momenta, int64_t p_cs,
                   int64_t p_ps, double *wghts, int64_t w_ps, double X0,
                   double dx, void *stream);
-/* keep flags of the absorbing boundary (species.py:351-398 SimDom test). */
-int chm_sp_keep_flags(const int32_t *ix, const float *fx, const float *y,
-                      const float *z, int64_t n, int win_k, float win_f,
-                      float xmin_cells, float xmax_cells, float r2max,
-                      int32_t *flag, void *stream);
+/* Absorbing boundary of the moving window (species.py:351-398, the SimDom
+ * test of chunk_and_damp).  A live particle outside xmin <= x <= xmax,
+ * y^2 + z^2 <= r2max (x in window cells) gets dead[i] = 1 and w = 0, so it
+ * deposits nothing; counters[0] (device uint64) counts dead particles.
+ * chm_sp_compact later drops them. */
+int chm_sp_absorb(const int32_t *ix, const float *fx, const float *y,
+                  const float *z, float *w, uint8_t *dead, int64_t n, int win_k,
+                  float win_f, float xmin_cells, float xmax_cells, float r2max,
+                  uint64_t *counters, void *stream);
+/* counters[1] += n - counters[0] (live particles of the step, for rates). */
+int chm_sp_count_live(uint64_t *counters, int64_t n, void *stream);
+/* Stable compaction of the particles with dead[i] == 0 into the *_out
+ * arrays; *n_out (device int64) receives their number.  n < 2^31. */
+int64_t chm_sp_compact_ws_bytes(int64_t n);
+int chm_sp_compact(const int32_t *ix, const float *fx, const float *y,
+                   const float *z, const float *px, const float *py,
+                   const float *pz, const float *w, const uint8_t *dead, int64_t n,
+                   int32_t *ix_out, float *fx_out, float *y_out, float *z_out,
+                   float *px_out, float *py_out, float *pz_out, float *w_out,
+                   int64_t *n_out, void *ws, int64_t ws_bytes, void *stream);
 
 /* Spectral stage on complex64 (nx, nkr, nm, comps) planes. */
 int64_t chm_sp_fb_ws_bytes(int64_t nx, int64_t nr, int64_t nkr, int64_t nm);

@@ -181,3 +181,174 @@ def test_split_steps_track_fp64_form(mods, nsteps):
     a0_sp = s_sp.Data["EB"][:, 1, 0, 2].real.max().item()
     assert abs(a0_sp - a0_ref) < 0.01 * abs(a0_ref)
     assert _lib.load().chm_sp_umma_status() == 0
+
+
+def _sp_particles(torch, n, nx, nr, dr, seed, runs=True):
+    """Split-layout particles: runs of 8 in one cell (as generated cell by
+    cell) or fully random positions; thermal momenta; a few zero weights."""
+    rng = np.random.default_rng(seed)
+    if runs:
+        ncell = (n + 7) // 8
+        cx = rng.integers(-2, nx + 1, ncell).repeat(8)[:n]
+        cr = rng.integers(0, nr - 1, ncell).repeat(8)[:n]
+        fx = (rng.integers(0, 4, n) + 0.5) / 4.0
+        r = (cr + (rng.integers(0, 2, n) + 0.25) / 2.0) * dr
+    else:
+        cx = rng.integers(-2, nx + 1, n)
+        fx = rng.random(n)
+        r = rng.random(n) * (nr - 1) * dr
+    th = rng.random(n) * 2 * np.pi
+    cols = {"ix": cx.astype(np.int32) + 100, "fx": fx.astype(np.float32),
+            "y": (r * np.cos(th)).astype(np.float32), "z": (r * np.sin(th)).astype(np.float32),
+            "px": (0.05 * rng.standard_normal(n)).astype(np.float32),
+            "py": (0.05 * rng.standard_normal(n)).astype(np.float32),
+            "pz": (0.05 * rng.standard_normal(n)).astype(np.float32),
+            "w": (1e-3 * (0.5 + rng.random(n))).astype(np.float32)}
+    cols["w"][rng.random(n) < 0.01] = 0.0
+    return {k: torch.from_numpy(v).cuda() for k, v in cols.items()}
+
+
+@pytest.mark.parametrize("nm,runs,push", [(2, True, 1), (2, False, 1), (1, True, 1), (2, True, 0)])
+def test_cell_run_deposit_equals_generic_kernel(mods, monkeypatch, nm, runs, push):
+    """The cell-run push/deposit kernel (nm 1, 2) and the per-particle kernel
+    agree (accumulators within 1e-6 relative L2, same pushed positions)."""
+    torch, _lib, fm, split = mods
+    nx, nr, dr, n = 64, 32, 0.5, 40000 + 37
+    P0 = _sp_particles(torch, n, nx, nr, dr, 7 + nm, runs)
+    names = ("ix", "fx", "y", "z", "px", "py", "pz", "w")
+    st = _st(torch)
+    sws = torch.empty(_lib.query("chm_sp_scale_ws_bytes"), dtype=torch.uint8, device="cuda")
+    scale = torch.zeros(2, dtype=torch.float64, device="cuda")
+    _lib.call("chm_sp_weight_scale", scale.data_ptr(), P0["w"].data_ptr(), n, sws.data_ptr(),
+              sws.numel(), st)
+    out = {}
+    for variant in ("run", "generic"):
+        if variant == "generic":
+            monkeypatch.setenv("CHIMERA_GB300_DEPOSIT", "generic")
+        else:
+            monkeypatch.delenv("CHIMERA_GB300_DEPOSIT", raising=False)
+        P = {k: v.clone() for k, v in P0.items()}
+        accJ = torch.zeros(nx * nr * nm * 3 * 2, dtype=torch.int64, device="cuda")
+        accR = torch.zeros(nx * nr * nm * 2, dtype=torch.int64, device="cuda")
+        _lib.call("chm_sp_push_deposit", *[P[k].data_ptr() for k in names], n, 100, 0.25,
+                  1 / 0.1, 1 / dr, 0.1, nx, nr, nm, push,
+                  accJ.data_ptr() if push else None, scale.data_ptr() if push else None,
+                  accR.data_ptr(), scale.data_ptr(), st)
+        torch.cuda.synchronize()
+        out[variant] = (accJ.cpu().numpy(), accR.cpu().numpy(),
+                        {k: P[k].cpu().numpy() for k in names})
+    a, b = out["run"], out["generic"]
+    # the cell-run kernel sums a run's values in FP32 before rounding them to
+    # the fixed-point quantum; the generic kernel rounds every particle
+    for u, v in ((a[0], b[0]), (a[1], b[1])):
+        assert rel_l2(u.astype(np.float64), v.astype(np.float64)) < 1e-6
+    assert np.abs(a[1]).sum() > 0 and (not push or np.abs(a[0]).sum() > 0)
+    xa = a[2]["ix"] + a[2]["fx"].astype(np.float64)
+    xb = b[2]["ix"] + b[2]["fx"].astype(np.float64)
+    assert np.abs(xa - xb).max() < 1e-5
+    for k in ("y", "z", "px", "py", "pz", "w"):
+        assert np.allclose(a[2][k], b[2][k], rtol=1e-6, atol=1e-7), k
+
+
+def test_absorb_and_compact(mods):
+    """chm_sp_absorb marks exactly the particles outside the box; compaction
+    keeps the live ones in order and counts them."""
+    torch, _lib, fm, split = mods
+    n, nx, nr, dr = 30011, 64, 32, 0.5
+    P = _sp_particles(torch, n, nx, nr, dr, 3, runs=False)
+    names = ("ix", "fx", "y", "z", "px", "py", "pz", "w")
+    ref = {k: v.cpu().numpy().copy() for k, v in P.items()}
+    dead = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    dead[:50] = 1  # already dead stay dead and are not counted again
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+    st = _st(torch)
+    k, f, xmin, xmax, r2 = 100, 0.25, 8.0, 60.0, (12.0 * dr) ** 2
+    _lib.call("chm_sp_absorb", P["ix"].data_ptr(), P["fx"].data_ptr(), P["y"].data_ptr(),
+              P["z"].data_ptr(), P["w"].data_ptr(), dead.data_ptr(), n, k, f, xmin, xmax, r2,
+              cnt.data_ptr(), st)
+    _lib.call("chm_sp_count_live", cnt.data_ptr(), n, st)
+    xc = (ref["ix"] - k).astype(np.float32) + (ref["fx"] - np.float32(f))
+    r2p = ref["y"] * ref["y"] + ref["z"] * ref["z"]
+    out_box = ~((xc >= xmin) & (xc <= xmax) & (r2p <= np.float32(r2)))
+    dead_ref = out_box.copy()
+    dead_ref[:50] = True
+    newly = out_box.copy()
+    newly[:50] = False
+    torch.cuda.synchronize()
+    assert np.array_equal(dead.cpu().numpy().astype(bool), dead_ref)
+    assert int(cnt[0]) == int(newly.sum())
+    assert int(cnt[1]) == n - int(newly.sum())
+    w = P["w"].cpu().numpy()
+    assert np.all(w[newly] == 0) and np.array_equal(w[~dead_ref], ref["w"][~dead_ref])
+    Q = {k: torch.empty_like(v) for k, v in P.items()}
+    ws = torch.empty(_lib.query("chm_sp_compact_ws_bytes", n), dtype=torch.uint8, device="cuda")
+    n_out = torch.zeros(1, dtype=torch.int64, device="cuda")
+    _lib.call("chm_sp_compact", *[P[k].data_ptr() for k in names], dead.data_ptr(), n,
+              *[Q[k].data_ptr() for k in names], n_out.data_ptr(), ws.data_ptr(), ws.numel(), st)
+    torch.cuda.synchronize()
+    m = int(n_out.item())
+    assert m == int((~dead_ref).sum())
+    for key in names:
+        exp = (ref[key] if key != "w" else w)[~dead_ref]
+        assert np.array_equal(Q[key][:m].cpu().numpy(), exp), key
+
+
+def _window_comps(seed):
+    comps = _lpa_comps(seed)
+    dx = 0.1
+    prof = lambda x: np.interp(x, [-4.0, -3.0, 10.0], [0.0, 1.0, 1.0])  # noqa: E731
+    comps["MovingFrames"] = ({"TimeStep": dx, "Steps": 1, "Velocity": 1.0, "AbsorbLayer": 6,
+                              "AddPlasma": prof, "Features": ("IonsOnTop",)},)
+    return comps
+
+
+def test_split_window_with_injection_tracks_fp64_form(mods):
+    """Moving window with absorption and plasma injection (the demos'
+    AbsorbLayer + AddPlasma + IonsOnTop): same particle counts as the FP64
+    form and fields within 1e-4 after 8 steps, with compactions in between."""
+    torch, _lib, fm, split = mods
+    from chimera_gb300 import ChimeraRun
+    ref = ChimeraRun(_window_comps(2024))
+    run = split.SplitRun(_window_comps(2024))
+    run.compact_every = 3
+    live = 0
+    for i in range(1, 9):
+        np.random.seed(500 + i)  # the same injected plasma in both runs
+        ref.make_step(i)
+        np.random.seed(500 + i)
+        run.make_step(i)
+        live += ref.Particles[0].num_particles
+    assert run.live_particle_steps() == live
+    run.to_fp64()
+    for s_ref, s_sp in ((ref.Particles[0], run.fp.Particles[0]), (ref.Particles[1], run.fp.Particles[1])):
+        assert s_sp.num_particles == s_ref.num_particles
+    err = rel_l2(run.solver.Data["EG_fb"].cpu().numpy(), ref.Solvers[0].Data["EG_fb"].cpu().numpy())
+    assert err < 1e-4, err
+    assert _lib.load().chm_sp_umma_status() == 0
+
+
+@pytest.mark.parametrize("nm,runs", [(2, True), (2, False), (1, True)])
+def test_cell_run_gather_matches_generic_kernel(mods, monkeypatch, nm, runs):
+    """Cell-run gather + Boris (nm 1, 2) against the per-particle kernel."""
+    torch, _lib, fm, split = mods
+    nx, nr, dr, n = 64, 32, 0.5, 40000 + 37
+    P0 = _sp_particles(torch, n, nx, nr, dr, 11 + nm, runs)
+    names = ("ix", "fx", "y", "z", "px", "py", "pz", "w")
+    rng = np.random.default_rng(5)
+    eb = np.asfortranarray((rng.standard_normal((nx, nr, nm, 6)) +
+                            1j * rng.standard_normal((nx, nr, nm, 6))).astype(np.complex64))
+    ebd = torch.from_numpy(eb).cuda()
+    out = {}
+    for variant in ("run", "generic"):
+        if variant == "generic":
+            monkeypatch.setenv("CHIMERA_GB300_DEPOSIT", "generic")
+        else:
+            monkeypatch.delenv("CHIMERA_GB300_DEPOSIT", raising=False)
+        P = {k: v.clone() for k, v in P0.items()}
+        _lib.call("chm_sp_gather_push", *[P[k].data_ptr() for k in names], n, 100, 0.25, 1 / dr,
+                  ebd.data_ptr(), nx, nr, nm, 0.05, _st(torch))
+        torch.cuda.synchronize()
+        out[variant] = np.stack([P[k].cpu().numpy() for k in ("px", "py", "pz")])
+    p0 = np.stack([P0[k].cpu().numpy() for k in ("px", "py", "pz")])
+    assert np.abs(out["run"] - p0).max() > 1e-3  # the fields did push
+    assert np.abs(out["run"] - out["generic"]).max() <= 1e-6 * np.abs(out["generic"]).max()
