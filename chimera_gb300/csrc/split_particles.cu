@@ -112,6 +112,17 @@ __device__ __forceinline__ void deposit_at(const Loc &L, const float *val, int n
   }
 }
 
+// round-to-nearest float -> int64 without the 64-bit conversion unit: below
+// 2^31 the 32-bit conversion, above it the float is an integer and its bits
+// give the value (|v| < 2^62 for accumulator values)
+__device__ __forceinline__ long long f2ll(float v) {
+  if (fabsf(v) < 2147483520.0f) return (long long)__float2int_rn(v);
+  const unsigned u = __float_as_uint(v);
+  const int sh = (int)((u >> 23) & 0xffu) - 127 - 23;
+  const long long r = (long long)((u & 0x7fffffu) | 0x800000u) << min(sh, 39);
+  return (u >> 31) ? -r : r;
+}
+
 struct PushDepArgs {
   SpParts P;
   SpGrid G;
@@ -152,22 +163,24 @@ __device__ __forceinline__ void box_put(const BoxGeo &B, long long plane, int r,
   atomicAdd(&acc[2 * ((pl * B.nr + r) * B.nx + x) + im], (unsigned long long)v);
 }
 
-// Adds the block box into the global accumulators.
+// Adds the block box into the global accumulators: warp w takes the box
+// rows w, w + 8, ... (a row: 2 bnx values of one plane and r), lanes stride
+// along x.
 __device__ void flush_box(const BoxGeo &B, long long nvals) {
-  for (long long t = threadIdx.x; t < nvals; t += blockDim.x) {
-    const unsigned long long v = B.box[t];
-    if (v == 0) continue;
-    const long long c2 = t & 1;
-    const long long b = t >> 1;
-    const long long bx = b % B.bnx;
-    const long long rest = b / B.bnx;
-    const long long br = rest % B.bnr;
-    const long long plane = rest / B.bnr;
+  const int rowlen = 2 * (int)B.bnx, bnr = (int)B.bnr;
+  const int nrows = (int)(nvals / rowlen);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  for (int row = warp; row < nrows; row += nwarp) {
+    const int plane = row / bnr, rr = row - plane * bnr;
     const bool isj = plane < B.nmj;
-    const long long pl = isj ? plane : plane - B.nmj;
-    const i64 e = (pl * B.nr + (br + B.br0)) * B.nx + (bx + B.bx0);
-    unsigned long long *acc = isj ? B.gJ : B.gR;
-    atomicAdd(&acc[2 * e + c2], v);
+    const int pl = isj ? plane : plane - B.nmj;
+    unsigned long long *acc = (isj ? B.gJ : B.gR) +
+                              2 * (((i64)pl * B.nr + (rr + B.br0)) * B.nx + B.bx0);
+    const unsigned long long *src = B.box + (i64)row * rowlen;
+    for (int t = lane; t < rowlen; t += 32) {
+      const unsigned long long v = src[t];
+      if (v) atomicAdd(acc + t, v);
+    }
   }
 }
 
@@ -316,7 +329,7 @@ __global__ void __launch_bounds__(kSpThreads) push_deposit_kernel(PushDepArgs A)
       if (A.dep_j) {
         const Loc L = locate(q.ixh, q.fxh, q.yh, q.zh, A.G);
         deposit_at(L, q.vj, 3, 0, A.G, [&](int plane, int r, int x, float re, float im) {
-          const long long qr = __float2ll_rn(re * geo.sJ), qi = __float2ll_rn(im * geo.sJ);
+          const long long qr = f2ll(re * geo.sJ), qi = f2ll(im * geo.sJ);
           if (Pl.use_box) {
             if (qr) box_put(geo, plane, r, x, 0, qr);
             if (qi) box_put(geo, plane, r, x, 1, qi);
@@ -331,7 +344,7 @@ __global__ void __launch_bounds__(kSpThreads) push_deposit_kernel(PushDepArgs A)
         const Loc L = locate(q.ixn, q.fxn, q.yn, q.zn, A.G);
         const float wv[1] = {w};
         deposit_at(L, wv, 1, 3 * A.G.nm, A.G, [&](int plane, int r, int x, float re, float im) {
-          const long long qr = __float2ll_rn(re * geo.sR), qi = __float2ll_rn(im * geo.sR);
+          const long long qr = f2ll(re * geo.sR), qi = f2ll(im * geo.sR);
           if (Pl.use_box) {
             if (qr) box_put(geo, plane, r, x, 0, qr);
             if (qi) box_put(geo, plane, r, x, 1, qi);
@@ -468,6 +481,27 @@ template <int NM, int NC>
 __device__ __forceinline__ void acc_flush(CellAcc<NM, NC> &c, int plane0, const SpGrid &G,
                                           const BoxGeo &B) {
   if (!c.live) return;
+  c.live = false;
+  const int rr = c.cr - (int)B.br0, xx = c.cx - (int)B.bx0;
+  if (rr >= 0 && rr + 1 < B.bnr && xx >= 0 && xx + 1 < B.bnx) {
+    // all four nodes inside the box (x nodes inside the grid as the box is)
+    const int rs = 2 * (int)B.bnx, ps = rs * (int)B.bnr;
+    unsigned long long *b0 = B.box + (rr * rs + 2 * xx);
+#pragma unroll
+    for (int l = 0; l < NC; ++l)
+#pragma unroll
+      for (int p = 0; p < 2 * NM - 1; ++p) {
+        const int m = (p + 1) >> 1;
+        const int im = (p > 0 && (p & 1) == 0) ? 1 : 0;
+        unsigned long long *bp = b0 + (plane0 + m + G.nm * l) * ps + im;
+#pragma unroll
+        for (int nd = 0; nd < 4; ++nd) {
+          const long long v = f2ll(c.v[l][p][nd]);
+          if (v) atomicAdd(bp + (nd >> 1) * rs + 2 * (nd & 1), (unsigned long long)v);
+        }
+      }
+    return;
+  }
 #pragma unroll
   for (int l = 0; l < NC; ++l)
 #pragma unroll
@@ -477,14 +511,13 @@ __device__ __forceinline__ void acc_flush(CellAcc<NM, NC> &c, int plane0, const 
       const long long plane = plane0 + m + (long long)G.nm * l;
 #pragma unroll
       for (int nd = 0; nd < 4; ++nd) {
-        const long long v = __float2ll_rn(c.v[l][p][nd]);
+        const long long v = f2ll(c.v[l][p][nd]);
         const int j = nd >> 1, k = nd & 1;
         const int gx = c.cx + k;
         if (v == 0 || gx < 0 || gx >= G.nx) continue;
         box_put(B, plane, c.cr + j, gx, im, v);
       }
     }
-  c.live = false;
 }
 
 // val: the particle's values already multiplied by the global scale
@@ -588,7 +621,7 @@ __global__ void __launch_bounds__(kSpThreads, 2) push_deposit_run_kernel(PushDep
         } else {
           deposit_at(L, vs, 3, 0, A.G, [&](int plane, int r, int x, float re, float im) {
             const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
-            const long long qr = __float2ll_rn(re), qi = __float2ll_rn(im);
+            const long long qr = f2ll(re), qi = f2ll(im);
             if (qr) atomicAdd(&A.accJ[2 * e], (unsigned long long)qr);
             if (qi) atomicAdd(&A.accJ[2 * e + 1], (unsigned long long)qi);
           });
@@ -602,7 +635,7 @@ __global__ void __launch_bounds__(kSpThreads, 2) push_deposit_run_kernel(PushDep
         } else {
           deposit_at(L, ws, 1, 0, A.G, [&](int plane, int r, int x, float re, float im) {
             const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
-            const long long qr = __float2ll_rn(re), qi = __float2ll_rn(im);
+            const long long qr = f2ll(re), qi = f2ll(im);
             if (qr) atomicAdd(&A.accR[2 * e], (unsigned long long)qr);
             if (qi) atomicAdd(&A.accR[2 * e + 1], (unsigned long long)qi);
           });

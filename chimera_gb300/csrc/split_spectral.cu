@@ -430,27 +430,14 @@ __global__ void psatd32_kernel(float2 *__restrict__ eg, const float2 *__restrict
 struct Batch32 {
   TcProblem p[64];
   int count;
+  void add(const float2 *A, float2 *C, const float *fac, const TcOperand &B) {
+    p[count++] = TcProblem{reinterpret_cast<const float *>(A), reinterpret_cast<float *>(C), fac, B};
+  }
 };
 
-// scratch of the tensor-core path, set per call from the workspace
-struct Scr {
-  void *p;
-  i64 bytes;
-};
-thread_local Scr g_scr{nullptr, 0};
-
-int gemm32(const Batch32 &b, int M, int N, int K, const TcOperand &bop, int epi,
-           const float2 *shift, cudaStream_t st) {
+int gemm32(const Batch32 &b, int M, int N, int K, int epi, const float2 *shift, cudaStream_t st) {
   if (b.count == 0) return CHM_OK;
-  return tc_gemm_launch(b.p, b.count, M, N, K, bop, epi, shift, g_scr.p, g_scr.bytes, st);
-}
-
-// carves the tensor-core scratch (up to 6 planes of M x K) from a workspace
-bool take_scratch(Ws &W, i64 M, i64 K) {
-  const i64 b = tc_scratch_bytes(M, K, 6);
-  g_scr.p = W.take<char>(b);
-  g_scr.bytes = g_scr.p ? b : 0;
-  return g_scr.p != nullptr;
+  return tc_gemm_launch(b.p, b.count, M, N, K, epi, shift, st);
 }
 
 struct Fb32 {
@@ -471,8 +458,7 @@ extern "C" {
 int64_t chm_sp_fb_ws_bytes(int64_t nx, int64_t nr, int64_t nkr, int64_t nm) {
   const i64 rows = nr - 1 > nkr ? nr - 1 : nkr;
   const i64 plane = 8 * nx * (rows > nkr ? rows : nkr);
-  return 4 * r256(8 * nx) + r256(plane * nm * 6) + 8 * r256(plane * (nm + 2)) +
-         r256(tc_scratch_bytes(2 * nx, rows, 6)) + 8192;
+  return 4 * r256(8 * nx) + r256(plane * nm * 6) + 8 * r256(plane * (nm + 2)) + 8192;
 }
 
 // fb_vec_in / fb_scl_in of a deposit accumulator (ncomp 3 or 1), with
@@ -489,7 +475,7 @@ int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, con
   float2 *shift = W.take<float2>(nx);
   const i64 nrr = nr - 1;
   float2 *tmp = W.take<float2>(nx * nrr * nm * ncomp);
-  if (!tmp || !take_scratch(W, 2 * nx, nrr)) {
+  if (!tmp) {
     set_error("sp_fb_in_acc: workspace exhausted");
     return CHM_ERR_WS;
   }
@@ -510,16 +496,12 @@ int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, con
   int rc = lines32_launch(L, (int)nx, nrr * nm * ncomp, tw, st);
   if (rc) return rc;
   const TcMatrices In = tc_matrices(reinterpret_cast<const chm_sp_ops *>(In_ops));
-  for (i64 m = 0; m < nm; ++m) {
-    Batch32 b{};
+  Batch32 b{};  // every mode and component in one launch
+  for (i64 m = 0; m < nm; ++m)
     for (i64 l = 0; l < ncomp; ++l)
-      b.p[b.count++] = TcProblem{reinterpret_cast<const float *>(tmp + nx * nrr * (m + nm * l)),
-                                 reinterpret_cast<float *>(out_c64) + 2 * nx * nkr * (m + nm * l),
-                                 fact + nx * nkr * m};
-    rc = gemm32(b, (int)(2 * nx), (int)nkr, (int)nrr, In.mode[m], TC_EPI_SHIFT_FAC, shift, st);
-    if (rc) return rc;
-  }
-  return CHM_OK;
+      b.add(tmp + nx * nrr * (m + nm * l), reinterpret_cast<float2 *>(out_c64) + nx * nkr * (m + nm * l),
+            fact + nx * nkr * m, In.mode[m]);
+  return gemm32(b, (int)(2 * nx), (int)nkr, (int)nrr, TC_EPI_SHIFT_FAC, shift, st);
 }
 
 // fb_eb_out + eb_correction (fb_io.f90:182-228, grid_deps.f90:219-266)
@@ -534,23 +516,21 @@ int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double 
   float2 *shift = W.take<float2>(nx);
   const i64 nrr = nr - 1;
   float2 *tmp = W.take<float2>(nx * nrr * nm * 6);
-  if (!tmp || !take_scratch(W, 2 * nx, nkr)) {
+  if (!tmp) {
     set_error("sp_fb_eb_out: workspace exhausted");
     return CHM_ERR_WS;
   }
   shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx); chm::count_launch();
   const TcMatrices Out = tc_matrices(reinterpret_cast<const chm_sp_ops *>(Out_ops));
-  for (i64 m = 0; m < nm; ++m) {
-    Batch32 b{};
+  Batch32 b{};  // every mode and component in one launch
+  for (i64 m = 0; m < nm; ++m)
     for (int l = 0; l < 6; ++l) {
       const float2 *src = (l < 3 ? reinterpret_cast<const float2 *>(e_c64) + nx * nkr * (m + nm * l)
                                  : reinterpret_cast<const float2 *>(b_c64) + nx * nkr * (m + nm * (l - 3)));
-      b.p[b.count++] = TcProblem{reinterpret_cast<const float *>(src),
-                                 reinterpret_cast<float *>(tmp + nx * nrr * (m + nm * l)), nullptr};
+      b.add(src, tmp + nx * nrr * (m + nm * l), nullptr, Out.mode[m]);
     }
-    int rc = gemm32(b, (int)(2 * nx), (int)nrr, (int)nkr, Out.mode[m], TC_EPI_SHIFT, shift, st);
-    if (rc) return rc;
-  }
+  int rc = gemm32(b, (int)(2 * nx), (int)nrr, (int)nkr, TC_EPI_SHIFT, shift, st);
+  if (rc) return rc;
   Lines32 L{};
   L.in = tmp;
   L.in_rows = L.in_rows_tot = (int)nrr;
@@ -601,31 +581,25 @@ int neighbours32(Fb32 &F, const float2 *in, i64 cs, int ncomp, int nin, int nout
                  const float2 *const *refl, float2 *lo[3], float2 *up[3], unsigned char *lo_ok,
                  unsigned char *up_ok) {
   const i64 plane = F.nx * F.nk;
+  Batch32 b{};  // every output mode, neighbour and component in one launch
   for (int m = 0; m < nout; ++m) {
     const int mlo = m - 1 + shift, mhi = m + 1 + shift;
-    Batch32 bl{}, bu{};
     lo_ok[m] = up_ok[m] = 0;
     for (int c = 0; c < ncomp; ++c) {
       const float2 *src = nullptr;
       if (mlo >= 0 && mlo < nin) src = in + c * cs + plane * mlo;
       else if (mlo == -1 && refl) src = refl[c];
       if (src) {
-        bl.p[bl.count++] = TcProblem{reinterpret_cast<const float *>(src),
-                                     reinterpret_cast<float *>(lo[c] + plane * m), nullptr};
+        b.add(src, lo[c] + plane * m, nullptr, F.Dm.mode[m]);
         lo_ok[m] = 1;
       }
       if (mhi >= 0 && mhi < nin) {
-        bu.p[bu.count++] = TcProblem{reinterpret_cast<const float *>(in + c * cs + plane * mhi),
-                                     reinterpret_cast<float *>(up[c] + plane * m), nullptr};
+        b.add(in + c * cs + plane * mhi, up[c] + plane * m, nullptr, F.Dp.mode[m]);
         up_ok[m] = 1;
       }
     }
-    int rc = gemm32(bl, (int)(2 * F.nx), (int)F.nk, (int)F.nk, F.Dm.mode[m], TC_EPI_STORE, nullptr, F.st);
-    if (rc) return rc;
-    rc = gemm32(bu, (int)(2 * F.nx), (int)F.nk, (int)F.nk, F.Dp.mode[m], TC_EPI_STORE, nullptr, F.st);
-    if (rc) return rc;
   }
-  return CHM_OK;
+  return gemm32(b, (int)(2 * F.nx), (int)F.nk, (int)F.nk, TC_EPI_STORE, nullptr, F.st);
 }
 
 }  // namespace
@@ -645,7 +619,7 @@ int chm_sp_fb_grad(void *out_c64, const void *scl_c64, const void *Dp_ops, const
   float2 *lo[3] = {F.ws.take<float2>(plane * nm), nullptr, nullptr};
   float2 *up[3] = {F.ws.take<float2>(plane * nm), nullptr, nullptr};
   float2 *ext = F.ws.take<float2>(plane);
-  if (!ext || !take_scratch(F.ws, 2 * nx, nkr)) {
+  if (!ext) {
     set_error("sp_fb_grad: workspace exhausted");
     return CHM_ERR_WS;
   }
@@ -697,7 +671,7 @@ int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, cons
   }
   float2 *ext[3];
   for (int c = 0; c < 3; ++c) ext[c] = F.ws.take<float2>(plane);
-  if (!ext[2] || !take_scratch(F.ws, 2 * nx, nkr)) {
+  if (!ext[2]) {
     set_error("sp_poisson: workspace exhausted");
     return CHM_ERR_WS;
   }
@@ -733,18 +707,14 @@ int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, cons
     // gradient back onto nm modes, fused with the J update
     if (nm > 1) { reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[0], scl + plane, nx, nkr); chm::count_launch(); }
     else { zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[0], plane); chm::count_launch(); }
+    Batch32 bg{};  // both neighbours of every mode in one launch
     for (int m = 0; m < (int)nm; ++m) {
-      Batch32 bl{}, bu{};
       const float2 *lsrc = (m - 1 >= 0) ? scl + plane * (m - 1) : ext[0];
-      bl.p[bl.count++] = TcProblem{reinterpret_cast<const float *>(lsrc),
-                                   reinterpret_cast<float *>(lo[0] + plane * m), nullptr};
-      bu.p[bu.count++] = TcProblem{reinterpret_cast<const float *>(scl + plane * (m + 1)),
-                                   reinterpret_cast<float *>(up[0] + plane * m), nullptr};
-      rc = gemm32(bl, (int)(2 * nx), (int)nkr, (int)nkr, F.Dm.mode[m], TC_EPI_STORE, nullptr, F.st);
-      if (rc) return rc;
-      rc = gemm32(bu, (int)(2 * nx), (int)nkr, (int)nkr, F.Dp.mode[m], TC_EPI_STORE, nullptr, F.st);
-      if (rc) return rc;
+      bg.add(lsrc, lo[0] + plane * m, nullptr, F.Dm.mode[m]);
+      bg.add(scl + plane * (m + 1), up[0] + plane * m, nullptr, F.Dp.mode[m]);
     }
+    rc = gemm32(bg, (int)(2 * nx), (int)nkr, (int)nkr, TC_EPI_STORE, nullptr, F.st);
+    if (rc) return rc;
     GradArgs A{};
     A.nx = nx;
     A.nk = nkr;
@@ -784,7 +754,7 @@ int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf, const void *Dp
     lo[c] = F.ws.take<float2>(plane * nm);
     up[c] = F.ws.take<float2>(plane * nm);
   }
-  if (!take_scratch(F.ws, 2 * nx, nkr)) {
+  if (!up[2]) {
     set_error("sp_rot_b: workspace exhausted");
     return CHM_ERR_WS;
   }

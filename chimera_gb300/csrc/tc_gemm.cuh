@@ -18,19 +18,20 @@ struct TcMatrices {
   TcOperand mode[16];
 };
 
+// One product of a batch; every problem of a batch has the same M, N, K and
+// epilogue but its own operator (mode).
 struct TcProblem {
   const float *A;    // (M, K) column-major, ld = M
   float *C;          // (M, N) column-major, ld = M
   const float *fac;  // optional (M/2, N) real factor
+  TcOperand B;
 };
 
 enum { TC_EPI_STORE = 0, TC_EPI_SHIFT = 1, TC_EPI_SHIFT_FAC = 2 };
 
-// scratch: caller-provided device memory for the split A operand,
-// tc_scratch_bytes(M, K, count) bytes
-int tc_gemm_launch(const TcProblem *p, int count, int M, int N, int K, const TcOperand &B, int epi,
-                   const float2 *shift, void *scratch, int64_t scratch_bytes, cudaStream_t st);
-int64_t tc_scratch_bytes(int64_t M, int64_t K, int64_t count);
+// Batched product; no scratch (the split of A happens inside the kernel).
+int tc_gemm_launch(const TcProblem *p, int count, int M, int N, int K, int epi,
+                   const float2 *shift, cudaStream_t st);
 
 // Host view of a prepared operator set (chm_sp_ops) as per-mode operands.
 TcMatrices tc_matrices(const chm_sp_ops *ops);

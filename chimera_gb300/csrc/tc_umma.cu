@@ -4,18 +4,21 @@
 //   operator mode; computed as sum_{i+j<=2} A_i B_j with A = A0+A1+A2 and
 //   B = B0+B1+B2 the 3-term BF16 splits, accumulated in FP32 in TMEM.
 //
-// Structure:
-//   1. split kernel: A (FP32) -> three BF16 planes written in the tensor-core
-//      operand layout (K-major, core matrices of 8 rows x 16 bytes), one
-//      128 x 32 tile per (M tile, K block), contiguous;
-//   2. MMA kernel: one CTA per 128-row M tile and problem.  Thread 0 streams
-//      the A and B tiles of each 32-wide K block into a 3-stage shared-memory
-//      ring with bulk-copy TMA (cp.async.bulk, completion on an mbarrier),
-//      issues 12 tcgen05.mma (6 term pairs x 2 K steps of 16) per block into
-//      a TMEM accumulator and releases stages with tcgen05.commit; the four
-//      warps then read TMEM (tcgen05.ld 32x32b) and apply the epilogue.
-// Every mbarrier wait has an iteration limit; on timeout the CTA records an
-// error, waits (bounded) for its own transfers, frees its TMEM and returns.
+// One CTA computes a 256-row tile of one problem of a batch, as two 128-row
+// accumulators of up to 256 FP32 columns each in TMEM:
+//   - warps 0-7 (one thread per row) load the FP32 A block of every 32-wide
+//     K step, split it into the three BF16 terms and store them into the
+//     stage in the tensor-core operand layout (K-major core matrices of
+//     8 rows x 16 bytes);
+//   - warp 8 lane 0 streams the prepared B terms of the step with bulk-copy
+//     TMA (cp.async.bulk, completion on an mbarrier) and issues the 24
+//     tcgen05.mma of the step (6 term pairs x 2 K halves x 2 row halves),
+//     releasing the stage with tcgen05.commit;
+//   - warps 0-7 then read the accumulators (tcgen05.ld 32x32b) and apply the
+//     epilogue.
+// Two stages double-buffer the K loop.  Every mbarrier wait has an iteration
+// limit; on timeout the CTA records an error, waits (bounded) for its own
+// bulk copies, frees its TMEM and returns.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -25,62 +28,19 @@ using namespace chm;
 
 namespace {
 
-constexpr int TM = 128;        // rows per CTA (UMMA M)
-constexpr int KB = 32;         // K block (elements)
-constexpr int STAGES = 3;
-constexpr int kSplitThreads = 256;
+constexpr int TH = 128;                   // rows per accumulator (UMMA M)
+constexpr int TM = 2 * TH;                // rows per CTA
+constexpr int KB = 32;                    // K step (elements)
+constexpr int STAGES = 2;
+constexpr int kProducers = TM;            // warps 0-7, one row each
+constexpr int kThreads = kProducers + 32; // + warp 8: B copies and MMA issue
+constexpr int kMaxBatch = 64;
 constexpr long long kSpinLimit = 1LL << 20;  // try_wait polls; each may block briefly
+constexpr uint32_t kAHalfBytes = TH * KB * 2;       // one term, one row half
+constexpr uint32_t kATermBytes = 2 * kAHalfBytes;   // one term, both halves
+constexpr uint32_t kABytes = 3 * kATermBytes;       // the A part of a stage
 
 __device__ int g_umma_error;  // first failing CTA records a code here
-
-// ----------------------------------------------------------------------
-// A -> 3 BF16 planes in tile layout
-// ----------------------------------------------------------------------
-struct SplitProb {
-  const float *A[64];
-  __nv_bfloat16 *T[64];  // 3 planes of tiles, plane stride = tile_stride
-  int count;
-};
-
-// tile (mt, kb) of a plane holds rows mt*128.., k kb*32..; element (r, k) at
-// ((r/8)*(KB/8) + k/8)*64 + (r%8)*8 + k%8
-__global__ void __launch_bounds__(kSplitThreads)
-    split_a_kernel(SplitProb P, int M, int K, int Kp, long long plane_elems) {
-  __shared__ float tile[KB][TM + 1];
-  const int prob = blockIdx.z;
-  const int mt = blockIdx.x, kb = blockIdx.y;
-  const float *A = P.A[prob];
-  // coalesced load along m
-  for (int t = threadIdx.x; t < TM * KB; t += kSplitThreads) {
-    const int r = t % TM, k = t / TM;
-    const int gm = mt * TM + r, gk = kb * KB + k;
-    tile[k][r] = (gm < M && gk < K) ? A[gm + (long long)gk * M] : 0.0f;
-  }
-  __syncthreads();
-  const int nkb = Kp / KB;
-  const long long tbase = ((long long)mt * nkb + kb) * (TM * KB);
-  // each thread writes 8 consecutive k of one row (16 bytes) per term
-  for (int t = threadIdx.x; t < TM * (KB / 8); t += kSplitThreads) {
-    const int r = t % TM, kg = t / TM;
-    __align__(16) __nv_bfloat16 o0[8], o1[8], o2[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const float v = tile[kg * 8 + q][r];
-      const __nv_bfloat16 b0 = __float2bfloat16_rn(v);
-      const float r1 = v - __bfloat162float(b0);
-      const __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
-      const float r2 = r1 - __bfloat162float(b1);
-      o0[q] = b0;
-      o1[q] = b1;
-      o2[q] = __float2bfloat16_rn(r2);
-    }
-    const long long off = tbase + ((long long)(r / 8) * (KB / 8) + kg) * 64 + (r % 8) * 8;
-    __nv_bfloat16 *T = P.T[prob];
-    *reinterpret_cast<uint4 *>(T + off) = *reinterpret_cast<uint4 *>(o0);
-    *reinterpret_cast<uint4 *>(T + plane_elems + off) = *reinterpret_cast<uint4 *>(o1);
-    *reinterpret_cast<uint4 *>(T + 2 * plane_elems + off) = *reinterpret_cast<uint4 *>(o2);
-  }
-}
 
 // ----------------------------------------------------------------------
 // PTX helpers
@@ -97,6 +57,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                "r"(bytes)
                : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 // bounded wait for the phase with parity `parity` to complete
@@ -163,47 +127,55 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
                : "memory");
 }
 
+__device__ __forceinline__ uint32_t bf16_bits(__nv_bfloat16 b) {
+  return (uint32_t)__bfloat16_as_ushort(b);
+}
+
 // ----------------------------------------------------------------------
 // MMA kernel
 // ----------------------------------------------------------------------
 struct UmmaProb {
-  const __nv_bfloat16 *At[64];  // split A planes (3 consecutive, plane stride)
-  float *C[64];
-  const float *fac[64];
-  int count;
+  const float *A;
+  float *C;
+  const float *fac;
+  const __nv_bfloat16 *B[3];  // split B terms of this problem's mode
+};
+
+struct UmmaBatch {
+  UmmaProb p[kMaxBatch];
 };
 
 struct UmmaArgs {
   int M, N, Np, K, Kp;
-  long long a_plane;             // elements per A term plane
-  const __nv_bfloat16 *B[3];     // B term tiles for this mode
   const float2 *shift;
   int epi;
   uint32_t tmem_cols;
 };
 
-__global__ void __launch_bounds__(128, 1) umma_kernel(UmmaProb P, UmmaArgs A) {
+__global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant__ UmmaBatch P,
+                                                           UmmaArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], done;
+  __shared__ __align__(8) uint64_t afull[STAGES], bfull[STAGES], empty[STAGES], done;
   __shared__ uint32_t tmem_base;
   __shared__ int fail;
   const int prob = blockIdx.y, mt = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t a_bytes = TM * KB * 2;          // one A term tile
-  const uint32_t b_bytes = (uint32_t)A.Np * KB * 2;  // one B term tile
-  const uint32_t stage_bytes = 3 * a_bytes + 3 * b_bytes;
+  const uint32_t b_term = (uint32_t)A.Np * KB * 2;  // one B term of a stage
+  const uint32_t stage_bytes = kABytes + 3 * b_term;
   const int nkb = A.Kp / KB;
+  const UmmaProb &Q = P.p[prob];
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
-      mbar_init(&full[s], 1);
+      mbar_init(&afull[s], kProducers);
+      mbar_init(&bfull[s], 1);
       mbar_init(&empty[s], 1);
     }
     mbar_init(&done, 1);
     fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == kProducers / 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base)),
                  "r"(A.tmem_cols)
@@ -215,26 +187,83 @@ __global__ void __launch_bounds__(128, 1) umma_kernel(UmmaProb P, UmmaArgs A) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
 
-  if (threadIdx.x == 0) {
-    const __nv_bfloat16 *Abase = P.At[prob];
-    auto load_stage = [&](int kb) {
-      unsigned char *st = smem + (size_t)(kb % STAGES) * stage_bytes;
-      mbar_expect_tx(&full[kb % STAGES], stage_bytes);
-      for (int t = 0; t < 3; ++t) {
-        const __nv_bfloat16 *src = Abase + (long long)t * A.a_plane + ((long long)mt * nkb + kb) * (TM * KB);
-        bulk_g2s(st + t * a_bytes, src, a_bytes, &full[kb % STAGES]);
-      }
-      for (int t = 0; t < 3; ++t) {
-        const __nv_bfloat16 *src = A.B[t] + (long long)kb * A.Np * KB;
-        bulk_g2s(st + 3 * a_bytes + t * b_bytes, src, b_bytes, &full[kb % STAGES]);
+  if (threadIdx.x < kProducers) {
+    // ---- producers: FP32 A row -> three BF16 terms in the stage
+    const int r = threadIdx.x, h = r / TH, rr = r % TH;
+    const long long gm = (long long)mt * TM + r;
+    const bool row_ok = gm < A.M;
+    const float *Arow = Q.A + (row_ok ? gm : 0);
+    float v[KB];
+    auto load = [&](int kb) {
+#pragma unroll
+      for (int k = 0; k < KB; ++k) {
+        const int gk = kb * KB + k;
+        v[k] = (row_ok && gk < A.K) ? Arow[(long long)gk * A.M] : 0.0f;
       }
     };
-    const uint32_t idesc = idesc_bf16(TM, A.Np);
+    load(0);
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int s = kb % STAGES;
+      bool ok = true;
+      if (kb >= STAGES) ok = mbar_wait(&empty[s], (uint32_t)(kb / STAGES - 1) & 1u);
+      if (!ok) {
+        fail = 1;
+        atomicCAS(&g_umma_error, 0, 3);
+      } else {
+        unsigned char *st = smem + (size_t)s * stage_bytes + h * kAHalfBytes;
+#pragma unroll
+        for (int kg = 0; kg < KB / 8; ++kg) {
+          uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            uint32_t t0[2], t1[2], t2[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+              const float x = v[kg * 8 + 2 * q + e];
+              const __nv_bfloat16 b0 = __float2bfloat16_rn(x);
+              const float r1 = x - __bfloat162float(b0);
+              const __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
+              const float r2 = r1 - __bfloat162float(b1);
+              t0[e] = bf16_bits(b0);
+              t1[e] = bf16_bits(b1);
+              t2[e] = bf16_bits(__float2bfloat16_rn(r2));
+            }
+            w0[q] = t0[0] | (t0[1] << 16);
+            w1[q] = t1[0] | (t1[1] << 16);
+            w2[q] = t2[0] | (t2[1] << 16);
+          }
+          // element (rr, k) of a 128 x 32 term block at ((rr/8)*4 + k/8)*64 + (rr%8)*8 + k%8
+          const uint32_t off = (((rr >> 3) * (KB / 8) + kg) * 64 + (rr & 7) * 8) * 2;
+          *reinterpret_cast<uint4 *>(st + off) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+          *reinterpret_cast<uint4 *>(st + kATermBytes + off) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+          *reinterpret_cast<uint4 *>(st + 2 * kATermBytes + off) =
+              make_uint4(w2[0], w2[1], w2[2], w2[3]);
+        }
+      }
+      // generic-proxy stores -> visible to the tensor core (async proxy)
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(&afull[s]);
+      if (kb + 1 < nkb) load(kb + 1);
+    }
+  } else if (threadIdx.x == kProducers) {
+    // ---- B streaming and MMA issue
+    const uint32_t idesc = idesc_bf16(TH, A.Np);
+    int last_b[STAGES];
+    for (int s = 0; s < STAGES; ++s) last_b[s] = -1;
+    auto load_b = [&](int kb) {
+      const int s = kb % STAGES;
+      unsigned char *st = smem + (size_t)s * stage_bytes + kABytes;
+      mbar_expect_tx(&bfull[s], 3 * b_term);
+      for (int t = 0; t < 3; ++t)
+        bulk_g2s(st + t * b_term, Q.B[t] + (long long)kb * A.Np * KB, b_term, &bfull[s]);
+      last_b[s] = kb;
+    };
     bool ok = true;
-    for (int kb = 0; kb < STAGES && kb < nkb; ++kb) load_stage(kb);
+    for (int kb = 0; kb < STAGES && kb < nkb; ++kb) load_b(kb);
     for (int kb = 0; kb < nkb && ok; ++kb) {
       const int s = kb % STAGES;
-      if (!mbar_wait(&full[s], (uint32_t)(kb / STAGES) & 1u)) {
+      const uint32_t par = (uint32_t)(kb / STAGES) & 1u;
+      if (!mbar_wait(&bfull[s], par) || !mbar_wait(&afull[s], par)) {
         ok = false;
         break;
       }
@@ -246,20 +275,25 @@ __global__ void __launch_bounds__(128, 1) umma_kernel(UmmaProb P, UmmaArgs A) {
       for (int q = 0; q < 6; ++q) {
 #pragma unroll
         for (int ks = 0; ks < KB / 16; ++ks) {
-          const uint64_t ad = smem_desc(st + pi[q] * a_bytes + ks * 256, 128, (KB / 8) * 128);
-          const uint64_t bd = smem_desc(st + 3 * a_bytes + pj[q] * b_bytes + ks * 256, 128, (KB / 8) * 128);
-          umma_bf16(tmem, ad, bd, idesc, (kb > 0 || q > 0 || ks > 0) ? 1u : 0u);
+          const uint64_t bd = smem_desc(st + kABytes + pj[q] * b_term + ks * 256, 128, (KB / 8) * 128);
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            const uint64_t ad =
+                smem_desc(st + pi[q] * kATermBytes + hh * kAHalfBytes + ks * 256, 128, (KB / 8) * 128);
+            umma_bf16(tmem + (uint32_t)(hh * A.Np), ad, bd, idesc,
+                      (kb > 0 || q > 0 || ks > 0) ? 1u : 0u);
+          }
         }
       }
       umma_commit(&empty[s]);
-      // refill the stage of the previous block once its MMAs have drained
+      // refill the stage of the previous step once its MMAs have drained
       if (kb >= 1 && kb - 1 + STAGES < nkb) {
         const int sp = (kb - 1) % STAGES;
         if (!mbar_wait(&empty[sp], (uint32_t)((kb - 1) / STAGES) & 1u)) {
           ok = false;
           break;
         }
-        load_stage(kb - 1 + STAGES);
+        load_b(kb - 1 + STAGES);
       }
     }
     umma_commit(&done);
@@ -267,25 +301,27 @@ __global__ void __launch_bounds__(128, 1) umma_kernel(UmmaProb P, UmmaArgs A) {
       fail = 1;
       atomicCAS(&g_umma_error, 0, 1);
       // let the bulk copies already issued land before the CTA exits
-      for (int s = 0; s < STAGES; ++s) mbar_wait(&full[s], 0), mbar_wait(&full[s], 1);
+      for (int s = 0; s < STAGES; ++s)
+        if (last_b[s] >= 0) mbar_wait(&bfull[s], (uint32_t)(last_b[s] / STAGES) & 1u);
     }
   }
   __syncthreads();
-  // all MMAs complete before the accumulator is read (bounded wait)
+  // all MMAs complete before the accumulators are read (bounded wait)
   const bool drained = mbar_wait(&done, 0);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const bool use = __syncthreads_and(drained && !fail);
   if (!drained && threadIdx.x == 0) atomicCAS(&g_umma_error, 0, 2);
-  if (use) {
-    const int row = warp * 32 + lane;  // TMEM lane = row of the tile
-    const int gm = mt * TM + row;
+  if (use && threadIdx.x < kProducers) {
+    const int qd = warp & 3, hh = warp >> 2;       // TMEM lane quarter, row half
+    const int row = hh * TH + qd * 32 + lane;      // row of the tile
+    const long long gm = (long long)mt * TM + row;
     float2 sh = make_float2(1.f, 0.f);
     if (A.epi != TC_EPI_STORE && gm < A.M) sh = A.shift[gm >> 1];
-    float *C = P.C[prob];
-    const float *fac = P.fac[prob];
+    float *C = Q.C;
+    const float *fac = Q.fac;
     for (int c0 = 0; c0 < A.Np; c0 += 16) {
       uint32_t v[16];
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      const uint32_t taddr = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(hh * A.Np + c0);
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
           : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
@@ -296,22 +332,22 @@ __global__ void __launch_bounds__(128, 1) umma_kernel(UmmaProb P, UmmaArgs A) {
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         float x = __uint_as_float(v[j]);
+        const int n = c0 + j;
         if (A.epi != TC_EPI_STORE) {
           // rows 2x (re) and 2x+1 (im) sit in adjacent lanes
           const float other = __shfl_xor_sync(0xffffffffu, x, 1);
           const float re = (row & 1) ? other : x, im = (row & 1) ? x : other;
           x = (row & 1) ? (re * sh.y + im * sh.x) : (re * sh.x - im * sh.y);
-          const int n = c0 + j;
-          if (A.epi == TC_EPI_SHIFT_FAC && gm < A.M && n < A.N) x *= fac[(gm >> 1) + (long long)(A.M >> 1) * n];
+          if (A.epi == TC_EPI_SHIFT_FAC && gm < A.M && n < A.N)
+            x *= fac[(gm >> 1) + (long long)(A.M >> 1) * n];
         }
-        const int n = c0 + j;
         if (gm < A.M && n < A.N) C[gm + (long long)n * A.M] = x;
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) {
+  if (warp == kProducers / 32) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(A.tmem_cols)
                  : "memory");
   }
@@ -323,15 +359,9 @@ inline long long rup(long long a, long long b) { return (a + b - 1) / b * b; }
 
 namespace chm {
 
-int64_t tc_scratch_bytes(int64_t M, int64_t K, int64_t count) {
-  const int64_t c = count < 64 ? count : 64;
-  return (int64_t)3 * rup(M, TM) * rup(K, KB) * 2 * c + 256;
-}
-
-int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, const TcOperand &B, int epi,
-                   const float2 *shift, void *scratch, int64_t scratch_bytes, cudaStream_t st) {
+int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, const float2 *shift,
+                   cudaStream_t st) {
   const int Np = (int)rup(N, 16), Kp = (int)rup(K, KB);
-  const int Kp_ops = Kp;
   if (Np > 256) {
     set_error("umma: N must be <= 256");
     return CHM_ERR_RANGE;
@@ -340,49 +370,37 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, const TcO
     set_error("umma: M must be even (complex rows)");
     return CHM_ERR_ARG;
   }
+  for (int i = 0; i < count; ++i)
+    if (!p[i].B.bf[0] || !p[i].B.bf[1] || !p[i].B.bf[2] || p[i].B.K != K || p[i].B.N != N) {
+      set_error("umma: problem %d has no prepared %dx%d operator", i, K, N);
+      return CHM_ERR_ARG;
+    }
   const int mt = (int)((M + TM - 1) / TM);
-  const long long a_plane = (long long)mt * TM * Kp;  // elements per term plane
-  (void)Kp_ops;
-  if (!scratch || scratch_bytes < tc_scratch_bytes(M, K, count)) {
-    set_error("umma: scratch of %lld bytes < %lld required", (long long)scratch_bytes,
-              (long long)tc_scratch_bytes(M, K, count));
-    return CHM_ERR_WS;
-  }
-  struct {
-    void *p;
-  } S{scratch};
-  const uint32_t a_bytes = TM * KB * 2, b_bytes = (uint32_t)Np * KB * 2;
-  const size_t smem = (size_t)STAGES * (3 * a_bytes + 3 * b_bytes) + 1024;
+  const uint32_t b_term = (uint32_t)Np * KB * 2;
+  const size_t smem = (size_t)STAGES * (kABytes + 3 * b_term) + 1024;
   cudaFuncSetAttribute(umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   uint32_t cols = 32;
-  while (cols < (uint32_t)Np) cols <<= 1;
-  for (int c0 = 0; c0 < count; c0 += 64) {
-    const int cnt = count - c0 < 64 ? count - c0 : 64;
-    SplitProb sp{};
-    UmmaProb up{};
-    sp.count = up.count = cnt;
+  while (cols < (uint32_t)(2 * Np)) cols <<= 1;
+  UmmaArgs ua{};
+  ua.M = M;
+  ua.N = N;
+  ua.Np = Np;
+  ua.K = K;
+  ua.Kp = Kp;
+  ua.shift = shift;
+  ua.epi = epi;
+  ua.tmem_cols = cols;
+  for (int c0 = 0; c0 < count; c0 += kMaxBatch) {
+    const int cnt = count - c0 < kMaxBatch ? count - c0 : kMaxBatch;
+    UmmaBatch ub;
     for (int i = 0; i < cnt; ++i) {
-      __nv_bfloat16 *T = reinterpret_cast<__nv_bfloat16 *>(S.p) + (size_t)3 * a_plane * i;
-      sp.A[i] = p[c0 + i].A;
-      sp.T[i] = T;
-      up.At[i] = T;
-      up.C[i] = p[c0 + i].C;
-      up.fac[i] = p[c0 + i].fac;
+      const TcProblem &q = p[c0 + i];
+      ub.p[i] = UmmaProb{q.A, q.C, q.fac,
+                         {reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[0]),
+                          reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[1]),
+                          reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[2])}};
     }
-    split_a_kernel<<<dim3(mt, Kp / KB, cnt), kSplitThreads, 0, st>>>(sp, M, K, Kp, a_plane);
-    count_launch();
-    UmmaArgs ua{};
-    ua.M = M;
-    ua.N = N;
-    ua.Np = Np;
-    ua.K = K;
-    ua.Kp = Kp;
-    ua.a_plane = a_plane;
-    for (int t = 0; t < 3; ++t) ua.B[t] = reinterpret_cast<const __nv_bfloat16 *>(B.bf[t]);
-    ua.shift = shift;
-    ua.epi = epi;
-    ua.tmem_cols = cols;
-    umma_kernel<<<dim3(mt, cnt), 128, smem, st>>>(up, ua);
+    umma_kernel<<<dim3(mt, cnt), kThreads, smem, st>>>(ub, ua);
     count_launch();
   }
   cudaError_t e = cudaGetLastError();
