@@ -190,6 +190,7 @@ struct Pushed {
   int ixh, ixn;
   float fxh, fxn, yh, zh, yn, zn;
   float vj[3];
+  bool moving;  // nonzero momentum (particles at rest carry no current)
 };
 
 __device__ __forceinline__ Pushed push_vals(const PushDepArgs &A, int ix, float fx, float y, float z,
@@ -210,6 +211,7 @@ __device__ __forceinline__ Pushed push_vals(const PushDepArgs &A, int ix, float 
   o.zn = z + pz * dtg;
   // grid_deps.f90:42: particles at rest deposit no current
   const bool moving = (fabsf(px) + fabsf(py) + fabsf(pz)) != 0.0f;
+  o.moving = moving;
   const float wg = moving ? w * ig : 0.0f;
   o.vj[0] = px * wg;
   o.vj[1] = py * wg;
@@ -613,7 +615,7 @@ __global__ void __launch_bounds__(kSpThreads, 2) push_deposit_run_kernel(PushDep
         oz[j] = u.zn;
       }
       if (q.w[j] == 0.0f) continue;
-      if (DJ) {
+      if (DJ && u.moving) {  // grid_deps.f90:42: no current from particles at rest
         const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, A.G);
         const float vs[3] = {u.vj[0] * Pl.sJ, u.vj[1] * Pl.sJ, u.vj[2] * Pl.sJ};
         if (Pl.use_box) {

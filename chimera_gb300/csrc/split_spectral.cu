@@ -32,12 +32,19 @@ __device__ __forceinline__ float2 fmi(float2 a) { return make_float2(-a.y, a.x);
 struct Plan {
   int n, ns;
   int radix[24];
+  int log2n;  // >= 0 when n is a power of two (radix-4/2 passes, shift index math)
 };
 
 bool make_plan(int n, Plan *p) {
   if (n < 1 || n > kMaxN) return false;
   p->n = n;
   p->ns = 0;
+  p->log2n = -1;
+  if ((n & (n - 1)) == 0 && n >= 4) {
+    int l = 0;
+    while ((1 << l) < n) ++l;
+    p->log2n = l;
+  }
   int m = n;
   while (m % 4 == 0) {
     p->radix[p->ns++] = 4;
@@ -141,6 +148,72 @@ __device__ float2 *run32(const Plan &P, float2 *a, float2 *b, const float2 *tw, 
   return a;
 }
 
+// Power-of-two Stockham passes: the index arithmetic of pass32 with shifts
+// and the twiddles read from a shared-memory table.
+__device__ void pass4p(const float2 *__restrict__ src, float2 *__restrict__ dst, int n, int l2n,
+                       int lNs, const float2 *__restrict__ tw, int sign) {
+  const int nb = n >> 2, Ns = 1 << lNs;
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+    const int k = j & (Ns - 1);
+    const int tstep = k << (l2n - lNs - 2);
+    const int base = ((j >> lNs) << (lNs + 2)) + k;
+    float2 v[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      float2 a = src[j + r * nb];
+      if (r > 0) a = fmul(a, tw32(tw, r * tstep, sign));
+      v[r] = a;
+    }
+    float2 a0 = fadd(v[0], v[2]), a1 = fsub(v[0], v[2]);
+    float2 a2 = fadd(v[1], v[3]), a3 = fsub(v[1], v[3]);
+    float2 a3r = sign < 0 ? make_float2(a3.y, -a3.x) : make_float2(-a3.y, a3.x);
+    dst[base] = fadd(a0, a2);
+    dst[base + Ns] = fadd(a1, a3r);
+    dst[base + 2 * Ns] = fsub(a0, a2);
+    dst[base + 3 * Ns] = fsub(a1, a3r);
+  }
+}
+
+__device__ void pass2p(const float2 *__restrict__ src, float2 *__restrict__ dst, int n, int l2n,
+                       int lNs, const float2 *__restrict__ tw, int sign) {
+  const int nb = n >> 1, Ns = 1 << lNs;
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+    const int k = j & (Ns - 1);
+    const int tstep = k << (l2n - lNs - 1);
+    const int base = ((j >> lNs) << (lNs + 1)) + k;
+    const float2 a = src[j], b = fmul(src[j + nb], tw32(tw, tstep, sign));
+    dst[base] = fadd(a, b);
+    dst[base + Ns] = fsub(a, b);
+  }
+}
+
+__device__ float2 *run32p(const Plan &P, float2 *a, float2 *b, const float2 *tw, int sign) {
+  int lNs = 0;
+  for (; lNs + 2 <= P.log2n; lNs += 2) {
+    __syncthreads();
+    pass4p(a, b, P.n, P.log2n, lNs, tw, sign);
+    float2 *t = a;
+    a = b;
+    b = t;
+  }
+  if (lNs < P.log2n) {
+    __syncthreads();
+    pass2p(a, b, P.n, P.log2n, lNs, tw, sign);
+    float2 *t = a;
+    a = b;
+    b = t;
+  }
+  __syncthreads();
+  return a;
+}
+
+// 64-bit fixed-point value -> FP32 (two 32-bit conversions, no 64-bit unit)
+__device__ __forceinline__ float fix2f(long long v) {
+  const int hi = (int)(v >> 32);
+  const unsigned lo = (unsigned)(v & 0xffffffffULL);
+  return fmaf((float)hi, 4294967296.0f, (float)lo);
+}
+
 // Line sources/sinks of the FP32 FFT.
 struct Lines32 {
   // input: either complex64 rows or a 64-bit deposit accumulator
@@ -158,36 +231,54 @@ struct Lines32 {
   const float *filtr;
 };
 
+template <bool POW2>
 __global__ void lines32_kernel(Plan P, const float2 *__restrict__ tw, Lines32 L) {
   extern __shared__ __align__(16) float2 sm32[];
   const int n = P.n;
   float2 *a = sm32, *b = sm32 + n;
+  if (POW2) {
+    // exp(-2 pi i t / n) for the power-of-two passes
+    float2 *tws = sm32 + 2 * n;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+      float sv, cv;
+      sincospif(2.0f * (float)t / (float)n, &sv, &cv);
+      tws[t] = make_float2(cv, -sv);
+    }
+    tw = tws;  // the first pass synchronises before reading it
+  }
   const i64 line = blockIdx.x;
   const i64 ib = line / L.in_rows, ir = line % L.in_rows;
   const i64 row = ib * L.in_rows_tot + ir + L.in_row_off;
   if (L.acc) {
     // deposit accumulator: value / scale with the ghost fold row1 -= row0
-    const double inv = 1.0 / L.acc_scale[0];
-    const double inv2 = L.acc2 ? 1.0 / L.acc2_scale[0] : 0.0;
+    // (the scales are powers of two, so the FP32 inverses are exact)
+    const float inv = 1.0f / (float)L.acc_scale[0];
+    const float inv2 = L.acc2 ? 1.0f / (float)L.acc2_scale[0] : 0.0f;
     const bool fold = (ir + L.in_row_off) == 1;
     const i64 row0 = ib * L.in_rows_tot;
+    const longlong2 *A1 = reinterpret_cast<const longlong2 *>(L.acc);
+    const longlong2 *A2 = reinterpret_cast<const longlong2 *>(L.acc2);
     for (int x = threadIdx.x; x < n; x += blockDim.x) {
       const i64 e = row * n + x;
-      double re = (double)L.acc[2 * e] * inv, im = (double)L.acc[2 * e + 1] * inv;
-      if (L.acc2) {
-        re += (double)L.acc2[2 * e] * inv2;
-        im += (double)L.acc2[2 * e + 1] * inv2;
+      const longlong2 q = A1[e];
+      float re = fix2f(q.x) * inv, im = fix2f(q.y) * inv;
+      if (A2) {
+        const longlong2 q2 = A2[e];
+        re += fix2f(q2.x) * inv2;
+        im += fix2f(q2.y) * inv2;
       }
       if (fold) {
         const i64 e0 = row0 * n + x;
-        re -= (double)L.acc[2 * e0] * inv;
-        im -= (double)L.acc[2 * e0 + 1] * inv;
-        if (L.acc2) {
-          re -= (double)L.acc2[2 * e0] * inv2;
-          im -= (double)L.acc2[2 * e0 + 1] * inv2;
+        const longlong2 q0 = A1[e0];
+        re -= fix2f(q0.x) * inv;
+        im -= fix2f(q0.y) * inv;
+        if (A2) {
+          const longlong2 q2 = A2[e0];
+          re -= fix2f(q2.x) * inv2;
+          im -= fix2f(q2.y) * inv2;
         }
       }
-      a[x] = make_float2((float)re, (float)im);
+      a[x] = make_float2(re, im);
     }
   } else {
     const float2 *src = L.in + row * (i64)n;
@@ -197,7 +288,7 @@ __global__ void lines32_kernel(Plan P, const float2 *__restrict__ tw, Lines32 L)
       a[x] = v;
     }
   }
-  float2 *res = run32(P, a, b, tw, L.sign);
+  float2 *res = POW2 ? run32p(P, a, b, tw, L.sign) : run32(P, a, b, tw, L.sign);
   if (L.filt_mode >= 0) {
     for (int x = threadIdx.x; x < L.nxfilt; x += blockDim.x)
       if (L.filt_mode == 0 || L.filt_mode == 2) res[x] = fscl(res[x], L.filtr[x]);
@@ -205,7 +296,7 @@ __global__ void lines32_kernel(Plan P, const float2 *__restrict__ tw, Lines32 L)
     for (int x = threadIdx.x; x < L.nxfilt; x += blockDim.x)
       if (L.filt_mode == 1 || L.filt_mode == 2) res[n - 1 - x] = fscl(res[n - 1 - x], L.filtr[x]);
     float2 *other = (res == a) ? b : a;
-    res = run32(P, res, other, tw, -1);
+    res = POW2 ? run32p(P, res, other, tw, -1) : run32(P, res, other, tw, -1);
   }
   const i64 ob = line / L.out_rows, orow = line % L.out_rows;
   float2 *dst = L.out + (ob * L.out_rows_tot + orow + L.out_row_off) * (i64)n;
@@ -237,11 +328,19 @@ int lines32_launch(const Lines32 &L, int n, i64 nlines, float2 *tw, cudaStream_t
     return CHM_ERR_RANGE;
   }
   if (nlines <= 0) return CHM_OK;
-  twiddle32_kernel<<<(n + 255) / 256, 256, 0, st>>>(tw, n); chm::count_launch();
-  const size_t smem = 2 * (size_t)n * sizeof(float2);
-  cudaFuncSetAttribute(lines32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int threads = n >= 1024 ? 512 : (n >= 256 ? 256 : 128);
-  lines32_kernel<<<(unsigned)nlines, threads, smem, st>>>(P, tw, L); chm::count_launch();
+  if (P.log2n >= 0) {
+    // twiddle table built per block in shared memory
+    const size_t smem = 3 * (size_t)n * sizeof(float2);
+    cudaFuncSetAttribute(lines32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    lines32_kernel<true><<<(unsigned)nlines, threads, smem, st>>>(P, nullptr, L);
+  } else {
+    twiddle32_kernel<<<(n + 255) / 256, 256, 0, st>>>(tw, n); chm::count_launch();
+    const size_t smem = 2 * (size_t)n * sizeof(float2);
+    cudaFuncSetAttribute(lines32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    lines32_kernel<false><<<(unsigned)nlines, threads, smem, st>>>(P, tw, L);
+  }
+  chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -268,16 +367,6 @@ inline i64 r256(i64 b) { return (b + 255) / 256 * 256; }
 // -------------------------------------------------------------------------
 // Elementwise / combine kernels
 // -------------------------------------------------------------------------
-__global__ void reflect32_kernel(float2 *__restrict__ dst, const float2 *__restrict__ src, i64 nx, i64 nk) {
-  const i64 n = nx * nk;
-  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x) {
-    i64 x = t % nx, k = t / nx;
-    i64 xs = x == 0 ? 0 : nx - x;
-    float2 v = src[xs + k * nx];
-    dst[t] = make_float2(-v.x, v.y);
-  }
-}
-
 __global__ void zero32_kernel(float2 *p, i64 n) {
   for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x)
     p[t] = make_float2(0.f, 0.f);
@@ -430,8 +519,9 @@ __global__ void psatd32_kernel(float2 *__restrict__ eg, const float2 *__restrict
 struct Batch32 {
   TcProblem p[64];
   int count;
-  void add(const float2 *A, float2 *C, const float *fac, const TcOperand &B) {
-    p[count++] = TcProblem{reinterpret_cast<const float *>(A), reinterpret_cast<float *>(C), fac, B};
+  void add(const float2 *A, float2 *C, const float *fac, const TcOperand &B, int reflect = 0) {
+    p[count++] = TcProblem{reinterpret_cast<const float *>(A), reinterpret_cast<float *>(C), fac, B,
+                           reflect};
   }
 };
 
@@ -575,8 +665,9 @@ int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx, const float *
 namespace {
 
 // lower / upper neighbour products of `ncomp` components for output modes
-// 0..nout-1 (input mode m-1+shift / m+1+shift, D mode m); the lower
-// neighbour of input mode -1 is the reflected m = 1 plane `refl[c]`.
+// 0..nout-1 (input mode m-1+shift / m+1+shift, D mode m).  The lower
+// neighbour of input mode -1 is the m = 1 plane `refl[c]` read reflected by
+// the product; without one (a single mode) that product is zero.
 int neighbours32(Fb32 &F, const float2 *in, i64 cs, int ncomp, int nin, int nout, int shift,
                  const float2 *const *refl, float2 *lo[3], float2 *up[3], unsigned char *lo_ok,
                  unsigned char *up_ok) {
@@ -586,12 +677,15 @@ int neighbours32(Fb32 &F, const float2 *in, i64 cs, int ncomp, int nin, int nout
     const int mlo = m - 1 + shift, mhi = m + 1 + shift;
     lo_ok[m] = up_ok[m] = 0;
     for (int c = 0; c < ncomp; ++c) {
-      const float2 *src = nullptr;
-      if (mlo >= 0 && mlo < nin) src = in + c * cs + plane * mlo;
-      else if (mlo == -1 && refl) src = refl[c];
-      if (src) {
-        b.add(src, lo[c] + plane * m, nullptr, F.Dm.mode[m]);
+      if (mlo >= 0 && mlo < nin) {
+        b.add(in + c * cs + plane * mlo, lo[c] + plane * m, nullptr, F.Dm.mode[m]);
         lo_ok[m] = 1;
+      } else if (mlo == -1 && refl) {
+        b.add(refl[c], lo[c] + plane * m, nullptr, F.Dm.mode[m], 1);
+        lo_ok[m] = 1;
+      } else if (mlo == -1) {
+        zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(lo[c] + plane * m, plane);
+        chm::count_launch();
       }
       if (mhi >= 0 && mhi < nin) {
         b.add(in + c * cs + plane * mhi, up[c] + plane * m, nullptr, F.Dp.mode[m]);
@@ -618,16 +712,13 @@ int chm_sp_fb_grad(void *out_c64, const void *scl_c64, const void *Dp_ops, const
   const float2 *s = reinterpret_cast<const float2 *>(scl_c64);
   float2 *lo[3] = {F.ws.take<float2>(plane * nm), nullptr, nullptr};
   float2 *up[3] = {F.ws.take<float2>(plane * nm), nullptr, nullptr};
-  float2 *ext = F.ws.take<float2>(plane);
-  if (!ext) {
+  if (!up[0]) {
     set_error("sp_fb_grad: workspace exhausted");
     return CHM_ERR_WS;
   }
-  if (nm > 1) { reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext, s + plane, nx, nkr); chm::count_launch(); }
-  else { zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext, plane); chm::count_launch(); }
-  const float2 *refl[3] = {ext, nullptr, nullptr};
+  const float2 *refl[3] = {s + plane, nullptr, nullptr};
   unsigned char lok[16], uok[16];
-  int rc = neighbours32(F, s, 0, 1, (int)nm, (int)nm, 0, refl, lo, up, lok, uok);
+  int rc = neighbours32(F, s, 0, 1, (int)nm, (int)nm, 0, nm > 1 ? refl : nullptr, lo, up, lok, uok);
   if (rc) return rc;
   GradArgs A{};
   A.nx = nx;
@@ -669,25 +760,17 @@ int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, cons
     lo[c] = F.ws.take<float2>(plane * ns);
     up[c] = F.ws.take<float2>(plane * ns);
   }
-  float2 *ext[3];
-  for (int c = 0; c < 3; ++c) ext[c] = F.ws.take<float2>(plane);
-  if (!ext[2]) {
+  if (!up[2]) {
     set_error("sp_poisson: workspace exhausted");
     return CHM_ERR_WS;
   }
   for (int it = 0; it < iters; ++it) {
     // divergence on nm + 1 modes
-    if (nm > 1) {
-      reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[1], J + cs + plane, nx, nkr); chm::count_launch();
-      reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[2], J + 2 * cs + plane, nx, nkr); chm::count_launch();
-    } else {
-      zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[1], plane); chm::count_launch();
-      zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[2], plane); chm::count_launch();
-    }
-    const float2 *refl23[3] = {ext[1], ext[2], nullptr};
+    const float2 *refl23[3] = {J + cs + plane, J + 2 * cs + plane, nullptr};
     float2 *lo23[3] = {lo[1], lo[2], nullptr}, *up23[3] = {up[1], up[2], nullptr};
     DivArgs D{};
-    int rc = neighbours32(F, J + cs, cs, 2, (int)nm, ns, 0, refl23, lo23, up23, D.lo_ok, D.up_ok);
+    int rc = neighbours32(F, J + cs, cs, 2, (int)nm, ns, 0, nm > 1 ? refl23 : nullptr, lo23, up23,
+                          D.lo_ok, D.up_ok);
     if (rc) return rc;
     for (int ms = 0; ms < ns; ++ms)
       if (!(ms < (int)nm - 1)) D.up_ok[ms] = 0;
@@ -704,13 +787,19 @@ int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, cons
     D.kx = kx;
     D.scl = scl;
     div32_kernel<<<grid_for(plane * ns, 256), 256, 0, F.st>>>(D); chm::count_launch();
-    // gradient back onto nm modes, fused with the J update
-    if (nm > 1) { reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[0], scl + plane, nx, nkr); chm::count_launch(); }
-    else { zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[0], plane); chm::count_launch(); }
+    // gradient of the nm + 1 scalar modes back onto nm modes, fused with the
+    // J update; the m = -1 neighbour of mode 0 is scalar mode 1 reflected
+    // (zero with a single mode)
     Batch32 bg{};  // both neighbours of every mode in one launch
     for (int m = 0; m < (int)nm; ++m) {
-      const float2 *lsrc = (m - 1 >= 0) ? scl + plane * (m - 1) : ext[0];
-      bg.add(lsrc, lo[0] + plane * m, nullptr, F.Dm.mode[m]);
+      if (m >= 1) {
+        bg.add(scl + plane * (m - 1), lo[0] + plane * m, nullptr, F.Dm.mode[m]);
+      } else if (nm > 1) {
+        bg.add(scl + plane, lo[0], nullptr, F.Dm.mode[0], 1);
+      } else {
+        zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(lo[0], plane);
+        chm::count_launch();
+      }
       bg.add(scl + plane * (m + 1), up[0] + plane * m, nullptr, F.Dp.mode[m]);
     }
     rc = gemm32(bg, (int)(2 * nx), (int)nkr, (int)nkr, TC_EPI_STORE, nullptr, F.st);
@@ -749,7 +838,7 @@ int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf, const void *Dp
   const i64 plane = nx * nkr;
   const i64 cs = plane * nm;
   const float2 *G = reinterpret_cast<const float2 *>(G_c64);
-  float2 *lo[3], *up[3], *ext[3];
+  float2 *lo[3], *up[3];
   for (int c = 0; c < 3; ++c) {
     lo[c] = F.ws.take<float2>(plane * nm);
     up[c] = F.ws.take<float2>(plane * nm);
@@ -758,14 +847,9 @@ int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf, const void *Dp
     set_error("sp_rot_b: workspace exhausted");
     return CHM_ERR_WS;
   }
-  for (int c = 0; c < 3; ++c) {
-    ext[c] = F.ws.take<float2>(plane);
-    if (nm > 1) { reflect32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[c], G + c * cs + plane, nx, nkr); chm::count_launch(); }
-    else { zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(ext[c], plane); chm::count_launch(); }
-  }
-  const float2 *refl[3] = {ext[0], ext[1], ext[2]};
+  const float2 *refl[3] = {G + plane, G + cs + plane, G + 2 * cs + plane};
   unsigned char lok[16], uok[16];
-  int rc = neighbours32(F, G, cs, 3, (int)nm, (int)nm, 0, refl, lo, up, lok, uok);
+  int rc = neighbours32(F, G, cs, 3, (int)nm, (int)nm, 0, nm > 1 ? refl : nullptr, lo, up, lok, uok);
   if (rc) return rc;
   RotArgs A{};
   A.nx = nx;

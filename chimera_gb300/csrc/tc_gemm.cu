@@ -39,7 +39,18 @@ __global__ void __launch_bounds__(kThreads)
     for (int t = threadIdx.x; t < TB_M * TB_K; t += kThreads) {
       int mm = t % TB_M, kk = t / TB_M;
       int gm = m0 + mm, gk = k0 + kk;
-      As[kk][mm] = (gm < M && gk < K) ? P.A[gm + (i64)gk * M] : 0.0f;
+      float a = 0.0f;
+      if (gm < M && gk < K) {
+        int src = gm;
+        float sgn = 1.0f;
+        if (P.reflect) {
+          const int x = gm >> 1;
+          src = 2 * (x == 0 ? 0 : (M >> 1) - x) + (gm & 1);
+          if ((gm & 1) == 0) sgn = -1.0f;
+        }
+        a = sgn * P.A[src + (i64)gk * M];
+      }
+      As[kk][mm] = a;
     }
     for (int t = threadIdx.x; t < TB_N * TB_K; t += kThreads) {
       int kk = t % TB_K, nn = t / TB_K;
@@ -231,7 +242,7 @@ int chm_sp_gemm(float *C, const float *A, const chm_sp_ops *ops, int64_t mode, i
   (void)ws;
   (void)ws_bytes;
   TcMatrices T = tc_matrices(ops);
-  TcProblem p{A, C, nullptr, T.mode[mode]};
+  TcProblem p{A, C, nullptr, T.mode[mode], 0};
   return launch(&p, 1, (int)M, p.B.N, p.B.K, TC_EPI_STORE, nullptr, as_stream(stream), engine);
 }
 

@@ -25,6 +25,10 @@ struct TcProblem {
   float *C;          // (M, N) column-major, ld = M
   const float *fac;  // optional (M/2, N) real factor
   TcOperand B;
+  // read A as the reflected complex plane: row (x, c) of A is
+  // (c ? 1 : -1) * row ((M/2 - x) mod M/2, c) of the stored plane, the
+  // m = -1 neighbour of a mode-1 field (fb_math.f90 reflection)
+  int reflect;
 };
 
 enum { TC_EPI_STORE = 0, TC_EPI_SHIFT = 1, TC_EPI_SHIFT_FAC = 2 };

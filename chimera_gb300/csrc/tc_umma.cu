@@ -139,6 +139,7 @@ struct UmmaProb {
   float *C;
   const float *fac;
   const __nv_bfloat16 *B[3];  // split B terms of this problem's mode
+  int reflect;                // read A reflected (see TcProblem)
 };
 
 struct UmmaBatch {
@@ -152,6 +153,7 @@ struct UmmaArgs {
   uint32_t tmem_cols;
 };
 
+template <int EPI>
 __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant__ UmmaBatch P,
                                                            UmmaArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -192,7 +194,14 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
     const int r = threadIdx.x, h = r / TH, rr = r % TH;
     const long long gm = (long long)mt * TM + r;
     const bool row_ok = gm < A.M;
-    const float *Arow = Q.A + (row_ok ? gm : 0);
+    long long src = gm;
+    uint32_t neg = 0;  // sign flip of the BF16 terms (reflected real part)
+    if (Q.reflect && row_ok) {
+      const long long x = gm >> 1, nxh = A.M >> 1;
+      src = 2 * (x == 0 ? 0 : nxh - x) + (gm & 1);
+      if ((gm & 1) == 0) neg = 0x80008000u;
+    }
+    const float *Arow = Q.A + src;
     float v[KB];
     auto load = [&](int kb) {
 #pragma unroll
@@ -228,9 +237,9 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
               t1[e] = bf16_bits(b1);
               t2[e] = bf16_bits(__float2bfloat16_rn(r2));
             }
-            w0[q] = t0[0] | (t0[1] << 16);
-            w1[q] = t1[0] | (t1[1] << 16);
-            w2[q] = t2[0] | (t2[1] << 16);
+            w0[q] = (t0[0] | (t0[1] << 16)) ^ neg;
+            w1[q] = (t1[0] | (t1[1] << 16)) ^ neg;
+            w2[q] = (t2[0] | (t2[1] << 16)) ^ neg;
           }
           // element (rr, k) of a 128 x 32 term block at ((rr/8)*4 + k/8)*64 + (rr%8)*8 + k%8
           const uint32_t off = (((rr >> 3) * (KB / 8) + kg) * 64 + (rr & 7) * 8) * 2;
@@ -316,10 +325,20 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
     const int row = hh * TH + qd * 32 + lane;      // row of the tile
     const long long gm = (long long)mt * TM + row;
     float2 sh = make_float2(1.f, 0.f);
-    if (A.epi != TC_EPI_STORE && gm < A.M) sh = A.shift[gm >> 1];
+    if (EPI != TC_EPI_STORE && gm < A.M) sh = A.shift[gm >> 1];
     float *C = Q.C;
     const float *fac = Q.fac;
+    const bool rok = gm < A.M;
     for (int c0 = 0; c0 < A.Np; c0 += 16) {
+      // factors of the 16 columns loaded before the accumulator wait
+      float fv[16];
+      if (EPI == TC_EPI_SHIFT_FAC) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int n = c0 + j;
+          fv[j] = (rok && n < A.N) ? __ldg(fac + (gm >> 1) + (long long)(A.M >> 1) * n) : 1.0f;
+        }
+      }
       uint32_t v[16];
       const uint32_t taddr = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(hh * A.Np + c0);
       asm volatile(
@@ -333,15 +352,14 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
       for (int j = 0; j < 16; ++j) {
         float x = __uint_as_float(v[j]);
         const int n = c0 + j;
-        if (A.epi != TC_EPI_STORE) {
+        if (EPI != TC_EPI_STORE) {
           // rows 2x (re) and 2x+1 (im) sit in adjacent lanes
           const float other = __shfl_xor_sync(0xffffffffu, x, 1);
           const float re = (row & 1) ? other : x, im = (row & 1) ? x : other;
           x = (row & 1) ? (re * sh.y + im * sh.x) : (re * sh.x - im * sh.y);
-          if (A.epi == TC_EPI_SHIFT_FAC && gm < A.M && n < A.N)
-            x *= fac[(gm >> 1) + (long long)(A.M >> 1) * n];
+          if (EPI == TC_EPI_SHIFT_FAC) x *= fv[j];
         }
-        if (gm < A.M && n < A.N) C[gm + (long long)n * A.M] = x;
+        if (rok && n < A.N) C[gm + (long long)n * A.M] = x;
       }
     }
   }
@@ -378,7 +396,10 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
   const int mt = (int)((M + TM - 1) / TM);
   const uint32_t b_term = (uint32_t)Np * KB * 2;
   const size_t smem = (size_t)STAGES * (kABytes + 3 * b_term) + 1024;
-  cudaFuncSetAttribute(umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  void (*kern)(const UmmaBatch, UmmaArgs) =
+      epi == TC_EPI_STORE ? umma_kernel<TC_EPI_STORE>
+                          : (epi == TC_EPI_SHIFT ? umma_kernel<TC_EPI_SHIFT> : umma_kernel<TC_EPI_SHIFT_FAC>);
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   uint32_t cols = 32;
   while (cols < (uint32_t)(2 * Np)) cols <<= 1;
   UmmaArgs ua{};
@@ -398,9 +419,10 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
       ub.p[i] = UmmaProb{q.A, q.C, q.fac,
                          {reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[0]),
                           reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[1]),
-                          reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[2])}};
+                          reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[2])},
+                         q.reflect};
     }
-    umma_kernel<<<dim3(mt, cnt), kThreads, smem, st>>>(ub, ua);
+    kern<<<dim3(mt, cnt), kThreads, smem, st>>>(ub, ua);
     count_launch();
   }
   cudaError_t e = cudaGetLastError();
