@@ -42,6 +42,9 @@ WORKLOAD = "lwfa_nx2048_nr256_m2_ppc2x2x8"
 
 SIZES = {  # name: (nx, nkr, ppc)
     "cfg2": (2048, 256, (2, 2, 8)),
+    # quarter radius: 4.2M electrons (134 MB of split-form particle state,
+    # above the 129 MB L2) and ~3 GB on the device, for ncu captures
+    "prof": (2048, 64, (2, 2, 8)),
     "small": (512, 64, (2, 2, 4)),
 }
 
@@ -188,6 +191,11 @@ SPLIT_BYTES = {"push_electrons": 32 + 16,  # read ix,fx,y,z,p,w; write ix,fx,y,z
                "gather_push": 32 + 12}    # read ix,fx,y,z,p,w; write p
 FP64_BYTES = {"push_velocs": 48 + 48 + 24, "push_coords": 24 + 24 + 24 + 24,
               "dep_curr": 24 + 24 + 8, "dep_dens": 24 + 8, "proj_fld": 24 + 8 + 48 + 48}
+# DRAM bytes (read + write) per particle of the dominant split-form stage,
+# from one ncu --set full capture of the quarter-radius case (--size prof,
+# 4.13M particles per species; traffic grows with the particle count):
+# electrons (push + J + rho) 179.5 MB, still ions (rho) 89.5 MB
+SPLIT_TRAFFIC = {"push_electrons": 179.5e6 / 4128768, "deposit_still": 89.5e6 / 4128768}
 GEMM_STAGES = ("chm_fb_graddiv", "chm_fb_rot", "chm_fb_grad", "chm_fb_div", "chm_fb_in",
                "chm_fb_out", "chm_fb_eb_out", "chm_sp_poisson", "chm_sp_fb_in_acc",
                "chm_sp_fb_eb_out", "chm_sp_rot_b", "chm_sp_fb_grad")
@@ -234,6 +242,10 @@ def stage_roofline(form, prof, nprof, n_e, n_i, peaks, peak_kind):
     top = dict(rows[0]) if rows else {"stage": None}
     top["kernel"] = top.pop("stage")
     top["traffic"] = None
+    if form == "split" and top.get("kernel") == "chm_sp_push_deposit":
+        top["traffic"] = n_e * SPLIT_TRAFFIC["push_electrons"] + n_i * SPLIT_TRAFFIC["deposit_still"]
+        top["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
+                                 "quarter-radius case, scaled by particle count")
     top["peak_source"] = f"MEASURED_PEAKS.json ({peak_kind})" if top.get("bound") != "fp64" else \
         "FP64 FMA probe on this pool (1.20 TFLOP/s)"
     top["stages"] = rows
@@ -341,8 +353,9 @@ def run_gb300(args):
     for i in range(1, args.warmup + 1):
         run.make_step(i)
     torch.cuda.synchronize()
-    # L2: the particle state (~1.9 GB for the electrons alone) is far larger
-    # than the 129 MB L2, so every step streams from HBM.
+    # L2: the particle state (0.53 GB per species in the split form, 1.9 GB
+    # in the FP64 form) is far larger than the 129 MB L2, so every step
+    # streams from HBM.
     clocks = ClockSampler(local)
     clocks.start()
     barrier(world)
@@ -484,7 +497,7 @@ def main():
     ap.add_argument("--form", default="split", choices=["fp64", "split"],
                     help="fp64 = plain FP64 form; split = split-precision form")
     ap.add_argument("--size", default="cfg2", choices=sorted(SIZES),
-                    help="cfg2 = the benchmark workload; small = a reduced case for profiling")
+                    help="cfg2 = the benchmark workload; prof, small = reduced cases for profiling")
     args = ap.parse_args()
     global WORKLOAD_SIZE, WORKLOAD
     WORKLOAD_SIZE = args.size
