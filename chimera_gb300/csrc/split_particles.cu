@@ -653,31 +653,140 @@ __global__ void __launch_bounds__(kSpThreads, 2) push_deposit_run_kernel(PushDep
   flush_box(geo, Pl.nvals);
 }
 
-// Global scale 2^(61 - ceil(log2 B)), B = sum |w| (deterministic order).
-__global__ void sp_wsum_kernel(const float *__restrict__ w, i64 n, double *__restrict__ partial) {
-  __shared__ double sh[256];
-  const i64 per = (n + gridDim.x - 1) / gridDim.x;
-  const i64 b0 = blockIdx.x * per, b1 = min(n, b0 + per);
-  double s = 0.0;
-  for (i64 i = b0 + threadIdx.x; i < b1; i += blockDim.x) s += fabs((double)w[i]);
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int st = 128; st > 0; st >>= 1) {
-    if (threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+// Weight sums for the global scale 2^(61 - ceil(log2 B)), B = sum |w|, in a
+// fixed order: block b sums [b R, (b+1) R) (R a multiple of 16), thread t the
+// 16-particle chunks b R + 16 t + 4096 k in FP32, the block adds its threads'
+// sums in FP64 in a fixed tree, the final kernel adds the block sums.  With
+// ABSORB the same pass applies the absorbing boundary first (species.py:
+// 351-398, SimDom test): a live particle outside xmin <= x <= xmax,
+// r^2 <= r2max (window cells, (k, f) convention) is marked dead and its
+// weight zeroed, so it deposits nothing until a compaction drops it;
+// counters[0] counts the dead particles.
+constexpr int kWsThreads = 256;
+constexpr int kWsChunk = 16;
+constexpr int kWsMaxBlocks = 4096;
+
+struct AbsorbBox {
+  int win_k;
+  float win_f, xmin, xmax, r2max;
+};
+
+__device__ __forceinline__ bool outside(const AbsorbBox &Bx, int ix, float fx, float y, float z) {
+  const float xc = (float)(ix - Bx.win_k) + (fx - Bx.win_f);
+  const float r2 = y * y + z * z;
+  return !(xc >= Bx.xmin && xc <= Bx.xmax && r2 <= Bx.r2max);
 }
 
-__global__ void sp_scale_kernel(const double *__restrict__ partial, int np, double *out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
+template <bool ABSORB>
+__global__ void __launch_bounds__(kWsThreads) weights_kernel(SpParts P, uint8_t *__restrict__ dead,
+                                                             AbsorbBox Bx, i64 R,
+                                                             double *__restrict__ partial,
+                                                             unsigned long long *counters) {
+  const i64 b0 = (i64)blockIdx.x * R, b1 = min(P.n, b0 + R);
+  float s = 0.0f;
+  unsigned cnt = 0;
+  for (i64 c = b0 + (i64)threadIdx.x * kWsChunk; c < b1; c += (i64)kWsThreads * kWsChunk) {
+    const int m = (int)min((i64)kWsChunk, b1 - c);
+    if (m == kWsChunk) {
+      float wv[16];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 t = *reinterpret_cast<const float4 *>(P.w + c + 4 * q);
+        wv[4 * q] = t.x, wv[4 * q + 1] = t.y, wv[4 * q + 2] = t.z, wv[4 * q + 3] = t.w;
+      }
+      if (ABSORB) {
+        uint4 dv = *reinterpret_cast<const uint4 *>(dead + c);
+        uint8_t *db = reinterpret_cast<uint8_t *>(&dv);
+        bool changed = false;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int4 ixq = *reinterpret_cast<const int4 *>(P.ix + c + 4 * q);
+          const float4 fq = *reinterpret_cast<const float4 *>(P.fx + c + 4 * q);
+          const float4 yq = *reinterpret_cast<const float4 *>(P.y + c + 4 * q);
+          const float4 zq = *reinterpret_cast<const float4 *>(P.z + c + 4 * q);
+          const int xi[4] = {ixq.x, ixq.y, ixq.z, ixq.w};
+          const float xf[4] = {fq.x, fq.y, fq.z, fq.w}, yy[4] = {yq.x, yq.y, yq.z, yq.w},
+                      zz[4] = {zq.x, zq.y, zq.z, zq.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int j = 4 * q + e;
+            if (!db[j] && outside(Bx, xi[e], xf[e], yy[e], zz[e])) {
+              db[j] = 1;
+              wv[j] = 0.0f;
+              ++cnt;
+              changed = true;
+            }
+          }
+        }
+        if (changed) {
+          *reinterpret_cast<uint4 *>(dead + c) = dv;
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            *reinterpret_cast<float4 *>(P.w + c + 4 * q) =
+                make_float4(wv[4 * q], wv[4 * q + 1], wv[4 * q + 2], wv[4 * q + 3]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kWsChunk; ++j) s += fabsf(wv[j]);
+    } else {
+      for (int j = 0; j < m; ++j) {
+        const i64 i = c + j;
+        float w = P.w[i];
+        if (ABSORB && !dead[i] && outside(Bx, P.ix[i], P.fx[i], P.y[i], P.z[i])) {
+          dead[i] = 1;
+          P.w[i] = 0.0f;
+          w = 0.0f;
+          ++cnt;
+        }
+        s += fabsf(w);
+      }
+    }
+  }
+  double d = (double)s;
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+  __shared__ double wsm[kWsThreads / 32];
+  if ((threadIdx.x & 31) == 0) wsm[threadIdx.x >> 5] = d;
+  if (ABSORB) {
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&counters[0], (unsigned long long)cnt);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < kWsThreads / 32; ++k) t += wsm[k];
+    partial[blockIdx.x] = t;
+  }
+}
+
+// sum of the block sums (fixed order: 4 consecutive per thread, then a fixed
+// tree) -> out[0] = 2^min(61 - ceil(log2 B), 120), out[1] = B
+__global__ void __launch_bounds__(1024) sp_scale_kernel(const double *__restrict__ partial, int np,
+                                                        double *out) {
+  __shared__ double wsm[32];
+  double d = 0.0;
+  for (int i = threadIdx.x * 4; i < min(np, (int)threadIdx.x * 4 + 4); ++i) d += partial[i];
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+  if ((threadIdx.x & 31) == 0) wsm[threadIdx.x >> 5] = d;
+  __syncthreads();
+  if (threadIdx.x == 0) {
     double B = 0.0;
-    for (int i = 0; i < np; ++i) B += partial[i];
+    for (int k = 0; k < 32; ++k) B += wsm[k];
     if (!(B > 0.0) || !isfinite(B)) B = 1.0;
     // the exponent stays inside the FP32 range the deposit kernels use
     out[0] = ldexp(1.0, min(61 - ceil_log2(B), 120));
     out[1] = B;
   }
+}
+
+// blocks and per-block range of the fixed partition for n particles
+inline void ws_partition(i64 n, int *nblocks, i64 *R) {
+  i64 nb = (n + 4095) / 4096;
+  if (nb > kWsMaxBlocks) nb = kWsMaxBlocks;
+  if (nb < 1) nb = 1;
+  i64 r = (n + nb - 1) / nb;
+  r = (r + kWsChunk - 1) / kWsChunk * kWsChunk;
+  *nblocks = (int)nb;
+  *R = r;
 }
 
 // Boris rotation (particle_tools.f90:18-56) of one momentum in FP32: 1/gamma
@@ -889,30 +998,6 @@ __global__ void to_f64_kernel(SpParts P, double *__restrict__ x, i64 x_cs, i64 x
   }
 }
 
-// Absorbing boundary (species.py:351-398, SimDom test) in place: a live
-// particle outside xmin <= x <= xmax, r^2 <= r2max (window-relative cell
-// units of the (k, f) convention) is marked dead and its weight zeroed, so
-// that it deposits nothing until a compaction drops it.  counters[0] counts
-// the dead particles.
-__global__ void __launch_bounds__(256) absorb_kernel(SpParts P, uint8_t *__restrict__ dead,
-                                                     int win_k, float win_f, float xmin_cells,
-                                                     float xmax_cells, float r2max,
-                                                     unsigned long long *counters) {
-  unsigned cnt = 0;
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < P.n; i += (i64)gridDim.x * blockDim.x) {
-    if (dead[i]) continue;
-    const float xc = (float)(P.ix[i] - win_k) + (P.fx[i] - win_f);
-    const float r2 = P.y[i] * P.y[i] + P.z[i] * P.z[i];
-    if (!(xc >= xmin_cells && xc <= xmax_cells && r2 <= r2max)) {
-      dead[i] = 1;
-      P.w[i] = 0.0f;
-      ++cnt;
-    }
-  }
-  cnt = __reduce_add_sync(0xffffffffu, cnt);
-  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&counters[0], (unsigned long long)cnt);
-}
-
 // counters[1] += n - counters[0]: live particles of this step
 __global__ void live_steps_kernel(unsigned long long *counters, i64 n) {
   if (threadIdx.x == 0 && blockIdx.x == 0) counters[1] += (unsigned long long)n - counters[0];
@@ -1008,7 +1093,7 @@ extern "C" {
 // The split-form particle entry points take the eight SoA arrays in the
 // order ix, fx, y, z, px, py, pz, w (n particles).
 
-int64_t chm_sp_scale_ws_bytes(void) { return 8 * 512 + 256; }
+int64_t chm_sp_scale_ws_bytes(void) { return 8 * (int64_t)kWsMaxBlocks + 256; }
 
 int chm_sp_weight_scale(double *scale2, const float *w, int64_t n, void *ws, int64_t ws_bytes,
                         void *stream) {
@@ -1016,13 +1101,18 @@ int chm_sp_weight_scale(double *scale2, const float *w, int64_t n, void *ws, int
               "sp_weight_scale: bad args");
   cudaStream_t st = as_stream(stream);
   double *partial = reinterpret_cast<double *>(ws);
+  int nb = 1;
   if (n > 0) {
     CHM_REQUIRE(w, "sp_weight_scale: null weights");
-    sp_wsum_kernel<<<512, 256, 0, st>>>(w, n, partial); chm::count_launch();
+    i64 R;
+    ws_partition(n, &nb, &R);
+    SpParts P{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, const_cast<float *>(w), n};
+    weights_kernel<false><<<nb, kWsThreads, 0, st>>>(P, nullptr, AbsorbBox{}, R, partial, nullptr);
+    chm::count_launch();
   } else {
-    cudaMemsetAsync(partial, 0, 8 * 512, st);
+    cudaMemsetAsync(partial, 0, 8, st);
   }
-  sp_scale_kernel<<<1, 32, 0, st>>>(partial, 512, scale2); chm::count_launch();
+  sp_scale_kernel<<<1, 1024, 0, st>>>(partial, nb, scale2); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -1151,16 +1241,31 @@ int chm_sp_to_f64(const int32_t *ix, const float *fx, const float *y, const floa
 
 int chm_sp_absorb(const int32_t *ix, const float *fx, const float *y, const float *z, float *w,
                   uint8_t *dead, int64_t n, int win_k, float win_f, float xmin_cells,
-                  float xmax_cells, float r2max, uint64_t *counters, void *stream) {
-  CHM_REQUIRE(n >= 0 && counters, "sp_absorb: bad args");
-  if (n == 0) return CHM_OK;
-  CHM_REQUIRE(ix && fx && y && z && w && dead, "sp_absorb: null pointer");
-  SpParts P{const_cast<int32_t *>(ix), const_cast<float *>(fx), const_cast<float *>(y),
-            const_cast<float *>(z), nullptr, nullptr, nullptr, w, n};
-  absorb_kernel<<<grid_for(n, 256, 8), 256, 0, as_stream(stream)>>>(
-      P, dead, win_k, win_f, xmin_cells, xmax_cells, r2max,
-      reinterpret_cast<unsigned long long *>(counters));
-  chm::count_launch();
+                  float xmax_cells, float r2max, uint64_t *counters, double *scale2, void *ws,
+                  int64_t ws_bytes, void *stream) {
+  CHM_REQUIRE(n >= 0 && counters && scale2, "sp_absorb: bad args");
+  CHM_REQUIRE(ws && ws_bytes >= chm_sp_scale_ws_bytes(), "sp_absorb: workspace too small");
+  cudaStream_t st = as_stream(stream);
+  double *partial = reinterpret_cast<double *>(ws);
+  int nb = 1;
+  if (n > 0) {
+    CHM_REQUIRE(ix && fx && y && z && w && dead, "sp_absorb: null pointer");
+    CHM_REQUIRE(((reinterpret_cast<uintptr_t>(ix) | reinterpret_cast<uintptr_t>(fx) |
+                  reinterpret_cast<uintptr_t>(y) | reinterpret_cast<uintptr_t>(z) |
+                  reinterpret_cast<uintptr_t>(w) | reinterpret_cast<uintptr_t>(dead)) & 15u) == 0,
+                "sp_absorb: arrays must start on 16-byte boundaries");
+    i64 R;
+    ws_partition(n, &nb, &R);
+    SpParts P{const_cast<int32_t *>(ix), const_cast<float *>(fx), const_cast<float *>(y),
+              const_cast<float *>(z), nullptr, nullptr, nullptr, w, n};
+    weights_kernel<true><<<nb, kWsThreads, 0, st>>>(
+        P, dead, AbsorbBox{win_k, win_f, xmin_cells, xmax_cells, r2max}, R, partial,
+        reinterpret_cast<unsigned long long *>(counters));
+    chm::count_launch();
+  } else {
+    cudaMemsetAsync(partial, 0, 8, st);
+  }
+  sp_scale_kernel<<<1, 1024, 0, st>>>(partial, nb, scale2); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }

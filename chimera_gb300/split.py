@@ -249,9 +249,10 @@ class SplitRun:
         mov = self._moving()
         # one species deposits into each accumulator in the benchmark; with
         # several, the largest bound times the species count is used
-        for target, group in ((self.scaleJ, mov), (self.scaleR, mov), (self.scaleBG, self._still())):
+        for targets, group in (((self.scaleJ, self.scaleR), mov), ((self.scaleBG,), self._still())):
             if not group:
-                target.fill_(1.0)
+                for t in targets:
+                    t.fill_(1.0)
                 continue
             vals = []
             for spc, P in group:
@@ -260,12 +261,14 @@ class SplitRun:
                           self.scale_ws.data_ptr(), self.scale_ws.numel(), st)
                 vals.append(tmp)
             if len(vals) == 1:
-                target.copy_(vals[0])
+                for t in targets:
+                    t.copy_(vals[0])
             else:
                 B = torch.stack([v[1] for v in vals]).sum()
-                e = torch.ceil(torch.log2(B))
-                target[0] = torch.pow(2.0, 61.0 - e)
-                target[1] = B
+                e = torch.clamp(61.0 - torch.ceil(torch.log2(B)), max=120.0)
+                for t in targets:
+                    t[0] = torch.pow(2.0, e)
+                    t[1] = B
         self._scales_valid = True
 
     def _deposit(self, P, push, accJ, accR, scaleJ, scaleR):
@@ -418,7 +421,9 @@ class SplitRun:
 
     def _absorb(self, wind):
         """species.py:351-398 absorption (SimDom test) on the split layout:
-        marks in place, compacts every ``compact_every`` window moves."""
+        marks in place (compacting every ``compact_every`` window moves) and
+        refreshes the deposit scales in the same pass."""
+        scales = {}
         for spc, P in zip(self.fp.Particles, self.parts):
             if P.n == 0:
                 continue
@@ -428,14 +433,27 @@ class SplitRun:
             xmin = (a["leftX"] + wind["AbsorbLayer"] * a["dx"] - self.solver.Args["leftX"]) / self.dx
             xmax = (a["rightX"] - self.solver.Args["leftX"]) / self.dx
             b = P.buf
+            sc = torch.empty(2, dtype=torch.float64, device=self.device)
             _lib.call("chm_sp_absorb", b["ix"].data_ptr(), b["fx"].data_ptr(), b["y"].data_ptr(),
                       b["z"].data_ptr(), b["w"].data_ptr(), P.dead.data_ptr(), P.n, k, f,
                       float(xmin), float(xmax), float(a["upperR"] ** 2),
-                      P.counters.data_ptr(), _stream())
+                      P.counters.data_ptr(), sc.data_ptr(), self.scale_ws.data_ptr(),
+                      self.scale_ws.numel(), _stream())
+            scales[id(P)] = sc
             P.moves += 1
             if P.moves >= self.compact_every:
                 P.compact()
-        self._scales_valid = False
+        # with one species per accumulator the absorbing pass gives the scales
+        mov, still = self._moving(), self._still()
+        if (len(mov) == 1 and len(still) <= 1 and id(mov[0][1]) in scales
+                and (not still or id(still[0][1]) in scales)):
+            self.scaleJ.copy_(scales[id(mov[0][1])])
+            self.scaleR.copy_(scales[id(mov[0][1])])
+            if still:
+                self.scaleBG.copy_(scales[id(still[0][1])])
+            self._scales_valid = True
+        else:
+            self._scales_valid = False
 
     # ------------------------------------------------------------------
     @property

@@ -451,11 +451,14 @@ int chm_sp_to_f64(const int32_t *ix, const float *fx, const float *y,
  * test of chunk_and_damp).  A live particle outside xmin <= x <= xmax,
  * y^2 + z^2 <= r2max (x in window cells) gets dead[i] = 1 and w = 0, so it
  * deposits nothing; counters[0] (device uint64) counts dead particles.
- * chm_sp_compact later drops them. */
+ * chm_sp_compact later drops them.  The same pass refreshes the deposit
+ * scale of the surviving weights into scale2 (as chm_sp_weight_scale);
+ * ws: chm_sp_scale_ws_bytes().  Arrays start on 16-byte boundaries. */
 int chm_sp_absorb(const int32_t *ix, const float *fx, const float *y,
                   const float *z, float *w, uint8_t *dead, int64_t n, int win_k,
                   float win_f, float xmin_cells, float xmax_cells, float r2max,
-                  uint64_t *counters, void *stream);
+                  uint64_t *counters, double *scale2, void *ws, int64_t ws_bytes,
+                  void *stream);
 /* counters[1] += n - counters[0] (live particles of the step, for rates). */
 int chm_sp_count_live(uint64_t *counters, int64_t n, void *stream);
 /* Stable compaction of the particles with dead[i] == 0 into the *_out

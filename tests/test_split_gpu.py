@@ -263,9 +263,11 @@ def test_absorb_and_compact(mods):
     cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
     st = _st(torch)
     k, f, xmin, xmax, r2 = 100, 0.25, 8.0, 60.0, (12.0 * dr) ** 2
+    scale = torch.zeros(2, dtype=torch.float64, device="cuda")
+    sws = torch.empty(_lib.query("chm_sp_scale_ws_bytes"), dtype=torch.uint8, device="cuda")
     _lib.call("chm_sp_absorb", P["ix"].data_ptr(), P["fx"].data_ptr(), P["y"].data_ptr(),
               P["z"].data_ptr(), P["w"].data_ptr(), dead.data_ptr(), n, k, f, xmin, xmax, r2,
-              cnt.data_ptr(), st)
+              cnt.data_ptr(), scale.data_ptr(), sws.data_ptr(), sws.numel(), st)
     _lib.call("chm_sp_count_live", cnt.data_ptr(), n, st)
     xc = (ref["ix"] - k).astype(np.float32) + (ref["fx"] - np.float32(f))
     r2p = ref["y"] * ref["y"] + ref["z"] * ref["z"]
@@ -280,6 +282,11 @@ def test_absorb_and_compact(mods):
     assert int(cnt[1]) == n - int(newly.sum())
     w = P["w"].cpu().numpy()
     assert np.all(w[newly] == 0) and np.array_equal(w[~dead_ref], ref["w"][~dead_ref])
+    # the same pass gives the deposit scale of the surviving weights
+    B = float(np.abs(w.astype(np.float64)).sum())
+    sc = scale.cpu().numpy()
+    assert abs(sc[1] - B) <= 1e-6 * B
+    assert sc[0] == 2.0 ** (61 - int(np.ceil(np.log2(sc[1]))))
     Q = {k: torch.empty_like(v) for k, v in P.items()}
     ws = torch.empty(_lib.query("chm_sp_compact_ws_bytes", n), dtype=torch.uint8, device="cuda")
     n_out = torch.zeros(1, dtype=torch.int64, device="cuda")
