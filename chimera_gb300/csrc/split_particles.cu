@@ -10,11 +10,19 @@
 // the host and enters as (k, f): leftX = X0 + (k + f) dx, k integer, f in
 // [0, 1); the grid-relative position is (ix - k) + (fx - f).
 //
+// Order in memory: tiles of 512 particles.  Particle i (its place in the
+// species) is run r = (i / 16) mod 32, slot j = i mod 16 of tile i / 512, and
+// sits at tile * 512 + 32 j + r.  A warp takes a tile, lane r the run r: the
+// 16 consecutive particles of a run (one deposit cell when the particles are
+// stored cell by cell) belong to one thread, and every load of a warp reads
+// 32 consecutive words.  Arrays hold whole tiles; slots past the last
+// particle are not read.
+//
 // Deposition stays deterministic without float atomics: values are rounded
 // to the global 64-bit fixed-point quantum 2^-e (2^e = 2^(61 - ceil(log2
 // sum |w|))) and added as integers, first into a shared-memory box of the
 // block's nodes, then into the global accumulator.  Integer sums are
-// order-independent; the cell-run kernel sums the particles of a run in FP32
+// order-independent; the run kernel sums the particles of a run in FP32
 // before rounding, which depends only on the (fixed) particle order.
 #include <climits>
 #include <cstdlib>
@@ -27,10 +35,22 @@ using namespace chm;
 
 namespace {
 
-constexpr int kSpThreads = 256;
-constexpr int kSpPerThread = 8;
-constexpr int kSpPerBlock = kSpThreads * kSpPerThread;
-constexpr int kSpBoxBytes = 96 * 1024;  // 12288 int64 values
+constexpr int kRunLen = 16;                        // particles per run
+constexpr int kTileRuns = 32;                      // runs per tile (lanes of a warp)
+constexpr int kTile = kRunLen * kTileRuns;         // 512 particles per tile
+constexpr int kDepWarps = 4;                       // tiles per block
+constexpr int kDepThreads = 32 * kDepWarps;        // 128
+constexpr int kDepBlock = kTile * kDepWarps;       // 2048 particles per block
+constexpr int kSpBoxBytes = 56 * 1024;             // 7168 int64 values
+
+// physical slot of particle i and the particle of a slot
+__host__ __device__ __forceinline__ i64 phys_of(i64 i) {
+  return (i & ~(i64)(kTile - 1)) | ((i & (kRunLen - 1)) << 5) | ((i >> 4) & (kTileRuns - 1));
+}
+__host__ __device__ __forceinline__ i64 logical_of(i64 p) {
+  return (p & ~(i64)(kTile - 1)) | ((p & (kTileRuns - 1)) << 4) | ((p >> 5) & (kRunLen - 1));
+}
+inline i64 tiles_of(i64 n) { return (n + kTile - 1) / kTile; }
 
 struct SpParts {
   int32_t *ix;
@@ -224,28 +244,18 @@ __device__ __forceinline__ Pushed push_one(const PushDepArgs &A, i64 i) {
   return push_vals(A, P.ix[i], P.fx[i], P.y[i], P.z[i], P.px[i], P.py[i], P.pz[i], P.w[i]);
 }
 
-// Block plan shared by both deposit kernels: the box of nodes the block's
-// deposits can touch.  Thread t reads the run p0 + 8t .. p0 + 8t + 7.  The
-// box is bounded without pushing: a particle moves less than c dt, so its
-// deposit cells lie within ceil(dt/dx) cells of its x cell and within dt of
-// its radius.
+// Block plan shared by the deposit kernels: the box of nodes the block's
+// deposits can touch, from every particle of its 2048 slots.  The box is
+// bounded without pushing: a particle moves less than c dt, so its deposit
+// cells lie within ceil(dt/dx) cells of its x cell and within dt of its
+// radius.  (Nodes outside the box go straight to the global accumulator.)
 struct BlockPlan {
   long long bx0, br0, bnx, bnr, nvals;
   bool use_box;
   float sJ, sR;  // global scales 2^eJ, 2^eR
 };
 
-__device__ __forceinline__ void bound_one(int ix, float y, float z, float w, int &xlo, int &xhi,
-                                          float &r2lo, float &r2hi) {
-  if (w == 0.0f) return;
-  xlo = min(xlo, ix);
-  xhi = max(xhi, ix);
-  const float r2 = y * y + z * z;
-  r2lo = fminf(r2lo, r2);
-  r2hi = fmaxf(r2hi, r2);
-}
-
-__device__ BlockPlan plan_block(const PushDepArgs &A, i64 p0, i64 p1, bool vec, int *bb) {
+__device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb) {
   if (threadIdx.x == 0) {
     bb[0] = INT_MAX;
     bb[1] = INT_MIN;
@@ -253,25 +263,23 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 p0, i64 p1, bool vec, 
     bb[3] = INT_MIN;
   }
   __syncthreads();
-  const i64 r0i = p0 + (i64)threadIdx.x * (kSpPerBlock / kSpThreads);
-  const i64 r1i = min(p1, r0i + (i64)(kSpPerBlock / kSpThreads));
   int xlo = INT_MAX, xhi = INT_MIN;
   float r2lo = INFINITY, r2hi = -INFINITY;
-  if (vec && r1i - r0i == kSpPerBlock / kSpThreads) {
-#pragma unroll
-    for (int h = 0; h < kSpPerBlock / kSpThreads; h += 4) {
-      const int4 a = *reinterpret_cast<const int4 *>(A.P.ix + r0i + h);
-      const float4 y = *reinterpret_cast<const float4 *>(A.P.y + r0i + h);
-      const float4 z = *reinterpret_cast<const float4 *>(A.P.z + r0i + h);
-      const float4 w = *reinterpret_cast<const float4 *>(A.P.w + r0i + h);
-      bound_one(a.x, y.x, z.x, w.x, xlo, xhi, r2lo, r2hi);
-      bound_one(a.y, y.y, z.y, w.y, xlo, xhi, r2lo, r2hi);
-      bound_one(a.z, y.z, z.z, w.z, xlo, xhi, r2lo, r2hi);
-      bound_one(a.w, y.w, z.w, w.w, xlo, xhi, r2lo, r2hi);
-    }
-  } else {
-    for (i64 i = r0i; i < r1i; ++i)
-      bound_one(A.P.ix[i], A.P.y[i], A.P.z[i], A.P.w[i], xlo, xhi, r2lo, r2hi);
+  // independent loads (no load depends on another), 4 slots per step
+#pragma unroll 4
+  for (int s = threadIdx.x; s < kDepBlock; s += blockDim.x) {
+    const i64 p = base + s;
+    const bool valid = logical_of(p) < A.P.n;
+    const i64 q = valid ? p : base;  // slot 0 of the block always holds a particle
+    const float w = A.P.w[q];
+    const int ix = A.P.ix[q];
+    const float y = A.P.y[q], z = A.P.z[q];
+    if (!valid || w == 0.0f) continue;
+    xlo = min(xlo, ix);
+    xhi = max(xhi, ix);
+    const float r2 = y * y + z * z;
+    r2lo = fminf(r2lo, r2);
+    r2hi = fmaxf(r2hi, r2);
   }
   int x0 = INT_MAX, x1 = INT_MIN, r0 = INT_MAX, r1 = INT_MIN;
   if (xlo <= xhi) {
@@ -313,20 +321,22 @@ __device__ __forceinline__ BoxGeo make_geo(unsigned long long *box, const BlockP
                 A.G.nx, A.G.nr, 3 * A.G.nm};
 }
 
-// Generic push + deposit (any nm): one particle per thread and iteration,
-// each value rounded to the global quantum and added to the box.
-__global__ void __launch_bounds__(kSpThreads) push_deposit_kernel(PushDepArgs A) {
+// Generic push + deposit (any nm): one particle per thread and slot, each
+// value rounded to the global quantum and added to the box.
+__global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A) {
   extern __shared__ __align__(16) unsigned long long box[];
   __shared__ int bb[4];
-  const i64 p0 = (i64)blockIdx.x * kSpPerBlock, p1 = min(A.P.n, p0 + (i64)kSpPerBlock);
-  const BlockPlan Pl = plan_block(A, p0, p1, false, bb);
+  const i64 base = (i64)blockIdx.x * kDepBlock;
+  const BlockPlan Pl = plan_block(A, base, bb);
   if (Pl.use_box)
-    for (long long t = threadIdx.x; t < Pl.nvals; t += kSpThreads) box[t] = 0;
+    for (long long t = threadIdx.x; t < Pl.nvals; t += kDepThreads) box[t] = 0;
   __syncthreads();
   const BoxGeo geo = make_geo(box, Pl, A);
-  for (i64 i = p0 + threadIdx.x; i < p1; i += kSpThreads) {
-    const float w = A.P.w[i];
-    const Pushed q = push_one(A, i);
+  for (int s = threadIdx.x; s < kDepBlock; s += kDepThreads) {
+    const i64 p = base + s;
+    if (logical_of(p) >= A.P.n) continue;
+    const float w = A.P.w[p];
+    const Pushed q = push_one(A, p);
     if (w != 0.0f) {
       if (A.dep_j) {
         const Loc L = locate(q.ixh, q.fxh, q.yh, q.zh, A.G);
@@ -359,10 +369,10 @@ __global__ void __launch_bounds__(kSpThreads) push_deposit_kernel(PushDepArgs A)
       }
     }
     if (A.push) {
-      A.P.ix[i] = q.ixn;
-      A.P.fx[i] = q.fxn;
-      A.P.y[i] = q.yn;
-      A.P.z[i] = q.zn;
+      A.P.ix[p] = q.ixn;
+      A.P.fx[p] = q.fxn;
+      A.P.y[p] = q.yn;
+      A.P.z[p] = q.zn;
     }
   }
   if (!Pl.use_box) return;
@@ -371,107 +381,15 @@ __global__ void __launch_bounds__(kSpThreads) push_deposit_kernel(PushDepArgs A)
 }
 
 // ----------------------------------------------------------------------
-// Cell-run form of push + deposit for nm = 1, 2.  Particles generated cell
-// by cell (and the x-chunk sort) leave runs of consecutive particles in one
-// deposit cell, so each thread takes kRun consecutive particles, sums their
-// node values (already at the global scale) in FP32 registers while the
-// cell stays the same, and adds the sums, rounded to the global quantum, to
-// the block box when the cell changes.
+// Run form of push + deposit for nm = 1, 2: lane r of a warp walks the 16
+// particles of run r of its tile, sums their node values (already at the
+// global fixed-point scale) in FP32 registers while the deposit cell stays
+// the same, and adds the sums, rounded to the global quantum, to the block
+// box when the cell changes and at the end.
 // ----------------------------------------------------------------------
-constexpr int kRun = 8;  // consecutive particles per thread (kSpThreads * kRun = kSpPerBlock)
-static_assert(kSpThreads * kRun == kSpPerBlock, "block = threads x run");
 
-template <int V>
-struct RunV {
-  int ix[V];
-  float fx[V], y[V], z[V], px[V], py[V], pz[V], w[V];
-};
-
-template <int V>
-struct VecT;
-template <>
-struct VecT<4> {
-  typedef int4 I;
-  typedef float4 F;
-};
-template <>
-struct VecT<2> {
-  typedef int2 I;
-  typedef float2 F;
-};
-
-template <int V, typename T, typename S>
-__device__ __forceinline__ void unpack(const T &t, S *o) {
-  o[0] = t.x;
-  o[1] = t.y;
-  if constexpr (V == 4) {
-    o[2] = t.z;
-    o[3] = t.w;
-  }
-}
-
-// particles i0 .. i0+V-1 (cnt of them valid); vec: V-wide vector loads allowed
-template <int V>
-__device__ __forceinline__ void load_run(const SpParts &P, i64 i0, int cnt, bool vec, RunV<V> &q) {
-  typedef typename VecT<V>::I VI;
-  typedef typename VecT<V>::F VF;
-  if (vec && cnt == V) {
-    unpack<V>(*reinterpret_cast<const VI *>(P.ix + i0), q.ix);
-    unpack<V>(*reinterpret_cast<const VF *>(P.fx + i0), q.fx);
-    unpack<V>(*reinterpret_cast<const VF *>(P.y + i0), q.y);
-    unpack<V>(*reinterpret_cast<const VF *>(P.z + i0), q.z);
-    unpack<V>(*reinterpret_cast<const VF *>(P.px + i0), q.px);
-    unpack<V>(*reinterpret_cast<const VF *>(P.py + i0), q.py);
-    unpack<V>(*reinterpret_cast<const VF *>(P.pz + i0), q.pz);
-    unpack<V>(*reinterpret_cast<const VF *>(P.w + i0), q.w);
-  } else {
-#pragma unroll
-    for (int j = 0; j < V; ++j) {
-      const bool ok = j < cnt;
-      const i64 i = ok ? i0 + j : i0;
-      q.ix[j] = P.ix[i];
-      q.fx[j] = P.fx[i];
-      q.y[j] = P.y[i];
-      q.z[j] = P.z[i];
-      q.px[j] = P.px[i];
-      q.py[j] = P.py[i];
-      q.pz[j] = P.pz[i];
-      q.w[j] = ok ? P.w[i] : 0.0f;
-    }
-  }
-}
-
-template <int V>
-__device__ __forceinline__ void store_pos(const SpParts &P, i64 i0, int cnt, bool vec,
-                                          const int *oix, const float *ofx, const float *oy,
-                                          const float *oz) {
-  if (vec && cnt == V) {
-    if constexpr (V == 4) {
-      *reinterpret_cast<int4 *>(P.ix + i0) = make_int4(oix[0], oix[1], oix[2], oix[3]);
-      *reinterpret_cast<float4 *>(P.fx + i0) = make_float4(ofx[0], ofx[1], ofx[2], ofx[3]);
-      *reinterpret_cast<float4 *>(P.y + i0) = make_float4(oy[0], oy[1], oy[2], oy[3]);
-      *reinterpret_cast<float4 *>(P.z + i0) = make_float4(oz[0], oz[1], oz[2], oz[3]);
-    } else {
-      *reinterpret_cast<int2 *>(P.ix + i0) = make_int2(oix[0], oix[1]);
-      *reinterpret_cast<float2 *>(P.fx + i0) = make_float2(ofx[0], ofx[1]);
-      *reinterpret_cast<float2 *>(P.y + i0) = make_float2(oy[0], oy[1]);
-      *reinterpret_cast<float2 *>(P.z + i0) = make_float2(oz[0], oz[1]);
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < V; ++j)
-      if (j < cnt) {
-        P.ix[i0 + j] = oix[j];
-        P.fx[i0 + j] = ofx[j];
-        P.y[i0 + j] = oy[j];
-        P.z[i0 + j] = oz[j];
-      }
-  }
-}
-
-// node sums of one deposit cell at the global scale (FP32, summed over the
-// particles of a run): v[comp][part][node], part 0 = mode 0 re, then
-// (re, im) of modes 1 .. NM-1; node = 2 j + k (r + j, x + k)
+// node sums of one deposit cell: v[comp][part][node], part 0 = mode 0 re,
+// then (re, im) of modes 1 .. NM-1; node = 2 j + k (r + j, x + k)
 template <int NM, int NC>
 struct CellAcc {
   int cx, cr;
@@ -571,50 +489,77 @@ __device__ __forceinline__ void acc_add(CellAcc<NM, NC> &c, const Loc &L, const 
 }
 
 template <int NM, bool PUSH, bool DJ, bool DR>
-__global__ void __launch_bounds__(kSpThreads, 2) push_deposit_run_kernel(PushDepArgs A, int vec) {
+__global__ void __launch_bounds__(kDepThreads, 4) push_deposit_run_kernel(PushDepArgs A) {
   extern __shared__ __align__(16) unsigned long long box[];
   __shared__ int bb[4];
-  const i64 p0 = (i64)blockIdx.x * kSpPerBlock, p1 = min(A.P.n, p0 + (i64)kSpPerBlock);
-  const BlockPlan Pl = plan_block(A, p0, p1, vec != 0, bb);
+  const i64 base = (i64)blockIdx.x * kDepBlock;
+  const BlockPlan Pl = plan_block(A, base, bb);
   if (Pl.use_box)
-    for (long long t = threadIdx.x; t < Pl.nvals; t += kSpThreads) box[t] = 0;
+    for (long long t = threadIdx.x; t < Pl.nvals; t += kDepThreads) box[t] = 0;
   __syncthreads();
-  const i64 r0i = p0 + (i64)threadIdx.x * kRun;  // this thread's run
-  const int rcnt = (int)max((i64)0, min((i64)kRun, p1 - r0i));
   const BoxGeo geo = make_geo(box, Pl, A);
+  const int lane = threadIdx.x & 31;
+  const i64 tile = base + (i64)(threadIdx.x >> 5) * kTile;
+  const i64 first = tile + (i64)lane * kRunLen;  // this lane's run, in particle order
   CellAcc<NM, 3> cj;
   CellAcc<NM, 1> cr;
   cj.live = false;
   cr.live = false;
-  // vector width: the fused moving-species kernel at nm = 2 holds the most
-  // accumulators and loads two particles at a time
-  constexpr int V = (NM == 2 && PUSH && DJ && DR) ? 2 : 4;
-  for (int h = 0; h < kRun / V; ++h) {
-    const int cnt = rcnt - V * h;
-    if (cnt <= 0) break;
-    const i64 i0 = r0i + V * h;
-    RunV<V> q;
-    load_run<V>(A.P, i0, cnt, vec != 0, q);
-    int oix[V];
-    float ofx[V], oy[V], oz[V];
+  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - first));
+  // software pipeline: the next group of particles is loaded before this
+  // group's results are stored (the stores could alias the loads
+  // otherwise); G particles per group, more for the lighter rho-only pass
+  constexpr int G = DJ ? 1 : 4;
+  struct Part {
+    int ix;
+    float fx, y, z, px, py, pz, w;
+  };
+  auto load = [&](int j) {
+    Part q;
+    const i64 p = tile + (i64)j * kTileRuns + lane;
+    q.w = A.P.w[p];
+    q.ix = A.P.ix[p];
+    q.fx = A.P.fx[p];
+    q.y = A.P.y[p];
+    q.z = A.P.z[p];
+    if (PUSH || DJ) {
+      q.px = A.P.px[p];
+      q.py = A.P.py[p];
+      q.pz = A.P.pz[p];
+    }
+    return q;
+  };
+  Part cur[G], nxt[G];
 #pragma unroll
-    for (int j = 0; j < V; ++j) {
+  for (int g = 0; g < G; ++g)
+    if (g < cnt) cur[g] = load(g);
+  for (int j0 = 0; j0 < cnt; j0 += G) {
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+      if (j0 + G + g < cnt) nxt[g] = load(j0 + G + g);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int j = j0 + g;
+      if (j >= cnt) break;
+      const Part &c = cur[g];
+      const i64 p = tile + (i64)j * kTileRuns + lane;
+      const float w = c.w;
       Pushed u;
       if (PUSH || DJ) {
-        u = push_vals(A, q.ix[j], q.fx[j], q.y[j], q.z[j], q.px[j], q.py[j], q.pz[j], q.w[j]);
+        u = push_vals(A, c.ix, c.fx, c.y, c.z, c.px, c.py, c.pz, w);
       } else {
-        u.ixh = u.ixn = q.ix[j];
-        u.fxh = u.fxn = q.fx[j];
-        u.yh = u.yn = q.y[j];
-        u.zh = u.zn = q.z[j];
+        u.ixh = u.ixn = c.ix;
+        u.fxh = u.fxn = c.fx;
+        u.yh = u.yn = c.y;
+        u.zh = u.zn = c.z;
       }
       if (PUSH) {
-        oix[j] = u.ixn;
-        ofx[j] = u.fxn;
-        oy[j] = u.yn;
-        oz[j] = u.zn;
+        A.P.ix[p] = u.ixn;
+        A.P.fx[p] = u.fxn;
+        A.P.y[p] = u.yn;
+        A.P.z[p] = u.zn;
       }
-      if (q.w[j] == 0.0f) continue;
+      if (w == 0.0f) continue;
       if (DJ && u.moving) {  // grid_deps.f90:42: no current from particles at rest
         const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, A.G);
         const float vs[3] = {u.vj[0] * Pl.sJ, u.vj[1] * Pl.sJ, u.vj[2] * Pl.sJ};
@@ -631,7 +576,7 @@ __global__ void __launch_bounds__(kSpThreads, 2) push_deposit_run_kernel(PushDep
       }
       if (DR) {
         const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, A.G);
-        const float ws[1] = {q.w[j] * Pl.sR};
+        const float ws[1] = {w * Pl.sR};
         if (Pl.use_box) {
           acc_add(cr, L, ws, 3 * NM, A.G, geo);
         } else {
@@ -644,7 +589,8 @@ __global__ void __launch_bounds__(kSpThreads, 2) push_deposit_run_kernel(PushDep
         }
       }
     }
-    if (PUSH) store_pos<V>(A.P, i0, cnt, vec != 0, oix, ofx, oy, oz);
+#pragma unroll
+    for (int g = 0; g < G; ++g) cur[g] = nxt[g];
   }
   if (!Pl.use_box) return;
   if (DJ) acc_flush(cj, 0, A.G, geo);
@@ -654,12 +600,12 @@ __global__ void __launch_bounds__(kSpThreads, 2) push_deposit_run_kernel(PushDep
 }
 
 // Weight sums for the global scale 2^(61 - ceil(log2 B)), B = sum |w|, in a
-// fixed order: block b sums [b R, (b+1) R) (R a multiple of 16), thread t the
-// 16-particle chunks b R + 16 t + 4096 k in FP32, the block adds its threads'
-// sums in FP64 in a fixed tree, the final kernel adds the block sums.  With
-// ABSORB the same pass applies the absorbing boundary first (species.py:
-// 351-398, SimDom test): a live particle outside xmin <= x <= xmax,
-// r^2 <= r2max (window cells, (k, f) convention) is marked dead and its
+// fixed order: block b sums the slots [b R, (b+1) R) (R a multiple of 16),
+// thread t the 16-slot chunks b R + 16 t + 4096 k in FP32, the block adds its
+// threads' sums in FP64 in a fixed tree, the final kernel adds the block
+// sums.  With ABSORB the same pass applies the absorbing boundary first
+// (species.py:351-398, SimDom test): a live particle outside xmin <= x <=
+// xmax, r^2 <= r2max (window cells, (k, f) convention) is marked dead and its
 // weight zeroed, so it deposits nothing until a compaction drops it;
 // counters[0] counts the dead particles.
 constexpr int kWsThreads = 256;
@@ -679,68 +625,57 @@ __device__ __forceinline__ bool outside(const AbsorbBox &Bx, int ix, float fx, f
 
 template <bool ABSORB>
 __global__ void __launch_bounds__(kWsThreads) weights_kernel(SpParts P, uint8_t *__restrict__ dead,
-                                                             AbsorbBox Bx, i64 R,
+                                                             AbsorbBox Bx, i64 nphys, i64 R,
                                                              double *__restrict__ partial,
                                                              unsigned long long *counters) {
-  const i64 b0 = (i64)blockIdx.x * R, b1 = min(P.n, b0 + R);
+  const i64 b0 = (i64)blockIdx.x * R, b1 = min(nphys, b0 + R);
   float s = 0.0f;
   unsigned cnt = 0;
   for (i64 c = b0 + (i64)threadIdx.x * kWsChunk; c < b1; c += (i64)kWsThreads * kWsChunk) {
-    const int m = (int)min((i64)kWsChunk, b1 - c);
-    if (m == kWsChunk) {
-      float wv[16];
+    // a chunk of 16 slots (16-aligned, inside one tile)
+    float wv[16];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 t = *reinterpret_cast<const float4 *>(P.w + c + 4 * q);
+      wv[4 * q] = t.x, wv[4 * q + 1] = t.y, wv[4 * q + 2] = t.z, wv[4 * q + 3] = t.w;
+    }
+#pragma unroll
+    for (int j = 0; j < kWsChunk; ++j)
+      if (logical_of(c + j) >= P.n) wv[j] = 0.0f;  // slots past the last particle
+    if (ABSORB) {
+      uint4 dv = *reinterpret_cast<const uint4 *>(dead + c);
+      uint8_t *db = reinterpret_cast<uint8_t *>(&dv);
+      bool changed = false;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const float4 t = *reinterpret_cast<const float4 *>(P.w + c + 4 * q);
-        wv[4 * q] = t.x, wv[4 * q + 1] = t.y, wv[4 * q + 2] = t.z, wv[4 * q + 3] = t.w;
-      }
-      if (ABSORB) {
-        uint4 dv = *reinterpret_cast<const uint4 *>(dead + c);
-        uint8_t *db = reinterpret_cast<uint8_t *>(&dv);
-        bool changed = false;
+        const int4 ixq = *reinterpret_cast<const int4 *>(P.ix + c + 4 * q);
+        const float4 fq = *reinterpret_cast<const float4 *>(P.fx + c + 4 * q);
+        const float4 yq = *reinterpret_cast<const float4 *>(P.y + c + 4 * q);
+        const float4 zq = *reinterpret_cast<const float4 *>(P.z + c + 4 * q);
+        const int xi[4] = {ixq.x, ixq.y, ixq.z, ixq.w};
+        const float xf[4] = {fq.x, fq.y, fq.z, fq.w}, yy[4] = {yq.x, yq.y, yq.z, yq.w},
+                    zz[4] = {zq.x, zq.y, zq.z, zq.w};
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int4 ixq = *reinterpret_cast<const int4 *>(P.ix + c + 4 * q);
-          const float4 fq = *reinterpret_cast<const float4 *>(P.fx + c + 4 * q);
-          const float4 yq = *reinterpret_cast<const float4 *>(P.y + c + 4 * q);
-          const float4 zq = *reinterpret_cast<const float4 *>(P.z + c + 4 * q);
-          const int xi[4] = {ixq.x, ixq.y, ixq.z, ixq.w};
-          const float xf[4] = {fq.x, fq.y, fq.z, fq.w}, yy[4] = {yq.x, yq.y, yq.z, yq.w},
-                      zz[4] = {zq.x, zq.y, zq.z, zq.w};
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int j = 4 * q + e;
-            if (!db[j] && outside(Bx, xi[e], xf[e], yy[e], zz[e])) {
-              db[j] = 1;
-              wv[j] = 0.0f;
-              ++cnt;
-              changed = true;
-            }
+        for (int e = 0; e < 4; ++e) {
+          const int j = 4 * q + e;
+          if (logical_of(c + j) < P.n && !db[j] && outside(Bx, xi[e], xf[e], yy[e], zz[e])) {
+            db[j] = 1;
+            wv[j] = 0.0f;
+            ++cnt;
+            changed = true;
           }
         }
-        if (changed) {
-          *reinterpret_cast<uint4 *>(dead + c) = dv;
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-            *reinterpret_cast<float4 *>(P.w + c + 4 * q) =
-                make_float4(wv[4 * q], wv[4 * q + 1], wv[4 * q + 2], wv[4 * q + 3]);
-        }
       }
+      if (changed) {  // (slots past the last particle get a zero weight)
+        *reinterpret_cast<uint4 *>(dead + c) = dv;
 #pragma unroll
-      for (int j = 0; j < kWsChunk; ++j) s += fabsf(wv[j]);
-    } else {
-      for (int j = 0; j < m; ++j) {
-        const i64 i = c + j;
-        float w = P.w[i];
-        if (ABSORB && !dead[i] && outside(Bx, P.ix[i], P.fx[i], P.y[i], P.z[i])) {
-          dead[i] = 1;
-          P.w[i] = 0.0f;
-          w = 0.0f;
-          ++cnt;
-        }
-        s += fabsf(w);
+        for (int q = 0; q < 4; ++q)
+          *reinterpret_cast<float4 *>(P.w + c + 4 * q) =
+              make_float4(wv[4 * q], wv[4 * q + 1], wv[4 * q + 2], wv[4 * q + 3]);
       }
     }
+#pragma unroll
+    for (int j = 0; j < kWsChunk; ++j) s += fabsf(wv[j]);
   }
   double d = (double)s;
   for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
@@ -778,12 +713,12 @@ __global__ void __launch_bounds__(1024) sp_scale_kernel(const double *__restrict
   }
 }
 
-// blocks and per-block range of the fixed partition for n particles
-inline void ws_partition(i64 n, int *nblocks, i64 *R) {
-  i64 nb = (n + 4095) / 4096;
+// blocks and per-block range of the fixed partition of nphys slots
+inline void ws_partition(i64 nphys, int *nblocks, i64 *R) {
+  i64 nb = (nphys + 4095) / 4096;
   if (nb > kWsMaxBlocks) nb = kWsMaxBlocks;
   if (nb < 1) nb = 1;
-  i64 r = (n + nb - 1) / nb;
+  i64 r = (nphys + nb - 1) / nb;
   r = (r + kWsChunk - 1) / kWsChunk * kWsChunk;
   *nblocks = (int)nb;
   *R = r;
@@ -812,15 +747,17 @@ struct GatherArgs {
   float dtq;          // push_fact * dt
 };
 
-__global__ void __launch_bounds__(256) gather_push_kernel(GatherArgs A) {
+// generic gather (any nm), one particle per thread and slot
+__global__ void __launch_bounds__(256) gather_push_kernel(GatherArgs A, i64 nphys) {
   const SpGrid &G = A.G;
   const i64 plane = (i64)G.nx * G.nr;
-  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < A.P.n;
-       i += (i64)gridDim.x * blockDim.x) {
+  for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < nphys;
+       p += (i64)gridDim.x * blockDim.x) {
+    if (logical_of(p) >= A.P.n) continue;
     float F[6] = {0, 0, 0, 0, 0, 0};
-    const float w = A.P.w[i];
+    const float w = A.P.w[p];
     if (w != 0.0f) {
-      Loc L = locate(A.P.ix[i], A.P.fx[i], A.P.y[i], A.P.z[i], G);
+      Loc L = locate(A.P.ix[p], A.P.fx[p], A.P.y[p], A.P.z[p], G);
       if (L.ok) {
         const float sx[2] = {1.0f - L.sx1, L.sx1};
         const float sr[2] = {1.0f - L.sr1, L.sr1};
@@ -852,118 +789,120 @@ __global__ void __launch_bounds__(256) gather_push_kernel(GatherArgs A) {
         }
       }
     }
-    float px = A.P.px[i], py = A.P.py[i], pz = A.P.pz[i];
+    float px = A.P.px[p], py = A.P.py[p], pz = A.P.pz[p];
     boris(px, py, pz, F, 0.5f * A.dtq);
-    A.P.px[i] = px;
-    A.P.py[i] = py;
-    A.P.pz[i] = pz;
+    A.P.px[p] = px;
+    A.P.py[p] = py;
+    A.P.pz[p] = pz;
   }
 }
 
-// Cell-run gather + Boris for nm = 1, 2: a thread takes kRun consecutive
-// particles and keeps the fields of the 4 nodes of the current cell in
-// registers (mode 0: real parts; modes >= 1: complex), reloading them only
-// when the cell changes.  Same interpolation and rotation as
-// gather_push_kernel.
+// Run form of gather + Boris for nm = 1, 2: lane r walks run r of its tile
+// and keeps the fields of the 4 nodes of the current cell in registers
+// (mode 0: real parts; modes >= 1: complex), reloading them only when the
+// cell changes.  Same interpolation and rotation as gather_push_kernel.
 template <int NM>
-__global__ void __launch_bounds__(256, 2) gather_push_run_kernel(GatherArgs A, int vec) {
-  constexpr int V = 2;
+__global__ void __launch_bounds__(kDepThreads, 4) gather_push_run_kernel(GatherArgs A) {
   const SpGrid &G = A.G;
   const i64 plane = (i64)G.nx * G.nr;
-  const i64 r0i = ((i64)blockIdx.x * blockDim.x + threadIdx.x) * kRun;
-  if (r0i >= A.P.n) return;
-  const int rcnt = (int)min((i64)kRun, A.P.n - r0i);
+  const int lane = threadIdx.x & 31;
+  const i64 tile = (i64)blockIdx.x * kDepBlock + (i64)(threadIdx.x >> 5) * kTile;
+  const i64 first = tile + (i64)lane * kRunLen;
   int ccx = INT_MIN, ccr = INT_MIN;
   float f0[6][4];
   float2 f1[NM > 1 ? NM - 1 : 1][6][4];
-  for (int h = 0; h < kRun / V; ++h) {
-    const int cnt = rcnt - V * h;
-    if (cnt <= 0) break;
-    const i64 i0 = r0i + V * h;
-    RunV<V> q;
-    load_run<V>(A.P, i0, cnt, vec != 0, q);
-    float opx[V], opy[V], opz[V];
+  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - first));
+  struct Part {
+    int ix;
+    float fx, y, z, px, py, pz, w;
+  };
+  auto load = [&](int j) {
+    Part q;
+    const i64 p = tile + (i64)j * kTileRuns + lane;
+    q.w = A.P.w[p];
+    q.ix = A.P.ix[p];
+    q.fx = A.P.fx[p];
+    q.y = A.P.y[p];
+    q.z = A.P.z[p];
+    q.px = A.P.px[p];
+    q.py = A.P.py[p];
+    q.pz = A.P.pz[p];
+    return q;
+  };
+  Part cur;
+  if (cnt > 0) cur = load(0);
+  for (int j = 0; j < cnt; ++j) {
+    Part nxt;
+    if (j + 1 < cnt) nxt = load(j + 1);  // loaded before this particle's store
+    const i64 p = tile + (i64)j * kTileRuns + lane;
+    float F[6] = {0, 0, 0, 0, 0, 0};
+    if (cur.w != 0.0f) {
+      const Loc L = locate(cur.ix, cur.fx, cur.y, cur.z, G);
+      if (L.ok) {
+        if (L.cx != ccx || L.cr != ccr) {
+          ccx = L.cx;
+          ccr = L.cr;
 #pragma unroll
-    for (int j = 0; j < V; ++j) {
-      float F[6] = {0, 0, 0, 0, 0, 0};
-      if (q.w[j] != 0.0f) {
-        const Loc L = locate(q.ix[j], q.fx[j], q.y[j], q.z[j], G);
-        if (L.ok) {
-          if (L.cx != ccx || L.cr != ccr) {
-            ccx = L.cx;
-            ccr = L.cr;
+          for (int nd = 0; nd < 4; ++nd) {
+            const int gx = L.cx + (nd & 1), gr = L.cr + (nd >> 1);
+            const bool okx = gx >= 0 && gx < G.nx;
 #pragma unroll
-            for (int nd = 0; nd < 4; ++nd) {
-              const int gx = L.cx + (nd & 1), gr = L.cr + (nd >> 1);
-              const bool okx = gx >= 0 && gx < G.nx;
+            for (int l = 0; l < 6; ++l) {
+              const float2 *b = A.eb + (i64)(G.nm * l) * plane + (i64)gr * G.nx + gx;
+              f0[l][nd] = okx ? b[0].x : 0.0f;
 #pragma unroll
-              for (int l = 0; l < 6; ++l) {
-                const float2 *b = A.eb + (i64)(G.nm * l) * plane + (i64)gr * G.nx + gx;
-                f0[l][nd] = okx ? b[0].x : 0.0f;
-#pragma unroll
-                for (int m = 1; m < NM; ++m)
-                  f1[m - 1][l][nd] = okx ? b[(i64)m * plane] : make_float2(0.0f, 0.0f);
-              }
+              for (int m = 1; m < NM; ++m)
+                f1[m - 1][l][nd] = okx ? b[(i64)m * plane] : make_float2(0.0f, 0.0f);
             }
           }
-          const float sx[2] = {1.0f - L.sx1, L.sx1};
-          const float sr[2] = {1.0f - L.sr1, L.sr1};
+        }
+        const float sx[2] = {1.0f - L.sx1, L.sx1};
+        const float sr[2] = {1.0f - L.sr1, L.sr1};
+#pragma unroll
+        for (int l = 0; l < 6; ++l) {
+          float acc = 0.0f;
+#pragma unroll
+          for (int jj = 0; jj < 2; ++jj) {
+            acc += sr[jj] * sx[0] * f0[l][2 * jj];
+            acc += sr[jj] * sx[1] * f0[l][2 * jj + 1];
+          }
+          F[l] += acc;
+        }
+        float pr = 1.0f, pi = 0.0f;  // e^{+i m theta}
+#pragma unroll
+        for (int m = 1; m < NM; ++m) {
+          const float a = pr * L.phr - pi * L.phi, b2 = pr * L.phi + pi * L.phr;
+          pr = a;
+          pi = b2;
 #pragma unroll
           for (int l = 0; l < 6; ++l) {
             float acc = 0.0f;
 #pragma unroll
             for (int jj = 0; jj < 2; ++jj) {
-              acc += sr[jj] * sx[0] * f0[l][2 * jj];
-              acc += sr[jj] * sx[1] * f0[l][2 * jj + 1];
+              const float2 u0 = f1[m - 1][l][2 * jj], u1 = f1[m - 1][l][2 * jj + 1];
+              acc += sr[jj] * sx[0] * (pr * u0.x - pi * u0.y);
+              acc += sr[jj] * sx[1] * (pr * u1.x - pi * u1.y);
             }
             F[l] += acc;
           }
-          float pr = 1.0f, pi = 0.0f;  // e^{+i m theta}
-#pragma unroll
-          for (int m = 1; m < NM; ++m) {
-            const float a = pr * L.phr - pi * L.phi, b2 = pr * L.phi + pi * L.phr;
-            pr = a;
-            pi = b2;
-#pragma unroll
-            for (int l = 0; l < 6; ++l) {
-              float acc = 0.0f;
-#pragma unroll
-              for (int jj = 0; jj < 2; ++jj) {
-                const float2 u0 = f1[m - 1][l][2 * jj], u1 = f1[m - 1][l][2 * jj + 1];
-                acc += sr[jj] * sx[0] * (pr * u0.x - pi * u0.y);
-                acc += sr[jj] * sx[1] * (pr * u1.x - pi * u1.y);
-              }
-              F[l] += acc;
-            }
-          }
         }
       }
-      opx[j] = q.px[j];
-      opy[j] = q.py[j];
-      opz[j] = q.pz[j];
-      boris(opx[j], opy[j], opz[j], F, 0.5f * A.dtq);
     }
-    if (vec && cnt == V) {
-      *reinterpret_cast<float2 *>(A.P.px + i0) = make_float2(opx[0], opx[1]);
-      *reinterpret_cast<float2 *>(A.P.py + i0) = make_float2(opy[0], opy[1]);
-      *reinterpret_cast<float2 *>(A.P.pz + i0) = make_float2(opz[0], opz[1]);
-    } else {
-#pragma unroll
-      for (int j = 0; j < V; ++j)
-        if (j < cnt) {
-          A.P.px[i0 + j] = opx[j];
-          A.P.py[i0 + j] = opy[j];
-          A.P.pz[i0 + j] = opz[j];
-        }
-    }
+    float px = cur.px, py = cur.py, pz = cur.pz;
+    boris(px, py, pz, F, 0.5f * A.dtq);
+    A.P.px[p] = px;
+    A.P.py[p] = py;
+    A.P.pz[p] = pz;
+    cur = nxt;
   }
 }
 
-// FP64 (3, n) strided particle arrays -> split layout
-__global__ void from_f64_kernel(SpParts P, i64 off, const double *__restrict__ x, i64 x_cs, i64 x_ps,
-                                const double *__restrict__ p, i64 p_cs, i64 p_ps,
-                                const double *__restrict__ w, i64 w_ps, double X0, double dx_inv,
-                                i64 n) {
+// FP64 (3, n) strided particle arrays -> split layout, as particles off ..
+// off + n - 1 (their dead flags cleared)
+__global__ void from_f64_kernel(SpParts P, uint8_t *dead, i64 off, const double *__restrict__ x,
+                                i64 x_cs, i64 x_ps, const double *__restrict__ p, i64 p_cs,
+                                i64 p_ps, const double *__restrict__ w, i64 w_ps, double X0,
+                                double dx_inv, i64 n) {
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
     const double s = (x[i * x_ps] - X0) * dx_inv;
     const double fl = floor(s);
@@ -973,14 +912,16 @@ __global__ void from_f64_kernel(SpParts P, i64 off, const double *__restrict__ x
       fr = 0.0f;
       ix += 1;
     }
-    P.ix[off + i] = ix;
-    P.fx[off + i] = fr;
-    P.y[off + i] = (float)x[x_cs + i * x_ps];
-    P.z[off + i] = (float)x[2 * x_cs + i * x_ps];
-    P.px[off + i] = (float)p[i * p_ps];
-    P.py[off + i] = (float)p[p_cs + i * p_ps];
-    P.pz[off + i] = (float)p[2 * p_cs + i * p_ps];
-    P.w[off + i] = (float)w[i * w_ps];
+    const i64 q = phys_of(off + i);
+    P.ix[q] = ix;
+    P.fx[q] = fr;
+    P.y[q] = (float)x[x_cs + i * x_ps];
+    P.z[q] = (float)x[2 * x_cs + i * x_ps];
+    P.px[q] = (float)p[i * p_ps];
+    P.py[q] = (float)p[p_cs + i * p_ps];
+    P.pz[q] = (float)p[2 * p_cs + i * p_ps];
+    P.w[q] = (float)w[i * w_ps];
+    if (dead) dead[q] = 0;
   }
 }
 
@@ -988,13 +929,14 @@ __global__ void to_f64_kernel(SpParts P, double *__restrict__ x, i64 x_cs, i64 x
                               double *__restrict__ p, i64 p_cs, i64 p_ps, double *__restrict__ w,
                               i64 w_ps, double X0, double dx) {
   for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < P.n; i += (i64)gridDim.x * blockDim.x) {
-    x[i * x_ps] = X0 + ((double)P.ix[i] + (double)P.fx[i]) * dx;
-    x[x_cs + i * x_ps] = P.y[i];
-    x[2 * x_cs + i * x_ps] = P.z[i];
-    p[i * p_ps] = P.px[i];
-    p[p_cs + i * p_ps] = P.py[i];
-    p[2 * p_cs + i * p_ps] = P.pz[i];
-    if (w) w[i * w_ps] = P.w[i];
+    const i64 q = phys_of(i);
+    x[i * x_ps] = X0 + ((double)P.ix[q] + (double)P.fx[q]) * dx;
+    x[x_cs + i * x_ps] = P.y[q];
+    x[2 * x_cs + i * x_ps] = P.z[q];
+    p[i * p_ps] = P.px[q];
+    p[p_cs + i * p_ps] = P.py[q];
+    p[2 * p_cs + i * p_ps] = P.pz[q];
+    if (w) w[i * w_ps] = P.w[q];
   }
 }
 
@@ -1003,15 +945,16 @@ __global__ void live_steps_kernel(unsigned long long *counters, i64 n) {
   if (threadIdx.x == 0 && blockIdx.x == 0) counters[1] += (unsigned long long)n - counters[0];
 }
 
-// Stable compaction of the live particles: tile counts, one scan, scatter.
+// Stable compaction of the live particles (in particle order): counts per
+// 4096 particles, one scan, scatter.
 constexpr int kCmpThreads = 256;
-constexpr int kCmpTile = 4096;  // particles per tile
+constexpr int kCmpTile = 4096;  // particles per count
 
 __global__ void __launch_bounds__(kCmpThreads) compact_count_kernel(const uint8_t *__restrict__ dead,
                                                                     i64 n, int *__restrict__ cnt) {
   const i64 t0 = (i64)blockIdx.x * kCmpTile, t1 = min(n, t0 + kCmpTile);
   int c = 0;
-  for (i64 i = t0 + threadIdx.x; i < t1; i += kCmpThreads) c += dead[i] ? 0 : 1;
+  for (i64 i = t0 + threadIdx.x; i < t1; i += kCmpThreads) c += dead[phys_of(i)] ? 0 : 1;
   c = __reduce_add_sync(0xffffffffu, c);
   __shared__ int ws[kCmpThreads / 32];
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
@@ -1023,7 +966,7 @@ __global__ void __launch_bounds__(kCmpThreads) compact_count_kernel(const uint8_
   }
 }
 
-// exclusive scan of the tile counts in place (one block), total -> n_out
+// exclusive scan of the counts in place (one block), total -> n_out
 __global__ void __launch_bounds__(1024) compact_scan_kernel(int *__restrict__ cnt, int ntiles,
                                                             int64_t *__restrict__ n_out) {
   __shared__ long long part[1024];
@@ -1042,7 +985,7 @@ __global__ void __launch_bounds__(1024) compact_scan_kernel(int *__restrict__ cn
   long long run = threadIdx.x ? part[threadIdx.x - 1] : 0;
   for (int i = a; i < b; ++i) {
     const int c = cnt[i];
-    cnt[i] = (int)run;  // tile offsets stay below 2^31 tiles x 4096: checked on the host
+    cnt[i] = (int)run;  // offsets stay below 2^31: checked on the host
     run += c;
   }
   if (threadIdx.x == 1023) *n_out = part[1023];
@@ -1059,22 +1002,23 @@ __global__ void __launch_bounds__(kCmpThreads) compact_scatter_kernel(SpParts S,
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (i64 c0 = t0; c0 < t1; c0 += kCmpThreads) {
     const i64 i = c0 + threadIdx.x;
-    const bool live = i < t1 && !dead[i];
+    const i64 q = phys_of(i);
+    const bool live = i < t1 && !dead[q];
     const unsigned m = __ballot_sync(0xffffffffu, live);
     if (lane == 0) wsum[warp] = __popc(m);
     __syncthreads();
     int before = carry;
     for (int k = 0; k < warp; ++k) before += wsum[k];
     if (live) {
-      const i64 j = (i64)before + __popc(m & ((1u << lane) - 1u));
-      D.ix[j] = S.ix[i];
-      D.fx[j] = S.fx[i];
-      D.y[j] = S.y[i];
-      D.z[j] = S.z[i];
-      D.px[j] = S.px[i];
-      D.py[j] = S.py[i];
-      D.pz[j] = S.pz[i];
-      D.w[j] = S.w[i];
+      const i64 j = phys_of((i64)before + __popc(m & ((1u << lane) - 1u)));
+      D.ix[j] = S.ix[q];
+      D.fx[j] = S.fx[q];
+      D.y[j] = S.y[q];
+      D.z[j] = S.z[q];
+      D.px[j] = S.px[q];
+      D.py[j] = S.py[q];
+      D.pz[j] = S.pz[q];
+      D.w[j] = S.w[q];
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1091,7 +1035,12 @@ __global__ void __launch_bounds__(kCmpThreads) compact_scatter_kernel(SpParts S,
 extern "C" {
 
 // The split-form particle entry points take the eight SoA arrays in the
-// order ix, fx, y, z, px, py, pz, w (n particles).
+// order ix, fx, y, z, px, py, pz, w (n particles in the tile order above,
+// arrays of chm_sp_capacity(n) slots).
+
+int64_t chm_sp_capacity(int64_t n) { return n <= 0 ? 0 : tiles_of(n) * kTile; }
+
+int64_t chm_sp_slot(int64_t i) { return phys_of(i); }
 
 int64_t chm_sp_scale_ws_bytes(void) { return 8 * (int64_t)kWsMaxBlocks + 256; }
 
@@ -1103,11 +1052,14 @@ int chm_sp_weight_scale(double *scale2, const float *w, int64_t n, void *ws, int
   double *partial = reinterpret_cast<double *>(ws);
   int nb = 1;
   if (n > 0) {
-    CHM_REQUIRE(w, "sp_weight_scale: null weights");
+    CHM_REQUIRE(w && (reinterpret_cast<uintptr_t>(w) & 15u) == 0,
+                "sp_weight_scale: weights must start on a 16-byte boundary");
     i64 R;
-    ws_partition(n, &nb, &R);
+    const i64 nphys = tiles_of(n) * kTile;
+    ws_partition(nphys, &nb, &R);
     SpParts P{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, const_cast<float *>(w), n};
-    weights_kernel<false><<<nb, kWsThreads, 0, st>>>(P, nullptr, AbsorbBox{}, R, partial, nullptr);
+    weights_kernel<false><<<nb, kWsThreads, 0, st>>>(P, nullptr, AbsorbBox{}, nphys, R, partial,
+                                                     nullptr);
     chm::count_launch();
   } else {
     cudaMemsetAsync(partial, 0, 8, st);
@@ -1139,22 +1091,15 @@ int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, f
   A.accR = reinterpret_cast<unsigned long long *>(accR);
   A.scaleJ = scaleJ;
   A.scaleR = scaleR;
-  const unsigned blocks = (unsigned)((n + kSpPerBlock - 1) / kSpPerBlock);
-  // 16-byte vector access when every array starts on a 16-byte boundary
-  const uintptr_t al = reinterpret_cast<uintptr_t>(ix) | reinterpret_cast<uintptr_t>(fx) |
-                       reinterpret_cast<uintptr_t>(y) | reinterpret_cast<uintptr_t>(z) |
-                       reinterpret_cast<uintptr_t>(px) | reinterpret_cast<uintptr_t>(py) |
-                       reinterpret_cast<uintptr_t>(pz) | reinterpret_cast<uintptr_t>(w);
-  const int vec = (al & 15u) == 0;
+  const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
   cudaStream_t st = as_stream(stream);
   // CHIMERA_GB300_DEPOSIT=generic selects the per-particle kernels of the
-  // deposit and the gather for every nm (the deposit kernels produce
-  // identical accumulators)
+  // deposit and the gather for every nm
   const char *var = getenv("CHIMERA_GB300_DEPOSIT");
   const bool generic = var && strcmp(var, "generic") == 0;
-  // cell-run kernels for nm 1, 2 and the three uses: moving species (push,
-  // J, rho), moving species without the fused rho, still species (rho)
-  void (*kern)(PushDepArgs, int) = nullptr;
+  // run kernels for nm 1, 2 and the three uses: moving species (push, J,
+  // rho), moving species without the fused rho, still species (rho)
+  void (*kern)(PushDepArgs) = nullptr;
   if (!generic && (nm == 1 || nm == 2)) {
     const int mode = (push ? 4 : 0) | (A.dep_j ? 2 : 0) | (A.dep_rho ? 1 : 0);
     if (mode == 7) kern = nm == 1 ? push_deposit_run_kernel<1, true, true, true>
@@ -1164,14 +1109,9 @@ int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, f
     if (mode == 1) kern = nm == 1 ? push_deposit_run_kernel<1, false, false, true>
                                   : push_deposit_run_kernel<2, false, false, true>;
   }
-  if (kern) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpBoxBytes);
-    kern<<<blocks, kSpThreads, kSpBoxBytes, st>>>(A, vec);
-  } else {
-    cudaFuncSetAttribute(push_deposit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kSpBoxBytes);
-    push_deposit_kernel<<<blocks, kSpThreads, kSpBoxBytes, st>>>(A);
-  }
+  if (!kern) kern = push_deposit_kernel;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpBoxBytes);
+  kern<<<blocks, kDepThreads, kSpBoxBytes, st>>>(A);
   chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
@@ -1188,23 +1128,18 @@ int chm_sp_gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, fl
   A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
   A.eb = reinterpret_cast<const float2 *>(eb_c64);
   A.dtq = dtq;
-  const uintptr_t al = reinterpret_cast<uintptr_t>(ix) | reinterpret_cast<uintptr_t>(fx) |
-                       reinterpret_cast<uintptr_t>(y) | reinterpret_cast<uintptr_t>(z) |
-                       reinterpret_cast<uintptr_t>(px) | reinterpret_cast<uintptr_t>(py) |
-                       reinterpret_cast<uintptr_t>(pz) | reinterpret_cast<uintptr_t>(w);
-  const int vec = (al & 7u) == 0;  // 8-byte (two-particle) vector access
   const char *var = getenv("CHIMERA_GB300_DEPOSIT");
   const bool generic = var && strcmp(var, "generic") == 0;
   cudaStream_t st = as_stream(stream);
   if (!generic && (nm == 1 || nm == 2)) {
-    const i64 threads = (n + kRun - 1) / kRun;
-    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
     if (nm == 1)
-      gather_push_run_kernel<1><<<blocks, 256, 0, st>>>(A, vec);
+      gather_push_run_kernel<1><<<blocks, kDepThreads, 0, st>>>(A);
     else
-      gather_push_run_kernel<2><<<blocks, 256, 0, st>>>(A, vec);
+      gather_push_run_kernel<2><<<blocks, kDepThreads, 0, st>>>(A);
   } else {
-    gather_push_kernel<<<grid_for(n, 256, 16), 256, 0, st>>>(A);
+    const i64 nphys = tiles_of(n) * kTile;
+    gather_push_kernel<<<grid_for(nphys, 256, 16), 256, 0, st>>>(A, nphys);
   }
   chm::count_launch();
   CHM_CHECK_LAUNCH();
@@ -1212,14 +1147,16 @@ int chm_sp_gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, fl
 }
 
 int chm_sp_from_f64(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,
-                    float *w, int64_t offset, const double *coord, int64_t x_cs, int64_t x_ps,
-                    const double *momenta, int64_t p_cs, int64_t p_ps, const double *wghts,
-                    int64_t w_ps, double X0, double dx, int64_t n, void *stream) {
+                    float *w, uint8_t *dead, int64_t offset, const double *coord, int64_t x_cs,
+                    int64_t x_ps, const double *momenta, int64_t p_cs, int64_t p_ps,
+                    const double *wghts, int64_t w_ps, double X0, double dx, int64_t n,
+                    void *stream) {
   CHM_REQUIRE(n >= 0 && offset >= 0 && dx > 0, "sp_from_f64: bad args");
   if (n == 0) return CHM_OK;
   SpParts P{ix, fx, y, z, px, py, pz, w, offset + n};
   from_f64_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
-      P, offset, coord, x_cs, x_ps, momenta, p_cs, p_ps, wghts, w_ps, X0, 1.0 / dx, n); chm::count_launch();
+      P, dead, offset, coord, x_cs, x_ps, momenta, p_cs, p_ps, wghts, w_ps, X0, 1.0 / dx, n);
+  chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -1234,7 +1171,8 @@ int chm_sp_to_f64(const int32_t *ix, const float *fx, const float *y, const floa
             const_cast<float *>(z), const_cast<float *>(px), const_cast<float *>(py),
             const_cast<float *>(pz), const_cast<float *>(w), n};
   to_f64_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(P, coord, x_cs, x_ps, momenta,
-                                                                 p_cs, p_ps, wghts, w_ps, X0, dx); chm::count_launch();
+                                                                 p_cs, p_ps, wghts, w_ps, X0, dx);
+  chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -1255,11 +1193,12 @@ int chm_sp_absorb(const int32_t *ix, const float *fx, const float *y, const floa
                   reinterpret_cast<uintptr_t>(w) | reinterpret_cast<uintptr_t>(dead)) & 15u) == 0,
                 "sp_absorb: arrays must start on 16-byte boundaries");
     i64 R;
-    ws_partition(n, &nb, &R);
+    const i64 nphys = tiles_of(n) * kTile;
+    ws_partition(nphys, &nb, &R);
     SpParts P{const_cast<int32_t *>(ix), const_cast<float *>(fx), const_cast<float *>(y),
               const_cast<float *>(z), nullptr, nullptr, nullptr, w, n};
     weights_kernel<true><<<nb, kWsThreads, 0, st>>>(
-        P, dead, AbsorbBox{win_k, win_f, xmin_cells, xmax_cells, r2max}, R, partial,
+        P, dead, AbsorbBox{win_k, win_f, xmin_cells, xmax_cells, r2max}, nphys, R, partial,
         reinterpret_cast<unsigned long long *>(counters));
     chm::count_launch();
   } else {

@@ -60,8 +60,34 @@ def _f32(a, device) -> torch.Tensor:
     return torch.from_numpy(arr).to(device)
 
 
+def _slots(n: int) -> int:
+    """Slots of the tile layout holding n particles (whole tiles of 512)."""
+    return (int(n) + 511) // 512 * 512
+
+
+def cell_order(coords, group: int, X0: float, dx: float, dr: float):
+    """Stable permutation that puts the particles of each generation cell
+    (consecutive groups of `group`) in deposit-cell order, so that the runs
+    of 16 consecutive particles of the tile layout share a deposit cell.
+    coords: (3, n) numpy or torch array (x, y, z)."""
+    if isinstance(coords, torch.Tensor):
+        x, y, z = coords[0], coords[1], coords[2]
+        cx = torch.floor((x - X0) / dx).to(torch.int64)
+        cr = torch.floor(torch.sqrt(y * y + z * z) / dr + 0.5).to(torch.int64)
+        g = torch.arange(x.shape[0], device=x.device, dtype=torch.int64) // max(int(group), 1)
+        cx = cx - cx.min() if x.shape[0] else cx
+        key = (g * 4096 + cr.clamp(0, 4095)) * (1 << 22) + cx.clamp(0, (1 << 22) - 1)
+        return torch.argsort(key, stable=True)
+    x, y, z = coords[0], coords[1], coords[2]
+    cx = np.floor((x - X0) / dx).astype(np.int64)
+    cr = np.floor(np.sqrt(y * y + z * z) / dr + 0.5).astype(np.int64)
+    g = np.arange(x.shape[0], dtype=np.int64) // max(int(group), 1)
+    return np.lexsort((cx, cr, g))
+
+
 class _SpParticles:
-    """Split-layout SoA buffers of one species (capacity-allocated).
+    """Split-layout SoA buffers of one species (tile layout, see
+    chm_sp_slot; whole tiles allocated with spare capacity).
 
     Absorbed particles stay in place, marked in ``dead`` with zero weight,
     until ``compact`` drops them; ``counters`` (device) holds the number of
@@ -85,15 +111,16 @@ class _SpParticles:
                                device=self.device) for k in self.NAMES}
 
     def reserve(self, cap):
-        cap = int(max(cap, 1024))
+        cap = _slots(max(cap, 1024))
         if cap <= self.cap:
             return
         new = self._alloc(cap)
         dead = torch.zeros(cap, dtype=torch.uint8, device=self.device)
         if self.n:
+            used = _slots(self.n)  # whole tiles keep the slot of every particle
             for k in self.NAMES:
-                new[k][: self.n].copy_(self.buf[k][: self.n])
-            dead[: self.n].copy_(self.dead[: self.n])
+                new[k][:used].copy_(self.buf[k][:used])
+            dead[:used].copy_(self.dead[:used])
         self.buf, self.dead, self.cap = new, dead, cap
         self.spare = None
 
@@ -105,7 +132,7 @@ class _SpParticles:
         m = int(coords.shape[-1])
         if m == 0:
             return
-        if self.n + m > self.cap:
+        if _slots(self.n + m) > self.cap:
             self.reserve(max(self.n + m, int(1.5 * self.cap)))
         dev = self.device
         tx = coords if isinstance(coords, torch.Tensor) else torch.from_numpy(
@@ -117,10 +144,9 @@ class _SpParticles:
         if tx.device.type != "cuda":
             chimera.io_bytes["h2d"] += (tx.numel() + tp.numel() + tw.numel()) * 8
         tx, tp, tw = (t.to(dev, torch.float64) for t in (tx, tp, tw))
-        _lib.call("chm_sp_from_f64", *self.ptrs(), self.n, tx.data_ptr(), tx.stride(0),
-                  tx.stride(1), tp.data_ptr(), tp.stride(0), tp.stride(1), tw.data_ptr(),
-                  tw.stride(0), float(X0), float(dx), m, _stream())
-        self.dead[self.n: self.n + m].zero_()
+        _lib.call("chm_sp_from_f64", *self.ptrs(), self.dead.data_ptr(), self.n, tx.data_ptr(),
+                  tx.stride(0), tx.stride(1), tp.data_ptr(), tp.stride(0), tp.stride(1),
+                  tw.data_ptr(), tw.stride(0), float(X0), float(dx), m, _stream())
         self.n += m
 
     def compact(self):
@@ -137,7 +163,7 @@ class _SpParticles:
         chimera.io_bytes["d2h"] += 8
         self.buf, self.spare = self.spare, self.buf
         self.n = n
-        self.dead[:n].zero_()
+        self.dead[:_slots(n)].zero_()
         self.counters[0].zero_()
         self.moves = 0
 
@@ -210,13 +236,18 @@ class SplitRun:
                               dtype=torch.uint8, device=dev)
         self.scale_ws = torch.empty(_lib.query("chm_sp_scale_ws_bytes"), dtype=torch.uint8,
                                     device=dev)
-        # particles
+        # particles, each generation cell's particles in deposit-cell order
+        # (runs of 16 of the tile layout then share a deposit cell)
+        self.dr = float(A["dr"])
         self.parts = []
+        self.order0 = []  # the initial permutation of each species (particle order of to_fp64)
         for spc in self.fp.Particles:
             P = _SpParticles(dev, spc.num_particles)
             d = spc.Data
-            P.append_f64(d["coords"], d["momenta"], d["weights"], self.X0, self.dx)
+            o = cell_order(d["coords"], spc.Args.get("Num_p", 1), self.X0, self.dx, self.dr)
+            P.append_f64(d["coords"][:, o], d["momenta"][:, o], d["weights"][o], self.X0, self.dx)
             self.parts.append(P)
+            self.order0.append(o)
         self.scaleJ = torch.zeros(2, dtype=torch.float64, device=dev)
         self.scaleR = torch.zeros(2, dtype=torch.float64, device=dev)
         self.scaleBG = torch.zeros(2, dtype=torch.float64, device=dev)
@@ -407,16 +438,20 @@ class SplitRun:
         fp = self.fp
         xsteps = int(wind["shiftX"] / wind["TimeStep"]) + 1
         idx = {id(s): i for i, s in enumerate(fp.Particles)}
+        def ordered(spc, parts):
+            o = cell_order(parts[0], spc.Args.get("Num_p", 1), self.X0, self.dx, self.dr)
+            return [parts[0][:, o], parts[1][:, o], parts[2][o]]
+
         if "IonsOnTop" in wind["Features"]:
             s1, s2 = fp.Particles[:2]
-            parts = s1.gen_parts(Xsteps=xsteps, ProfileFunc=wind["AddPlasma"])
+            parts = ordered(s1, s1.gen_parts(Xsteps=xsteps, ProfileFunc=wind["AddPlasma"]))
             self.parts[idx[id(s1)]].append_f64(*parts, self.X0, self.dx)
             parts[-1] = parts[-1] * -1
             self.parts[idx[id(s2)]].append_f64(*parts, self.X0, self.dx)
         else:
             for s in fp.Particles:
-                self.parts[idx[id(s)]].append_f64(
-                    *s.gen_parts(Xsteps=xsteps, ProfileFunc=wind["AddPlasma"]), self.X0, self.dx)
+                parts = ordered(s, s.gen_parts(Xsteps=xsteps, ProfileFunc=wind["AddPlasma"]))
+                self.parts[idx[id(s)]].append_f64(*parts, self.X0, self.dx)
         self._scales_valid = False
 
     def _absorb(self, wind):

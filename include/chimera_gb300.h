@@ -408,6 +408,16 @@ int64_t chm_sp_ops_bytes(int64_t K, int64_t N, int64_t nmodes);
 int chm_sp_prepare_ops(chm_sp_ops *ops, const double *mats, int64_t K, int64_t N,
                        int64_t nmodes, void *buf, int64_t buf_bytes, void *stream);
 
+/* Split-form particle storage: eight SoA arrays ix (int32), fx, y, z, px,
+ * py, pz, w (float) in tiles of 512: particle i (its index in the species)
+ * sits at slot chm_sp_slot(i) = (i / 512) * 512 + 32 (i % 16) + (i / 16) % 32,
+ * so the 16 consecutive particles of a run belong to one GPU thread and a
+ * warp's loads are contiguous.  Arrays (and the uint8 dead flags) hold
+ * chm_sp_capacity(n) slots; slots of the last tile past n are not read.
+ * Arrays start on 16-byte boundaries. */
+int64_t chm_sp_capacity(int64_t n);
+int64_t chm_sp_slot(int64_t i);
+
 /* Deterministic global deposit scale: scale2[0] = 2^min(61 - ceil(log2 B),
  * 120), scale2[1] = B = sum |w| (device doubles). */
 int64_t chm_sp_scale_ws_bytes(void);
@@ -434,9 +444,11 @@ int chm_sp_gather_push(int32_t *ix, float *fx, float *y, float *z, float *px,
                        float win_f, float dr_inv, const void *eb_c64, int nx,
                        int nr, int nm, float dtq, void *stream);
 
-/* FP64 (3,n)/(n) particle arrays <-> split layout (offset = first slot). */
+/* FP64 (3,n)/(n) particle arrays (particle order) <-> split layout; from_f64
+ * writes particles offset .. offset+n-1 and clears their dead flags (dead
+ * may be NULL). */
 int chm_sp_from_f64(int32_t *ix, float *fx, float *y, float *z, float *px,
-                    float *py, float *pz, float *w, int64_t offset,
+                    float *py, float *pz, float *w, uint8_t *dead, int64_t offset,
                     const double *coord, int64_t x_cs, int64_t x_ps,
                     const double *momenta, int64_t p_cs, int64_t p_ps,
                     const double *wghts, int64_t w_ps, double X0, double dx,

@@ -169,10 +169,13 @@ def test_split_steps_track_fp64_form(mods, nsteps):
     s_ref, s_sp = ref.Solvers[0], run.solver
     err_eg = rel_l2(s_sp.Data["EG_fb"].cpu().numpy(), s_ref.Data["EG_fb"].cpu().numpy())
     err_eb = rel_l2(s_sp.Data["EB"].cpu().numpy(), s_ref.Data["EB"].cpu().numpy())
-    p_ref = ref.Particles[0].Data["momenta"].cpu().numpy()
+    # the split form stores each generation cell's particles in deposit-cell
+    # order; compare in that order
+    o = run.order0[0].cpu().numpy()
+    p_ref = ref.Particles[0].Data["momenta"].cpu().numpy()[:, o]
     p_sp = run.fp.Particles[0].Data["momenta"].cpu().numpy()
     err_p = rel_l2(p_sp, p_ref)
-    x_ref = ref.Particles[0].Data["coords"].cpu().numpy()
+    x_ref = ref.Particles[0].Data["coords"].cpu().numpy()[:, o]
     x_sp = run.fp.Particles[0].Data["coords"].cpu().numpy()
     print(f"split vs fp64 after {nsteps} steps: EG {err_eg:.2e} EB {err_eb:.2e} "
           f"p {err_p:.2e} x {np.abs(x_sp - x_ref).max():.2e}")
@@ -205,7 +208,26 @@ def _sp_particles(torch, n, nx, nr, dr, seed, runs=True):
             "pz": (0.05 * rng.standard_normal(n)).astype(np.float32),
             "w": (1e-3 * (0.5 + rng.random(n))).astype(np.float32)}
     cols["w"][rng.random(n) < 0.01] = 0.0
-    return {k: torch.from_numpy(v).cuda() for k, v in cols.items()}
+    # tile layout: particle i at slot chm_sp_slot(i) of arrays of whole tiles
+    cap = (n + 511) // 512 * 512
+    slot = _slots(n)
+    out = {}
+    for k, v in cols.items():
+        a = np.zeros(cap, dtype=v.dtype)
+        a[slot] = v
+        out[k] = torch.from_numpy(a).cuda()
+    return out
+
+
+def _slots(n):
+    """chm_sp_slot(i) for i < n (the tile layout of the split form)."""
+    i = np.arange(n, dtype=np.int64)
+    return (i & ~511) | ((i & 15) << 5) | ((i >> 4) & 31)
+
+
+def _gather(a, n):
+    """particle-order values 0 .. n-1 of a tile-layout array"""
+    return a[_slots(n)]
 
 
 @pytest.mark.parametrize("nm,runs,push", [(2, True, 1), (2, False, 1), (1, True, 1), (2, True, 0)])
@@ -251,15 +273,16 @@ def test_cell_run_deposit_equals_generic_kernel(mods, monkeypatch, nm, runs, pus
 
 
 def test_absorb_and_compact(mods):
-    """chm_sp_absorb marks exactly the particles outside the box; compaction
-    keeps the live ones in order and counts them."""
+    """chm_sp_absorb marks exactly the particles outside the box and returns
+    the scale of the survivors; compaction keeps the live ones in order."""
     torch, _lib, fm, split = mods
     n, nx, nr, dr = 30011, 64, 32, 0.5
     P = _sp_particles(torch, n, nx, nr, dr, 3, runs=False)
     names = ("ix", "fx", "y", "z", "px", "py", "pz", "w")
-    ref = {k: v.cpu().numpy().copy() for k, v in P.items()}
-    dead = torch.zeros(n, dtype=torch.uint8, device="cuda")
-    dead[:50] = 1  # already dead stay dead and are not counted again
+    ref = {k: _gather(v.cpu().numpy(), n) for k, v in P.items()}
+    cap = P["w"].numel()
+    dead = torch.zeros(cap, dtype=torch.uint8, device="cuda")
+    dead[torch.from_numpy(_slots(50)).cuda()] = 1  # already dead: stay dead, not counted again
     cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
     st = _st(torch)
     k, f, xmin, xmax, r2 = 100, 0.25, 8.0, 60.0, (12.0 * dr) ** 2
@@ -277,10 +300,10 @@ def test_absorb_and_compact(mods):
     newly = out_box.copy()
     newly[:50] = False
     torch.cuda.synchronize()
-    assert np.array_equal(dead.cpu().numpy().astype(bool), dead_ref)
+    assert np.array_equal(_gather(dead.cpu().numpy(), n).astype(bool), dead_ref)
     assert int(cnt[0]) == int(newly.sum())
     assert int(cnt[1]) == n - int(newly.sum())
-    w = P["w"].cpu().numpy()
+    w = _gather(P["w"].cpu().numpy(), n)
     assert np.all(w[newly] == 0) and np.array_equal(w[~dead_ref], ref["w"][~dead_ref])
     # the same pass gives the deposit scale of the surviving weights
     B = float(np.abs(w.astype(np.float64)).sum())
@@ -297,7 +320,17 @@ def test_absorb_and_compact(mods):
     assert m == int((~dead_ref).sum())
     for key in names:
         exp = (ref[key] if key != "w" else w)[~dead_ref]
-        assert np.array_equal(Q[key][:m].cpu().numpy(), exp), key
+        assert np.array_equal(_gather(Q[key].cpu().numpy(), m), exp), key
+
+
+def test_tile_slot_map(mods):
+    """chm_sp_slot / chm_sp_capacity follow the documented tile layout."""
+    torch, _lib, fm, split = mods
+    lib = _lib.load()
+    for i in (0, 1, 15, 16, 31, 511, 512, 513, 10**6 + 7):
+        assert lib.chm_sp_slot(i) == int(_slots(i + 1)[-1])
+    assert lib.chm_sp_capacity(1) == 512 and lib.chm_sp_capacity(513) == 1024
+    assert sorted(_slots(1024)) == list(range(1024))
 
 
 def _window_comps(seed):
