@@ -109,7 +109,8 @@ def build_run(device_kind, window, seed=1002):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples during the timed region."""
+    """nvidia-smi clock / throttle samples (every 100 ms) from the warm-up
+    through the timed region."""
 
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -125,7 +126,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -350,14 +351,16 @@ def run_gb300(args):
             return el.num_particles
     n_moving = nmov()
     stream = torch.cuda.current_stream()
+    # the clock sampler starts before the warm-up (its start-up stays out of
+    # the timed region) and samples through warm-up and timed steps
+    clocks = ClockSampler(local)
+    clocks.start()
     for i in range(1, args.warmup + 1):
         run.make_step(i)
     torch.cuda.synchronize()
     # L2: the particle state (0.53 GB per species in the split form, 1.9 GB
     # in the FP64 form) is far larger than the 129 MB L2, so every step
     # streams from HBM.
-    clocks = ClockSampler(local)
-    clocks.start()
     barrier(world)
     torch.cuda.synchronize()
     launches0 = lib.chm_launch_count()

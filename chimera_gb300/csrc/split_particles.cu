@@ -41,7 +41,7 @@ constexpr int kTile = kRunLen * kTileRuns;         // 512 particles per tile
 constexpr int kDepWarps = 4;                       // tiles per block
 constexpr int kDepThreads = 32 * kDepWarps;        // 128
 constexpr int kDepBlock = kTile * kDepWarps;       // 2048 particles per block
-constexpr int kSpBoxBytes = 56 * 1024;             // 7168 int64 values
+constexpr int kSpBoxBytes = 44 * 1024;             // 5632 int64 values
 
 // physical slot of particle i and the particle of a slot
 __host__ __device__ __forceinline__ i64 phys_of(i64 i) {
@@ -156,50 +156,61 @@ struct PushDepArgs {
   const double *scaleJ, *scaleR;  // global scales 2^e
 };
 
-// Block box: 64-bit fixed-point values at the global scales, planes (J: 3 nm,
-// then rho: nm) of bnr x bnx nodes starting at (br0, bx0), {re, im}
-// interleaved.
+// Block box: 64-bit fixed-point values at the global scales.  A node holds
+// 4 (2 nm - 1) values: for each of the components J_x, J_y, J_z, rho the
+// parts (mode 0 re; mode 1 re, im; ...) -- mode 0 has no imaginary part.
+// Value (c, part) of node (r, x) sits at ((c P + part) bnr + r - br0) bnx +
+// x - bx0, P = 2 nm - 1.
 struct BoxGeo {
   unsigned long long *box;
   long long bx0, br0, bnx, bnr;
   float sJ, sR;                  // 2^eJ, 2^eR
   unsigned long long *gJ, *gR;   // global accumulators
-  int nx, nr, nmj;               // grid; the nmj = 3 nm J planes precede rho
+  int nx, nr, nm;                // grid
 };
 
-// Adds v at node (r, x) of a plane, part im, to the box; a node outside the
-// box (the plan bounds every deposit location, so this is a guard only) goes
-// to the global accumulator directly -- both hold the same scale.
+// part index of (mode m, imaginary flag)
+__device__ __forceinline__ int part_of(int m, int im) { return m == 0 ? 0 : 2 * m - 1 + im; }
+
+// Adds v at node (r, x) of plane (m + nm l for J, 3 nm + m for rho), part
+// im, to the box; a node outside the box (the plan bounds every deposit
+// location, so this is a guard only) goes to the global accumulator
+// directly -- both hold the same scale.
 __device__ __forceinline__ void box_put(const BoxGeo &B, long long plane, int r, int x, int im,
                                         long long v) {
+  const int c = (int)(plane / B.nm), m = (int)(plane - (long long)c * B.nm);
+  if (m == 0 && im) return;  // mode 0 deposits no imaginary part
   const long long rr = r - B.br0, xx = x - B.bx0;
   if (rr >= 0 && rr < B.bnr && xx >= 0 && xx < B.bnx) {
-    atomicAdd(&B.box[((plane * B.bnr + rr) * B.bnx + xx) * 2 + im], (unsigned long long)v);
+    const long long cp = (long long)c * (2 * B.nm - 1) + part_of(m, im);
+    atomicAdd(&B.box[(cp * B.bnr + rr) * B.bnx + xx], (unsigned long long)v);
     return;
   }
-  const bool isj = plane < B.nmj;
-  const long long pl = isj ? plane : plane - B.nmj;
+  const bool isj = c < 3;
+  const long long pl = isj ? plane : m;
   unsigned long long *acc = isj ? B.gJ : B.gR;
   atomicAdd(&acc[2 * ((pl * B.nr + r) * B.nx + x) + im], (unsigned long long)v);
 }
 
 // Adds the block box into the global accumulators: warp w takes the box
-// rows w, w + 8, ... (a row: 2 bnx values of one plane and r), lanes stride
-// along x.
+// rows w, w + nwarp, ... (a row: bnx values of one component, part and r),
+// lanes stride along x.
 __device__ void flush_box(const BoxGeo &B, long long nvals) {
-  const int rowlen = 2 * (int)B.bnx, bnr = (int)B.bnr;
-  const int nrows = (int)(nvals / rowlen);
+  const int bnx = (int)B.bnx, bnr = (int)B.bnr, P = 2 * B.nm - 1;
+  const int nrows = (int)(nvals / bnx);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int row = warp; row < nrows; row += nwarp) {
-    const int plane = row / bnr, rr = row - plane * bnr;
-    const bool isj = plane < B.nmj;
-    const int pl = isj ? plane : plane - B.nmj;
+    const int cp = row / bnr, rr = row - cp * bnr;
+    const int c = cp / P, part = cp - c * P;
+    const int m = (part + 1) >> 1, im = (part > 0 && (part & 1) == 0) ? 1 : 0;
+    const bool isj = c < 3;
+    const int pl = isj ? m + B.nm * c : m;
     unsigned long long *acc = (isj ? B.gJ : B.gR) +
-                              2 * (((i64)pl * B.nr + (rr + B.br0)) * B.nx + B.bx0);
-    const unsigned long long *src = B.box + (i64)row * rowlen;
-    for (int t = lane; t < rowlen; t += 32) {
+                              2 * (((i64)pl * B.nr + (rr + B.br0)) * B.nx + B.bx0) + im;
+    const unsigned long long *src = B.box + (i64)row * bnx;
+    for (int t = lane; t < bnx; t += 32) {
       const unsigned long long v = src[t];
-      if (v) atomicAdd(acc + t, v);
+      if (v) atomicAdd(acc + 2 * t, v);
     }
   }
 }
@@ -307,8 +318,8 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb) {
   const long long bx1 = min(bb[1], A.G.nx - 1), br1 = min(bb[3], A.G.nr - 1);
   P.bnx = bx1 - P.bx0 + 1;
   P.bnr = br1 - P.br0 + 1;
-  const int nplanes = A.G.nm * 4;  // J: 3 nm planes, rho: nm planes
-  P.nvals = (bb[0] <= bb[1] && P.bnx > 0 && P.bnr > 0) ? P.bnx * P.bnr * nplanes * 2 : 0;
+  const int per_node = 4 * (2 * A.G.nm - 1);  // J_x, J_y, J_z, rho x mode parts
+  P.nvals = (bb[0] <= bb[1] && P.bnx > 0 && P.bnr > 0) ? P.bnx * P.bnr * per_node : 0;
   P.use_box = P.nvals > 0 && P.nvals * 8 <= kSpBoxBytes;
   P.sJ = A.scaleJ ? (float)A.scaleJ[0] : 1.0f;
   P.sR = A.scaleR ? (float)A.scaleR[0] : 1.0f;
@@ -318,7 +329,7 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb) {
 __device__ __forceinline__ BoxGeo make_geo(unsigned long long *box, const BlockPlan &P,
                                            const PushDepArgs &A) {
   return BoxGeo{box, P.bx0, P.br0, P.bnx, P.bnr, P.sJ, P.sR, A.accJ, A.accR,
-                A.G.nx, A.G.nr, 3 * A.G.nm};
+                A.G.nx, A.G.nr, A.G.nm};
 }
 
 // Generic push + deposit (any nm): one particle per thread and slot, each
@@ -405,19 +416,18 @@ __device__ __forceinline__ void acc_flush(CellAcc<NM, NC> &c, int plane0, const 
   const int rr = c.cr - (int)B.br0, xx = c.cx - (int)B.bx0;
   if (rr >= 0 && rr + 1 < B.bnr && xx >= 0 && xx + 1 < B.bnx) {
     // all four nodes inside the box (x nodes inside the grid as the box is)
-    const int rs = 2 * (int)B.bnx, ps = rs * (int)B.bnr;
-    unsigned long long *b0 = B.box + (rr * rs + 2 * xx);
+    const int rs = (int)B.bnx, ps = rs * (int)B.bnr;  // row and (component, part) strides
+    unsigned long long *b0 = B.box + (rr * rs + xx);
+    const int c0 = plane0 / NM;  // first component: 0 (J) or 3 (rho)
 #pragma unroll
     for (int l = 0; l < NC; ++l)
 #pragma unroll
       for (int p = 0; p < 2 * NM - 1; ++p) {
-        const int m = (p + 1) >> 1;
-        const int im = (p > 0 && (p & 1) == 0) ? 1 : 0;
-        unsigned long long *bp = b0 + (plane0 + m + G.nm * l) * ps + im;
+        unsigned long long *bp = b0 + ((c0 + l) * (2 * NM - 1) + p) * ps;
 #pragma unroll
         for (int nd = 0; nd < 4; ++nd) {
           const long long v = f2ll(c.v[l][p][nd]);
-          if (v) atomicAdd(bp + (nd >> 1) * rs + 2 * (nd & 1), (unsigned long long)v);
+          if (v) atomicAdd(bp + (nd >> 1) * rs + (nd & 1), (unsigned long long)v);
         }
       }
     return;
