@@ -502,6 +502,69 @@ def run_gb300(args):
     return 0
 
 
+def run_batched(args):
+    """Batched workload: `args.batched` laser-wakefield instances of uneven
+    size (chimera_gb300.batched.draw_instances, seed 1005) advanced together,
+    one CUDA stream each, in the split form; against the same instances
+    advanced one by one in the plain FP64 form."""
+    import torch
+
+    from chimera_gb300 import _lib
+    from chimera_gb300.batched import BatchedRun, draw_instances, lwfa_instance
+    from chimera_gb300.messages import msg
+    msg.quiet = True
+    lib = _lib.load()
+    params = draw_instances(args.batched, 1005)
+    batch = BatchedRun([lwfa_instance(**p) for p in params])
+    for i in range(1, args.warmup + 1):
+        batch.make_step(i)
+    batch.synchronize()
+    torch.cuda.synchronize()
+    launches0 = lib.chm_launch_count()
+    t0 = time.perf_counter()
+    psteps = 0
+    for i in range(args.warmup + 1, args.warmup + args.steps + 1):
+        batch.make_step(i)
+        psteps += batch.num_moving
+    batch.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    launches = lib.chm_launch_count() - launches0
+    value = psteps / wall
+    # the same instances one by one in the plain FP64 form (their FP64 runs,
+    # two steps each after one warm-up step)
+    t_fp = 0.0
+    n_fp = 0
+    for run in batch.runs:
+        fp = run.fp
+        fp.make_step(args.warmup + args.steps + 1)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for i in range(args.warmup + args.steps + 2, args.warmup + args.steps + 4):
+            fp.make_step(i)
+        torch.cuda.synchronize()
+        t_fp += (time.perf_counter() - t1) / 2
+        n_fp += sum(sp.num_particles for sp in fp.Particles if "Still" not in sp.Args["Features"])
+    fp_value = n_fp / t_fp
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (bf16x3 split tensor-core GEMMs)",
+        "data": "synthetic",
+        "config": {"workload": f"batched_lwfa_{args.batched}", "instances": len(params),
+                   "particles_moving": psteps // args.steps,
+                   "nx": sorted({p["nx"] for p in params}), "nr": sorted({p["nr"] for p in params}),
+                   "modes": sorted({p["max_mode"] + 1 for p in params}),
+                   "streams": len(batch.streams), "timing": "host wall clock, all streams synced"},
+        "gpu_launches": launches,
+        "fp64_one_by_one": {"value": fp_value, "unit": METRIC,
+                            "what": "each instance's plain FP64 step alone, summed over instances"},
+        "batched_over_fp64": value / fp_value,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -514,6 +577,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--form", default="split", choices=["fp64", "split"],
                     help="fp64 = plain FP64 form; split = split-precision form")
+    ap.add_argument("--batched", type=int, default=0,
+                    help="run the batched workload with this many instances instead")
     ap.add_argument("--size", default="cfg2", choices=sorted(SIZES),
                     help="cfg2 = the benchmark workload; prof, small = reduced cases for profiling")
     args = ap.parse_args()
@@ -526,6 +591,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.batched:
+        return run_batched(args)
     return run_gb300(args)
 
 

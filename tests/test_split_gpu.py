@@ -133,13 +133,13 @@ def test_split_spectral_operators_match_fp64(mods, lpa):
     assert rel_l2(EBs.cpu().numpy(), EBd.cpu().numpy()) < TOL_T
 
 
-def _lpa_comps(seed, xchunked=False):
+def _lpa_comps(seed, xchunked=False, max_mode=1):
     from chimera_gb300 import Solver, Specie
     from chimera_gb300.messages import msg
     msg.quiet = True
     np.random.seed(seed)
     dx, dr = 0.1, 0.25
-    solver = Solver({"Grid": (-6.0, 0.4, 4.0, dx, dr), "TimeStep": dx, "MaxAzimuthMode": 1,
+    solver = Solver({"Grid": (-6.0, 0.4, 4.0, dx, dr), "TimeStep": dx, "MaxAzimuthMode": max_mode,
                      "Features": ("SpaceCharge", "StillAsBackground")})
     solver.add_gauss_beam({"a0": 1.0, "k0": 1.0, "x0": -2.5, "x_foc": 2.0, "Lx": 1.5, "LR": 2.5})
     el_in = {"Grid": (-6.0, 0.4, 4.0, dx, dr), "TimeStep": dx, "Density": 0.02,
@@ -156,12 +156,13 @@ def _lpa_comps(seed, xchunked=False):
             "MovingFrames": ({"TimeStep": dx, "Steps": 1, "Velocity": 1.0},)}
 
 
-@pytest.mark.parametrize("nsteps", [1, 6])
-def test_split_steps_track_fp64_form(mods, nsteps):
+@pytest.mark.parametrize("nsteps,max_mode", [(1, 1), (6, 1), (6, 2)])
+def test_split_steps_track_fp64_form(mods, nsteps, max_mode):
+    """max_mode 2 (three stored modes) runs the per-particle kernels."""
     torch, _lib, fm, split = mods
     from chimera_gb300 import ChimeraRun
-    ref = ChimeraRun(_lpa_comps(1001))
-    run = split.SplitRun(_lpa_comps(1001))
+    ref = ChimeraRun(_lpa_comps(1001, max_mode=max_mode))
+    run = split.SplitRun(_lpa_comps(1001, max_mode=max_mode))
     for i in range(1, nsteps + 1):
         ref.make_step(i)
         run.make_step(i)
@@ -392,3 +393,29 @@ def test_cell_run_gather_matches_generic_kernel(mods, monkeypatch, nm, runs):
     p0 = np.stack([P0[k].cpu().numpy() for k in ("px", "py", "pz")])
     assert np.abs(out["run"] - p0).max() > 1e-3  # the fields did push
     assert np.abs(out["run"] - out["generic"]).max() <= 1e-6 * np.abs(out["generic"]).max()
+
+
+def test_batched_instances_match_single_runs(mods):
+    """Instances advanced together on separate streams give bitwise the
+    fields and particles they give when advanced alone."""
+    torch, _lib, fm, split = mods
+    from chimera_gb300.batched import BatchedRun, draw_instances, lwfa_instance
+    from chimera_gb300.messages import msg
+    msg.quiet = True
+    params = [dict(p, nx=min(p["nx"], 256), nr=min(p["nr"], 32)) for p in draw_instances(3, 7)]
+    batch = BatchedRun([lwfa_instance(**p) for p in params])
+    for i in range(1, 4):
+        batch.make_step(i)
+    batch.synchronize()
+    for p, run in zip(params, batch.runs):
+        alone = split.SplitRun(lwfa_instance(**p))
+        for i in range(1, 4):
+            alone.make_step(i)
+        torch.cuda.synchronize()
+        assert torch.equal(alone.EG, run.EG) and torch.equal(alone.EB, run.EB)
+        for Pa, Pb in zip(alone.parts, run.parts):
+            assert Pa.n == Pb.n
+            for k in Pa.NAMES:
+                assert torch.equal(Pa.buf[k][: Pa.n], Pb.buf[k][: Pb.n]), k
+    assert batch.num_moving == sum(r.num_moving for r in batch.runs) > 0
+    assert _lib.load().chm_sp_umma_status() == 0
