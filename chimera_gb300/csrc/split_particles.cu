@@ -18,12 +18,13 @@
 // 32 consecutive words.  Arrays hold whole tiles; slots past the last
 // particle are not read.
 //
-// Deposition stays deterministic without float atomics: values are rounded
-// to the global 64-bit fixed-point quantum 2^-e (2^e = 2^(61 - ceil(log2
-// sum |w|))) and added as integers, first into a shared-memory box of the
-// block's nodes, then into the global accumulator.  Integer sums are
-// order-independent; the run kernel sums the particles of a run in FP32
-// before rounding, which depends only on the (fixed) particle order.
+// Deposition stays deterministic without float atomics: each block adds its
+// values as 32-bit integers at its own power-of-two scale (from the block's
+// sum |w|) into a shared-memory box of its nodes, then adds the box into the
+// global 64-bit accumulator (scale 2^(61 - ceil(log2 sum |w|))) with an exact
+// power-of-two shift.  Integer sums are order-independent; the run kernel
+// sums the particles of a run in FP32 before rounding, which depends only on
+// the (fixed) particle order.
 #include <climits>
 #include <cstdlib>
 #include <cstring>
@@ -41,7 +42,7 @@ constexpr int kTile = kRunLen * kTileRuns;         // 512 particles per tile
 constexpr int kDepWarps = 4;                       // tiles per block
 constexpr int kDepThreads = 32 * kDepWarps;        // 128
 constexpr int kDepBlock = kTile * kDepWarps;       // 2048 particles per block
-constexpr int kSpBoxBytes = 44 * 1024;             // 5632 int64 values
+constexpr int kSpBoxBytes = 40 * 1024;             // 10240 int32 values
 
 // physical slot of particle i and the particle of a slot
 __host__ __device__ __forceinline__ i64 phys_of(i64 i) {
@@ -156,40 +157,57 @@ struct PushDepArgs {
   const double *scaleJ, *scaleR;  // global scales 2^e
 };
 
-// Block box: 64-bit fixed-point values at the global scales.  A node holds
-// 4 (2 nm - 1) values: for each of the components J_x, J_y, J_z, rho the
-// parts (mode 0 re; mode 1 re, im; ...) -- mode 0 has no imaginary part.
-// Value (c, part) of node (r, x) sits at ((c P + part) bnr + r - br0) bnx +
-// x - bx0, P = 2 nm - 1.
+// Block box: 32-bit fixed-point values at the block's own scales 2^elJ,
+// 2^elR (from bounds of the block's sum of |J| and |rho| values, so the box
+// cannot overflow), added into the global 64-bit grid (scales 2^eJ, 2^eR) by
+// an exact power-of-two shift when the block is done.  A node holds
+// ncomp (2 nm - 1) values: for each deposited component (J_x, J_y, J_z and/or
+// rho; c0 the first) the parts (mode 0 re; mode 1 re, im; ...) -- mode 0 has
+// no imaginary part.  Value (c, part) of node (r, x) sits at
+// (((c - c0) P + part) bnr + r - br0) bnx + x - bx0, P = 2 nm - 1.
 struct BoxGeo {
-  unsigned long long *box;
+  int *box;
   long long bx0, br0, bnx, bnr;
-  float sJ, sR;                  // 2^eJ, 2^eR
+  int c0;                        // first component held (0: J and rho, 3: rho only)
+  int elJ, elR, eJ, eR;          // local (J, rho) and global quantum exponents
   unsigned long long *gJ, *gR;   // global accumulators
   int nx, nr, nm;                // grid
 };
 
+// value at the local quantum 2^-el -> global quantum 2^-eg: an exact left
+// shift when eg >= el (the usual case: a block holds a small share of the
+// total weight), otherwise a right shift rounded half away from zero
+__device__ __forceinline__ long long rescale(long long q, int el, int eg) {
+  const int s = el - eg;
+  if (s <= 0) return q << min(-s, 62);
+  if (s >= 62) return 0;
+  const long long h = 1LL << (s - 1);
+  return (q >= 0) ? ((q + h) >> s) : -((-q + h) >> s);
+}
+
 // part index of (mode m, imaginary flag)
 __device__ __forceinline__ int part_of(int m, int im) { return m == 0 ? 0 : 2 * m - 1 + im; }
 
-// Adds v at node (r, x) of plane (m + nm l for J, 3 nm + m for rho), part
-// im, to the box; a node outside the box (the plan bounds every deposit
-// location, so this is a guard only) goes to the global accumulator
-// directly -- both hold the same scale.
+// Adds v (local quantum) at node (r, x) of plane (m + nm l for J, 3 nm + m
+// for rho), part im, to the box; a node outside the box (the plan bounds
+// every deposit location, so this is a guard only) goes to the global
+// accumulator directly.
 __device__ __forceinline__ void box_put(const BoxGeo &B, long long plane, int r, int x, int im,
-                                        long long v) {
+                                        int v) {
   const int c = (int)(plane / B.nm), m = (int)(plane - (long long)c * B.nm);
   if (m == 0 && im) return;  // mode 0 deposits no imaginary part
   const long long rr = r - B.br0, xx = x - B.bx0;
   if (rr >= 0 && rr < B.bnr && xx >= 0 && xx < B.bnx) {
-    const long long cp = (long long)c * (2 * B.nm - 1) + part_of(m, im);
-    atomicAdd(&B.box[(cp * B.bnr + rr) * B.bnx + xx], (unsigned long long)v);
+    const long long cp = (long long)(c - B.c0) * (2 * B.nm - 1) + part_of(m, im);
+    atomicAdd(&B.box[(cp * B.bnr + rr) * B.bnx + xx], v);
     return;
   }
   const bool isj = c < 3;
+  const long long q = isj ? rescale(v, B.elJ, B.eJ) : rescale(v, B.elR, B.eR);
+  if (q == 0) return;
   const long long pl = isj ? plane : m;
   unsigned long long *acc = isj ? B.gJ : B.gR;
-  atomicAdd(&acc[2 * ((pl * B.nr + r) * B.nx + x) + im], (unsigned long long)v);
+  atomicAdd(&acc[2 * ((pl * B.nr + r) * B.nx + x) + im], (unsigned long long)q);
 }
 
 // Adds the block box into the global accumulators: warp w takes the box
@@ -201,16 +219,19 @@ __device__ void flush_box(const BoxGeo &B, long long nvals) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   for (int row = warp; row < nrows; row += nwarp) {
     const int cp = row / bnr, rr = row - cp * bnr;
-    const int c = cp / P, part = cp - c * P;
+    const int cb = cp / P, part = cp - cb * P, c = cb + B.c0;
     const int m = (part + 1) >> 1, im = (part > 0 && (part & 1) == 0) ? 1 : 0;
     const bool isj = c < 3;
     const int pl = isj ? m + B.nm * c : m;
+    const int eg = isj ? B.eJ : B.eR, el = isj ? B.elJ : B.elR;
     unsigned long long *acc = (isj ? B.gJ : B.gR) +
                               2 * (((i64)pl * B.nr + (rr + B.br0)) * B.nx + B.bx0) + im;
-    const unsigned long long *src = B.box + (i64)row * bnx;
+    const int *src = B.box + (i64)row * bnx;
     for (int t = lane; t < bnx; t += 32) {
-      const unsigned long long v = src[t];
-      if (v) atomicAdd(acc + 2 * t, v);
+      const int v = src[t];
+      if (v == 0) continue;
+      const long long q = rescale(v, el, eg);
+      if (q) atomicAdd(acc + 2 * t, (unsigned long long)q);
     }
   }
 }
@@ -262,11 +283,16 @@ __device__ __forceinline__ Pushed push_one(const PushDepArgs &A, i64 i) {
 // radius.  (Nodes outside the box go straight to the global accumulator.)
 struct BlockPlan {
   long long bx0, br0, bnx, bnr, nvals;
+  int c0;          // first component held by the box
   bool use_box;
-  float sJ, sR;  // global scales 2^eJ, 2^eR
+  float lJ, lR;    // local scales 2^elJ, 2^elR
+  int elJ, elR;    // local quantum exponents
+  int eJ, eR;      // global quantum exponents
+  float sJ, sR;    // global scales 2^eJ, 2^eR (path without a box)
 };
 
 __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb) {
+  __shared__ float wsm[2][kDepThreads / 32];
   if (threadIdx.x == 0) {
     bb[0] = INT_MAX;
     bb[1] = INT_MIN;
@@ -275,7 +301,7 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb) {
   }
   __syncthreads();
   int xlo = INT_MAX, xhi = INT_MIN;
-  float r2lo = INFINITY, r2hi = -INFINITY;
+  float r2lo = INFINITY, r2hi = -INFINITY, wsum = 0.0f, jsum = 0.0f;
   // independent loads (no load depends on another), 4 slots per step
 #pragma unroll 4
   for (int s = threadIdx.x; s < kDepBlock; s += blockDim.x) {
@@ -285,12 +311,23 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb) {
     const float w = A.P.w[q];
     const int ix = A.P.ix[q];
     const float y = A.P.y[q], z = A.P.z[q];
+    float pp = 0.0f;
+    if (A.dep_j) {
+      const float px = A.P.px[q], py = A.P.py[q], pz = A.P.pz[q];
+      // max_l |v_l| = max_l |p_l| / gamma
+      pp = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz))) *
+           rsqrtf(1.0f + (px * px + py * py + pz * pz));
+    }
     if (!valid || w == 0.0f) continue;
     xlo = min(xlo, ix);
     xhi = max(xhi, ix);
     const float r2 = y * y + z * z;
     r2lo = fminf(r2lo, r2);
     r2hi = fmaxf(r2hi, r2);
+    wsum += fabsf(w);
+    // |w v_l| <= |w| max_l |v_l|: a bound of the current values (with a
+    // little room for the reciprocal square root)
+    jsum += fabsf(w) * fminf(1.0f, pp * 1.0001f);
   }
   int x0 = INT_MAX, x1 = INT_MIN, r0 = INT_MAX, r1 = INT_MIN;
   if (xlo <= xhi) {
@@ -305,37 +342,58 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb) {
   x1 = __reduce_max_sync(0xffffffffu, x1);
   r0 = __reduce_min_sync(0xffffffffu, r0);
   r1 = __reduce_max_sync(0xffffffffu, r1);
+  for (int o = 16; o > 0; o >>= 1) {
+    wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+    jsum += __shfl_xor_sync(0xffffffffu, jsum, o);
+  }
   if ((threadIdx.x & 31) == 0) {
     atomicMin(&bb[0], x0);
     atomicMax(&bb[1], x1);
     atomicMin(&bb[2], r0);
     atomicMax(&bb[3], r1);
+    wsm[0][threadIdx.x >> 5] = wsum;
+    wsm[1][threadIdx.x >> 5] = jsum;
   }
   __syncthreads();
   BlockPlan P;
+  float Bl = 0.0f, Bj = 0.0f;
+  for (int k = 0; k < kDepThreads / 32; ++k) {  // fixed order
+    Bl += wsm[0][k];
+    Bj += wsm[1][k];
+  }
   P.bx0 = max(bb[0], 0);
   P.br0 = max(bb[2], 0);
   const long long bx1 = min(bb[1], A.G.nx - 1), br1 = min(bb[3], A.G.nr - 1);
   P.bnx = bx1 - P.bx0 + 1;
   P.bnr = br1 - P.br0 + 1;
-  const int per_node = 4 * (2 * A.G.nm - 1);  // J_x, J_y, J_z, rho x mode parts
+  // deposited components (J_x, J_y, J_z and/or rho) x mode parts
+  const int per_node = (3 * (A.dep_j ? 1 : 0) + (A.dep_rho ? 1 : 0)) * (2 * A.G.nm - 1);
+  P.c0 = A.dep_j ? 0 : 3;
   P.nvals = (bb[0] <= bb[1] && P.bnx > 0 && P.bnr > 0) ? P.bnx * P.bnr * per_node : 0;
-  P.use_box = P.nvals > 0 && P.nvals * 8 <= kSpBoxBytes;
+  P.use_box = P.nvals > 0 && P.nvals * 4 <= kSpBoxBytes && Bl > 0.0f && isfinite(Bl);
+  // a node value of a particle is at most |w| (rho) or |w| max_l |v_l| (J),
+  // so each part of the box stays below 2^30 (one bit of margin for the
+  // FP32 sums and the per-run rounding)
+  P.elR = P.use_box ? 30 - ceil_log2((double)Bl) : 0;
+  P.elJ = (P.use_box && Bj > 0.0f) ? min(30 - ceil_log2((double)Bj), 120) : P.elR;
+  P.lR = ldexpf(1.0f, P.elR);
+  P.lJ = ldexpf(1.0f, P.elJ);
   P.sJ = A.scaleJ ? (float)A.scaleJ[0] : 1.0f;
   P.sR = A.scaleR ? (float)A.scaleR[0] : 1.0f;
+  P.eJ = A.scaleJ ? ilogb(A.scaleJ[0]) : 0;
+  P.eR = A.scaleR ? ilogb(A.scaleR[0]) : 0;
   return P;
 }
 
-__device__ __forceinline__ BoxGeo make_geo(unsigned long long *box, const BlockPlan &P,
-                                           const PushDepArgs &A) {
-  return BoxGeo{box, P.bx0, P.br0, P.bnx, P.bnr, P.sJ, P.sR, A.accJ, A.accR,
+__device__ __forceinline__ BoxGeo make_geo(int *box, const BlockPlan &P, const PushDepArgs &A) {
+  return BoxGeo{box, P.bx0, P.br0, P.bnx, P.bnr, P.c0, P.elJ, P.elR, P.eJ, P.eR, A.accJ, A.accR,
                 A.G.nx, A.G.nr, A.G.nm};
 }
 
 // Generic push + deposit (any nm): one particle per thread and slot, each
 // value rounded to the global quantum and added to the box.
 __global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A) {
-  extern __shared__ __align__(16) unsigned long long box[];
+  extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
   const i64 base = (i64)blockIdx.x * kDepBlock;
   const BlockPlan Pl = plan_block(A, base, bb);
@@ -352,11 +410,12 @@ __global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A
       if (A.dep_j) {
         const Loc L = locate(q.ixh, q.fxh, q.yh, q.zh, A.G);
         deposit_at(L, q.vj, 3, 0, A.G, [&](int plane, int r, int x, float re, float im) {
-          const long long qr = f2ll(re * geo.sJ), qi = f2ll(im * geo.sJ);
           if (Pl.use_box) {
+            const int qr = __float2int_rn(re * Pl.lJ), qi = __float2int_rn(im * Pl.lJ);
             if (qr) box_put(geo, plane, r, x, 0, qr);
             if (qi) box_put(geo, plane, r, x, 1, qi);
           } else {
+            const long long qr = f2ll(re * Pl.sJ), qi = f2ll(im * Pl.sJ);
             const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
             if (qr) atomicAdd(&A.accJ[2 * e], (unsigned long long)qr);
             if (qi) atomicAdd(&A.accJ[2 * e + 1], (unsigned long long)qi);
@@ -367,11 +426,12 @@ __global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A
         const Loc L = locate(q.ixn, q.fxn, q.yn, q.zn, A.G);
         const float wv[1] = {w};
         deposit_at(L, wv, 1, 3 * A.G.nm, A.G, [&](int plane, int r, int x, float re, float im) {
-          const long long qr = f2ll(re * geo.sR), qi = f2ll(im * geo.sR);
           if (Pl.use_box) {
+            const int qr = __float2int_rn(re * Pl.lR), qi = __float2int_rn(im * Pl.lR);
             if (qr) box_put(geo, plane, r, x, 0, qr);
             if (qi) box_put(geo, plane, r, x, 1, qi);
           } else {
+            const long long qr = f2ll(re * Pl.sR), qi = f2ll(im * Pl.sR);
             const i64 e = ((i64)(plane - 3 * A.G.nm) * A.G.nr + r) * A.G.nx + x;
             if (qr) atomicAdd(&A.accR[2 * e], (unsigned long long)qr);
             if (qi) atomicAdd(&A.accR[2 * e + 1], (unsigned long long)qi);
@@ -399,8 +459,9 @@ __global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A
 // box when the cell changes and at the end.
 // ----------------------------------------------------------------------
 
-// node sums of one deposit cell: v[comp][part][node], part 0 = mode 0 re,
-// then (re, im) of modes 1 .. NM-1; node = 2 j + k (r + j, x + k)
+// node sums of one deposit cell at the block scale: v[comp][part][node],
+// part 0 = mode 0 re, then (re, im) of modes 1 .. NM-1; node = 2 j + k
+// (r + j, x + k)
 template <int NM, int NC>
 struct CellAcc {
   int cx, cr;
@@ -417,17 +478,17 @@ __device__ __forceinline__ void acc_flush(CellAcc<NM, NC> &c, int plane0, const 
   if (rr >= 0 && rr + 1 < B.bnr && xx >= 0 && xx + 1 < B.bnx) {
     // all four nodes inside the box (x nodes inside the grid as the box is)
     const int rs = (int)B.bnx, ps = rs * (int)B.bnr;  // row and (component, part) strides
-    unsigned long long *b0 = B.box + (rr * rs + xx);
+    int *b0 = B.box + (rr * rs + xx);
     const int c0 = plane0 / NM;  // first component: 0 (J) or 3 (rho)
 #pragma unroll
     for (int l = 0; l < NC; ++l)
 #pragma unroll
       for (int p = 0; p < 2 * NM - 1; ++p) {
-        unsigned long long *bp = b0 + ((c0 + l) * (2 * NM - 1) + p) * ps;
+        int *bp = b0 + ((c0 + l - B.c0) * (2 * NM - 1) + p) * ps;
 #pragma unroll
         for (int nd = 0; nd < 4; ++nd) {
-          const long long v = f2ll(c.v[l][p][nd]);
-          if (v) atomicAdd(bp + (nd >> 1) * rs + (nd & 1), (unsigned long long)v);
+          const int v = __float2int_rn(c.v[l][p][nd]);
+          if (v) atomicAdd(bp + (nd >> 1) * rs + (nd & 1), v);
         }
       }
     return;
@@ -441,7 +502,7 @@ __device__ __forceinline__ void acc_flush(CellAcc<NM, NC> &c, int plane0, const 
       const long long plane = plane0 + m + (long long)G.nm * l;
 #pragma unroll
       for (int nd = 0; nd < 4; ++nd) {
-        const long long v = f2ll(c.v[l][p][nd]);
+        const int v = __float2int_rn(c.v[l][p][nd]);
         const int j = nd >> 1, k = nd & 1;
         const int gx = c.cx + k;
         if (v == 0 || gx < 0 || gx >= G.nx) continue;
@@ -450,7 +511,7 @@ __device__ __forceinline__ void acc_flush(CellAcc<NM, NC> &c, int plane0, const 
     }
 }
 
-// val: the particle's values already multiplied by the global scale
+// val: the particle's values already multiplied by the block scale
 template <int NM, int NC>
 __device__ __forceinline__ void acc_add(CellAcc<NM, NC> &c, const Loc &L, const float *val,
                                         int plane0, const SpGrid &G, const BoxGeo &B) {
@@ -500,7 +561,7 @@ __device__ __forceinline__ void acc_add(CellAcc<NM, NC> &c, const Loc &L, const 
 
 template <int NM, bool PUSH, bool DJ, bool DR>
 __global__ void __launch_bounds__(kDepThreads, 4) push_deposit_run_kernel(PushDepArgs A) {
-  extern __shared__ __align__(16) unsigned long long box[];
+  extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
   const i64 base = (i64)blockIdx.x * kDepBlock;
   const BlockPlan Pl = plan_block(A, base, bb);
@@ -572,10 +633,11 @@ __global__ void __launch_bounds__(kDepThreads, 4) push_deposit_run_kernel(PushDe
       if (w == 0.0f) continue;
       if (DJ && u.moving) {  // grid_deps.f90:42: no current from particles at rest
         const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, A.G);
-        const float vs[3] = {u.vj[0] * Pl.sJ, u.vj[1] * Pl.sJ, u.vj[2] * Pl.sJ};
         if (Pl.use_box) {
+          const float vs[3] = {u.vj[0] * Pl.lJ, u.vj[1] * Pl.lJ, u.vj[2] * Pl.lJ};
           acc_add(cj, L, vs, 0, A.G, geo);
         } else {
+          const float vs[3] = {u.vj[0] * Pl.sJ, u.vj[1] * Pl.sJ, u.vj[2] * Pl.sJ};
           deposit_at(L, vs, 3, 0, A.G, [&](int plane, int r, int x, float re, float im) {
             const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
             const long long qr = f2ll(re), qi = f2ll(im);
@@ -586,10 +648,11 @@ __global__ void __launch_bounds__(kDepThreads, 4) push_deposit_run_kernel(PushDe
       }
       if (DR) {
         const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, A.G);
-        const float ws[1] = {w * Pl.sR};
         if (Pl.use_box) {
+          const float ws[1] = {w * Pl.lR};
           acc_add(cr, L, ws, 3 * NM, A.G, geo);
         } else {
+          const float ws[1] = {w * Pl.sR};
           deposit_at(L, ws, 1, 0, A.G, [&](int plane, int r, int x, float re, float im) {
             const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
             const long long qr = f2ll(re), qi = f2ll(im);

@@ -261,10 +261,12 @@ def test_cell_run_deposit_equals_generic_kernel(mods, monkeypatch, nm, runs, pus
         out[variant] = (accJ.cpu().numpy(), accR.cpu().numpy(),
                         {k: P[k].cpu().numpy() for k in names})
     a, b = out["run"], out["generic"]
-    # the cell-run kernel sums a run's values in FP32 before rounding them to
-    # the fixed-point quantum; the generic kernel rounds every particle
-    for u, v in ((a[0], b[0]), (a[1], b[1])):
-        assert rel_l2(u.astype(np.float64), v.astype(np.float64)) < 1e-6
+    # the run kernel sums a run's values in FP32 before rounding them to the
+    # block's 32-bit quantum (2^-30 of a bound of the block's summed |values|);
+    # the generic kernel rounds every particle.  With random momenta (little
+    # current per node against the bound) the two differ by ~1e-6.
+    for u, v, tol in ((a[0], b[0], 1e-5), (a[1], b[1], 1e-6)):
+        assert rel_l2(u.astype(np.float64), v.astype(np.float64)) < tol
     assert np.abs(a[1]).sum() > 0 and (not push or np.abs(a[0]).sum() > 0)
     xa = a[2]["ix"] + a[2]["fx"].astype(np.float64)
     xb = b[2]["ix"] + b[2]["fx"].astype(np.float64)
