@@ -43,6 +43,11 @@ constexpr int kDepWarps = 4;                       // tiles per block
 constexpr int kDepThreads = 32 * kDepWarps;        // 128
 constexpr int kDepBlock = kTile * kDepWarps;       // 2048 particles per block
 constexpr int kSpBoxBytes = 40 * 1024;             // 10240 int32 values
+// rho-only run kernel (still species): a smaller box (a block's box holds
+// 2 nm - 1 values per node) and fewer registers, for more resident blocks
+constexpr int kRhoBoxBytes = 16 * 1024;
+constexpr int kRhoMinBlocks = 8;
+constexpr int kRhoGroup = 1;  // particles loaded ahead per lane
 
 // physical slot of particle i and the particle of a slot
 __host__ __device__ __forceinline__ i64 phys_of(i64 i) {
@@ -210,29 +215,34 @@ __device__ __forceinline__ void box_put(const BoxGeo &B, long long plane, int r,
   atomicAdd(&acc[2 * ((pl * B.nr + r) * B.nx + x) + im], (unsigned long long)q);
 }
 
-// Adds the block box into the global accumulators: warp w takes the box
-// rows w, w + nwarp, ... (a row: bnx values of one component, part and r),
-// lanes stride along x.
+// q = t / d for t < 2^16, 2 <= d < 2^16 by a multiply-high with
+// m = floor((2^32 - 1) / d) + 1: m d = 2^32 + e with 0 <= e < d, and
+// t e < 2^32 keeps floor(t m / 2^32) = floor(t / d); d = 1 is passed through
+__device__ __forceinline__ unsigned div_magic(unsigned d) { return d > 1 ? 0xffffffffu / d + 1u : 0u; }
+__device__ __forceinline__ unsigned div_small(unsigned t, unsigned m) { return m ? __umulhi(t, m) : t; }
+
+// Adds the block box into the global accumulators: the threads walk the box
+// values in storage order (a warp reads 32 consecutive values, whatever the
+// box width), each nonzero value rescaled to the global quantum.
 __device__ void flush_box(const BoxGeo &B, long long nvals) {
-  const int bnx = (int)B.bnx, bnr = (int)B.bnr, P = 2 * B.nm - 1;
-  const int nrows = (int)(nvals / bnx);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  for (int row = warp; row < nrows; row += nwarp) {
-    const int cp = row / bnr, rr = row - cp * bnr;
-    const int cb = cp / P, part = cp - cb * P, c = cb + B.c0;
+  const unsigned bnx = (unsigned)B.bnx, plane_n = (unsigned)(B.bnx * B.bnr);
+  const unsigned P = 2 * B.nm - 1;
+  const unsigned mx = div_magic(bnx), mp = div_magic(plane_n), mP = div_magic(P);
+  for (unsigned t = threadIdx.x; t < (unsigned)nvals; t += blockDim.x) {
+    const int v = B.box[t];
+    if (v == 0) continue;
+    const unsigned cp = div_small(t, mp), rem = t - cp * plane_n;
+    const unsigned rr = div_small(rem, mx), xx = rem - rr * bnx;
+    const unsigned cb = div_small(cp, mP);
+    const int part = (int)(cp - cb * P), c = (int)cb + B.c0;
     const int m = (part + 1) >> 1, im = (part > 0 && (part & 1) == 0) ? 1 : 0;
     const bool isj = c < 3;
+    const long long q = rescale(v, isj ? B.elJ : B.elR, isj ? B.eJ : B.eR);
+    if (q == 0) continue;
     const int pl = isj ? m + B.nm * c : m;
-    const int eg = isj ? B.eJ : B.eR, el = isj ? B.elJ : B.elR;
-    unsigned long long *acc = (isj ? B.gJ : B.gR) +
-                              2 * (((i64)pl * B.nr + (rr + B.br0)) * B.nx + B.bx0) + im;
-    const int *src = B.box + (i64)row * bnx;
-    for (int t = lane; t < bnx; t += 32) {
-      const int v = src[t];
-      if (v == 0) continue;
-      const long long q = rescale(v, el, eg);
-      if (q) atomicAdd(acc + 2 * t, (unsigned long long)q);
-    }
+    unsigned long long *acc = isj ? B.gJ : B.gR;
+    atomicAdd(acc + 2 * (((i64)pl * B.nr + (rr + B.br0)) * B.nx + B.bx0 + xx) + im,
+              (unsigned long long)q);
   }
 }
 
@@ -291,7 +301,7 @@ struct BlockPlan {
   float sJ, sR;    // global scales 2^eJ, 2^eR (path without a box)
 };
 
-__device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb) {
+__device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box_bytes) {
   __shared__ float wsm[2][kDepThreads / 32];
   if (threadIdx.x == 0) {
     bb[0] = INT_MAX;
@@ -370,7 +380,7 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb) {
   const int per_node = (3 * (A.dep_j ? 1 : 0) + (A.dep_rho ? 1 : 0)) * (2 * A.G.nm - 1);
   P.c0 = A.dep_j ? 0 : 3;
   P.nvals = (bb[0] <= bb[1] && P.bnx > 0 && P.bnr > 0) ? P.bnx * P.bnr * per_node : 0;
-  P.use_box = P.nvals > 0 && P.nvals * 4 <= kSpBoxBytes && Bl > 0.0f && isfinite(Bl);
+  P.use_box = P.nvals > 0 && P.nvals * 4 <= box_bytes && Bl > 0.0f && isfinite(Bl);
   // a node value of a particle is at most |w| (rho) or |w| max_l |v_l| (J),
   // so each part of the box stays below 2^30 (one bit of margin for the
   // FP32 sums and the per-run rounding)
@@ -396,7 +406,7 @@ __global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A
   extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
   const i64 base = (i64)blockIdx.x * kDepBlock;
-  const BlockPlan Pl = plan_block(A, base, bb);
+  const BlockPlan Pl = plan_block(A, base, bb, kSpBoxBytes);
   if (Pl.use_box)
     for (long long t = threadIdx.x; t < Pl.nvals; t += kDepThreads) box[t] = 0;
   __syncthreads();
@@ -560,11 +570,12 @@ __device__ __forceinline__ void acc_add(CellAcc<NM, NC> &c, const Loc &L, const 
 }
 
 template <int NM, bool PUSH, bool DJ, bool DR>
-__global__ void __launch_bounds__(kDepThreads, 4) push_deposit_run_kernel(PushDepArgs A) {
+__global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
+    push_deposit_run_kernel(PushDepArgs A) {
   extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
   const i64 base = (i64)blockIdx.x * kDepBlock;
-  const BlockPlan Pl = plan_block(A, base, bb);
+  const BlockPlan Pl = plan_block(A, base, bb, DJ ? kSpBoxBytes : kRhoBoxBytes);
   if (Pl.use_box)
     for (long long t = threadIdx.x; t < Pl.nvals; t += kDepThreads) box[t] = 0;
   __syncthreads();
@@ -580,7 +591,7 @@ __global__ void __launch_bounds__(kDepThreads, 4) push_deposit_run_kernel(PushDe
   // software pipeline: the next group of particles is loaded before this
   // group's results are stored (the stores could alias the loads
   // otherwise); G particles per group, more for the lighter rho-only pass
-  constexpr int G = DJ ? 1 : 4;
+  constexpr int G = DJ ? 1 : kRhoGroup;
   struct Part {
     int ix;
     float fx, y, z, px, py, pz, w;
@@ -1182,9 +1193,11 @@ int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, f
     if (mode == 1) kern = nm == 1 ? push_deposit_run_kernel<1, false, false, true>
                                   : push_deposit_run_kernel<2, false, false, true>;
   }
+  int box_bytes = kSpBoxBytes;
   if (!kern) kern = push_deposit_kernel;
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSpBoxBytes);
-  kern<<<blocks, kDepThreads, kSpBoxBytes, st>>>(A);
+  else if (!A.dep_j) box_bytes = kRhoBoxBytes;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, box_bytes);
+  kern<<<blocks, kDepThreads, box_bytes, st>>>(A);
   chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;

@@ -65,24 +65,39 @@ def _slots(n: int) -> int:
     return (int(n) + 511) // 512 * 512
 
 
-def cell_order(coords, group: int, X0: float, dx: float, dr: float):
-    """Stable permutation that puts the particles of each generation cell
-    (consecutive groups of `group`) in deposit-cell order, so that the runs
-    of 16 consecutive particles of the tile layout share a deposit cell.
-    coords: (3, n) numpy or torch array (x, y, z)."""
-    if isinstance(coords, torch.Tensor):
-        x, y, z = coords[0], coords[1], coords[2]
-        cx = torch.floor((x - X0) / dx).to(torch.int64)
-        cr = torch.floor(torch.sqrt(y * y + z * z) / dr + 0.5).to(torch.int64)
-        g = torch.arange(x.shape[0], device=x.device, dtype=torch.int64) // max(int(group), 1)
-        cx = cx - cx.min() if x.shape[0] else cx
-        key = (g * 4096 + cr.clamp(0, 4095)) * (1 << 22) + cx.clamp(0, (1 << 22) - 1)
-        return torch.argsort(key, stable=True)
+def cell_order(coords, X0: float, dx: float, dr: float, patch: int = 4):
+    """Stable permutation of particles into deposit order: patches of
+    patch x patch generation cells (cells [X0 + i dx, X0 + (i+1) dx) x
+    [j dr, (j+1) dr)), patch rows in a serpentine order (so consecutive
+    patches are neighbours), the cells of a patch in serpentine order too,
+    and within a cell its two deposit cells (r nodes at (j - 1/2) dr) in
+    turn.  A block of particles then covers a compact patch of the grid (a
+    small deposit box), and the runs of 16 consecutive particles of the tile
+    layout share a deposit cell.  coords: (3, n) numpy or torch array."""
+    lib = torch if isinstance(coords, torch.Tensor) else np
     x, y, z = coords[0], coords[1], coords[2]
-    cx = np.floor((x - X0) / dx).astype(np.int64)
-    cr = np.floor(np.sqrt(y * y + z * z) / dr + 0.5).astype(np.int64)
-    g = np.arange(x.shape[0], dtype=np.int64) // max(int(group), 1)
-    return np.lexsort((cx, cr, g))
+    n = x.shape[0]
+    if n == 0:
+        return torch.arange(0, device=x.device) if lib is torch else np.arange(0)
+    s = lib.sqrt(y * y + z * z) / dr
+    gx = lib.floor((x - X0) / dx)
+    gr = lib.floor(s)
+    half = (s - gr >= 0.5)  # upper deposit cell of the generation cell
+    if lib is torch:
+        gx, gr, half = gx.to(torch.int64), gr.to(torch.int64).clamp(min=0), half.to(torch.int64)
+    else:
+        gx, gr, half = gx.astype(np.int64), np.maximum(gr.astype(np.int64), 0), half.astype(np.int64)
+    gx = gx - gx.min()
+    P = int(patch)
+    px, lx = gx // P, gx % P
+    pr, lr = gr // P, gr % P
+    npx = int(px.max()) + 1
+    px = lib.where(pr % 2 == 1, npx - 1 - px, px)  # serpentine patch rows
+    lx = lib.where(lr % 2 == 1, P - 1 - lx, lx)    # serpentine rows in a patch
+    key = (((pr * npx + px) * P + lr) * P + lx) * 2 + half
+    if lib is torch:
+        return torch.argsort(key, stable=True)
+    return np.argsort(key, kind="stable")
 
 
 class _SpParticles:
@@ -236,15 +251,15 @@ class SplitRun:
                               dtype=torch.uint8, device=dev)
         self.scale_ws = torch.empty(_lib.query("chm_sp_scale_ws_bytes"), dtype=torch.uint8,
                                     device=dev)
-        # particles, each generation cell's particles in deposit-cell order
-        # (runs of 16 of the tile layout then share a deposit cell)
+        # particles in deposit order (cell_order: serpentine patches of cells,
+        # runs of 16 of the tile layout sharing a deposit cell)
         self.dr = float(A["dr"])
         self.parts = []
         self.order0 = []  # the initial permutation of each species (particle order of to_fp64)
         for spc in self.fp.Particles:
             P = _SpParticles(dev, spc.num_particles)
             d = spc.Data
-            o = cell_order(d["coords"], spc.Args.get("Num_p", 1), self.X0, self.dx, self.dr)
+            o = cell_order(d["coords"], self.X0, self.dx, self.dr)
             P.append_f64(d["coords"][:, o], d["momenta"][:, o], d["weights"][o], self.X0, self.dx)
             self.parts.append(P)
             self.order0.append(o)
@@ -439,7 +454,7 @@ class SplitRun:
         xsteps = int(wind["shiftX"] / wind["TimeStep"]) + 1
         idx = {id(s): i for i, s in enumerate(fp.Particles)}
         def ordered(spc, parts):
-            o = cell_order(parts[0], spc.Args.get("Num_p", 1), self.X0, self.dx, self.dr)
+            o = cell_order(parts[0], self.X0, self.dx, self.dr)
             return [parts[0][:, o], parts[1][:, o], parts[2][o]]
 
         if "IonsOnTop" in wind["Features"]:

@@ -77,3 +77,52 @@ def test_moving_frame_defaults():
     run.init_Moving_Frames()
     assert run.MovingFrames[0]["shiftX"] == 1.0
     assert abs(run.MovingFrames[1]["shiftX"] - 0.05) < 1e-15
+
+
+def test_cell_order_patches_and_deposit_cells():
+    """cell_order: a stable permutation; consecutive particles stay in one
+    generation cell until it is exhausted, a cell's lower deposit cell
+    (r < (j + 1/2) dr) comes before its upper one, the cells of a patch are
+    contiguous, and consecutive cells/patches are neighbours."""
+    torch = pytest.importorskip("torch")
+    from chimera_gb300.split import cell_order
+    rng = np.random.default_rng(7)
+    dx, dr, X0 = 0.04, 0.4, -3.0
+    nxc, nrc, ppc = 37, 21, 6
+    gx = np.repeat(np.arange(nxc), nrc * ppc)
+    gr = np.tile(np.repeat(np.arange(nrc), ppc), nxc)
+    x = X0 + (gx + rng.uniform(0.01, 0.99, gx.size)) * dx
+    r = (gr + rng.uniform(0.01, 0.99, gr.size)) * dr
+    th = rng.uniform(0, 2 * np.pi, gx.size)
+    coords = np.vstack([x, r * np.cos(th), r * np.sin(th)])
+    perm = rng.permutation(gx.size)
+    coords, gx, gr = coords[:, perm], gx[perm], gr[perm]
+    P = 8
+    o = cell_order(coords, X0, dx, dr, patch=P)
+    assert sorted(o.tolist()) == list(range(gx.size))
+    cx, cr = gx[o], gr[o]
+    half = (np.sqrt(coords[1] ** 2 + coords[2] ** 2) / dr - gr >= 0.5)[o]
+    cell = cx * 1000 + cr
+    # each generation cell is one contiguous stretch, lower half first
+    starts = np.flatnonzero(np.diff(cell)) + 1
+    assert len(starts) == nxc * nrc - 1
+    for a, b in zip(np.r_[0, starts], np.r_[starts, cell.size]):
+        h = half[a:b]
+        assert np.all(np.diff(h.astype(int)) >= 0)
+        # stable: original order kept within a deposit cell
+        for v in (False, True):
+            idx = o[a:b][h == v]
+            assert np.all(np.diff(idx) > 0)
+    # consecutive cells are neighbours (serpentine) inside a patch, and
+    # consecutive patches are neighbours
+    seq_x, seq_r = cx[np.r_[0, starts]], cr[np.r_[0, starts]]
+    pseq = (seq_x // P) * 1000 + seq_r // P
+    pch = np.flatnonzero(np.diff(pseq)) + 1
+    assert len(np.unique(pseq)) == len(pch) + 1  # every patch contiguous
+    inner = np.setdiff1d(np.arange(1, seq_x.size), pch)
+    assert np.all(np.abs(np.diff(seq_x))[inner - 1] + np.abs(np.diff(seq_r))[inner - 1] == 1)
+    px, pr = seq_x[np.r_[0, pch]] // P, seq_r[np.r_[0, pch]] // P
+    assert np.all(np.abs(np.diff(px)) + np.abs(np.diff(pr)) == 1)
+    # the torch path gives the same permutation
+    ot = cell_order(torch.from_numpy(coords), X0, dx, dr, patch=P)
+    assert np.array_equal(ot.numpy(), o)
