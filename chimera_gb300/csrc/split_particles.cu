@@ -29,6 +29,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <math.h>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -172,7 +173,7 @@ struct PushDepArgs {
 // (((c - c0) P + part) bnr + r - br0) bnx + x - bx0, P = 2 nm - 1.
 struct BoxGeo {
   int *box;
-  long long bx0, br0, bnx, bnr;
+  int bx0, br0, bnx, bnr;
   int c0;                        // first component held (0: J and rho, 3: rho only)
   int elJ, elR, eJ, eR;          // local (J, rho) and global quantum exponents
   unsigned long long *gJ, *gR;   // global accumulators
@@ -201,9 +202,9 @@ __device__ __forceinline__ void box_put(const BoxGeo &B, long long plane, int r,
                                         int v) {
   const int c = (int)(plane / B.nm), m = (int)(plane - (long long)c * B.nm);
   if (m == 0 && im) return;  // mode 0 deposits no imaginary part
-  const long long rr = r - B.br0, xx = x - B.bx0;
+  const int rr = r - B.br0, xx = x - B.bx0;
   if (rr >= 0 && rr < B.bnr && xx >= 0 && xx < B.bnx) {
-    const long long cp = (long long)(c - B.c0) * (2 * B.nm - 1) + part_of(m, im);
+    const int cp = (c - B.c0) * (2 * B.nm - 1) + part_of(m, im);
     atomicAdd(&B.box[(cp * B.bnr + rr) * B.bnx + xx], v);
     return;
   }
@@ -233,6 +234,8 @@ __device__ void flush_box(const BoxGeo &B, long long nvals) {
     if (v == 0) continue;
     const unsigned cp = div_small(t, mp), rem = t - cp * plane_n;
     const unsigned rr = div_small(rem, mx), xx = rem - rr * bnx;
+    const int gx = B.bx0 + (int)xx;
+    if (gx < 0 || gx >= B.nx) continue;  // the nodes beyond the grid's ends
     const unsigned cb = div_small(cp, mP);
     const int part = (int)(cp - cb * P), c = (int)cb + B.c0;
     const int m = (part + 1) >> 1, im = (part > 0 && (part & 1) == 0) ? 1 : 0;
@@ -241,7 +244,7 @@ __device__ void flush_box(const BoxGeo &B, long long nvals) {
     if (q == 0) continue;
     const int pl = isj ? m + B.nm * c : m;
     unsigned long long *acc = isj ? B.gJ : B.gR;
-    atomicAdd(acc + 2 * (((i64)pl * B.nr + (rr + B.br0)) * B.nx + B.bx0 + xx) + im,
+    atomicAdd(acc + 2 * (((i64)pl * B.nr + (rr + B.br0)) * B.nx + gx) + im,
               (unsigned long long)q);
   }
 }
@@ -292,7 +295,8 @@ __device__ __forceinline__ Pushed push_one(const PushDepArgs &A, i64 i) {
 // cells lie within ceil(dt/dx) cells of its x cell and within dt of its
 // radius.  (Nodes outside the box go straight to the global accumulator.)
 struct BlockPlan {
-  long long bx0, br0, bnx, bnr, nvals;
+  int bx0, br0, bnx, bnr;
+  long long nvals;
   int c0;          // first component held by the box
   bool use_box;
   float lJ, lR;    // local scales 2^elJ, 2^elR
@@ -319,6 +323,8 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box
     const bool valid = logical_of(p) < A.P.n;
     const i64 q = valid ? p : base;  // slot 0 of the block always holds a particle
     const float w = A.P.w[q];
+    // the run loop reads fx, which this pass does not: start it towards L2
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(A.P.fx + q));
     const int ix = A.P.ix[q];
     const float y = A.P.y[q], z = A.P.z[q];
     float pp = 0.0f;
@@ -371,15 +377,18 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box
     Bl += wsm[0][k];
     Bj += wsm[1][k];
   }
-  P.bx0 = max(bb[0], 0);
+  // in x the box reaches one node beyond the grid on each side, so that the
+  // cells at the grid's ends stay inside it (those nodes are dropped at the
+  // flush, as the reference drops them)
+  P.bx0 = max(bb[0], -1);
   P.br0 = max(bb[2], 0);
-  const long long bx1 = min(bb[1], A.G.nx - 1), br1 = min(bb[3], A.G.nr - 1);
+  const int bx1 = min(bb[1], A.G.nx), br1 = min(bb[3], A.G.nr - 1);
   P.bnx = bx1 - P.bx0 + 1;
   P.bnr = br1 - P.br0 + 1;
   // deposited components (J_x, J_y, J_z and/or rho) x mode parts
   const int per_node = (3 * (A.dep_j ? 1 : 0) + (A.dep_rho ? 1 : 0)) * (2 * A.G.nm - 1);
   P.c0 = A.dep_j ? 0 : 3;
-  P.nvals = (bb[0] <= bb[1] && P.bnx > 0 && P.bnr > 0) ? P.bnx * P.bnr * per_node : 0;
+  P.nvals = (bb[0] <= bb[1] && P.bnx > 0 && P.bnr > 0) ? (long long)P.bnx * P.bnr * per_node : 0;
   P.use_box = P.nvals > 0 && P.nvals * 4 <= box_bytes && Bl > 0.0f && isfinite(Bl);
   // a node value of a particle is at most |w| (rho) or |w| max_l |v_l| (J),
   // so each part of the box stays below 2^30 (one bit of margin for the
@@ -484,10 +493,10 @@ __device__ __forceinline__ void acc_flush(CellAcc<NM, NC> &c, int plane0, const 
                                           const BoxGeo &B) {
   if (!c.live) return;
   c.live = false;
-  const int rr = c.cr - (int)B.br0, xx = c.cx - (int)B.bx0;
+  const int rr = c.cr - B.br0, xx = c.cx - B.bx0;
   if (rr >= 0 && rr + 1 < B.bnr && xx >= 0 && xx + 1 < B.bnx) {
-    // all four nodes inside the box (x nodes inside the grid as the box is)
-    const int rs = (int)B.bnx, ps = rs * (int)B.bnr;  // row and (component, part) strides
+    // all four nodes inside the box
+    const int rs = B.bnx, ps = rs * B.bnr;  // row and (component, part) strides
     int *b0 = B.box + (rr * rs + xx);
     const int c0 = plane0 / NM;  // first component: 0 (J) or 3 (rho)
 #pragma unroll
@@ -503,6 +512,9 @@ __device__ __forceinline__ void acc_flush(CellAcc<NM, NC> &c, int plane0, const 
       }
     return;
   }
+  // guard: a cell with nodes outside the block box (the plan bounds every
+  // deposit location of finite particles) adds its in-grid node values
+  // through box_put
 #pragma unroll
   for (int l = 0; l < NC; ++l)
 #pragma unroll
@@ -574,20 +586,23 @@ __global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
     push_deposit_run_kernel(PushDepArgs A) {
   extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
-  const i64 base = (i64)blockIdx.x * kDepBlock;
+  // slot indices: 32-bit in the rho-only kernel (measured faster there; the
+  // host launches it for n < 2^31 only), 64-bit otherwise
+  using Idx = typename std::conditional<DJ, i64, unsigned>::type;
+  const Idx base = (Idx)blockIdx.x * kDepBlock;
   const BlockPlan Pl = plan_block(A, base, bb, DJ ? kSpBoxBytes : kRhoBoxBytes);
   if (Pl.use_box)
-    for (long long t = threadIdx.x; t < Pl.nvals; t += kDepThreads) box[t] = 0;
+    for (int t = threadIdx.x; t < (int)Pl.nvals; t += kDepThreads) box[t] = 0;
   __syncthreads();
   const BoxGeo geo = make_geo(box, Pl, A);
   const int lane = threadIdx.x & 31;
-  const i64 tile = base + (i64)(threadIdx.x >> 5) * kTile;
-  const i64 first = tile + (i64)lane * kRunLen;  // this lane's run, in particle order
+  const Idx tile = base + (Idx)(threadIdx.x >> 5) * kTile;
+  const Idx first = tile + (Idx)lane * kRunLen;  // this lane's run, in particle order
   CellAcc<NM, 3> cj;
   CellAcc<NM, 1> cr;
   cj.live = false;
   cr.live = false;
-  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - first));
+  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - (i64)first));
   // software pipeline: the next group of particles is loaded before this
   // group's results are stored (the stores could alias the loads
   // otherwise); G particles per group, more for the lighter rho-only pass
@@ -598,7 +613,7 @@ __global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
   };
   auto load = [&](int j) {
     Part q;
-    const i64 p = tile + (i64)j * kTileRuns + lane;
+    const Idx p = tile + (Idx)j * kTileRuns + lane;
     q.w = A.P.w[p];
     q.ix = A.P.ix[p];
     q.fx = A.P.fx[p];
@@ -624,7 +639,7 @@ __global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
       const int j = j0 + g;
       if (j >= cnt) break;
       const Part &c = cur[g];
-      const i64 p = tile + (i64)j * kTileRuns + lane;
+      const Idx p = tile + (Idx)j * kTileRuns + lane;
       const float w = c.w;
       Pushed u;
       if (PUSH || DJ) {
@@ -1190,8 +1205,9 @@ int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, f
                                   : push_deposit_run_kernel<2, true, true, true>;
     if (mode == 6) kern = nm == 1 ? push_deposit_run_kernel<1, true, true, false>
                                   : push_deposit_run_kernel<2, true, true, false>;
-    if (mode == 1) kern = nm == 1 ? push_deposit_run_kernel<1, false, false, true>
-                                  : push_deposit_run_kernel<2, false, false, true>;
+    if (mode == 1 && n < (i64)INT32_MAX - kDepBlock)
+      kern = nm == 1 ? push_deposit_run_kernel<1, false, false, true>
+                     : push_deposit_run_kernel<2, false, false, true>;
   }
   int box_bytes = kSpBoxBytes;
   if (!kern) kern = push_deposit_kernel;
