@@ -65,6 +65,22 @@ struct SpParts {
   i64 n;
 };
 
+// Starts the particle data of one tile (512 slots; 16 rows of 32
+// consecutive slots per array) towards L2: one prefetch per 128-byte row,
+// the warp's lanes taking rows in turn.  The arrays are read slot by slot
+// afterwards, so this turns their DRAM latency into L2 latency.  Tiles past
+// the last particle are not touched (the arrays hold whole tiles up to n).
+__device__ __forceinline__ void prefetch_tile(const SpParts &P, i64 tile, int lane, bool momenta) {
+  if (tile >= P.n) return;
+  const int narr = momenta ? 8 : 5;
+  for (int k = lane; k < kRunLen * narr; k += 32) {
+    const int row = k & (kRunLen - 1), arr = k >> 4;
+    const float *b = arr == 0 ? P.w : arr == 1 ? (const float *)P.ix : arr == 2 ? P.fx
+                   : arr == 3 ? P.y : arr == 4 ? P.z : arr == 5 ? P.px : arr == 6 ? P.py : P.pz;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(b + tile + (i64)row * kTileRuns));
+  }
+}
+
 struct SpGrid {
   int win_k;      // window origin, whole cells from X0
   float win_f;    // window origin, fraction of a cell
@@ -323,8 +339,7 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box
     const bool valid = logical_of(p) < A.P.n;
     const i64 q = valid ? p : base;  // slot 0 of the block always holds a particle
     const float w = A.P.w[q];
-    // the run loop reads fx, which this pass does not: start it towards L2
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(A.P.fx + q));
+    if (!A.push && !A.dep_j) asm volatile("prefetch.global.L2 [%0];" ::"l"(A.P.fx + q));
     const int ix = A.P.ix[q];
     const float y = A.P.y[q], z = A.P.z[q];
     float pp = 0.0f;
@@ -590,6 +605,9 @@ __global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
   // host launches it for n < 2^31 only), 64-bit otherwise
   using Idx = typename std::conditional<DJ, i64, unsigned>::type;
   const Idx base = (Idx)blockIdx.x * kDepBlock;
+  // (the rho-only pass starts only fx towards L2, in the plan: measured
+  // faster there than the whole tile)
+  if (PUSH || DJ) prefetch_tile(A.P, (i64)base + (threadIdx.x >> 5) * kTile, threadIdx.x & 31, true);
   const BlockPlan Pl = plan_block(A, base, bb, DJ ? kSpBoxBytes : kRhoBoxBytes);
   if (Pl.use_box)
     for (int t = threadIdx.x; t < (int)Pl.nvals; t += kDepThreads) box[t] = 0;
@@ -928,6 +946,7 @@ __global__ void __launch_bounds__(kDepThreads, 4) gather_push_run_kernel(GatherA
     q.pz = A.P.pz[p];
     return q;
   };
+  prefetch_tile(A.P, tile, lane, true);
   Part cur;
   if (cnt > 0) cur = load(0);
   for (int j = 0; j < cnt; ++j) {
