@@ -38,9 +38,8 @@ __host__ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// Grid size helper: enough blocks to cover n, capped to keep every SM busy
-// with several resident blocks.
-inline unsigned grid_for(i64 n, int threads, int cap_per_sm = 32) {
+// SMs of the current device (read once)
+inline int sm_count() {
   static int nsm = 0;
   if (nsm == 0) {
     int dev = 0;
@@ -48,8 +47,14 @@ inline unsigned grid_for(i64 n, int threads, int cap_per_sm = 32) {
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (nsm <= 0) nsm = 152;
   }
+  return nsm;
+}
+
+// Grid size helper: enough blocks to cover n, capped to keep every SM busy
+// with several resident blocks.
+inline unsigned grid_for(i64 n, int threads, int cap_per_sm = 32) {
   i64 b = (n + threads - 1) / threads;
-  i64 cap = (i64)nsm * cap_per_sm;
+  i64 cap = (i64)sm_count() * cap_per_sm;
   if (b > cap) b = cap;
   if (b < 1) b = 1;
   return (unsigned)b;

@@ -4,21 +4,22 @@
 //   operator mode; computed as sum_{i+j<=2} A_i B_j with A = A0+A1+A2 and
 //   B = B0+B1+B2 the 3-term BF16 splits, accumulated in FP32 in TMEM.
 //
-// One CTA computes a 256-row tile of one problem of a batch, as two 128-row
-// accumulators of up to 256 FP32 columns each in TMEM:
-//   - warps 0-7 (one thread per row) load the FP32 A block of every 32-wide
+// One CTA computes a TM-row tile of one problem of a batch, as NH 128-row
+// accumulators of up to 256 FP32 columns each in TMEM (NH = 1: 128-row
+// tiles, so that a batch of few products still spreads over the SMs):
+//   - warps 0..4NH-1 (one thread per row) load the FP32 A block of every 32-wide
 //     K step, split it into the three BF16 terms and store them into the
 //     stage in the tensor-core operand layout (K-major core matrices of
 //     8 rows x 16 bytes);
-//   - warp 8 lane 0 streams the prepared B terms of the step with bulk-copy
-//     TMA (cp.async.bulk, completion on an mbarrier) and issues the 24
-//     tcgen05.mma of the step (6 term pairs x 2 K halves x 2 row halves),
-//     releasing the stage with tcgen05.commit;
-//   - warps 0-7 then read the accumulators (tcgen05.ld 32x32b) and apply the
-//     epilogue.
-// Two stages double-buffer the K loop.  Every mbarrier wait has an iteration
-// limit; on timeout the CTA records an error, waits (bounded) for its own
-// bulk copies, frees its TMEM and returns.
+//   - the next warp's lane 0 streams the prepared B terms of the step with
+//     bulk-copy TMA (cp.async.bulk, completion on an mbarrier) and issues the
+//     12 NH tcgen05.mma of the step (6 term pairs x 2 K halves x NH row
+//     halves), releasing the stage with tcgen05.commit;
+//   - the producer warps then read the accumulators (tcgen05.ld 32x32b) and
+//     apply the epilogue.
+// STAGES stages (3 with NH = 1: 72 KB each at N = 256) pipeline the K loop.
+// Every mbarrier wait has an iteration limit; on timeout the CTA records an
+// error, waits (bounded) for its own bulk copies, frees its TMEM and returns.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -29,16 +30,21 @@ using namespace chm;
 namespace {
 
 constexpr int TH = 128;                   // rows per accumulator (UMMA M)
-constexpr int TM = 2 * TH;                // rows per CTA
 constexpr int KB = 32;                    // K step (elements)
-constexpr int STAGES = 2;
-constexpr int kProducers = TM;            // warps 0-7, one row each
-constexpr int kThreads = kProducers + 32; // + warp 8: B copies and MMA issue
 constexpr int kMaxBatch = 64;
 constexpr long long kSpinLimit = 1LL << 20;  // try_wait polls; each may block briefly
 constexpr uint32_t kAHalfBytes = TH * KB * 2;       // one term, one row half
-constexpr uint32_t kATermBytes = 2 * kAHalfBytes;   // one term, both halves
-constexpr uint32_t kABytes = 3 * kATermBytes;       // the A part of a stage
+
+// tile configuration for NH accumulators (row halves) per CTA
+template <int NH>
+struct TileCfg {
+  static constexpr int TM = NH * TH;                // rows per CTA
+  static constexpr int STAGES = NH == 1 ? 3 : 2;
+  static constexpr int kProducers = TM;             // one thread per row
+  static constexpr int kThreads = kProducers + 32;  // + one warp: B copies and MMA issue
+  static constexpr uint32_t kATermBytes = NH * kAHalfBytes;  // one term, all halves
+  static constexpr uint32_t kABytes = 3 * kATermBytes;       // the A part of a stage
+};
 
 __device__ int g_umma_error;  // first failing CTA records a code here
 
@@ -153,9 +159,12 @@ struct UmmaArgs {
   uint32_t tmem_cols;
 };
 
-template <int EPI>
-__global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant__ UmmaBatch P,
+template <int EPI, int NH>
+__global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __grid_constant__ UmmaBatch P,
                                                            UmmaArgs A) {
+  using Cfg = TileCfg<NH>;
+  constexpr int TM = Cfg::TM, STAGES = Cfg::STAGES, kProducers = Cfg::kProducers;
+  constexpr uint32_t kATermBytes = Cfg::kATermBytes, kABytes = Cfg::kABytes;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t afull[STAGES], bfull[STAGES], empty[STAGES], done;
   __shared__ uint32_t tmem_base;
@@ -286,7 +295,7 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
         for (int ks = 0; ks < KB / 16; ++ks) {
           const uint64_t bd = smem_desc(st + kABytes + pj[q] * b_term + ks * 256, 128, (KB / 8) * 128);
 #pragma unroll
-          for (int hh = 0; hh < 2; ++hh) {
+          for (int hh = 0; hh < NH; ++hh) {
             const uint64_t ad =
                 smem_desc(st + pi[q] * kATermBytes + hh * kAHalfBytes + ks * 256, 128, (KB / 8) * 128);
             umma_bf16(tmem + (uint32_t)(hh * A.Np), ad, bd, idesc,
@@ -393,15 +402,29 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
       set_error("umma: problem %d has no prepared %dx%d operator", i, K, N);
       return CHM_ERR_ARG;
     }
+  // 128-row tiles (one accumulator per CTA, a deeper K pipeline) when all
+  // of them run in one wave, else 256-row tiles (two accumulators per CTA:
+  // the same number of waves of twice the work, half the B traffic)
+  const bool two = 2LL * count * ((M + 255) / 256) > sm_count();
+  const int NH = two ? 2 : 1;
+  const int TM = NH * TH, STAGES = two ? TileCfg<2>::STAGES : TileCfg<1>::STAGES;
+  const uint32_t kABytes = two ? TileCfg<2>::kABytes : TileCfg<1>::kABytes;
+  const int threads = two ? TileCfg<2>::kThreads : TileCfg<1>::kThreads;
   const int mt = (int)((M + TM - 1) / TM);
   const uint32_t b_term = (uint32_t)Np * KB * 2;
   const size_t smem = (size_t)STAGES * (kABytes + 3 * b_term) + 1024;
-  void (*kern)(const UmmaBatch, UmmaArgs) =
-      epi == TC_EPI_STORE ? umma_kernel<TC_EPI_STORE>
-                          : (epi == TC_EPI_SHIFT ? umma_kernel<TC_EPI_SHIFT> : umma_kernel<TC_EPI_SHIFT_FAC>);
+  void (*kern)(const UmmaBatch, UmmaArgs);
+  if (two)
+    kern = epi == TC_EPI_STORE ? umma_kernel<TC_EPI_STORE, 2>
+                               : (epi == TC_EPI_SHIFT ? umma_kernel<TC_EPI_SHIFT, 2>
+                                                      : umma_kernel<TC_EPI_SHIFT_FAC, 2>);
+  else
+    kern = epi == TC_EPI_STORE ? umma_kernel<TC_EPI_STORE, 1>
+                               : (epi == TC_EPI_SHIFT ? umma_kernel<TC_EPI_SHIFT, 1>
+                                                      : umma_kernel<TC_EPI_SHIFT_FAC, 1>);
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   uint32_t cols = 32;
-  while (cols < (uint32_t)(2 * Np)) cols <<= 1;
+  while (cols < (uint32_t)(NH * Np)) cols <<= 1;
   UmmaArgs ua{};
   ua.M = M;
   ua.N = N;
@@ -422,7 +445,7 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
                           reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[2])},
                          q.reflect};
     }
-    kern<<<dim3(mt, cnt), kThreads, smem, st>>>(ub, ua);
+    kern<<<dim3(mt, cnt), threads, smem, st>>>(ub, ua);
     count_launch();
   }
   cudaError_t e = cudaGetLastError();
