@@ -45,6 +45,9 @@ SIZES = {  # name: (nx, nkr, ppc)
     # quarter radius: 4.2M electrons (134 MB of split-form particle state,
     # above the 129 MB L2) and ~3 GB on the device, for ncu captures
     "prof": (2048, 64, (2, 2, 8)),
+    # the cfg2 grid with 1 particle per cell (0.5M electrons, small particle
+    # state), for ncu captures of the spectral kernels at their full size
+    "spec": (2048, 256, (1, 1, 1)),
     "small": (512, 64, (2, 2, 4)),
 }
 

@@ -88,6 +88,18 @@ struct SpGrid {
   int nx, nr, nm;  // spatial grid
 };
 
+// ceil(log2 v) of a positive finite float, and the exponent of a power of
+// two held in a double (from its bits): the per-block plan stays off the
+// FP64 pipe
+__device__ __forceinline__ int ceil_log2f(float v) {
+  int e;
+  const float m = frexpf(v, &e);  // v = m 2^e, m in [0.5, 1)
+  return (m == 0.5f) ? e - 1 : e;
+}
+__device__ __forceinline__ int pow2_exponent(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
+}
+
 __device__ __forceinline__ int ceil_log2(double v) {
   int e;
   double m = frexp(v, &e);  // v = m 2^e, m in [0.5, 1)
@@ -408,14 +420,15 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box
   // a node value of a particle is at most |w| (rho) or |w| max_l |v_l| (J),
   // so each part of the box stays below 2^30 (one bit of margin for the
   // FP32 sums and the per-run rounding)
-  P.elR = P.use_box ? 30 - ceil_log2((double)Bl) : 0;
-  P.elJ = (P.use_box && Bj > 0.0f) ? min(30 - ceil_log2((double)Bj), 120) : P.elR;
+  P.elR = P.use_box ? min(30 - ceil_log2f(Bl), 120) : 0;
+  P.elJ = (P.use_box && Bj > 0.0f) ? min(30 - ceil_log2f(Bj), 120) : P.elR;
   P.lR = ldexpf(1.0f, P.elR);
   P.lJ = ldexpf(1.0f, P.elJ);
-  P.sJ = A.scaleJ ? (float)A.scaleJ[0] : 1.0f;
-  P.sR = A.scaleR ? (float)A.scaleR[0] : 1.0f;
-  P.eJ = A.scaleJ ? ilogb(A.scaleJ[0]) : 0;
-  P.eR = A.scaleR ? ilogb(A.scaleR[0]) : 0;
+  // the global scales are powers of two 2^e, e <= 120
+  P.eJ = A.scaleJ ? pow2_exponent(A.scaleJ[0]) : 0;
+  P.eR = A.scaleR ? pow2_exponent(A.scaleR[0]) : 0;
+  P.sJ = ldexpf(1.0f, P.eJ);
+  P.sR = ldexpf(1.0f, P.eR);
   return P;
 }
 
