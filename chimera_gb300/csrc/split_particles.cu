@@ -19,8 +19,8 @@
 // particle are not read.
 //
 // Deposition stays deterministic without float atomics: each block adds its
-// values as 32-bit integers at its own power-of-two scale (from the block's
-// sum |w|) into a shared-memory box of its nodes, then adds the box into the
+// values as 32-bit integers at its own power-of-two scales (from the block's
+// sum |w| and sum |w| max|v|) into a shared-memory box of its nodes, then adds the box into the
 // global 64-bit accumulator (scale 2^(61 - ceil(log2 sum |w|))) with an exact
 // power-of-two shift.  Integer sums are order-independent; the run kernel
 // sums the particles of a run in FP32 before rounding, which depends only on
@@ -438,7 +438,8 @@ __device__ __forceinline__ BoxGeo make_geo(int *box, const BlockPlan &P, const P
 }
 
 // Generic push + deposit (any nm): one particle per thread and slot, each
-// value rounded to the global quantum and added to the box.
+// value rounded to the block quantum and added to the box (or, without a
+// box, to the global quantum and added to the global accumulator).
 __global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A) {
   extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
@@ -501,8 +502,8 @@ __global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A
 // ----------------------------------------------------------------------
 // Run form of push + deposit for nm = 1, 2: lane r of a warp walks the 16
 // particles of run r of its tile, sums their node values (already at the
-// global fixed-point scale) in FP32 registers while the deposit cell stays
-// the same, and adds the sums, rounded to the global quantum, to the block
+// block's fixed-point scale) in FP32 registers while the deposit cell stays
+// the same, and adds the sums, rounded to the block quantum, to the block
 // box when the cell changes and at the end.
 // ----------------------------------------------------------------------
 
