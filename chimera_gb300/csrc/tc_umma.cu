@@ -156,6 +156,7 @@ struct UmmaArgs {
   int M, N, Np, K, Kp;
   const float2 *shift;
   int epi;
+  int fac_bulk;  // factor columns copied to shared memory by bulk copies
   uint32_t tmem_cols;
 };
 
@@ -166,7 +167,7 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
   constexpr int TM = Cfg::TM, STAGES = Cfg::STAGES, kProducers = Cfg::kProducers;
   constexpr uint32_t kATermBytes = Cfg::kATermBytes, kABytes = Cfg::kABytes;
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t afull[STAGES], bfull[STAGES], empty[STAGES], done;
+  __shared__ __align__(8) uint64_t afull[STAGES], bfull[STAGES], empty[STAGES], done, facbar;
   __shared__ uint32_t tmem_base;
   __shared__ int fail;
   const int prob = blockIdx.y, mt = blockIdx.x;
@@ -183,6 +184,7 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
       mbar_init(&empty[s], 1);
     }
     mbar_init(&done, 1);
+    mbar_init(&facbar, 1);
     fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -329,7 +331,26 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const bool use = __syncthreads_and(drained && !fail);
   if (!drained && threadIdx.x == 0) atomicCAS(&g_umma_error, 0, 2);
-  if (use && threadIdx.x < kProducers) {
+  // factor epilogue: the tile's factor block (TM/2 x-rows x N columns, one
+  // contiguous run per column) lands in the drained stages by bulk copies,
+  // all in flight at once, instead of a dependent global load per column
+  // group
+  const int nxr = TM / 2, xr0 = mt * (TM / 2);
+  const float *facs = reinterpret_cast<const float *>(smem);
+  bool fac_smem = false;
+  if (EPI == TC_EPI_SHIFT_FAC && use && A.fac_bulk) {
+    if (threadIdx.x == kProducers) {
+      const int rows = min(nxr, (A.M >> 1) - xr0);  // a multiple of 4 (host check)
+      const uint32_t bytes = (uint32_t)rows * 4u;
+      mbar_expect_tx(&facbar, bytes * (uint32_t)A.N);
+      for (int n = 0; n < A.N; ++n)
+        bulk_g2s(smem + (size_t)n * nxr * 4, Q.fac + xr0 + (long long)(A.M >> 1) * n, bytes, &facbar);
+    }
+    const bool landed = mbar_wait(&facbar, 0);
+    if (!landed) atomicCAS(&g_umma_error, 0, 4);
+    fac_smem = __syncthreads_and(landed);
+  }
+  if (use && (EPI != TC_EPI_SHIFT_FAC || !A.fac_bulk || fac_smem) && threadIdx.x < kProducers) {
     const int qd = warp & 3, hh = warp >> 2;       // TMEM lane quarter, row half
     const int row = hh * TH + qd * 32 + lane;      // row of the tile
     const long long gm = (long long)mt * TM + row;
@@ -339,13 +360,15 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
     const float *fac = Q.fac;
     const bool rok = gm < A.M;
     for (int c0 = 0; c0 < A.Np; c0 += 16) {
-      // factors of the 16 columns loaded before the accumulator wait
+      // factors of the 16 columns read before the accumulator wait
       float fv[16];
       if (EPI == TC_EPI_SHIFT_FAC) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int n = c0 + j;
-          fv[j] = (rok && n < A.N) ? __ldg(fac + (gm >> 1) + (long long)(A.M >> 1) * n) : 1.0f;
+          fv[j] = !(rok && n < A.N) ? 1.0f
+                  : fac_smem ? facs[n * nxr + (row >> 1)]
+                             : __ldg(fac + (gm >> 1) + (long long)(A.M >> 1) * n);
         }
       }
       uint32_t v[16];
@@ -434,6 +457,13 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
   ua.shift = shift;
   ua.epi = epi;
   ua.tmem_cols = cols;
+  // bulk copies of the factor columns need 16-byte aligned runs: M/2 a
+  // multiple of 4 and 16-byte aligned factor planes; the factor block
+  // (TM/2 x Np FP32) fits in the stages
+  ua.fac_bulk = (epi == TC_EPI_SHIFT_FAC && (M / 2) % 4 == 0 &&
+                 (size_t)(TM / 2) * Np * 4 <= (size_t)STAGES * (kABytes + 3 * b_term)) ? 1 : 0;
+  for (int i = 0; i < count && ua.fac_bulk; ++i)
+    if (!p[i].fac || (reinterpret_cast<uintptr_t>(p[i].fac) & 15)) ua.fac_bulk = 0;
   for (int c0 = 0; c0 < count; c0 += kMaxBatch) {
     const int cnt = count - c0 < kMaxBatch ? count - c0 : kMaxBatch;
     UmmaBatch ub;
