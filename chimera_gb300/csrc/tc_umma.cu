@@ -265,6 +265,16 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
       mbar_arrive(&afull[s]);
       if (kb + 1 < nkb) load(kb + 1);
     }
+  } else if (EPI == TC_EPI_SHIFT_FAC && A.fac_bulk && threadIdx.x > kProducers) {
+    // idle lanes of the MMA warp: start the tile's factor block (read by
+    // the epilogue) towards L2, two 128-byte lines per column
+    const int xr0p = mt * (TM / 2);
+    const int rows = min(TM / 2, (A.M >> 1) - xr0p);
+    for (int t = threadIdx.x - kProducers - 1; t < 2 * A.N; t += 31) {
+      const int n = t >> 1, part = t & 1;
+      if (part * 32 < rows)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(Q.fac + xr0p + part * 32 + (long long)(A.M >> 1) * n));
+    }
   } else if (threadIdx.x == kProducers) {
     // ---- B streaming and MMA issue
     const uint32_t idesc = idesc_bf16(TH, A.Np);
@@ -339,11 +349,14 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
   const float *facs = reinterpret_cast<const float *>(smem);
   bool fac_smem = false;
   if (EPI == TC_EPI_SHIFT_FAC && use && A.fac_bulk) {
-    if (threadIdx.x == kProducers) {
+    if (warp == kProducers / 32) {
+      // the last warp issues the N copies, one lane per column in turn,
+      // after lane 0 has announced the byte count
       const int rows = min(nxr, (A.M >> 1) - xr0);  // a multiple of 4 (host check)
       const uint32_t bytes = (uint32_t)rows * 4u;
-      mbar_expect_tx(&facbar, bytes * (uint32_t)A.N);
-      for (int n = 0; n < A.N; ++n)
+      if (lane == 0) mbar_expect_tx(&facbar, bytes * (uint32_t)A.N);
+      __syncwarp();
+      for (int n = lane; n < A.N; n += 32)
         bulk_g2s(smem + (size_t)n * nxr * 4, Q.fac + xr0 + (long long)(A.M >> 1) * n, bytes, &facbar);
     }
     const bool landed = mbar_wait(&facbar, 0);
@@ -359,19 +372,8 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
     float *C = Q.C;
     const float *fac = Q.fac;
     const bool rok = gm < A.M;
-    for (int c0 = 0; c0 < A.Np; c0 += 16) {
-      // factors of the 16 columns read before the accumulator wait
-      float fv[16];
-      if (EPI == TC_EPI_SHIFT_FAC) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int n = c0 + j;
-          fv[j] = !(rok && n < A.N) ? 1.0f
-                  : fac_smem ? facs[n * nxr + (row >> 1)]
-                             : __ldg(fac + (gm >> 1) + (long long)(A.M >> 1) * n);
-        }
-      }
-      uint32_t v[16];
+    // 16-column groups in pairs: both accumulator loads issued before one wait
+    auto tmem_ld16 = [&](uint32_t (&v)[16], int c0) {
       const uint32_t taddr = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(hh * A.Np + c0);
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -379,7 +381,22 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
             "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
             "=r"(v[14]), "=r"(v[15])
           : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    };
+    auto finish16 = [&](const uint32_t (&v)[16], int c0) {
+      // factors of the 16 columns
+      float fv[16];
+      if (EPI == TC_EPI_SHIFT_FAC) {
+        if (fac_smem) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) fv[j] = facs[(c0 + j) * nxr + (row >> 1)];
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = c0 + j;
+            fv[j] = (rok && n < A.N) ? __ldg(fac + (gm >> 1) + (long long)(A.M >> 1) * n) : 1.0f;
+          }
+        }
+      }
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         float x = __uint_as_float(v[j]);
@@ -393,6 +410,15 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
         }
         if (rok && n < A.N) C[gm + (long long)n * A.M] = x;
       }
+    };
+    for (int c0 = 0; c0 < A.Np; c0 += 32) {
+      uint32_t va[16], vb[16];
+      const bool two = c0 + 16 < A.Np;
+      tmem_ld16(va, c0);
+      if (two) tmem_ld16(vb, c0 + 16);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      finish16(va, c0);
+      if (two) finish16(vb, c0 + 16);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
