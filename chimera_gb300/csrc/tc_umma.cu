@@ -156,7 +156,7 @@ struct UmmaArgs {
   int M, N, Np, K, Kp;
   const float2 *shift;
   int epi;
-  int fac_bulk;  // factor columns copied to shared memory by bulk copies
+  int fac_bulk;  // factor block staged in shared memory for the epilogue
   uint32_t tmem_cols;
 };
 
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
   constexpr int TM = Cfg::TM, STAGES = Cfg::STAGES, kProducers = Cfg::kProducers;
   constexpr uint32_t kATermBytes = Cfg::kATermBytes, kABytes = Cfg::kABytes;
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t afull[STAGES], bfull[STAGES], empty[STAGES], done, facbar;
+  __shared__ __align__(8) uint64_t afull[STAGES], bfull[STAGES], empty[STAGES], done;
   __shared__ uint32_t tmem_base;
   __shared__ int fail;
   const int prob = blockIdx.y, mt = blockIdx.x;
@@ -184,7 +184,6 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
       mbar_init(&empty[s], 1);
     }
     mbar_init(&done, 1);
-    mbar_init(&facbar, 1);
     fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -342,28 +341,37 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
   const bool use = __syncthreads_and(drained && !fail);
   if (!drained && threadIdx.x == 0) atomicCAS(&g_umma_error, 0, 2);
   // factor epilogue: the tile's factor block (TM/2 x-rows x N columns, one
-  // contiguous run per column) lands in the drained stages by bulk copies,
-  // all in flight at once, instead of a dependent global load per column
-  // group
+  // contiguous run per column, started towards L2 during the K loop) is
+  // copied into the drained stages with 16-byte loads, all threads at once,
+  // instead of a dependent global load per column group
   const int nxr = TM / 2, xr0 = mt * (TM / 2);
   const float *facs = reinterpret_cast<const float *>(smem);
   bool fac_smem = false;
   if (EPI == TC_EPI_SHIFT_FAC && use && A.fac_bulk) {
-    if (warp == kProducers / 32) {
-      // the last warp issues the N copies, one lane per column in turn,
-      // after lane 0 has announced the byte count
-      const int rows = min(nxr, (A.M >> 1) - xr0);  // a multiple of 4 (host check)
-      const uint32_t bytes = (uint32_t)rows * 4u;
-      if (lane == 0) mbar_expect_tx(&facbar, bytes * (uint32_t)A.N);
-      __syncwarp();
-      for (int n = lane; n < A.N; n += 32)
-        bulk_g2s(smem + (size_t)n * nxr * 4, Q.fac + xr0 + (long long)(A.M >> 1) * n, bytes, &facbar);
+    const int rows = min(nxr, (A.M >> 1) - xr0);  // a multiple of 4 (host check)
+    const int nq = nxr / 4, total = nq * A.N;       // float4 per column, in the block
+    float4 *dst = reinterpret_cast<float4 *>(smem);
+    constexpr int kBatch = 13;
+    for (int t0 = threadIdx.x; t0 < total; t0 += kBatch * (int)blockDim.x) {
+      float4 v[kBatch];
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int t = t0 + b * (int)blockDim.x;
+        const int n = t / nq, q = t - n * nq;
+        v[b] = (t < total && 4 * q < rows)
+                   ? __ldg(reinterpret_cast<const float4 *>(Q.fac + xr0 + (long long)(A.M >> 1) * n) + q)
+                   : make_float4(1.f, 1.f, 1.f, 1.f);
+      }
+#pragma unroll
+      for (int b = 0; b < kBatch; ++b) {
+        const int t = t0 + b * (int)blockDim.x;
+        if (t < total) dst[t] = v[b];
+      }
     }
-    const bool landed = mbar_wait(&facbar, 0);
-    if (!landed) atomicCAS(&g_umma_error, 0, 4);
-    fac_smem = __syncthreads_and(landed);
+    __syncthreads();
+    fac_smem = true;
   }
-  if (use && (EPI != TC_EPI_SHIFT_FAC || !A.fac_bulk || fac_smem) && threadIdx.x < kProducers) {
+  if (use && threadIdx.x < kProducers) {
     const int qd = warp & 3, hh = warp >> 2;       // TMEM lane quarter, row half
     const int row = hh * TH + qd * 32 + lane;      // row of the tile
     const long long gm = (long long)mt * TM + row;
@@ -483,9 +491,8 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
   ua.shift = shift;
   ua.epi = epi;
   ua.tmem_cols = cols;
-  // bulk copies of the factor columns need 16-byte aligned runs: M/2 a
-  // multiple of 4 and 16-byte aligned factor planes; the factor block
-  // (TM/2 x Np FP32) fits in the stages
+  // the staged factor block is read with 16-byte loads: M/2 a multiple of 4
+  // and 16-byte aligned factor planes; it (TM/2 x Np FP32) fits in the stages
   ua.fac_bulk = (epi == TC_EPI_SHIFT_FAC && (M / 2) % 4 == 0 &&
                  (size_t)(TM / 2) * Np * 4 <= (size_t)STAGES * (kABytes + 3 * b_term)) ? 1 : 0;
   for (int i = 0; i < count && ua.fac_bulk; ++i)
