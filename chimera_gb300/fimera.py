@@ -39,7 +39,7 @@ __all__ = [
     "field_drift", "omp_mult_vec", "omp_mult_scl", "omp_add_vec", "omp_add_scl",
     "undul_analytic", "undul_analytic_taper", "undul_mapped", "undul_mapped_tap",
     "planewave", "gaussbeam", "sortpartsout", "chunk_coords_boundaries",
-    "align_data_vec", "align_data_scl", "chunk_order",
+    "align_data_vec", "align_data_scl", "chunk_order", "intens_profo",
 ]
 
 
@@ -728,3 +728,49 @@ def gaussbeam(coord, Fld, time, a0, params):
     _lib.call("chm_gaussbeam", x, xcs, xps, f, fcs, fps, float(time), float(a0), p.ctypes.data,
               n, _stream())
     return Fld
+
+
+# ---------------------------------------------------------------------------
+# utils.f90 and the Diagnostics reductions
+# ---------------------------------------------------------------------------
+
+def intens_profo(Fld, NO):
+    """utils.f90:18-57: PWR_RO (NO, nr) float64 from Fld (nx+1, nr+1,
+    2 nkO + 1, 3) complex128 (f2py infers nkO, so the mode extent is odd)."""
+    f = _grid(Fld, "Fld", (4,))
+    NX, NR, NM, nc = f.shape
+    if nc != 3 or NM % 2 != 1:
+        raise ChimeraError("intens_profo: Fld must be (nx+1, nr+1, 2*nkO+1, 3)")
+    out = fortran_empty((int(NO), NR - 1), dtype=torch.float64, device=f.device)
+    _lib.call("chm_intens_profo", out.data_ptr(), f.data_ptr(), int(NO), NX, NR, NM, _stream())
+    return out
+
+
+def em_energy(EG_fb, EnergyFact):
+    """Electromagnetic energy per kx of diagnostics.py:112-114 (before its
+    reordering): sum over kr and modes of EnergyFact * sum_{l<3} |E_l|^2."""
+    eg = _grid(EG_fb, "EG_fb", (4,))
+    nx, nkr, nm = _dims(eg)
+    ef = to_device(EnergyFact, torch.float64, eg.device)
+    if tuple(ef.shape) != (nx, nkr, nm):
+        raise ChimeraError(f"EnergyFact has shape {tuple(ef.shape)}, expected {(nx, nkr, nm)}")
+    out = torch.empty(nx, dtype=torch.float64, device=eg.device)
+    _lib.call("chm_em_energy", out.data_ptr(), eg.data_ptr(), ef.data_ptr(), nx, nkr, nm,
+              eg.shape[3], _stream())
+    return out
+
+
+def power_profile(dat, Rgrid, fac):
+    """Power per x of diagnostics.py:134-143: fac * sum_r Rgrid[r] *
+    sum_{m, l} |dat(x, r, m, l)|^2 for a spatial vector field (nx, nr, nm, 3)."""
+    v = _grid(dat, "dat", (4,))
+    nx, nr, nm = _dims(v)
+    if v.shape[3] != 3:
+        raise ChimeraError("power_profile: expected a 3-component field")
+    rg = to_device(Rgrid, torch.float64, v.device)
+    if rg.numel() != nr:
+        raise ChimeraError(f"Rgrid has {rg.numel()} entries, field has nr={nr}")
+    out = torch.empty(nx, dtype=torch.float64, device=v.device)
+    _lib.call("chm_power_profile", out.data_ptr(), v.data_ptr(), rg.data_ptr(), float(fac), nx, nr,
+              nm, _stream())
+    return out

@@ -523,6 +523,31 @@ int chm_sp_gemm(float *C, const float *A, const chm_sp_ops *ops, int64_t mode,
 /* Nonzero if a tensor-core GEMM CTA hit a wait limit since load. */
 int chm_sp_umma_status(void);
 
+/* ------------------------------------------------------------------------
+ * Diagnostics (moduls/diagnostics.py, f90/utils.f90): device reductions of
+ * the FP64 grids, each in a fixed summation order (bitwise reproducible).
+ * ------------------------------------------------------------------------ */
+/* nrg_out (diagnostics.py:109-122), before its fftshift-style reordering:
+ * out[x] = sum_{kr, m} efact(x, kr, m) * sum_{l < 3} |eg(x, kr, m, l)|^2.
+ * eg: (nx, nkr, nm, ncomp) complex128 with the E field in components 0-2
+ * (the solver's EG_fb, ncomp = 6); efact: (nx, nkr, nm) EnergyFact
+ * (solvers.py:143-149); out: nx doubles. */
+int chm_em_energy(double *out, const chm_c128 *eg, const double *efact, int64_t nx, int64_t nkr,
+                  int64_t nm, int64_t ncomp, void *stream);
+/* pwr_out (diagnostics.py:124-149), power per x of a spatial field:
+ * out[x] = fac * sum_r rgrid[r] * sum_{m, l} |vec(x, r, m, l)|^2 with vec
+ * (nx, nr, nm, 3) complex128 (fb_vec_out of EG_fb[..., :3]), rgrid (nr)
+ * (RgridFull) and fac = PwrFctr * 2 dr. */
+int chm_power_profile(double *out, const chm_c128 *vec, const double *rgrid, double fac, int64_t nx,
+                      int64_t nr, int64_t nm, void *stream);
+/* intens_profO (utils.f90:18-57): pwr (NO, NR - 1) with
+ * pwr(iO, ir) = sum_l sum_ix |sum_k e^{i k 2 pi iO / (NO - 1)} fld(ix, ir, k, l)|^2
+ * for iO = 0 .. NO - 1, ir = 1 .. NR - 1 and k = -K .. K; fld is
+ * (NX, NR, NM = 2K + 1, 3) complex128 (the Fortran's Fld(0:nx, 0:nr,
+ * -nkO:nkO, 3); f2py infers nkO, so NM is odd). */
+int chm_intens_profo(double *pwr, const chm_c128 *fld, int64_t NO, int64_t NX, int64_t NR,
+                     int64_t NM, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1494,3 +1494,37 @@ void orc_gaussbeam(const double *coord, double *fld, double time, double a0,
     fld[6 * ip + 4] -= axis * E;
   }
 }
+
+/* ------------------------------------------------------------------------ */
+/* utils.f90:18-57 intens_profO.  pwr (NO, NR-1); fld (NX, NR, NM, 3) with    */
+/* NM = 2 nkO + 1 (modes -nkO..nkO).  The angle phases are built by repeated */
+/* products as the Fortran does (Os(iO) = Os(iO-1) * phase_p).               */
+/* ------------------------------------------------------------------------ */
+void orc_intens_profo(double *pwr, const cplx *fld, i64 NO, i64 NX, i64 NR, i64 NM) {
+  const i64 nkO = (NM - 1) / 2;
+  const i64 nr = NR - 1;
+  cplx *Os = (cplx *)malloc(sizeof(cplx) * (size_t)NO);
+  cplx *phaseO = (cplx *)malloc(sizeof(cplx) * (size_t)NM);
+  memset(pwr, 0, sizeof(double) * (size_t)(NO * nr));
+  Os[0] = 1.0;
+  const cplx step = cos(2.0 * PI / (double)(NO - 1)) + II * sin(2.0 * PI / (double)(NO - 1));
+  for (i64 io = 1; io < NO; ++io) Os[io] = Os[io - 1] * step;
+  for (i64 io = 0; io < NO; ++io) {
+    const cplx pp = Os[io], pm = 1.0 / Os[io];
+    for (i64 k = 0; k < NM; ++k) phaseO[k] = 1.0;
+    for (i64 k = 1; k <= nkO; ++k) {
+      phaseO[nkO + k] = phaseO[nkO + k - 1] * pp;
+      phaseO[nkO - k] = phaseO[nkO - k + 1] * pm;
+    }
+    for (int l = 0; l < 3; ++l)
+      for (i64 ir = 1; ir <= nr; ++ir)
+        for (i64 ix = 0; ix < NX; ++ix) {
+          cplx s = 0.0;
+          for (i64 k = 0; k < NM; ++k) s += phaseO[k] * fld[ix + NX * (ir + NR * (k + NM * l))];
+          const double a = cabs(s);
+          pwr[io + NO * (ir - 1)] += a * a;
+        }
+  }
+  free(Os);
+  free(phaseO);
+}

@@ -551,3 +551,33 @@ def fft(a, sign=-1):
     out = np.empty_like(a)
     lib().orc_fft(_vp(a), _vp(out), _n(a.size), C.c_int(sign))
     return out
+
+
+# ---------------------------------------------------------------------------
+# utils.f90 and diagnostics.py reductions
+# ---------------------------------------------------------------------------
+
+def intens_profo(Fld, NO):
+    """utils.f90:18-57: PWR_RO (NO, nr) from Fld (nx+1, nr+1, 2 nkO + 1, 3).
+    As f2py, nkO is inferred from the mode extent, which must be odd."""
+    f = _in(Fld, np.complex128)
+    NX, NR, NM, nc = f.shape
+    if nc != 3 or NM % 2 != 1:
+        raise ValueError("intens_profo: Fld must be (nx+1, nr+1, 2*nkO+1, 3)")
+    out = np.zeros((int(NO), NR - 1), dtype=np.float64, order="F")
+    lib().orc_intens_profo(_p(out), _vp(f), _n(NO), _n(NX), _n(NR), _n(NM))
+    return out
+
+
+def em_energy(EG_fb, EnergyFact):
+    """diagnostics.py:112-114 before the reordering, in the reference's
+    numpy order: (|E|^2 summed over the 3 components) * EnergyFact, summed
+    over modes, then over kr."""
+    eg = np.asarray(EG_fb)
+    return ((np.abs(eg[:, :, :, :3]) ** 2).sum(-1) * np.asarray(EnergyFact)).sum(-1).sum(-1)
+
+
+def power_profile(dat, Rgrid, fac):
+    """diagnostics.py:134-143: fac * sum_r Rgrid * sum_{m, l} |dat|^2."""
+    dat = np.asarray(dat)
+    return fac * ((np.abs(dat) ** 2).sum(-1).sum(-1) * np.asarray(Rgrid)[None, :]).sum(-1)

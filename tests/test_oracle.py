@@ -191,3 +191,20 @@ def test_psatd_vacuum_matches_analytic(orc, golden):
     C1, C2 = coeffs(5 * dt)
     b = orc.maxwell_push_wo_spchrg(eg.copy(order="F"), j, C1, C2)
     assert rel_l2(a, b) < 1e-12
+
+
+def test_oracle_intens_profo_is_the_angular_sum(orc):
+    """utils.f90:18-57 restated: |sum_k e^{i k phi} F_k|^2 summed over x and
+    components, per angle phi_iO = 2 pi iO / (NO - 1) and row ir >= 1."""
+    rng = np.random.default_rng(5)
+    F = rng.standard_normal((9, 6, 5, 3)) + 1j * rng.standard_normal((9, 6, 5, 3))
+    NO, K = 8, 2
+    got = orc.intens_profo(F, NO)
+    ref = np.zeros((NO, 5))
+    for io in range(NO):
+        ph = np.exp(1j * 2 * np.pi * io / (NO - 1) * np.arange(-K, K + 1))
+        s = (F[:, 1:] * ph[None, None, :, None]).sum(2)
+        ref[io] = (np.abs(s) ** 2).sum(-1).sum(0)
+    assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
+    with pytest.raises(ValueError):
+        orc.intens_profo(F[:, :, :4], NO)
