@@ -259,3 +259,19 @@ class ChimeraRun:
             a = self._args0()
             SimDom = np.asfortranarray([a["leftX"], a["rightX"], 0, a["Rgrid"].max() ** 2])
             species.chunk_and_damp(SimDom=SimDom, position="cntr")
+
+    # ------------------------------------------------------------------
+    # checkpoints (chimera_main.py:325-410), as .npz
+    def drop_snap(self, fname="./snap_", verbose=False):
+        """chimera_main.py:325-369: write every storable Data / Args entry of
+        the solvers and species; returns the file name."""
+        from . import snapshot
+        name = snapshot.snap_name(fname)
+        return snapshot.write(name, snapshot.snap_arrays(self.Solvers, self.Particles, verbose))
+
+    def read_snap(self, fname="./test.npz", verbose=False):
+        """chimera_main.py:371-410: restore the solvers' and species' Data /
+        Args from a drop_snap file."""
+        from . import snapshot
+        with np.load(fname, allow_pickle=False) as f:
+            snapshot.read_into(f, self.Solvers, self.Particles, verbose)

@@ -517,6 +517,56 @@ class SplitRun:
         step (one device->host read)."""
         return int(sum(int(P.counters[1].item()) for _, P in self._moving()))
 
+    # ------------------------------------------------------------------
+    # checkpoints: the FP64 run's drop_snap keys plus the split form's own
+    # state (deposit scales, background accumulator) under ``split/``
+    def drop_snap(self, fname="./snap_", verbose=False):
+        """chimera_main.py:325-369 for the split form: ``to_fp64()`` (which
+        compacts the particle arrays, in their split order) and the FP64
+        keys, plus ``split/...``; returns the file name."""
+        from . import snapshot
+        self.to_fp64()
+        arrays = snapshot.snap_arrays(self.fp.Solvers, self.fp.Particles, verbose)
+        arrays["split/scaleJ"] = self.scaleJ.cpu().numpy()
+        arrays["split/scaleR"] = self.scaleR.cpu().numpy()
+        arrays["split/scaleBG"] = self.scaleBG.cpu().numpy()
+        arrays["split/scales_valid"] = np.asarray(self._scales_valid)
+        arrays["split/have_bg"] = np.asarray(self.have_bg)
+        arrays["split/accBG"] = self.accBG.cpu().numpy()
+        return snapshot.write(snapshot.snap_name(fname), arrays)
+
+    def read_snap(self, fname="./test.npz", verbose=False):
+        """chimera_main.py:371-410 for the split form: the FP64 Data / Args,
+        then the split fields and particles from them (particles in the
+        stored order), and the split state; a restart continues bitwise as
+        the run that wrote the file."""
+        from . import snapshot
+        with np.load(fname, allow_pickle=False) as f:
+            snapshot.read_into(f, self.fp.Solvers, self.fp.Particles, verbose)
+            D = self.solver.Data
+            self.EG.copy_(D["EG_fb"])
+            if self.space_charge:
+                self.gprv.copy_(D["gradRho_fb_prv"])
+                self.gnxt.copy_(D["gradRho_fb_nxt"])
+            for spc, P in zip(self.fp.Particles, self.parts):
+                P.n = 0
+                P.moves = 0
+                P.counters.zero_()
+                d = spc.Data
+                P.append_f64(d["coords"], d["momenta"], d["weights"], self.X0, self.dx)
+            if "split/scaleJ" in f.files:
+                for t, k in ((self.scaleJ, "scaleJ"), (self.scaleR, "scaleR"),
+                             (self.scaleBG, "scaleBG"), (self.accBG, "accBG")):
+                    t.copy_(torch.from_numpy(np.ascontiguousarray(f["split/" + k])))
+                self._scales_valid = bool(f["split/scales_valid"])
+                self.have_bg = bool(f["split/have_bg"])
+            else:
+                self._scales_valid = False
+                self.have_bg = False
+                if self.space_charge and "BckGrndRho" in D and self._still():
+                    self._deposit_background()
+        return self
+
     def to_fp64(self):
         """Write the split state into the FP64 Data of the solver and species."""
         D = self.solver.Data

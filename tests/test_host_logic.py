@@ -126,3 +126,57 @@ def test_cell_order_patches_and_deposit_cells():
     # the torch path gives the same permutation
     ot = cell_order(torch.from_numpy(coords), X0, dx, dr, patch=P)
     assert np.array_equal(ot.numpy(), o)
+
+
+def test_snapshot_keys_and_restore_host(tmp_path):
+    """drop_snap / read_snap key layout (chimera_main.py:325-410) on stand-in
+    solver / species objects: containers and callables are skipped, arrays
+    and scalars round-trip, species are resized to the stored count."""
+    torch = pytest.importorskip("torch")
+    from chimera_gb300 import snapshot
+
+    class Store:
+        def __init__(self):
+            self.n = 3
+
+        def resize(self, n):
+            self.n = n
+
+    class Sp:
+        def __init__(self, n):
+            self.store = Store()
+            self.device = torch.device("cpu")
+            self.chunks = torch.arange(4)
+            self.w = torch.arange(8, dtype=torch.float64)
+            self.store.n = n
+            self.Data = {}
+            self._sync()
+            self.Args = {"dx": 0.1, "Features": ("Still",), "Xgrid": np.linspace(0, 1, 5),
+                         "ProfileFunc": (lambda x: x), "Nx": 4, "name": "el"}
+
+        def _sync(self):
+            self.Data["weights"] = self.w[:self.store.n]
+
+    class Sol:
+        def __init__(self):
+            self.Data = {"EB": torch.zeros((4, 3), dtype=torch.complex128), "nothing": None}
+            self.Args = {"leftX": -1.5, "Grid": (0, 1), "kx": np.arange(6.0).reshape(2, 3)}
+
+    sol, sp = Sol(), Sp(3)
+    sol.Data["EB"] += 1 + 2j
+    sp.w += 10
+    arrays = snapshot.snap_arrays([sol], [sp])
+    assert set(arrays) == {"solver0/Data/EB", "solver0/Args/leftX", "solver0/Args/kx",
+                           "specie0/Data/weights", "specie0/Args/dx", "specie0/Args/Xgrid",
+                           "specie0/Args/Nx", "specie0/Args/name", "specie0/chunks",
+                           "NumSolvers", "NumSpecies", "NumThreads"}
+    fname = snapshot.write(str(tmp_path / "s.npz"), arrays)
+    sol2, sp2 = Sol(), Sp(5)
+    sol2.Args["leftX"] = 0.0
+    with np.load(fname) as f:
+        snapshot.read_into(f, [sol2], [sp2])
+    assert torch.equal(sol2.Data["EB"], sol.Data["EB"])
+    assert sol2.Args["leftX"] == -1.5 and isinstance(sol2.Args["leftX"], float)
+    assert np.array_equal(sol2.Args["kx"], sol.Args["kx"]) and sol2.Args["kx"].flags.f_contiguous
+    assert sp2.store.n == 3 and torch.equal(sp2.Data["weights"], sp.Data["weights"])
+    assert torch.equal(sp2.chunks, sp.chunks) and sp2.Args["name"] == "el"
