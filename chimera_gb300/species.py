@@ -73,7 +73,10 @@ class ParticleStore:
                 t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64)))
                 if self.device.type == "cuda":
                     chimera.io_bytes["h2d"] += t.numel() * 8
-            t = t.to(self.device, torch.float64).reshape(nc, m)
+                    # pinned staging: an asynchronous copy (a pageable one
+                    # would wait for the work queued on the stream)
+                    t = t.pin_memory()
+            t = t.to(self.device, torch.float64, non_blocking=True).reshape(nc, m)
             self.buf[k][:, self.n: self.n + m].copy_(t)
         self.n += m
 

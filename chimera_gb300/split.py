@@ -150,15 +150,20 @@ class _SpParticles:
         if _slots(self.n + m) > self.cap:
             self.reserve(max(self.n + m, int(1.5 * self.cap)))
         dev = self.device
-        tx = coords if isinstance(coords, torch.Tensor) else torch.from_numpy(
-            np.ascontiguousarray(coords, dtype=np.float64))
-        tp = momenta if isinstance(momenta, torch.Tensor) else torch.from_numpy(
-            np.ascontiguousarray(momenta, dtype=np.float64))
-        tw = weights if isinstance(weights, torch.Tensor) else torch.from_numpy(
-            np.ascontiguousarray(weights, dtype=np.float64))
-        if tx.device.type != "cuda":
-            chimera.io_bytes["h2d"] += (tx.numel() + tp.numel() + tw.numel()) * 8
-        tx, tp, tw = (t.to(dev, torch.float64) for t in (tx, tp, tw))
+        if all(isinstance(a, torch.Tensor) and a.device.type == "cuda"
+               for a in (coords, momenta, weights)):
+            tx, tp, tw = (t.to(torch.float64) for t in (coords, momenta, weights))
+        else:
+            # host arrays: one pinned staging buffer and one asynchronous copy
+            # (a pageable copy would wait for the work queued on the stream)
+            stage = torch.empty(7 * m, dtype=torch.float64, pin_memory=True)
+            h = stage.numpy()
+            for a, lo, nc in ((coords, 0, 3), (momenta, 3 * m, 3), (weights, 6 * m, 1)):
+                src = a.cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+                h[lo:lo + nc * m].reshape(nc, m)[...] = src.reshape(nc, m)
+            chimera.io_bytes["h2d"] += 7 * m * 8
+            d = stage.to(dev, non_blocking=True)
+            tx, tp, tw = d[:3 * m].view(3, m), d[3 * m:6 * m].view(3, m), d[6 * m:]
         _lib.call("chm_sp_from_f64", *self.ptrs(), self.dead.data_ptr(), self.n, tx.data_ptr(),
                   tx.stride(0), tx.stride(1), tp.data_ptr(), tp.stride(0), tp.stride(1),
                   tw.data_ptr(), tw.stride(0), float(X0), float(dx), m, _stream())
