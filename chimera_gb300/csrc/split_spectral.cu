@@ -77,12 +77,18 @@ __global__ void twiddle32_kernel(float2 *tw, int n) {
   }
 }
 
-// exp(sign i kx leftX) evaluated in FP64 (the argument can be large), stored FP32
-__global__ void shift32_kernel(float2 *shift, const double *kx, double leftX, int sign, i64 nx) {
+// exp(sign i kx leftX) evaluated in FP64 (the argument can be large), stored
+// FP32; with tw, also the FFT twiddles exp(-2 pi i t / nx) (as twiddle32_kernel)
+__global__ void shift32_kernel(float2 *shift, const double *kx, double leftX, int sign, i64 nx,
+                               float2 *tw) {
   for (i64 x = blockIdx.x * (i64)blockDim.x + threadIdx.x; x < nx; x += (i64)gridDim.x * blockDim.x) {
     double s, c;
     sincos(leftX * kx[x], &s, &c);
     shift[x] = make_float2((float)c, (float)(sign * s));
+    if (tw) {
+      sincospi(2.0 * (double)x / (double)nx, &s, &c);
+      tw[x] = make_float2((float)c, (float)-s);
+    }
   }
 }
 
@@ -207,6 +213,157 @@ __device__ float2 *run32p(const Plan &P, float2 *a, float2 *b, const float2 *tw,
   return a;
 }
 
+// ---------------------------------------------------------------------------
+// Register passes for power-of-two n >= 512: each thread keeps 16 points in
+// registers and does a 16-point DFT (4 x 4) per pass, so a 2048-point line
+// takes three passes (16, 16, 8) through one shared-memory buffer instead of
+// six radix-4 passes through two.  Stockham indexing as pass32; the twiddles
+// come from a global table (L1/L2) of n entries exp(-2 pi i t / n).
+// ---------------------------------------------------------------------------
+// x * (sign i): -i x for sign < 0, +i x for sign > 0
+__device__ __forceinline__ float2 mul_si(float2 x, int sign) {
+  return sign < 0 ? make_float2(x.y, -x.x) : make_float2(-x.y, x.x);
+}
+
+__device__ __forceinline__ void dft2r(float2 &x0, float2 &x1) {
+  const float2 a = x0;
+  x0 = fadd(a, x1);
+  x1 = fsub(a, x1);
+}
+
+// 4-point DFT in place, natural order (exponent sign `sign`)
+__device__ __forceinline__ void dft4r(float2 &x0, float2 &x1, float2 &x2, float2 &x3, int sign) {
+  const float2 a0 = fadd(x0, x2), a1 = fsub(x0, x2), a2 = fadd(x1, x3);
+  const float2 a3 = mul_si(fsub(x1, x3), sign);
+  x0 = fadd(a0, a2);
+  x2 = fsub(a0, a2);
+  x1 = fadd(a1, a3);
+  x3 = fsub(a1, a3);
+}
+
+// e^{sign 2 pi i m / 16} for m = 0..9 (the exact values of the angles)
+__device__ __forceinline__ float2 w16(int m, int sign) {
+  const float c1 = 0.92387953251128674f, s1 = 0.38268343236508977f, h = 0.70710678118654752f;
+  float2 w;
+  switch (m) {
+    case 1: w = make_float2(c1, s1); break;
+    case 2: w = make_float2(h, h); break;
+    case 3: w = make_float2(s1, c1); break;
+    case 4: w = make_float2(0.f, 1.f); break;
+    case 6: w = make_float2(-h, h); break;
+    case 9: w = make_float2(-c1, -s1); break;
+    default: w = make_float2(1.f, 0.f); break;
+  }
+  if (sign < 0) w.y = -w.y;
+  return w;
+}
+
+// 16-point DFT: v in natural order; result X[k1 + 4 k2] left in v[4 k1 + k2]
+__device__ __forceinline__ void dft16r(float2 (&v)[16], int sign) {
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) dft4r(v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12], sign);
+#pragma unroll
+  for (int k1 = 1; k1 < 4; ++k1)
+#pragma unroll
+    for (int n2 = 1; n2 < 4; ++n2) v[n2 + 4 * k1] = fmul(v[n2 + 4 * k1], w16(n2 * k1, sign));
+  // A(k1, n2) sits at v[4 k1 + n2]: second stage over n2 for each k1
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) dft4r(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3], sign);
+}
+
+// 8-point DFT: result X[k1 + 4 k2] left in v[2 k1 + k2]
+__device__ __forceinline__ void dft8r(float2 (&v)[8], int sign) {
+#pragma unroll
+  for (int n2 = 0; n2 < 2; ++n2) dft4r(v[n2], v[n2 + 2], v[n2 + 4], v[n2 + 6], sign);
+  // A(k1, 1) at v[1 + 2 k1] times e^{sign 2 pi i k1 / 8}
+  v[3] = fmul(v[3], w16(2, sign));
+  v[5] = mul_si(v[5], sign);
+  v[7] = fmul(v[7], w16(6, sign));
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) dft2r(v[2 * k1], v[2 * k1 + 1]);
+}
+
+__device__ __forceinline__ float2 tw_at(const float2 *__restrict__ tw, int t, int sign) {
+  float2 w = __ldg(tw + t);
+  if (sign > 0) w.y = -w.y;
+  return w;
+}
+
+// One in-place Stockham pass of radix R over the line in a[0..n), T threads
+// (t = this thread), butterflies j = t, t + T, ... < n / R.
+template <int R, typename Src, typename Sink>
+__device__ void pass_reg(float2 *a, int n, int l2n, int lNs, const float2 *__restrict__ tw, int sign,
+                         int t, int T, Src src, Sink sink) {
+  constexpr int lR = R == 16 ? 4 : R == 8 ? 3 : R == 4 ? 2 : 1;
+  constexpr int B = 16 / R;  // butterflies per thread (T = n / 16)
+  const int nb = n >> lR, Ns = 1 << lNs;
+  const int tsh = l2n - lNs - lR;  // twiddle index stride log2
+  float2 v[B][R];
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int j = t + b * T;
+    const int k = j & (Ns - 1);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      float2 x = src(j + r * nb);
+      if (r > 0 && k > 0) x = fmul(x, tw_at(tw, (r * k) << tsh, sign));
+      v[b][r] = x;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < B; ++b) {
+    const int j = t + b * T;
+    const int k = j & (Ns - 1);
+    const int base = ((j >> lNs) << (lNs + lR)) + k;
+    if constexpr (R == 16) {
+      dft16r(v[b], sign);
+#pragma unroll
+      for (int q = 0; q < 16; ++q) sink(base + q * Ns, v[b][4 * (q & 3) + (q >> 2)]);
+    } else if constexpr (R == 8) {
+      dft8r(v[b], sign);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) sink(base + q * Ns, v[b][2 * (q & 3) + (q >> 2)]);
+    } else if constexpr (R == 4) {
+      dft4r(v[b][0], v[b][1], v[b][2], v[b][3], sign);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) sink(base + q * Ns, v[b][q]);
+    } else {
+      dft2r(v[b][0], v[b][1]);
+      sink(base, v[b][0]);
+      sink(base + Ns, v[b][1]);
+    }
+  }
+  __syncthreads();
+}
+
+// The whole transform (n = 2^l2n >= 512, blockDim = n / 16) through the
+// buffer a.  The first pass reads its 16 points per thread from `first`
+// (the line's source, or the buffer), the last one writes through `last`;
+// the passes between use the buffer.  A thread's points in the first pass
+// are x = t + m T, m = 0..15, the ones its load loop would take.  (Writing
+// the last pass straight to the line's sink measured slower than through
+// the buffer and a coalesced store loop.)
+template <typename First, typename Last>
+__device__ void run16(float2 *a, int n, int l2n, const float2 *__restrict__ tw, int sign,
+                      First first, Last last) {
+  const int t = threadIdx.x, T = blockDim.x;
+  auto src = [a](int i) { return a[i]; };
+  auto dst = [a](int i, float2 v) { a[i] = v; };
+  const int n16 = l2n >> 2, rem = l2n & 3;  // radix-16 passes, remainder
+  __syncthreads();
+  if (n16 == 1 && rem == 0) pass_reg<16>(a, n, l2n, 0, tw, sign, t, T, first, last);
+  else pass_reg<16>(a, n, l2n, 0, tw, sign, t, T, first, dst);
+  for (int p = 1; p < n16; ++p) {
+    if (p == n16 - 1 && rem == 0) pass_reg<16>(a, n, l2n, 4 * p, tw, sign, t, T, src, last);
+    else pass_reg<16>(a, n, l2n, 4 * p, tw, sign, t, T, src, dst);
+  }
+  const int lNs = 4 * n16;
+  if (rem == 3) pass_reg<8>(a, n, l2n, lNs, tw, sign, t, T, src, last);
+  else if (rem == 2) pass_reg<4>(a, n, l2n, lNs, tw, sign, t, T, src, last);
+  else if (rem == 1) pass_reg<2>(a, n, l2n, lNs, tw, sign, t, T, src, last);
+}
+
 // 64-bit fixed-point value -> FP32 (two 32-bit conversions, no 64-bit unit)
 __device__ __forceinline__ float fix2f(long long v) {
   const int hi = (int)(v >> 32);
@@ -231,9 +388,14 @@ struct Lines32 {
   const float *filtr;
 };
 
-template <bool POW2>
-__global__ void lines32_kernel(Plan P, const float2 *__restrict__ tw, Lines32 L) {
+// MODE 0: any n (run32, mixed radix); 1: power of two, radix-4 passes with a
+// per-block twiddle table; 2: power of two >= 512, register radix-16 passes
+// in place (one buffer, blockDim = n / 16, twiddles from the global table)
+template <int MODE>
+__global__ void __launch_bounds__(MODE == 2 ? 256 : 512, MODE == 2 ? 3 : 1)
+    lines32_kernel(Plan P, const float2 *__restrict__ tw, Lines32 L) {
   extern __shared__ __align__(16) float2 sm32[];
+  constexpr bool POW2 = MODE == 1;
   const int n = P.n;
   float2 *a = sm32, *b = sm32 + n;
   if (POW2) {
@@ -249,16 +411,22 @@ __global__ void lines32_kernel(Plan P, const float2 *__restrict__ tw, Lines32 L)
   const i64 line = blockIdx.x;
   const i64 ib = line / L.in_rows, ir = line % L.in_rows;
   const i64 row = ib * L.in_rows_tot + ir + L.in_row_off;
+  // the line's input value at x
+  float inv = 0.0f, inv2 = 0.0f;
+  bool fold = false;
+  i64 row0 = 0;
   if (L.acc) {
     // deposit accumulator: value / scale with the ghost fold row1 -= row0
     // (the scales are powers of two, so the FP32 inverses are exact)
-    const float inv = 1.0f / (float)L.acc_scale[0];
-    const float inv2 = L.acc2 ? 1.0f / (float)L.acc2_scale[0] : 0.0f;
-    const bool fold = (ir + L.in_row_off) == 1;
-    const i64 row0 = ib * L.in_rows_tot;
-    const longlong2 *A1 = reinterpret_cast<const longlong2 *>(L.acc);
-    const longlong2 *A2 = reinterpret_cast<const longlong2 *>(L.acc2);
-    for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    inv = 1.0f / (float)L.acc_scale[0];
+    inv2 = L.acc2 ? 1.0f / (float)L.acc2_scale[0] : 0.0f;
+    fold = (ir + L.in_row_off) == 1;
+    row0 = ib * L.in_rows_tot;
+  }
+  auto load_elem = [&](int x) -> float2 {
+    if (L.acc) {
+      const longlong2 *A1 = reinterpret_cast<const longlong2 *>(L.acc);
+      const longlong2 *A2 = reinterpret_cast<const longlong2 *>(L.acc2);
       const i64 e = row * n + x;
       const longlong2 q = A1[e];
       float re = fix2f(q.x) * inv, im = fix2f(q.y) * inv;
@@ -278,28 +446,18 @@ __global__ void lines32_kernel(Plan P, const float2 *__restrict__ tw, Lines32 L)
           im -= fix2f(q2.y) * inv2;
         }
       }
-      a[x] = make_float2(re, im);
+      return make_float2(re, im);
     }
-  } else {
-    const float2 *src = L.in + row * (i64)n;
-    for (int x = threadIdx.x; x < n; x += blockDim.x) {
-      float2 v = src[x];
-      if (L.pre_shift) v = fmul(v, L.pre_shift[x]);
-      a[x] = v;
-    }
-  }
-  float2 *res = POW2 ? run32p(P, a, b, tw, L.sign) : run32(P, a, b, tw, L.sign);
-  if (L.filt_mode >= 0) {
-    for (int x = threadIdx.x; x < L.nxfilt; x += blockDim.x)
-      if (L.filt_mode == 0 || L.filt_mode == 2) res[x] = fscl(res[x], L.filtr[x]);
-    __syncthreads();
-    for (int x = threadIdx.x; x < L.nxfilt; x += blockDim.x)
-      if (L.filt_mode == 1 || L.filt_mode == 2) res[n - 1 - x] = fscl(res[n - 1 - x], L.filtr[x]);
-    float2 *other = (res == a) ? b : a;
-    res = POW2 ? run32p(P, res, other, tw, -1) : run32(P, res, other, tw, -1);
-  }
+    float2 v = L.in[row * (i64)n + x];
+    if (L.pre_shift) v = fmul(v, L.pre_shift[x]);
+    return v;
+  };
+  if constexpr (MODE != 2)
+    for (int x = threadIdx.x; x < n; x += blockDim.x) a[x] = load_elem(x);
+  // the line's output at x (the inverse shift of the filter path, the
+  // eb_correction scale and ghost row)
   const i64 ob = line / L.out_rows, orow = line % L.out_rows;
-  float2 *dst = L.out + (ob * L.out_rows_tot + orow + L.out_row_off) * (i64)n;
+  float2 *dstl = L.out + (ob * L.out_rows_tot + orow + L.out_row_off) * (i64)n;
   float fac = 1.0f, sg = 1.0f;
   if (L.eb_mode) {
     const int m = (int)(ob % L.nm);
@@ -308,37 +466,74 @@ __global__ void lines32_kernel(Plan P, const float2 *__restrict__ tw, Lines32 L)
   }
   const bool ghost = L.eb_mode && orow == 0;
   float2 *gdst = L.out + (ob * L.out_rows_tot) * (i64)n;
-  for (int x = threadIdx.x; x < n; x += blockDim.x) {
-    float2 v = res[x];
+  auto store_elem = [&](int x, float2 v) {
     if (L.filt_mode >= 0) {
       float2 s = L.pre_shift[x];
       float inv = 1.0f / ((float)n * (s.x * s.x + s.y * s.y));
       v = fmul(v, make_float2(s.x * inv, -s.y * inv));
     }
     if (L.eb_mode) v = fscl(v, fac);
-    dst[x] = v;
+    dstl[x] = v;
     if (ghost) gdst[x] = fscl(v, sg);
+  };
+  auto edge_filter = [&](float2 *res) {
+    for (int x = threadIdx.x; x < L.nxfilt; x += blockDim.x)
+      if (L.filt_mode == 0 || L.filt_mode == 2) res[x] = fscl(res[x], L.filtr[x]);
+    __syncthreads();
+    for (int x = threadIdx.x; x < L.nxfilt; x += blockDim.x)
+      if (L.filt_mode == 1 || L.filt_mode == 2) res[n - 1 - x] = fscl(res[n - 1 - x], L.filtr[x]);
+  };
+  if constexpr (MODE == 2) {
+    auto buf_src = [a](int i) { return a[i]; };
+    auto buf_dst = [a](int i, float2 v) { a[i] = v; };
+    run16(a, n, P.log2n, tw, L.sign, load_elem, buf_dst);
+    if (L.filt_mode >= 0) {
+      edge_filter(a);
+      run16(a, n, P.log2n, tw, -1, buf_src, buf_dst);
+    }
+    for (int x = threadIdx.x; x < n; x += blockDim.x) store_elem(x, a[x]);
+    return;
   }
+  float2 *res = POW2 ? run32p(P, a, b, tw, L.sign) : run32(P, a, b, tw, L.sign);
+  if (L.filt_mode >= 0) {
+    edge_filter(res);
+    float2 *other = (res == a) ? b : a;
+    res = POW2 ? run32p(P, res, other, tw, -1) : run32(P, res, other, tw, -1);
+  }
+  for (int x = threadIdx.x; x < n; x += blockDim.x) store_elem(x, res[x]);
 }
 
-int lines32_launch(const Lines32 &L, int n, i64 nlines, float2 *tw, cudaStream_t st) {
+// tw: room for n twiddles exp(-2 pi i t / n); already filled (shift32_kernel)
+// when tw_ready
+int lines32_launch(const Lines32 &L, int n, i64 nlines, float2 *tw, cudaStream_t st,
+                   bool tw_ready = false) {
   Plan P;
   if (!make_plan(n, &P)) {
     set_error("split fft: unsupported length %d", n);
     return CHM_ERR_RANGE;
   }
   if (nlines <= 0) return CHM_OK;
-  const int threads = n >= 1024 ? 512 : (n >= 256 ? 256 : 128);
-  if (P.log2n >= 0) {
-    // twiddle table built per block in shared memory
+  if (P.log2n >= 9) {
+    if (!tw_ready) {
+      twiddle32_kernel<<<(n + 255) / 256, 256, 0, st>>>(tw, n);
+      chm::count_launch();
+    }
+    const size_t smem = (size_t)n * sizeof(float2);
+    cudaFuncSetAttribute(lines32_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    lines32_kernel<2><<<(unsigned)nlines, n / 16, smem, st>>>(P, tw, L);
+  } else if (P.log2n >= 0) {
+    // the twiddle table is built per block in shared memory
+    const int threads = n >= 256 ? 256 : 128;
     const size_t smem = 3 * (size_t)n * sizeof(float2);
-    cudaFuncSetAttribute(lines32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    lines32_kernel<true><<<(unsigned)nlines, threads, smem, st>>>(P, nullptr, L);
+    cudaFuncSetAttribute(lines32_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    lines32_kernel<1><<<(unsigned)nlines, threads, smem, st>>>(P, nullptr, L);
   } else {
-    twiddle32_kernel<<<(n + 255) / 256, 256, 0, st>>>(tw, n); chm::count_launch();
+    const int threads = n >= 1024 ? 512 : (n >= 256 ? 256 : 128);
+    twiddle32_kernel<<<(n + 255) / 256, 256, 0, st>>>(tw, n);
+    chm::count_launch();
     const size_t smem = 2 * (size_t)n * sizeof(float2);
-    cudaFuncSetAttribute(lines32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    lines32_kernel<false><<<(unsigned)nlines, threads, smem, st>>>(P, tw, L);
+    cudaFuncSetAttribute(lines32_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    lines32_kernel<0><<<(unsigned)nlines, threads, smem, st>>>(P, tw, L);
   }
   chm::count_launch();
   CHM_CHECK_LAUNCH();
@@ -569,7 +764,7 @@ int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, con
     set_error("sp_fb_in_acc: workspace exhausted");
     return CHM_ERR_WS;
   }
-  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, -1, nx); chm::count_launch();
+  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, -1, nx, tw); chm::count_launch();
   Lines32 L{};
   L.acc = reinterpret_cast<const long long *>(acc);
   L.acc_scale = scale;
@@ -583,7 +778,7 @@ int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, con
   L.nm = (int)nm;
   L.sign = -1;
   L.filt_mode = -1;
-  int rc = lines32_launch(L, (int)nx, nrr * nm * ncomp, tw, st);
+  int rc = lines32_launch(L, (int)nx, nrr * nm * ncomp, tw, st, true);
   if (rc) return rc;
   const TcMatrices In = tc_matrices(reinterpret_cast<const chm_sp_ops *>(In_ops));
   Batch32 b{};  // every mode and component in one launch
@@ -610,7 +805,7 @@ int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double 
     set_error("sp_fb_eb_out: workspace exhausted");
     return CHM_ERR_WS;
   }
-  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx); chm::count_launch();
+  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx, tw); chm::count_launch();
   const TcMatrices Out = tc_matrices(reinterpret_cast<const chm_sp_ops *>(Out_ops));
   Batch32 b{};  // every mode and component in one launch
   for (i64 m = 0; m < nm; ++m)
@@ -632,7 +827,7 @@ int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double 
   L.eb_mode = 1;
   L.sign = +1;
   L.filt_mode = -1;
-  return lines32_launch(L, (int)nx, nrr * nm * 6, tw, st);
+  return lines32_launch(L, (int)nx, nrr * nm * 6, tw, st, true);
 }
 
 // fb_filtr on complex64 planes (fb_io.f90:230-308)
@@ -646,7 +841,7 @@ int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx, const float *
   Ws W{(char *)ws, ws_bytes};
   float2 *tw = W.take<float2>(nx);
   float2 *shift = W.take<float2>(nx);
-  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx); chm::count_launch();
+  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx, tw); chm::count_launch();
   Lines32 L{};
   L.in = reinterpret_cast<const float2 *>(vec_c64);
   L.out = reinterpret_cast<float2 *>(vec_c64);
@@ -657,7 +852,7 @@ int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx, const float *
   L.filt_mode = modefilt;
   L.filtr = filtr;
   L.nxfilt = (int)nxfilt;
-  return lines32_launch(L, (int)nx, nkr * nm * ncomp, tw, st);
+  return lines32_launch(L, (int)nx, nkr * nm * ncomp, tw, st, true);
 }
 
 }  // extern "C"
