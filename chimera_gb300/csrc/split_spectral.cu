@@ -587,13 +587,15 @@ struct GradArgs {
   int up_to;
 };
 
+// The elementwise kernels below take one x line per block: blockIdx.x = kr,
+// blockIdx.y = mode, threads along x (no index division per element).
 __global__ void grad32_kernel(GradArgs A) {
   const i64 plane = A.nx * A.nk;
-  const i64 n = plane * A.nm;
-  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x) {
-    const i64 x = t % A.nx;
-    const int m = (int)(t / plane);
-    const i64 e = t - (i64)m * plane;
+  const int m = blockIdx.y;
+  const i64 line = A.nx * (i64)blockIdx.x;
+  for (int x = threadIdx.x; x < A.nx; x += blockDim.x) {
+    const i64 e = line + x;
+    const i64 t = e + (i64)m * plane;
     const float2 s = A.scl[e + plane * (m + A.off)];
     const float2 lo = A.lo[t];
     const float2 up = (m < A.up_to) ? A.up[t] : make_float2(0.f, 0.f);
@@ -633,11 +635,11 @@ struct DivArgs {
 
 __global__ void div32_kernel(DivArgs A) {
   const i64 plane = A.nx * A.nk;
-  const i64 n = plane * A.ns;
-  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x) {
-    const i64 x = t % A.nx;
-    const int ms = (int)(t / plane);
-    const i64 e = t - (i64)ms * plane;
+  const int ms = blockIdx.y;
+  const i64 line = A.nx * (i64)blockIdx.x;
+  for (int x = threadIdx.x; x < A.nx; x += blockDim.x) {
+    const i64 e = line + x;
+    const i64 t = e + (i64)ms * plane;
     float2 r = make_float2(0.f, 0.f);
     if (ms < A.nm) r = fscl(fmi(A.v[e + plane * ms]), A.kx[x]);
     if (A.lo_ok[ms]) r = fadd(r, fsub(fmi(A.lo3[t]), A.lo2[t]));
@@ -659,10 +661,10 @@ struct RotArgs {
 
 __global__ void rot32_kernel(RotArgs A) {
   const i64 plane = A.nx * A.nk;
-  const i64 n = plane * A.nm;
-  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < n; t += (i64)gridDim.x * blockDim.x) {
-    const i64 x = t % A.nx;
-    const int m = (int)(t / plane);
+  const int m = blockIdx.y;
+  const i64 line = A.nx * (i64)blockIdx.x;
+  for (int x = threadIdx.x; x < A.nx; x += blockDim.x) {
+    const i64 t = line + x + (i64)m * plane;
     const float kxv = A.kx[x];
     const float2 v2 = A.v[t + A.cs], v3 = A.v[t + 2 * A.cs];
     const bool hi = m < A.nm - 1;
@@ -927,7 +929,7 @@ int chm_sp_fb_grad(void *out_c64, const void *scl_c64, const void *Dp_ops, const
   A.out = reinterpret_cast<float2 *>(out_c64);
   A.cs = plane * nm;
   A.up_to = (int)nm - 1;
-  grad32_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A); chm::count_launch();
+  grad32_kernel<<<dim3((unsigned)nkr, (unsigned)nm), 256, 0, F.st>>>(A); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
@@ -981,7 +983,7 @@ int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, cons
     D.up3 = up[2];
     D.kx = kx;
     D.scl = scl;
-    div32_kernel<<<grid_for(plane * ns, 256), 256, 0, F.st>>>(D); chm::count_launch();
+    div32_kernel<<<dim3((unsigned)nkr, (unsigned)ns), 256, 0, F.st>>>(D); chm::count_launch();
     // gradient of the nm + 1 scalar modes back onto nm modes, fused with the
     // J update; the m = -1 neighbour of mode 0 is scalar mode 1 reflected
     // (zero with a single mode)
@@ -1016,7 +1018,7 @@ int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, cons
     A.pf = pf;
     A.dt_inv = dt_inv;
     A.up_to = (int)nm;
-    grad32_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A); chm::count_launch();
+    grad32_kernel<<<dim3((unsigned)nkr, (unsigned)nm), 256, 0, F.st>>>(A); chm::count_launch();
   }
   CHM_CHECK_LAUNCH();
   return CHM_OK;
@@ -1059,7 +1061,7 @@ int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf, const void *Dp
   A.kx = kx;
   A.pf = pf;
   A.out = reinterpret_cast<float2 *>(B_c64);
-  rot32_kernel<<<grid_for(plane * nm, 256), 256, 0, F.st>>>(A); chm::count_launch();
+  rot32_kernel<<<dim3((unsigned)nkr, (unsigned)nm), 256, 0, F.st>>>(A); chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }
