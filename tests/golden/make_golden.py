@@ -152,6 +152,30 @@ def fel_run(Solver, Specie, ChimeraRun, orc, nsteps):
     return solver, beam, init
 
 
+def static_run(Solver, Specie, ChimeraRun, nsteps):
+    """A beam-only space-charge run with the StaticKick solver, shaped as the
+    reference's space-charge demo (Staged co-moving frame, Xchunked)."""
+    np.random.seed(1006)
+    size = 1.0
+    xmin, xmax, lrg, nx, nr = -7.0 * size, 7.0 * size, 12.0 * size, 56, 24
+    dx, dr, dt = (xmax - xmin) / nx, lrg / nr, 1.0
+    solver = Solver({"Grid": (xmin, xmax, lrg, dx, dr), "TimeStep": dt, "MaxAzimuthMode": 1,
+                     "Features": ("StaticKick",), "Xchunked": (4, 6)})
+    beam = Specie({"Grid": (xmin, xmax, lrg, dx, dr), "TimeStep": dt, "Charge": -1., "Mass": 1.,
+                   "Density": 1e-3, "FixedCell": (2, 2, 4), "MomentaMeans": (50.0, 0., 0.),
+                   "Xchunked": (4, 6)})
+    fu = lambda x, y, z: np.exp(-0.5 * (x ** 2 + y ** 2 + z ** 2) / size ** 2)  # noqa: E731
+    beam.add_particles(*beam.gen_parts(Domain=(-3.5 * size, 3.5 * size, 0.0, 3.5 * size),
+                                       ProfileFunc=fu))
+    init = {k: v.copy() for k, v in beam.Data.items()}
+    run = ChimeraRun({"Solvers": (solver,), "Particles": (beam,),
+                      "MovingFrames": ({"TimeStep": dt, "Steps": 1,
+                                        "Features": ("NoSorting", "Staged")},)})
+    for i in range(nsteps):
+        run.make_step(i)
+    return solver, beam, init
+
+
 def main():
     Solver, Specie, ChimeraRun, orc = import_reference()
     out = {}
@@ -193,6 +217,15 @@ def main():
     for k in ("coords", "momenta", "EB"):
         out[f"fel/beam/{k}"] = beam.Data[k]
     out["fel/leftX"] = np.array(solver.Args["leftX"])
+    # 5) beam-only StaticKick run (space-charge demo shape)
+    solver, beam, init = static_run(Solver, Specie, ChimeraRun, 4)
+    for k in ("coords", "momenta", "weights"):
+        out[f"static/init/{k}"] = init[k]
+    for k in ("EG_fb", "J_fb", "EB"):
+        out[f"static/solver/{k}"] = solver.Data[k]
+    for k in ("coords", "coords_halfstep", "momenta"):
+        out[f"static/beam/{k}"] = beam.Data[k]
+    out["static/leftX"] = np.array(solver.Args["leftX"])
     path = os.path.join(HERE, "reference_golden.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB, {len(out)} arrays)")

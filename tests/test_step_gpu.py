@@ -92,3 +92,46 @@ def test_fel_steps_match_reference(cuda, golden):
         assert rel_l2(solver.Data[k].cpu().numpy(), golden[f"fel/solver/{k}"]) < TOL, k
     for k in ("coords", "momenta", "EB"):
         assert rel_l2(beam.Data[k].cpu().numpy(), golden[f"fel/beam/{k}"]) < TOL, k
+
+
+def test_static_kick_steps_match_reference(cuda, golden):
+    """Beam-only StaticKick run (the space-charge demo's solver: Poisson
+    correction, static field solve and field drift at the beam's mean
+    momentum, Staged frame, Xchunked deposits) against the reference's step
+    loop."""
+    from chimera_gb300 import ChimeraRun, Solver, Specie
+    from chimera_gb300.messages import msg
+    msg.quiet = True
+    np.random.seed(1006)
+    size = 1.0
+    xmin, xmax, lrg, nx, nr = -7.0 * size, 7.0 * size, 12.0 * size, 56, 24
+    dx, dr, dt = (xmax - xmin) / nx, lrg / nr, 1.0
+    solver = Solver({"Grid": (xmin, xmax, lrg, dx, dr), "TimeStep": dt, "MaxAzimuthMode": 1,
+                     "Features": ("StaticKick",), "Xchunked": (4, 6)})
+    beam = Specie({"Grid": (xmin, xmax, lrg, dx, dr), "TimeStep": dt, "Charge": -1., "Mass": 1.,
+                   "Density": 1e-3, "FixedCell": (2, 2, 4), "MomentaMeans": (50.0, 0., 0.),
+                   "Xchunked": (4, 6)})
+    fu = lambda x, y, z: np.exp(-0.5 * (x ** 2 + y ** 2 + z ** 2) / size ** 2)  # noqa: E731
+    beam.add_particles(*beam.gen_parts(Domain=(-3.5 * size, 3.5 * size, 0.0, 3.5 * size),
+                                       ProfileFunc=fu))
+    for k in ("coords", "momenta", "weights"):
+        assert rel_l2(beam.Data[k].cpu().numpy(), golden[f"static/init/{k}"]) < 1e-14, k
+    run = ChimeraRun({"Solvers": (solver,), "Particles": (beam,),
+                      "MovingFrames": ({"TimeStep": dt, "Steps": 1,
+                                        "Features": ("NoSorting", "Staged")},)})
+    for i in range(4):
+        run.make_step(i)
+    assert abs(solver.Args["leftX"] - float(golden["static/leftX"])) < 1e-12
+    for k in ("EG_fb", "J_fb", "EB"):
+        assert rel_l2(solver.Data[k].cpu().numpy(), golden[f"static/solver/{k}"]) < TOL, k
+    # the x-chunk sort orders particles inside a chunk differently (the
+    # reference's numpy quicksort vs a stable sort): compare particle sets,
+    # each run's particles in the order of their positions
+    got_c, ref_c = beam.Data["coords"].cpu().numpy(), golden["static/beam/coords"]
+    assert got_c.shape == ref_c.shape
+    key = lambda c: np.lexsort(np.round(c, 9)[::-1])  # noqa: E731  (round-off ties)
+    og, orf = key(got_c), key(ref_c)
+    for k in ("coords", "coords_halfstep", "momenta"):
+        got = beam.Data[k].cpu().numpy()[:, og]
+        ref = golden[f"static/beam/{k}"][:, orf]
+        assert rel_l2(got, ref) < TOL, k
