@@ -50,6 +50,10 @@ constexpr int kRhoBoxBytes = 16 * 1024;
 constexpr int kRhoMinBlocks = 8;
 constexpr int kRhoGroup = 1;  // particles loaded ahead per lane
 
+// deposit cells dropped outside a block box while inside the grid (corrupt
+// positions); read and reset by chm_sp_deposit_dropped
+__device__ unsigned int g_dep_dropped;
+
 // physical slot of particle i and the particle of a slot
 __host__ __device__ __forceinline__ i64 phys_of(i64 i) {
   return (i & ~(i64)(kTile - 1)) | ((i & (kRunLen - 1)) << 5) | ((i >> 4) & (kTileRuns - 1));
@@ -541,25 +545,13 @@ __device__ __forceinline__ void acc_flush(CellAcc<NM, NC> &c, int plane0, const 
       }
     return;
   }
-  // guard: a cell with nodes outside the block box (the plan bounds every
-  // deposit location of finite particles) adds its in-grid node values
-  // through box_put
-#pragma unroll
-  for (int l = 0; l < NC; ++l)
-#pragma unroll
-    for (int p = 0; p < 2 * NM - 1; ++p) {
-      const int m = (p + 1) >> 1;
-      const int im = (p > 0 && (p & 1) == 0) ? 1 : 0;
-      const long long plane = plane0 + m + (long long)G.nm * l;
-#pragma unroll
-      for (int nd = 0; nd < 4; ++nd) {
-        const int v = __float2int_rn(c.v[l][p][nd]);
-        const int j = nd >> 1, k = nd & 1;
-        const int gx = c.cx + k;
-        if (v == 0 || gx < 0 || gx >= G.nx) continue;
-        box_put(B, plane, c.cr + j, gx, im, v);
-      }
-    }
+  // a cell with nodes outside the block box: the plan bounds the deposit
+  // cells of every finite particle with |v| < c inside the box (and the box
+  // reaches one node past each x end of the grid), so such a cell has all its
+  // nodes past the grid's x ends (dropped, as the reference drops them), or
+  // comes from a corrupt position.  Its values are dropped; the second case
+  // is counted (chm_sp_deposit_dropped).
+  if (c.cx >= -1 && c.cx < G.nx && c.cr >= 0 && c.cr + 1 < G.nr) atomicAdd(&g_dep_dropped, 1u);
 }
 
 // val: the particle's values already multiplied by the block scale
@@ -1250,6 +1242,13 @@ int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, f
   chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
+}
+
+int64_t chm_sp_deposit_dropped(void) {
+  unsigned int v = 0, z = 0;
+  cudaMemcpyFromSymbol(&v, g_dep_dropped, sizeof(v));
+  cudaMemcpyToSymbol(g_dep_dropped, &z, sizeof(z));
+  return (int64_t)v;
 }
 
 int chm_sp_gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,

@@ -522,6 +522,11 @@ int chm_sp_gemm(float *C, const float *A, const chm_sp_ops *ops, int64_t mode,
                 int64_t M, int engine, void *ws, int64_t ws_bytes, void *stream);
 /* Nonzero if a tensor-core GEMM CTA hit a wait limit since load. */
 int chm_sp_umma_status(void);
+/* Deposit cells of the split-form run kernels that fell outside their
+ * block's box while inside the grid since the last call (then reset).  The
+ * block plan bounds every finite particle's deposit cells, so this is 0
+ * unless positions are corrupt (NaN or moved faster than c). */
+int64_t chm_sp_deposit_dropped(void);
 
 /* ------------------------------------------------------------------------
  * Diagnostics (moduls/diagnostics.py, f90/utils.f90): device reductions of

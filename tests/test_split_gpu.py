@@ -44,6 +44,7 @@ def test_tensor_core_gemm_matches_fp64(mods, M, K, N):
         err = rel_l2(Ct.cpu().numpy(), ref)
         assert err < 2e-6, (engine, err)
     assert _lib.load().chm_sp_umma_status() == 0
+    assert _lib.load().chm_sp_deposit_dropped() == 0  # every deposit cell inside its box
 
 
 def _ops(golden, name):
@@ -185,6 +186,7 @@ def test_split_steps_track_fp64_form(mods, nsteps, max_mode):
     a0_sp = s_sp.Data["EB"][:, 1, 0, 2].real.max().item()
     assert abs(a0_sp - a0_ref) < 0.01 * abs(a0_ref)
     assert _lib.load().chm_sp_umma_status() == 0
+    assert _lib.load().chm_sp_deposit_dropped() == 0  # every deposit cell inside its box
 
 
 def _sp_particles(torch, n, nx, nr, dr, seed, runs=True):
@@ -368,6 +370,7 @@ def test_split_window_with_injection_tracks_fp64_form(mods):
     err = rel_l2(run.solver.Data["EG_fb"].cpu().numpy(), ref.Solvers[0].Data["EG_fb"].cpu().numpy())
     assert err < 1e-4, err
     assert _lib.load().chm_sp_umma_status() == 0
+    assert _lib.load().chm_sp_deposit_dropped() == 0  # every deposit cell inside its box
 
 
 @pytest.mark.parametrize("nm,runs", [(2, True), (2, False), (1, True)])
@@ -421,3 +424,4 @@ def test_batched_instances_match_single_runs(mods):
                 assert torch.equal(Pa.buf[k][: Pa.n], Pb.buf[k][: Pb.n]), k
     assert batch.num_moving == sum(r.num_moving for r in batch.runs) > 0
     assert _lib.load().chm_sp_umma_status() == 0
+    assert _lib.load().chm_sp_deposit_dropped() == 0  # every deposit cell inside its box
