@@ -78,7 +78,9 @@ __global__ void twiddle32_kernel(float2 *tw, int n) {
 }
 
 // exp(sign i kx leftX) evaluated in FP64 (the argument can be large), stored
-// FP32; with tw, also the FFT twiddles exp(-2 pi i t / nx) (as twiddle32_kernel)
+// FP32; with tw, also the FFT twiddles exp(-2 pi i t / nx) (as twiddle32_kernel).
+// Launched with warp-sized blocks: the FP64 trigonometry spreads over as
+// many SMs as there are warps of work.
 __global__ void shift32_kernel(float2 *shift, const double *kx, double leftX, int sign, i64 nx,
                                float2 *tw) {
   for (i64 x = blockIdx.x * (i64)blockDim.x + threadIdx.x; x < nx; x += (i64)gridDim.x * blockDim.x) {
@@ -766,7 +768,7 @@ int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, con
     set_error("sp_fb_in_acc: workspace exhausted");
     return CHM_ERR_WS;
   }
-  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, -1, nx, tw); chm::count_launch();
+  shift32_kernel<<<grid_for(nx, 32), 32, 0, st>>>(shift, kx, leftX, -1, nx, tw); chm::count_launch();
   Lines32 L{};
   L.acc = reinterpret_cast<const long long *>(acc);
   L.acc_scale = scale;
@@ -807,7 +809,7 @@ int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double 
     set_error("sp_fb_eb_out: workspace exhausted");
     return CHM_ERR_WS;
   }
-  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx, tw); chm::count_launch();
+  shift32_kernel<<<grid_for(nx, 32), 32, 0, st>>>(shift, kx, leftX, +1, nx, tw); chm::count_launch();
   const TcMatrices Out = tc_matrices(reinterpret_cast<const chm_sp_ops *>(Out_ops));
   Batch32 b{};  // every mode and component in one launch
   for (i64 m = 0; m < nm; ++m)
@@ -843,7 +845,7 @@ int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx, const float *
   Ws W{(char *)ws, ws_bytes};
   float2 *tw = W.take<float2>(nx);
   float2 *shift = W.take<float2>(nx);
-  shift32_kernel<<<grid_for(nx, 256), 256, 0, st>>>(shift, kx, leftX, +1, nx, tw); chm::count_launch();
+  shift32_kernel<<<grid_for(nx, 32), 32, 0, st>>>(shift, kx, leftX, +1, nx, tw); chm::count_launch();
   Lines32 L{};
   L.in = reinterpret_cast<const float2 *>(vec_c64);
   L.out = reinterpret_cast<float2 *>(vec_c64);
