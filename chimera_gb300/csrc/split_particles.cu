@@ -1388,3 +1388,67 @@ int chm_sp_compact(const int32_t *ix, const float *fx, const float *y, const flo
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Plasma generation on the device (particle_tools.f90:84-128 genparts with
+// the fixed per-cell pattern, species.py:132-215 gen_parts): the host draws
+// the random numbers (the reference's RNG stream) and evaluates the pattern
+// positions and profile weights on the few distinct values; the kernel
+// builds every particle.
+// ---------------------------------------------------------------------------
+namespace {
+
+// candidate (ir, ix, ip) -> output particle row_base[ir] + ix row_count[ir]
+// + row_rank[ir, ip] (row_rank < 0: the pattern point is dropped, r <= 0)
+__global__ void gen_fixed_cell_kernel(double *__restrict__ coords, i64 cstride,
+                                      double *__restrict__ weights, const double *__restrict__ cx,
+                                      const double *__restrict__ cr, const double *__restrict__ wfac,
+                                      const double2 *__restrict__ packo,
+                                      const double *__restrict__ rand_o, i64 ldr,
+                                      const i64 *__restrict__ row_base,
+                                      const int *__restrict__ row_rank,
+                                      const int *__restrict__ row_count, i64 nxc, i64 nrc, i64 npc) {
+  const i64 ncand = nrc * nxc * npc;
+  for (i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x; t < ncand;
+       t += (i64)gridDim.x * blockDim.x) {
+    const i64 ip = t % npc, ix = (t / npc) % nxc, ir = t / (npc * nxc);
+    const int rank = row_rank[ir + nrc * ip];
+    if (rank < 0) continue;
+    const i64 o = row_base[ir] + ix * row_count[ir] + rank;
+    // angle 2 pi u of the cell; the pattern point packo rotated by it
+    // (complex product in the order (a c - b d, a d + b c), no contraction)
+    const double ang = __dmul_rn(6.283185307179586, rand_o[ix + ldr * ir]);
+    double s, c;
+    sincos(ang, &s, &c);
+    const double2 po = packo[ip];
+    const double ore = __dsub_rn(__dmul_rn(po.x, c), __dmul_rn(po.y, s));
+    const double oim = __dadd_rn(__dmul_rn(po.x, s), __dmul_rn(po.y, c));
+    const double r = cr[ir + nrc * ip];
+    coords[o] = cx[ix + nxc * ip];
+    coords[o + cstride] = __dmul_rn(r, oim);
+    coords[o + 2 * cstride] = __dmul_rn(r, ore);
+    weights[o] = __dmul_rn(r, wfac[ix + nxc * ip]);
+  }
+}
+
+}  // namespace
+
+extern "C" int chm_gen_fixed_cell(double *coords, int64_t cstride, double *weights,
+                                  const double *cx, const double *cr, const double *wfac,
+                                  const double *packo, const double *rand_o, int64_t ldr,
+                                  const int64_t *row_base, const int32_t *row_rank,
+                                  const int32_t *row_count, int64_t nxc, int64_t nrc, int64_t npc,
+                                  void *stream) {
+  CHM_REQUIRE(nxc >= 0 && nrc >= 0 && npc > 0 && ldr >= nxc, "gen_fixed_cell: bad dims");
+  if (nxc == 0 || nrc == 0) return CHM_OK;
+  CHM_REQUIRE(coords && weights && cx && cr && wfac && packo && rand_o && row_base && row_rank &&
+                  row_count,
+              "gen_fixed_cell: null pointer");
+  const i64 ncand = nrc * nxc * npc;
+  gen_fixed_cell_kernel<<<grid_for(ncand, 256), 256, 0, as_stream(stream)>>>(
+      coords, cstride, weights, cx, cr, wfac, reinterpret_cast<const double2 *>(packo), rand_o, ldr,
+      row_base, row_rank, row_count, nxc, nrc, npc);
+  count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}

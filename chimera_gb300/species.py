@@ -16,6 +16,7 @@ import numpy as np
 import torch
 from scipy.constants import c, e, epsilon_0, m_e
 
+from . import _lib
 from . import fimera as chimera
 
 _VEC = ("coords", "coords_halfstep", "momenta", "coords_init")
@@ -213,6 +214,85 @@ class Specie:
         mom = np.vstack([A["MomentaMeans"][k] + A["MomentaSpreads"][k] * rnd[k] for k in range(3)])
         return [np.asfortranarray(coords[0:3], dtype="d"), np.asfortranarray(mom, dtype="d"),
                 np.asfortranarray(coords[-1], dtype="d")]
+
+    def gen_parts_device(self, Xsteps=None, ProfileFunc=None):
+        """gen_parts(Xsteps=..., ProfileFunc=...) with the particles built on
+        the device (chm_gen_fixed_cell): the same random numbers are drawn on
+        the host in the same order (rand_o, then the momenta), the pattern
+        positions and the profile are evaluated on the host on the few
+        distinct values, and only rand_o (and non-constant momenta) go to
+        the device.  Returns device tensors [coords (3,Np), momenta (3,Np),
+        weights (Np,)] in gen_parts' particle order.  Only for FixedCell
+        species and a profile of x alone (or none); otherwise the host
+        generator's arrays are uploaded."""
+        A = self.Args
+        nargs = (len(inspect.signature(ProfileFunc).parameters)
+                 if ProfileFunc is not None else 0)
+        if "FixedCell" not in A or nargs > 1 or Xsteps is None:
+            c, p, w = self.gen_parts(Xsteps=Xsteps, ProfileFunc=ProfileFunc)
+            up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(self.device)  # noqa: E731
+            return [up(c), up(p), up(w)]
+        Xgrid = A["Xgrid"][-2 * Xsteps:-Xsteps]
+        Rgrid = A["Rgrid"]
+        nxg, nrg = Xgrid.shape[0], Rgrid.shape[0]
+        rand_o = np.random.rand(nxg, nrg).astype("d", order="F")  # the RNG stream of gen_parts
+        packx, packr, packo = A["Pax"]
+        npc = packx.shape[0]
+        dev = self.device
+        if nxg < 2 or nrg < 2:
+            num = 0
+        else:
+            # the pattern positions and the profile on their distinct values,
+            # with the host generator's expressions (fixed_cell_particles)
+            dr_2 = 0.5 * (Rgrid[1] - Rgrid[0])
+            rs = Rgrid + dr_2
+            cx = Xgrid[:-1][:, None] + (Xgrid[1:] - Xgrid[:-1])[:, None] * packx[None, :]
+            cr = rs[:-1][:, None] + (rs[1:] - rs[:-1])[:, None] * packr[None, :]
+            keep = cr > 0                                      # (nrc, npc)
+            count = keep.sum(1).astype(np.int32)               # kept points per r row
+            rank = np.where(keep, np.cumsum(keep, 1) - 1, -1).astype(np.int32)
+            nxc = nxg - 1
+            base = np.concatenate([[0], np.cumsum(count.astype(np.int64) * nxc)[:-1]])
+            num = int(count.sum()) * nxc
+        if "FlatSpectrum" in A["Features"]:
+            rnd = 2 * np.random.rand(3, num) - 1.0
+        else:
+            rnd = np.random.randn(3, num)
+        coords = torch.empty((3, num), dtype=torch.float64, device=dev)
+        weights = torch.empty(num, dtype=torch.float64, device=dev)
+        spreads = A.get("MomentaSpreads", (0.0, 0.0, 0.0))
+        if all(float(sp_) == 0.0 for sp_ in spreads):
+            momenta = torch.empty((3, num), dtype=torch.float64, device=dev)
+            for k in range(3):  # means + 0 * rnd
+                momenta[k].fill_(float(A["MomentaMeans"][k]))
+        else:
+            mom = np.vstack([A["MomentaMeans"][k] + spreads[k] * rnd[k] for k in range(3)])
+            momenta = torch.from_numpy(np.ascontiguousarray(mom)).pin_memory().to(
+                dev, non_blocking=True)
+            chimera.io_bytes["h2d"] += mom.nbytes
+        if num == 0:
+            return [coords, momenta, weights]
+        # the particles' (x, r) pattern positions in output order, for the
+        # caller's particle ordering (host values; no device read)
+        keep3 = np.broadcast_to(keep[:, None, :], (nrg - 1, nxc, npc))
+        self.last_gen_xr = (np.broadcast_to(cx[None, :, :], keep3.shape)[keep3],
+                            np.broadcast_to(cr[:, None, :], keep3.shape)[keep3])
+        prof = ProfileFunc(cx) if ProfileFunc is not None else 1.0
+        wfac = np.asfortranarray(np.broadcast_to(A["wght0"] * prof, cx.shape), dtype=np.float64)
+
+        def up(a, dt=None):
+            a = np.asfortranarray(a) if dt is None else np.asfortranarray(a, dtype=dt)
+            chimera.io_bytes["h2d"] += a.nbytes
+            return torch.from_numpy(a.ravel(order="F").copy()).pin_memory().to(dev, non_blocking=True)
+
+        t = [up(np.asfortranarray(cx)), up(np.asfortranarray(cr)), up(wfac),
+             up(packo.astype(np.complex128)), up(rand_o), up(base, np.int64), up(rank, np.int32),
+             up(count, np.int32)]
+        _lib.call("chm_gen_fixed_cell", coords.data_ptr(), num, weights.data_ptr(), t[0].data_ptr(),
+                  t[1].data_ptr(), t[2].data_ptr(), t[3].data_ptr(), t[4].data_ptr(), nxg,
+                  t[5].data_ptr(), t[6].data_ptr(), t[7].data_ptr(), nxc, nrg - 1, npc,
+                  torch.cuda.current_stream(dev).cuda_stream)
+        return [coords, momenta, weights]
 
     def gen_randcell(self, Xgrid, Rgrid):
         """Random in-cell particles (species.py:429-471), same RNG sequence."""

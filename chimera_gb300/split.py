@@ -91,7 +91,9 @@ def cell_order(coords, X0: float, dx: float, dr: float, patch: int = 4):
     P = int(patch)
     px, lx = gx // P, gx % P
     pr, lr = gr // P, gr % P
-    npx = int(px.max()) + 1
+    # patch columns: the exact count on the host; on the device a fixed bound
+    # (the order is the same, and no device-to-host read stalls the stream)
+    npx = int(px.max()) + 1 if lib is np else 1 << 20
     px = lib.where(pr % 2 == 1, npx - 1 - px, px)  # serpentine patch rows
     lx = lib.where(lr % 2 == 1, P - 1 - lx, lx)    # serpentine rows in a patch
     key = (((pr * npx + px) * P + lr) * P + lx) * 2 + half
@@ -278,6 +280,7 @@ class SplitRun:
         # the background density is deposited on window moves
         # (chimera_main.py:277-284); it starts empty, as the reference's
         self.have_bg = False
+        self._inject_order = {}  # particle order of injected batches, per shape
 
     # ------------------------------------------------------------------
     def _moving(self):
@@ -459,18 +462,35 @@ class SplitRun:
         xsteps = int(wind["shiftX"] / wind["TimeStep"]) + 1
         idx = {id(s): i for i, s in enumerate(fp.Particles)}
         def ordered(spc, parts):
-            o = cell_order(parts[0], self.X0, self.dx, self.dr)
+            # device-generated batches: the order from the host pattern
+            # positions (the same for every batch of a shape, as cell_order
+            # keys x relative to the batch's first cell), cached on the device
+            xr = getattr(spc, "last_gen_xr", None)
+            n = int(parts[0].shape[1])
+            if xr is not None and xr[0].shape[0] == n:
+                key = (id(spc), n, xsteps)
+                o = self._inject_order.get(key)
+                if o is None:
+                    x, r = xr
+                    o = torch.from_numpy(cell_order(np.vstack([x, r, 0.0 * r]), self.X0, self.dx,
+                                                    self.dr)).to(self.device)
+                    self._inject_order[key] = o
+                spc.last_gen_xr = None
+            else:
+                o = cell_order(parts[0], self.X0, self.dx, self.dr)
             return [parts[0][:, o], parts[1][:, o], parts[2][o]]
 
+        # the particles are built on the device (Specie.gen_parts_device: the
+        # host draws the reference's random numbers, the kernel the rest)
         if "IonsOnTop" in wind["Features"]:
             s1, s2 = fp.Particles[:2]
-            parts = ordered(s1, s1.gen_parts(Xsteps=xsteps, ProfileFunc=wind["AddPlasma"]))
+            parts = ordered(s1, s1.gen_parts_device(Xsteps=xsteps, ProfileFunc=wind["AddPlasma"]))
             self.parts[idx[id(s1)]].append_f64(*parts, self.X0, self.dx)
             parts[-1] = parts[-1] * -1
             self.parts[idx[id(s2)]].append_f64(*parts, self.X0, self.dx)
         else:
             for s in fp.Particles:
-                parts = ordered(s, s.gen_parts(Xsteps=xsteps, ProfileFunc=wind["AddPlasma"]))
+                parts = ordered(s, s.gen_parts_device(Xsteps=xsteps, ProfileFunc=wind["AddPlasma"]))
                 self.parts[idx[id(s)]].append_f64(*parts, self.X0, self.dx)
         self._scales_valid = False
 

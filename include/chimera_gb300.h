@@ -528,6 +528,19 @@ int chm_sp_umma_status(void);
  * unless positions are corrupt (NaN or moved faster than c). */
 int64_t chm_sp_deposit_dropped(void);
 
+/* Plasma generation (particle_tools.f90:84-128 genparts, fixed per-cell
+ * pattern; species.py:132-215): particle (ir, ix, ip) of the nrc x nxc cells
+ * and npc pattern points is written at row_base[ir] + ix row_count[ir] +
+ * row_rank[ir + nrc ip] (row_rank < 0: dropped) with x = cx[ix + nxc ip],
+ * (y, z) = cr[ir + nrc ip] (Im, Re) of packo[ip] e^{2 pi i rand_o[ix + ldr ir]},
+ * weight = cr[ir + nrc ip] wfac[ix + nxc ip].  coords: (3, n) with component
+ * stride cstride, part stride 1; packo complex128 (npc). */
+int chm_gen_fixed_cell(double *coords, int64_t cstride, double *weights, const double *cx,
+                       const double *cr, const double *wfac, const double *packo,
+                       const double *rand_o, int64_t ldr, const int64_t *row_base,
+                       const int32_t *row_rank, const int32_t *row_count, int64_t nxc, int64_t nrc,
+                       int64_t npc, void *stream);
+
 /* ------------------------------------------------------------------------
  * Diagnostics (moduls/diagnostics.py, f90/utils.f90): device reductions of
  * the FP64 grids, each in a fixed summation order (bitwise reproducible).

@@ -425,3 +425,30 @@ def test_batched_instances_match_single_runs(mods):
     assert batch.num_moving == sum(r.num_moving for r in batch.runs) > 0
     assert _lib.load().chm_sp_umma_status() == 0
     assert _lib.load().chm_sp_deposit_dropped() == 0  # every deposit cell inside its box
+
+
+@pytest.mark.parametrize("spreads,with_profile", [((0.0, 0.0, 0.0), True), ((0.1, 0.05, 0.05), False)])
+def test_device_plasma_generation_matches_host(mods, spreads, with_profile):
+    """Specie.gen_parts_device (chm_gen_fixed_cell) against the host
+    generator gen_parts (particle_tools.f90:84-128, species.py:132-215) from
+    the same RNG state: the same random numbers consumed, x, weights and
+    momenta bitwise, y and z to the device's FP64 cos/sin."""
+    torch, _lib, fm, split = mods
+    from chimera_gb300 import Specie
+    from chimera_gb300.messages import msg
+    msg.quiet = True
+    prof = (lambda x: np.interp(x, [-3.0, -1.0, 9.0], [0.0, 1.0, 1.0])) if with_profile else None
+    sp = Specie({"Grid": (-3.0, 1.0, 2.0, 0.1, 0.25), "TimeStep": 0.1, "Density": 0.01,
+                 "FixedCell": (2, 2, 3), "MomentaSpreads": spreads})
+    np.random.seed(11)
+    hc, hp, hw = sp.gen_parts(Xsteps=3, ProfileFunc=prof)
+    st_h = np.random.get_state()
+    np.random.seed(11)
+    dc, dp, dw = (t.cpu().numpy() for t in sp.gen_parts_device(Xsteps=3, ProfileFunc=prof))
+    st_d = np.random.get_state()
+    assert np.array_equal(st_h[1], st_d[1]) and st_h[2] == st_d[2]  # same RNG stream
+    assert dc.shape == hc.shape and dc.shape[1] > 0
+    assert np.array_equal(dc[0], hc[0])
+    assert np.abs(dc[1:] - hc[1:]).max() <= 1e-14 * np.abs(hc[1:]).max()
+    assert np.array_equal(dw, hw)
+    assert np.array_equal(dp, hp)
