@@ -10,11 +10,16 @@ synthetic (seeded numpy), of this shape.
 
   value  particle*steps/s of ChimeraRun.make_step with all state resident on
          the GPU (moving species only, as the metric counts them)
-  e2e    the same through the public API with the window's host-generated
-         plasma injection (AddPlasma + AbsorbLayer + IonsOnTop, as in the
-         reference's lpa-testrun.py) copied host->device every step and the
-         laser a0 read back every step
-  roofline / cpu_baseline / clocks
+  e2e    the same through the public API with the window's plasma
+         injection (AddPlasma + AbsorbLayer + IonsOnTop, as in the
+         reference's lpa-testrun.py): the generator's host data copied
+         host->device every step, and the laser a0 read back every step
+  roofline  the dominant stage's algorithmic bytes (or FLOPs) over its live
+         CUDA-event time against MEASURED_PEAKS.json, with the ncu DRAM
+         traffic of the deposit kernels scaled by particle count
+  cpu_baseline  the oracle's C/OpenMP step on all host cores, a bounded
+         sample of the e2e workload
+  clocks  nvidia-smi SM clock and throttle reasons sampled through the run
 
 --impl reference runs the oracle's CPU step driver (the reference's step
 loop over the C restatement of its Fortran kernels, OpenMP on every host
@@ -460,9 +465,11 @@ def run_gb300(args):
             d2h += 8 / args.steps  # the live-count read
         e2e = {"value": world * ps2 / t_e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "laser_a0_last": a0,
-               "what": "ChimeraRun.make_step with AddPlasma+AbsorbLayer window (host-generated "
-                       "plasma copied H2D each step) and a laser-a0 read back each step "
-                       "(asynchronous copy to pinned memory, consumed one step later)"}
+               "what": "make_step with AddPlasma+AbsorbLayer window (the injected plasma's "
+                       "host data copied H2D each step: random numbers and pattern tables in "
+                       "the split form, the generated particles in the FP64 form) and a "
+                       "laser-a0 read back each step (asynchronous copy to pinned memory, "
+                       "consumed one step later)"}
         del run2, solver2, el2
 
     cpu = None
