@@ -156,7 +156,7 @@ struct UmmaArgs {
   int M, N, Np, K, Kp;
   const float2 *shift;
   int epi;
-  int fac_bulk;  // factor block staged in shared memory for the epilogue
+  int fac_staged;  // factor block staged in shared memory for the epilogue
   uint32_t tmem_cols;
 };
 
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
       mbar_arrive(&afull[s]);
       if (kb + 1 < nkb) load(kb + 1);
     }
-  } else if (EPI == TC_EPI_SHIFT_FAC && A.fac_bulk && threadIdx.x > kProducers) {
+  } else if (EPI == TC_EPI_SHIFT_FAC && A.fac_staged && threadIdx.x > kProducers) {
     // idle lanes of the MMA warp: start the tile's factor block (read by
     // the epilogue) towards L2, two 128-byte lines per column
     const int xr0p = mt * (TM / 2);
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
   const int nxr = TM / 2, xr0 = mt * (TM / 2);
   const float *facs = reinterpret_cast<const float *>(smem);
   bool fac_smem = false;
-  if (EPI == TC_EPI_SHIFT_FAC && use && A.fac_bulk) {
+  if (EPI == TC_EPI_SHIFT_FAC && use && A.fac_staged) {
     const int rows = min(nxr, (A.M >> 1) - xr0);  // a multiple of 4 (host check)
     const int nq = nxr / 4, total = nq * A.N;       // float4 per column, in the block
     float4 *dst = reinterpret_cast<float4 *>(smem);
@@ -493,10 +493,10 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
   ua.tmem_cols = cols;
   // the staged factor block is read with 16-byte loads: M/2 a multiple of 4
   // and 16-byte aligned factor planes; it (TM/2 x Np FP32) fits in the stages
-  ua.fac_bulk = (epi == TC_EPI_SHIFT_FAC && (M / 2) % 4 == 0 &&
+  ua.fac_staged = (epi == TC_EPI_SHIFT_FAC && (M / 2) % 4 == 0 &&
                  (size_t)(TM / 2) * Np * 4 <= (size_t)STAGES * (kABytes + 3 * b_term)) ? 1 : 0;
-  for (int i = 0; i < count && ua.fac_bulk; ++i)
-    if (!p[i].fac || (reinterpret_cast<uintptr_t>(p[i].fac) & 15)) ua.fac_bulk = 0;
+  for (int i = 0; i < count && ua.fac_staged; ++i)
+    if (!p[i].fac || (reinterpret_cast<uintptr_t>(p[i].fac) & 15)) ua.fac_staged = 0;
   for (int c0 = 0; c0 < count; c0 += kMaxBatch) {
     const int cnt = count - c0 < kMaxBatch ? count - c0 : kMaxBatch;
     UmmaBatch ub;

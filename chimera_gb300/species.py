@@ -242,17 +242,8 @@ class Specie:
         if nxg < 2 or nrg < 2:
             num = 0
         else:
-            # the pattern positions and the profile on their distinct values,
-            # with the host generator's expressions (fixed_cell_particles)
-            dr_2 = 0.5 * (Rgrid[1] - Rgrid[0])
-            rs = Rgrid + dr_2
-            cx = Xgrid[:-1][:, None] + (Xgrid[1:] - Xgrid[:-1])[:, None] * packx[None, :]
-            cr = rs[:-1][:, None] + (rs[1:] - rs[:-1])[:, None] * packr[None, :]
-            keep = cr > 0                                      # (nrc, npc)
-            count = keep.sum(1).astype(np.int32)               # kept points per r row
-            rank = np.where(keep, np.cumsum(keep, 1) - 1, -1).astype(np.int32)
+            cx, cr, keep, count, rank, base = fixed_cell_tables(Xgrid, Rgrid, packx, packr)
             nxc = nxg - 1
-            base = np.concatenate([[0], np.cumsum(count.astype(np.int64) * nxc)[:-1]])
             num = int(count.sum()) * nxc
         if "FlatSpectrum" in A["Features"]:
             rnd = 2 * np.random.rand(3, num) - 1.0
@@ -409,6 +400,22 @@ class Specie:
         D["coords"][0] -= x_foc * (D["momenta"][0] - pzmean) / pzmean / gg ** 2
         D["coords"][1:3] -= D["momenta"][1:3] / pzmean * x_foc
         D["coords_halfstep"].copy_(D["coords"])
+
+
+def fixed_cell_tables(Xgrid, Rgrid, packx, packr):
+    """The tables of the device generator (chm_gen_fixed_cell): the pattern
+    x positions cx (nx-1, npc) and radii cr (nr-1, npc) with the expressions
+    of fixed_cell_particles, the kept points (cr > 0), their count and rank
+    per r row, and each r row's first output index (rows of (nx-1) cells)."""
+    dr_2 = 0.5 * (Rgrid[1] - Rgrid[0])
+    rs = Rgrid + dr_2
+    cx = Xgrid[:-1][:, None] + (Xgrid[1:] - Xgrid[:-1])[:, None] * packx[None, :]
+    cr = rs[:-1][:, None] + (rs[1:] - rs[:-1])[:, None] * packr[None, :]
+    keep = cr > 0
+    count = keep.sum(1).astype(np.int32)
+    rank = np.where(keep, np.cumsum(keep, 1) - 1, -1).astype(np.int32)
+    base = np.concatenate([[0], np.cumsum(count.astype(np.int64) * (Xgrid.shape[0] - 1))[:-1]])
+    return cx, cr, keep, count, rank, base
 
 
 def fixed_cell_particles(Xgrid, Rgrid, rand_o, packx, packr, packo):

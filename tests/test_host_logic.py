@@ -180,3 +180,40 @@ def test_snapshot_keys_and_restore_host(tmp_path):
     assert np.array_equal(sol2.Args["kx"], sol.Args["kx"]) and sol2.Args["kx"].flags.f_contiguous
     assert sp2.store.n == 3 and torch.equal(sp2.Data["weights"], sp.Data["weights"])
     assert torch.equal(sp2.chunks, sp.chunks) and sp2.Args["name"] == "el"
+
+
+def test_fixed_cell_tables_reproduce_the_host_generator():
+    """The device generator's tables (species.fixed_cell_tables) and its
+    index rule (particle (ir, ix, ip) at base[ir] + ix count[ir] +
+    rank[ir, ip]), restated in numpy with the kernel's arithmetic, give the
+    host generator's particles (fixed_cell_particles), including a grid
+    whose first row drops pattern points (r <= 0)."""
+    from chimera_gb300.species import fixed_cell_particles, fixed_cell_tables
+    rng = np.random.default_rng(4)
+    fc = (2, 3, 4)
+    px, pr, po = np.mgrid[1:fc[0]:fc[0] * 1j, 1:fc[1]:fc[1] * 1j, 1:fc[2]:fc[2] * 1j]
+    packx = (px.ravel() - 0.5) / fc[0]
+    packr = (pr.ravel() - 0.5) / fc[1]
+    packo = np.exp(2.j * np.pi * (po.ravel() - 1) / fc[2])
+    for Rgrid in (0.3 * (np.arange(7) - 0.5), 0.3 * (np.arange(7) - 1.2)):
+        Xgrid = -1.0 + 0.1 * np.arange(5)
+        rand_o = np.asfortranarray(rng.random((5, 7)))
+        ref = fixed_cell_particles(Xgrid, Rgrid, rand_o, packx, packr, packo)
+        cx, cr, keep, count, rank, base = fixed_cell_tables(Xgrid, Rgrid, packx, packr)
+        nxc, nrc, npc = cx.shape[0], cr.shape[0], packx.shape[0]
+        num = int(count.sum()) * nxc
+        assert num == ref.shape[1]
+        out = np.zeros((4, num))
+        for ir in range(nrc):
+            for ix in range(nxc):
+                for ip in range(npc):
+                    if rank[ir, ip] < 0:
+                        continue
+                    o = base[ir] + ix * count[ir] + rank[ir, ip]
+                    ang = 2.0 * np.pi * rand_o[ix, ir]
+                    c, s = np.cos(ang), np.sin(ang)
+                    ore = packo[ip].real * c - packo[ip].imag * s
+                    oim = packo[ip].real * s + packo[ip].imag * c
+                    out[:, o] = (cx[ix, ip], cr[ir, ip] * oim, cr[ir, ip] * ore, cr[ir, ip])
+        assert np.array_equal(out[0], ref[0]) and np.array_equal(out[3], ref[3])
+        assert np.abs(out[1:3] - ref[1:3]).max() <= 1e-15 * np.abs(ref[1:3]).max()
