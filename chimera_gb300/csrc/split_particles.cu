@@ -627,6 +627,52 @@ __global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
   cj.live = false;
   cr.live = false;
   const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - (i64)first));
+  if (!Pl.use_box) {
+    // a block whose nodes do not fit a box (a wide footprint): each particle
+    // straight to the global accumulators at the global scales, apart from
+    // the main loop so that the loop does not carry this path's registers
+    for (int j = 0; j < cnt; ++j) {
+      const Idx p = tile + (Idx)j * kTileRuns + lane;
+      const float w = A.P.w[p];
+      Pushed u;
+      if (PUSH || DJ) {
+        u = push_one(A, p);
+      } else {
+        u.ixh = u.ixn = A.P.ix[p];
+        u.fxh = u.fxn = A.P.fx[p];
+        u.yh = u.yn = A.P.y[p];
+        u.zh = u.zn = A.P.z[p];
+      }
+      if (PUSH) {
+        A.P.ix[p] = u.ixn;
+        A.P.fx[p] = u.fxn;
+        A.P.y[p] = u.yn;
+        A.P.z[p] = u.zn;
+      }
+      if (w == 0.0f) continue;
+      if (DJ && u.moving) {
+        const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, A.G);
+        const float vs[3] = {u.vj[0] * Pl.sJ, u.vj[1] * Pl.sJ, u.vj[2] * Pl.sJ};
+        deposit_at(L, vs, 3, 0, A.G, [&](int plane, int r, int x, float re, float im) {
+          const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
+          const long long qr = f2ll(re), qi = f2ll(im);
+          if (qr) atomicAdd(&A.accJ[2 * e], (unsigned long long)qr);
+          if (qi) atomicAdd(&A.accJ[2 * e + 1], (unsigned long long)qi);
+        });
+      }
+      if (DR) {
+        const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, A.G);
+        const float ws[1] = {w * Pl.sR};
+        deposit_at(L, ws, 1, 0, A.G, [&](int plane, int r, int x, float re, float im) {
+          const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
+          const long long qr = f2ll(re), qi = f2ll(im);
+          if (qr) atomicAdd(&A.accR[2 * e], (unsigned long long)qr);
+          if (qi) atomicAdd(&A.accR[2 * e + 1], (unsigned long long)qi);
+        });
+      }
+    }
+    return;
+  }
   // software pipeline: the next group of particles is loaded before this
   // group's results are stored (the stores could alias the loads
   // otherwise); G particles per group, more for the lighter rho-only pass
@@ -683,39 +729,18 @@ __global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
       if (w == 0.0f) continue;
       if (DJ && u.moving) {  // grid_deps.f90:42: no current from particles at rest
         const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, A.G);
-        if (Pl.use_box) {
-          const float vs[3] = {u.vj[0] * Pl.lJ, u.vj[1] * Pl.lJ, u.vj[2] * Pl.lJ};
-          acc_add(cj, L, vs, 0, A.G, geo);
-        } else {
-          const float vs[3] = {u.vj[0] * Pl.sJ, u.vj[1] * Pl.sJ, u.vj[2] * Pl.sJ};
-          deposit_at(L, vs, 3, 0, A.G, [&](int plane, int r, int x, float re, float im) {
-            const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
-            const long long qr = f2ll(re), qi = f2ll(im);
-            if (qr) atomicAdd(&A.accJ[2 * e], (unsigned long long)qr);
-            if (qi) atomicAdd(&A.accJ[2 * e + 1], (unsigned long long)qi);
-          });
-        }
+        const float vs[3] = {u.vj[0] * Pl.lJ, u.vj[1] * Pl.lJ, u.vj[2] * Pl.lJ};
+        acc_add(cj, L, vs, 0, A.G, geo);
       }
       if (DR) {
         const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, A.G);
-        if (Pl.use_box) {
-          const float ws[1] = {w * Pl.lR};
-          acc_add(cr, L, ws, 3 * NM, A.G, geo);
-        } else {
-          const float ws[1] = {w * Pl.sR};
-          deposit_at(L, ws, 1, 0, A.G, [&](int plane, int r, int x, float re, float im) {
-            const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
-            const long long qr = f2ll(re), qi = f2ll(im);
-            if (qr) atomicAdd(&A.accR[2 * e], (unsigned long long)qr);
-            if (qi) atomicAdd(&A.accR[2 * e + 1], (unsigned long long)qi);
-          });
-        }
+        const float ws[1] = {w * Pl.lR};
+        acc_add(cr, L, ws, 3 * NM, A.G, geo);
       }
     }
 #pragma unroll
     for (int g = 0; g < G; ++g) cur[g] = nxt[g];
   }
-  if (!Pl.use_box) return;
   if (DJ) acc_flush(cj, 0, A.G, geo);
   if (DR) acc_flush(cr, 3 * NM, A.G, geo);
   __syncthreads();
