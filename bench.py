@@ -261,17 +261,19 @@ def stage_roofline(form, prof, nprof, n_e, n_i, peaks, peak_kind):
     return top
 
 
-def dist_setup():
+def dist_setup(backend=None):
+    """One process per GPU (torchrun env): replicas, so the process group
+    only carries the barrier and the max-over-ranks timing (NCCL on GPUs,
+    gloo without one)."""
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    else:
-        torch.cuda.set_device(local)
+        dist.init_process_group(backend or ("nccl" if torch.cuda.is_available() else "gloo"))
     return world, rank, local
 
 
@@ -286,7 +288,8 @@ def max_over_ranks(world, v):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
