@@ -1,6 +1,7 @@
 """Host-side logic of the drop-in API against golden vectors produced by the
 reference's own Python (tests/golden/make_golden.py): the FP64 operator build
 and particle generation.  No kernel is called (tensors live on the CPU)."""
+import os
 from copy import deepcopy
 
 import numpy as np
@@ -217,3 +218,49 @@ def test_fixed_cell_tables_reproduce_the_host_generator():
                     out[:, o] = (cx[ix, ip], cr[ir, ip] * oim, cr[ir, ip] * ore, cr[ir, ip])
         assert np.array_equal(out[0], ref[0]) and np.array_equal(out[3], ref[3])
         assert np.abs(out[1:3] - ref[1:3]).max() <= 1e-15 * np.abs(ref[1:3]).max()
+
+
+def test_diagnostics_dispatch_and_files_host(tmp_path, monkeypatch):
+    """Diagnostics (diagnostics.py:27-149) host logic with stand-in solver /
+    species objects and the device reductions replaced by the oracle's numpy
+    restatements: Step selection, Return data, file names and contents."""
+    torch = pytest.importorskip("torch")
+    from oracle import oracle as orc
+    from chimera_gb300 import diagnostics as dg
+
+    monkeypatch.setattr(dg.chimera, "em_energy",
+                        lambda eg, ef: torch.from_numpy(orc.em_energy(eg.numpy(), np.asarray(ef))))
+    monkeypatch.setattr(dg.chimera, "power_profile",
+                        lambda d, rg, fac: torch.from_numpy(orc.power_profile(d.numpy(), rg, fac)))
+    monkeypatch.setattr(dg.chimera, "fb_vec_out", lambda v, leftX, kx, Out: v.clone())
+    monkeypatch.setattr(dg.chimera, "to_device", lambda a, dtype, dev=None: torch.as_tensor(a))
+    rng = np.random.default_rng(2)
+
+    class Sol:
+        Args = {"EnergyFact": rng.uniform(size=(8, 5, 2)), "RgridFull": np.linspace(-0.1, 1, 5),
+                "dr": 0.25, "leftX": 0.0, "FBoutFull": (None, None), "MaxAzimuthMode": 1}
+        Data = {"EG_fb": torch.from_numpy(rng.standard_normal((8, 5, 2, 6))
+                                          + 1j * rng.standard_normal((8, 5, 2, 6))),
+                "EB": torch.zeros((8, 6, 2, 6), dtype=torch.complex128)}
+
+    class Run:
+        Solvers = (Sol(),)
+        Particles = ()
+
+    sol = Run.Solvers[0]
+    D = dg.Diagnostics(Run(), ({"Type": "EnergyEM", "Step": 3}, {"Type": "Power", "Step": 2},
+                               {"Type": "Fields", "Step": 2}), out_folder=str(tmp_path / "d"))
+    D.do_diags(1)
+    assert sorted(os.listdir(tmp_path / "d")) == []
+    D.do_diags(2)
+    assert sorted(os.listdir(tmp_path / "d")) == ["ee_0_0000002.npy", "pwrX_0.txt"]
+    D.do_diags(6)
+    assert sorted(os.listdir(tmp_path / "d")) == ["ee_0_0000002.npy", "ee_0_0000006.npy",
+                                                  "nrg_0.txt", "pwrX_0.txt"]
+    e = orc.em_energy(sol.Data["EG_fb"].numpy(), sol.Args["EnergyFact"])
+    e = np.r_[e[8 // 2 + 1:], e[:8 // 2 + 1]]
+    assert np.allclose(np.loadtxt(tmp_path / "d" / "nrg_0.txt"), e, rtol=1e-14, atol=0)
+    p = np.loadtxt(tmp_path / "d" / "pwrX_0.txt")
+    assert p.shape == (2, 8)  # appended at steps 2 and 6
+    (ret,) = D.nrg_out({"Type": "EnergyEM", "Step": 1, "Features": {"Return": True}})
+    assert np.allclose(ret, e, rtol=1e-14, atol=0)
