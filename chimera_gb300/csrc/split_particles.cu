@@ -675,7 +675,8 @@ __global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
   }
   // software pipeline: the next group of particles is loaded before this
   // group's results are stored (the stores could alias the loads
-  // otherwise); G particles per group, more for the lighter rho-only pass
+  // otherwise); G particles per group (kRhoGroup for the rho-only pass:
+  // one measured best at its 64-register budget)
   constexpr int G = DJ ? 1 : kRhoGroup;
   struct Part {
     int ix;
