@@ -3,7 +3,7 @@
  * implementation of CHIMERA's per-step particle-in-cell hot path.
  *
  * Every entry point replaces one subroutine of the reference's f2py module
- * `chimera.moduls.fimera` (built from f90/*.f90, Makefile:6-11,32-34); the
+ * `chimera.moduls.fimera` (built from the f90 sources, Makefile:6-11,32-34); the
  * comment above each declaration cites the Fortran routine it replaces.  The
  * argument meaning follows the Fortran; the dimensions that f2py hides are
  * explicit.
