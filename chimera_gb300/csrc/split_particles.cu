@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A
 }
 
 // ----------------------------------------------------------------------
-// Run form of push + deposit for nm = 1, 2: lane r of a warp walks the 16
+// Run form of push + deposit for nm = 1..3: lane r of a warp walks the 16
 // particles of run r of its tile, sums their node values (already at the
 // block's fixed-point scale) in FP32 registers while the deposit cell stays
 // the same, and adds the sums, rounded to the block quantum, to the block
@@ -602,8 +602,13 @@ __device__ __forceinline__ void acc_add(CellAcc<NM, NC> &c, const Loc &L, const 
   }
 }
 
+// resident blocks per SM the register budget is set for: three modes carry
+// 5 instead of 3 mode parts per accumulated component
+template <int NM, bool DJ>
+constexpr int dep_min_blocks() { return DJ ? (NM >= 3 ? 3 : 4) : (NM >= 3 ? 6 : kRhoMinBlocks); }
+
 template <int NM, bool PUSH, bool DJ, bool DR>
-__global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
+__global__ void __launch_bounds__(kDepThreads, dep_min_blocks<NM, DJ>())
     push_deposit_run_kernel(PushDepArgs A) {
   extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
@@ -946,12 +951,12 @@ __global__ void __launch_bounds__(256) gather_push_kernel(GatherArgs A, i64 nphy
   }
 }
 
-// Run form of gather + Boris for nm = 1, 2: lane r walks run r of its tile
+// Run form of gather + Boris for nm = 1..3: lane r walks run r of its tile
 // and keeps the fields of the 4 nodes of the current cell in registers
 // (mode 0: real parts; modes >= 1: complex), reloading them only when the
 // cell changes.  Same interpolation and rotation as gather_push_kernel.
 template <int NM>
-__global__ void __launch_bounds__(kDepThreads, 4) gather_push_run_kernel(GatherArgs A) {
+__global__ void __launch_bounds__(kDepThreads, NM >= 3 ? 3 : 4) gather_push_run_kernel(GatherArgs A) {
   const SpGrid &G = A.G;
   const i64 plane = (i64)G.nx * G.nr;
   const int lane = threadIdx.x & 31;
@@ -1219,11 +1224,16 @@ int chm_sp_weight_scale(double *scale2, const float *w, int64_t n, void *ws, int
   return CHM_OK;
 }
 
-int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *py,
-                        float *pz, float *w, int64_t n, int win_k, float win_f, float dx_inv,
-                        float dr_inv, float dt, int nx, int nr, int nm, int push,
-                        uint64_t *accJ, const double *scaleJ, uint64_t *accR,
-                        const double *scaleR, void *stream) {
+}  // extern "C"
+
+namespace {
+
+// push + deposit with the cell-run kernels for nm <= 3 (the per-particle
+// kernel for more modes), or the per-particle kernel for every nm (generic)
+int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,
+                 float *w, int64_t n, int win_k, float win_f, float dx_inv, float dr_inv, float dt,
+                 int nx, int nr, int nm, int push, uint64_t *accJ, const double *scaleJ,
+                 uint64_t *accR, const double *scaleR, void *stream, bool generic) {
   CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && nm >= 1 && nm <= 8, "sp_push_deposit: bad dims");
   if (n == 0) return CHM_OK;
   CHM_REQUIRE(ix && fx && y && z && px && py && pz && w, "sp_push_deposit: null particle array");
@@ -1243,22 +1253,21 @@ int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, f
   A.scaleR = scaleR;
   const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
   cudaStream_t st = as_stream(stream);
-  // CHIMERA_GB300_DEPOSIT=generic selects the per-particle kernels of the
-  // deposit and the gather for every nm
-  const char *var = getenv("CHIMERA_GB300_DEPOSIT");
-  const bool generic = var && strcmp(var, "generic") == 0;
-  // run kernels for nm 1, 2 and the three uses: moving species (push, J,
+  // run kernels for nm 1..3 and the three uses: moving species (push, J,
   // rho), moving species without the fused rho, still species (rho)
   void (*kern)(PushDepArgs) = nullptr;
-  if (!generic && (nm == 1 || nm == 2)) {
+  if (!generic && nm >= 1 && nm <= 3) {
     const int mode = (push ? 4 : 0) | (A.dep_j ? 2 : 0) | (A.dep_rho ? 1 : 0);
     if (mode == 7) kern = nm == 1 ? push_deposit_run_kernel<1, true, true, true>
-                                  : push_deposit_run_kernel<2, true, true, true>;
+                        : nm == 2 ? push_deposit_run_kernel<2, true, true, true>
+                                  : push_deposit_run_kernel<3, true, true, true>;
     if (mode == 6) kern = nm == 1 ? push_deposit_run_kernel<1, true, true, false>
-                                  : push_deposit_run_kernel<2, true, true, false>;
+                        : nm == 2 ? push_deposit_run_kernel<2, true, true, false>
+                                  : push_deposit_run_kernel<3, true, true, false>;
     if (mode == 1 && n < (i64)INT32_MAX - kDepBlock)
       kern = nm == 1 ? push_deposit_run_kernel<1, false, false, true>
-                     : push_deposit_run_kernel<2, false, false, true>;
+           : nm == 2 ? push_deposit_run_kernel<2, false, false, true>
+                     : push_deposit_run_kernel<3, false, false, true>;
   }
   int box_bytes = kSpBoxBytes;
   if (!kern) kern = push_deposit_kernel;
@@ -1268,6 +1277,57 @@ int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, f
   chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
+}
+
+int gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,
+                float *w, int64_t n, int win_k, float win_f, float dr_inv, const void *eb_c64, int nx,
+                int nr, int nm, float dtq, void *stream, bool generic) {
+  CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && nm >= 1, "sp_gather_push: bad dims");
+  if (n == 0) return CHM_OK;
+  CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && eb_c64, "sp_gather_push: null pointer");
+  GatherArgs A;
+  A.P = SpParts{ix, fx, y, z, px, py, pz, w, n};
+  A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
+  A.eb = reinterpret_cast<const float2 *>(eb_c64);
+  A.dtq = dtq;
+  cudaStream_t st = as_stream(stream);
+  if (!generic && nm >= 1 && nm <= 3) {
+    const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
+    if (nm == 1)
+      gather_push_run_kernel<1><<<blocks, kDepThreads, 0, st>>>(A);
+    else if (nm == 2)
+      gather_push_run_kernel<2><<<blocks, kDepThreads, 0, st>>>(A);
+    else
+      gather_push_run_kernel<3><<<blocks, kDepThreads, 0, st>>>(A);
+  } else {
+    const i64 nphys = tiles_of(n) * kTile;
+    gather_push_kernel<<<grid_for(nphys, 256, 16), 256, 0, st>>>(A, nphys);
+  }
+  chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *py,
+                        float *pz, float *w, int64_t n, int win_k, float win_f, float dx_inv,
+                        float dr_inv, float dt, int nx, int nr, int nm, int push,
+                        uint64_t *accJ, const double *scaleJ, uint64_t *accR,
+                        const double *scaleR, void *stream) {
+  return push_deposit(ix, fx, y, z, px, py, pz, w, n, win_k, win_f, dx_inv, dr_inv, dt, nx, nr, nm,
+                      push, accJ, scaleJ, accR, scaleR, stream, false);
+}
+
+int chm_sp_push_deposit_generic(int32_t *ix, float *fx, float *y, float *z, float *px, float *py,
+                                float *pz, float *w, int64_t n, int win_k, float win_f,
+                                float dx_inv, float dr_inv, float dt, int nx, int nr, int nm,
+                                int push, uint64_t *accJ, const double *scaleJ, uint64_t *accR,
+                                const double *scaleR, void *stream) {
+  return push_deposit(ix, fx, y, z, px, py, pz, w, n, win_k, win_f, dx_inv, dr_inv, dt, nx, nr, nm,
+                      push, accJ, scaleJ, accR, scaleR, stream, true);
 }
 
 int64_t chm_sp_deposit_dropped(void) {
@@ -1280,30 +1340,16 @@ int64_t chm_sp_deposit_dropped(void) {
 int chm_sp_gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,
                        float *w, int64_t n, int win_k, float win_f, float dr_inv,
                        const void *eb_c64, int nx, int nr, int nm, float dtq, void *stream) {
-  CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && nm >= 1, "sp_gather_push: bad dims");
-  if (n == 0) return CHM_OK;
-  CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && eb_c64, "sp_gather_push: null pointer");
-  GatherArgs A;
-  A.P = SpParts{ix, fx, y, z, px, py, pz, w, n};
-  A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
-  A.eb = reinterpret_cast<const float2 *>(eb_c64);
-  A.dtq = dtq;
-  const char *var = getenv("CHIMERA_GB300_DEPOSIT");
-  const bool generic = var && strcmp(var, "generic") == 0;
-  cudaStream_t st = as_stream(stream);
-  if (!generic && (nm == 1 || nm == 2)) {
-    const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
-    if (nm == 1)
-      gather_push_run_kernel<1><<<blocks, kDepThreads, 0, st>>>(A);
-    else
-      gather_push_run_kernel<2><<<blocks, kDepThreads, 0, st>>>(A);
-  } else {
-    const i64 nphys = tiles_of(n) * kTile;
-    gather_push_kernel<<<grid_for(nphys, 256, 16), 256, 0, st>>>(A, nphys);
-  }
-  chm::count_launch();
-  CHM_CHECK_LAUNCH();
-  return CHM_OK;
+  return gather_push(ix, fx, y, z, px, py, pz, w, n, win_k, win_f, dr_inv, eb_c64, nx, nr, nm, dtq,
+                     stream, false);
+}
+
+int chm_sp_gather_push_generic(int32_t *ix, float *fx, float *y, float *z, float *px, float *py,
+                               float *pz, float *w, int64_t n, int win_k, float win_f,
+                               float dr_inv, const void *eb_c64, int nx, int nr, int nm, float dtq,
+                               void *stream) {
+  return gather_push(ix, fx, y, z, px, py, pz, w, n, win_k, win_f, dr_inv, eb_c64, nx, nr, nm, dtq,
+                     stream, true);
 }
 
 int chm_sp_from_f64(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,

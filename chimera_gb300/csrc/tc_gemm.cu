@@ -97,9 +97,10 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // FP64 matrices -> FP32 copy and 3-term BF16 split.  The split terms are
-// stored per (mode, 32-wide K block) as the tensor-core operand tile: core
-// matrices of 8 rows (n) x 16 bytes (8 k values), ordered k-group fastest
-// (LBO = 128 B), then row group (SBO = 512 B).
+// stored per (mode, 32-wide K block) as the tensor-core operand tile of
+// Np = tc_np(N) columns: core matrices of 8 rows (n) x 16 bytes (8 k
+// values), ordered k-group fastest (LBO = 128 B), then row group (SBO =
+// 512 B), so the columns of one column tile form a contiguous run.
 __global__ void prepare_kernel(const double *__restrict__ mats, int K, int N, int nmodes, int Kp,
                                int Np, float *__restrict__ f32, __nv_bfloat16 *__restrict__ t0,
                                __nv_bfloat16 *__restrict__ t1, __nv_bfloat16 *__restrict__ t2) {
@@ -135,23 +136,13 @@ namespace chm {
 int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, const float2 *shift,
                    cudaStream_t st);
 
-static int g_engine = -1;
-
-static int engine() {
-  if (g_engine < 0) {
-    const char *e = getenv("CHIMERA_GB300_GEMM");
-    g_engine = (e && strcmp(e, "simt") == 0) ? 0 : 1;
-  }
-  return g_engine;
-}
-
-// engine_override: -1 the process default, 0 SIMT, 1 tensor cores
+// engine 1: tensor cores (every product of the split form); 0: the FP32 SIMT
+// kernel, reached only through chm_sp_gemm as the tests' accuracy reference
 static int launch(const TcProblem *p, int count, int M, int N, int K, int epi, const float2 *shift,
-                  cudaStream_t st, int engine_override) {
+                  cudaStream_t st, int engine) {
   if (count <= 0) return CHM_OK;
   count_gemm_flops((double)count * 2.0 * M * N * K);
-  const int eng = engine_override >= 0 ? engine_override : engine();
-  if (eng == 1) return tc_umma_launch(p, count, M, N, K, epi, shift, st);
+  if (engine == 1) return tc_umma_launch(p, count, M, N, K, epi, shift, st);
   for (int c0 = 0; c0 < count; c0 += kMaxProb) {
     Prob32 b{};
     b.count = count - c0 < kMaxProb ? count - c0 : kMaxProb;
@@ -172,13 +163,13 @@ static int launch(const TcProblem *p, int count, int M, int N, int K, int epi, c
 
 int tc_gemm_launch(const TcProblem *p, int count, int M, int N, int K, int epi, const float2 *shift,
                    cudaStream_t st) {
-  return launch(p, count, M, N, K, epi, shift, st, -1);
+  return launch(p, count, M, N, K, epi, shift, st, 1);
 }
 
 TcMatrices tc_matrices(const chm_sp_ops *ops) {
   TcMatrices T;
   memset(&T, 0, sizeof(T));
-  const i64 Kp = rup(ops->K, 32), Np = rup(ops->N, 16);
+  const i64 Kp = rup(ops->K, 32), Np = tc_np(ops->N);
   for (int m = 0; m < ops->nmodes && m < 16; ++m) {
     TcOperand &o = T.mode[m];
     o.K = ops->K;
@@ -195,7 +186,8 @@ TcMatrices tc_matrices(const chm_sp_ops *ops) {
 extern "C" {
 
 int64_t chm_sp_ops_bytes(int64_t K, int64_t N, int64_t nmodes) {
-  const i64 Kp = rup(K, 32), Np = rup(N, 16);
+  if (K <= 0 || N <= 0 || N > 65536 || nmodes <= 0) return 0;
+  const i64 Kp = rup(K, 32), Np = tc_np((int)N);
   return rup(4 * K * N * nmodes, 256) + 3 * rup(2 * Kp * Np * nmodes, 256);
 }
 
@@ -203,9 +195,9 @@ int chm_sp_prepare_ops(chm_sp_ops *ops, const double *mats, int64_t K, int64_t N
                        void *buf, int64_t buf_bytes, void *stream) {
   CHM_REQUIRE(ops && mats && buf && K > 0 && N > 0 && nmodes > 0 && nmodes <= 16,
               "sp_prepare_ops: bad args");
-  CHM_REQUIRE(N <= 256, "sp_prepare_ops: N must be <= 256");
+  CHM_REQUIRE(N <= 65536, "sp_prepare_ops: N must be <= 65536");
   CHM_REQUIRE(buf_bytes >= chm_sp_ops_bytes(K, N, nmodes), "sp_prepare_ops: buffer too small");
-  const i64 Kp = rup(K, 32), Np = rup(N, 16);
+  const i64 Kp = rup(K, 32), Np = tc_np((int)N);
   char *p = reinterpret_cast<char *>(buf);
   float *f32 = reinterpret_cast<float *>(p);
   p += rup(4 * K * N * nmodes, 256);

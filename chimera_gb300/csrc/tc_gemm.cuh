@@ -6,6 +6,17 @@
 
 namespace chm {
 
+// Column tiling of the tensor-core products: N is cut into tc_col_tiles(N)
+// tiles of tc_tile_cols(N) columns (a multiple of 16, at most 128), and the
+// prepared split terms hold tc_np(N) = tiles x columns per K block (the
+// columns past N are zero), so every tile reads a whole block.
+inline int tc_col_tiles(int N) { return ((N + 15) / 16 * 16 + 127) / 128; }
+inline int tc_tile_cols(int N) {
+  const int nt = tc_col_tiles(N), np = (N + 15) / 16 * 16;
+  return ((np + nt - 1) / nt + 15) / 16 * 16;
+}
+inline int tc_np(int N) { return tc_col_tiles(N) * tc_tile_cols(N); }
+
 // One mode's B operand: FP32 copy and the 3-term BF16 split
 // (b = b0 + b1 + b2 exactly to ~2^-24) in the tensor-core operand layout.
 struct TcOperand {

@@ -2,24 +2,35 @@
 //
 //   C(M, N) = A(M, K) * B(K, N),  A, C FP32 column-major, B a prepared
 //   operator mode; computed as sum_{i+j<=2} A_i B_j with A = A0+A1+A2 and
-//   B = B0+B1+B2 the 3-term BF16 splits, accumulated in FP32 in TMEM.
+//   B = B0+B1+B2 the 3-term BF16 splits.
 //
-// One CTA computes a TM-row tile of one problem of a batch, as NH 128-row
-// accumulators of up to 256 FP32 columns each in TMEM (NH = 1: 128-row
-// tiles, so that a batch of few products still spreads over the SMs):
-//   - warps 0..4NH-1 (one thread per row) load the FP32 A block of every 32-wide
-//     K step, split it into the three BF16 terms and store them into the
-//     stage in the tensor-core operand layout (K-major core matrices of
-//     8 rows x 16 bytes);
-//   - the next warp's lane 0 streams the prepared B terms of the step with
-//     bulk-copy TMA (cp.async.bulk, completion on an mbarrier) and issues the
-//     12 NH tcgen05.mma of the step (6 term pairs x 2 K halves x NH row
-//     halves), releasing the stage with tcgen05.commit;
-//   - the producer warps then read the accumulators (tcgen05.ld 32x32b) and
-//     apply the epilogue.
-// STAGES stages (3 with NH = 1: 72 KB each at N = 256) pipeline the K loop.
-// Every mbarrier wait has an iteration limit; on timeout the CTA records an
-// error, waits (bounded) for its own bulk copies, frees its TMEM and returns.
+// Accumulation.  The tensor core's FP32 accumulation is not round-to-nearest:
+// with all six term pairs summed into one TMEM accumulator the error grows
+// about linearly with the number of MMAs per accumulator (measured on GB300:
+// 4e-7 relative at K = 64, 2.3e-6 at K = 256, against 2e-7 for an emulated
+// round-to-nearest FP32 sum).  So:
+//   - the leading pair A0 B0 goes into one of two TMEM accumulators H0 / H1
+//     that take turns over chunks of kChunk K steps (32 K values each); the
+//     row threads drain a finished chunk into FP32 registers (one
+//     round-to-nearest add per chunk) while the tensor core fills the other;
+//   - the five correction pairs (2^-8 and smaller relative to the result)
+//     go into a third accumulator L over the whole K range; its error is
+//     scaled by the same 2^-8.
+//
+// One CTA computes a 128-row x TNC-column tile (TNC <= 128, a multiple of
+// 16) of one problem of a batch; grid = (row tiles, column tiles, problems):
+//   - warps 0..3 (one thread per row) load the FP32 A block of every 32-wide
+//     K step, split it into the three BF16 terms, store them into the stage
+//     in the tensor-core operand layout (K-major core matrices of 8 rows x 16
+//     bytes), drain the H chunks into their registers and write the tile;
+//   - warp 4's lane 0 streams the prepared B terms of the step with bulk-copy
+//     TMA (cp.async.bulk, completion on an mbarrier) and issues the 12
+//     tcgen05.mma of the step (6 term pairs x 2 K halves), releasing the
+//     stage with tcgen05.commit.
+// Every mbarrier wait has an iteration limit.  The pipeline waits use a limit
+// set from the host (chm_sp_set_umma_spin_limit, so that a test can make
+// them run out); on a timeout the CTA records an error, waits with the full
+// limit for its own bulk copies and MMAs, frees its TMEM and returns.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -29,24 +40,19 @@ using namespace chm;
 
 namespace {
 
-constexpr int TH = 128;                   // rows per accumulator (UMMA M)
-constexpr int KB = 32;                    // K step (elements)
+constexpr int TH = 128;                 // rows per tile (UMMA M)
+constexpr int KB = 32;                  // K step (elements)
+constexpr int kChunk = 2;               // K steps per H accumulator chunk
+constexpr int STAGES = 4;
+constexpr int kProducers = TH;          // one thread per row
+constexpr int kThreads = kProducers + 32;
 constexpr int kMaxBatch = 64;
 constexpr long long kSpinLimit = 1LL << 20;  // try_wait polls; each may block briefly
-constexpr uint32_t kAHalfBytes = TH * KB * 2;       // one term, one row half
-
-// tile configuration for NH accumulators (row halves) per CTA
-template <int NH>
-struct TileCfg {
-  static constexpr int TM = NH * TH;                // rows per CTA
-  static constexpr int STAGES = NH == 1 ? 3 : 2;
-  static constexpr int kProducers = TM;             // one thread per row
-  static constexpr int kThreads = kProducers + 32;  // + one warp: B copies and MMA issue
-  static constexpr uint32_t kATermBytes = NH * kAHalfBytes;  // one term, all halves
-  static constexpr uint32_t kABytes = 3 * kATermBytes;       // the A part of a stage
-};
+constexpr uint32_t kATermBytes = TH * KB * 2;  // one BF16 term of the A block
+constexpr uint32_t kABytes = 3 * kATermBytes;
 
 __device__ int g_umma_error;  // first failing CTA records a code here
+long long g_spin_limit = kSpinLimit;
 
 // ----------------------------------------------------------------------
 // PTX helpers
@@ -70,9 +76,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 }
 
 // bounded wait for the phase with parity `parity` to complete
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit) {
   const uint32_t a = smem_u32(bar);
-  for (long long it = 0; it < kSpinLimit; ++it) {
+  for (long long it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n"
@@ -137,6 +143,41 @@ __device__ __forceinline__ uint32_t bf16_bits(__nv_bfloat16 b) {
   return (uint32_t)__bfloat16_as_ushort(b);
 }
 
+// 16 consecutive FP32 accumulator columns of this warp's 32 TMEM lanes
+__device__ __forceinline__ void tmem_ld16(uint32_t (&v)[16], uint32_t taddr) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// acc[0 .. tnc) += the tnc accumulator columns starting at column `col`
+// (tnc a multiple of 16, at most 128; loads issued in pairs before one wait)
+__device__ __forceinline__ void tmem_add_row(float (&acc)[TH], uint32_t tmem_lane, uint32_t col, int tnc) {
+#pragma unroll
+  for (int c0 = 0; c0 < TH; c0 += 32) {
+    if (c0 < tnc) {
+      uint32_t va[16], vb[16];
+      const bool two = c0 + 16 < tnc;
+      tmem_ld16(va, tmem_lane + col + (uint32_t)c0);
+      if (two) tmem_ld16(vb, tmem_lane + col + (uint32_t)(c0 + 16));
+      tmem_wait_ld();
+#pragma unroll
+      for (int j = 0; j < 16; ++j) acc[c0 + j] += __uint_as_float(va[j]);
+      if (two) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) acc[c0 + 16 + j] += __uint_as_float(vb[j]);
+      }
+    }
+  }
+}
+
 // ----------------------------------------------------------------------
 // MMA kernel
 // ----------------------------------------------------------------------
@@ -154,34 +195,39 @@ struct UmmaBatch {
 
 struct UmmaArgs {
   int M, N, Np, K, Kp;
+  int tnc;            // columns per tile (multiple of 16, <= 128)
   const float2 *shift;
-  int epi;
-  int fac_staged;  // factor block staged in shared memory for the epilogue
+  int fac_staged;     // factor block staged in shared memory for the epilogue
   uint32_t tmem_cols;
+  long long spin;     // iteration limit of the pipeline waits
 };
 
-template <int EPI, int NH>
-__global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __grid_constant__ UmmaBatch P,
-                                                           UmmaArgs A) {
-  using Cfg = TileCfg<NH>;
-  constexpr int TM = Cfg::TM, STAGES = Cfg::STAGES, kProducers = Cfg::kProducers;
-  constexpr uint32_t kATermBytes = Cfg::kATermBytes, kABytes = Cfg::kABytes;
+template <int EPI>
+__global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant__ UmmaBatch P, UmmaArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t afull[STAGES], bfull[STAGES], empty[STAGES], done;
+  __shared__ __align__(8) uint64_t afull[STAGES], bfull[STAGES], empty[STAGES], hfull[2], hempty[2],
+      done;
   __shared__ uint32_t tmem_base;
   __shared__ int fail;
-  const int prob = blockIdx.y, mt = blockIdx.x;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t b_term = (uint32_t)A.Np * KB * 2;  // one B term of a stage
+  const int prob = blockIdx.z, nt = blockIdx.y, mt = blockIdx.x;
+  const int warp = threadIdx.x >> 5;
+  const int tnc = A.tnc, n0 = nt * tnc;
+  const uint32_t b_term = (uint32_t)tnc * KB * 2;  // one B term of a stage
   const uint32_t stage_bytes = kABytes + 3 * b_term;
   const int nkb = A.Kp / KB;
+  const int nchunk = (nkb + kChunk - 1) / kChunk;
   const UmmaProb &Q = P.p[prob];
+  const long long spin = A.spin;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&afull[s], kProducers);
       mbar_init(&bfull[s], 1);
       mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&hfull[b], 1);
+      mbar_init(&hempty[b], kProducers);
     }
     mbar_init(&done, 1);
     fail = 0;
@@ -198,11 +244,18 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
+  const uint32_t colL = 2u * (uint32_t)tnc;  // the correction-pair accumulator
+
+  float acc[TH];  // this row's sum of the drained H chunks (producer threads)
+#pragma unroll
+  for (int j = 0; j < TH; ++j) acc[j] = 0.0f;
+  const uint32_t tmem_lane = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  volatile int *vfail = &fail;
 
   if (threadIdx.x < kProducers) {
-    // ---- producers: FP32 A row -> three BF16 terms in the stage
-    const int r = threadIdx.x, h = r / TH, rr = r % TH;
-    const long long gm = (long long)mt * TM + r;
+    // ---- producers: FP32 A row -> three BF16 terms in the stage; drain H
+    const int r = threadIdx.x;
+    const long long gm = (long long)mt * TH + r;
     const bool row_ok = gm < A.M;
     long long src = gm;
     uint32_t neg = 0;  // sign flip of the BF16 terms (reflected real part)
@@ -220,16 +273,32 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
         v[k] = (row_ok && gk < A.K) ? Arow[(long long)gk * A.M] : 0.0f;
       }
     };
+    // drain chunk c (H accumulator c & 1) into acc, then hand it back
+    auto drain = [&](int c) {
+      const int b = c & 1;
+      bool ok = !*vfail && mbar_wait(&hfull[b], (uint32_t)(c >> 1) & 1u, spin);
+      if (!ok) {
+        *vfail = 1;
+        atomicCAS(&g_umma_error, 0, 4);
+      } else {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        tmem_add_row(acc, tmem_lane, (uint32_t)(b * tnc), tnc);
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      }
+      mbar_arrive(&hempty[b]);
+    };
+    int drained = 0;
     load(0);
     for (int kb = 0; kb < nkb; ++kb) {
       const int s = kb % STAGES;
       bool ok = true;
-      if (kb >= STAGES) ok = mbar_wait(&empty[s], (uint32_t)(kb / STAGES - 1) & 1u);
+      if (kb >= STAGES) ok = !*vfail && mbar_wait(&empty[s], (uint32_t)(kb / STAGES - 1) & 1u, spin);
       if (!ok) {
-        fail = 1;
+        *vfail = 1;
         atomicCAS(&g_umma_error, 0, 3);
       } else {
-        unsigned char *st = smem + (size_t)s * stage_bytes + h * kAHalfBytes;
+        unsigned char *st = smem + (size_t)s * stage_bytes;
+        const int rr = r;
 #pragma unroll
         for (int kg = 0; kg < KB / 8; ++kg) {
           uint32_t w0[4], w1[4], w2[4];
@@ -263,20 +332,25 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&afull[s]);
       if (kb + 1 < nkb) load(kb + 1);
+      // chunk c is drained once the stages of chunk c + 1 are written, so the
+      // tensor core has the next chunk's operands while the rows drain
+      const int c_ready = (kb + 1) / kChunk - 2;
+      while (drained <= c_ready) drain(drained++);
     }
+    while (drained < nchunk) drain(drained++);
   } else if (EPI == TC_EPI_SHIFT_FAC && A.fac_staged && threadIdx.x > kProducers) {
-    // idle lanes of the MMA warp: start the tile's factor block (read by
-    // the epilogue) towards L2, two 128-byte lines per column
-    const int xr0p = mt * (TM / 2);
-    const int rows = min(TM / 2, (A.M >> 1) - xr0p);
-    for (int t = threadIdx.x - kProducers - 1; t < 2 * A.N; t += 31) {
-      const int n = t >> 1, part = t & 1;
-      if (part * 32 < rows)
+    // idle lanes of the MMA warp: start the tile's factor block (read by the
+    // epilogue) towards L2, one or two 128-byte lines per column
+    const int xr0p = mt * (TH / 2);
+    const int rows = min(TH / 2, (A.M >> 1) - xr0p);
+    for (int t = threadIdx.x - kProducers - 1; t < 2 * tnc; t += 31) {
+      const int n = n0 + (t >> 1), part = t & 1;
+      if (part * 32 < rows && n < A.N)
         asm volatile("prefetch.global.L2 [%0];" ::"l"(Q.fac + xr0p + part * 32 + (long long)(A.M >> 1) * n));
     }
   } else if (threadIdx.x == kProducers) {
     // ---- B streaming and MMA issue
-    const uint32_t idesc = idesc_bf16(TH, A.Np);
+    const uint32_t idesc = idesc_bf16(TH, tnc);
     int last_b[STAGES];
     for (int s = 0; s < STAGES; ++s) last_b[s] = -1;
     auto load_b = [&](int kb) {
@@ -284,7 +358,8 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
       unsigned char *st = smem + (size_t)s * stage_bytes + kABytes;
       mbar_expect_tx(&bfull[s], 3 * b_term);
       for (int t = 0; t < 3; ++t)
-        bulk_g2s(st + t * b_term, Q.B[t] + (long long)kb * A.Np * KB, b_term, &bfull[s]);
+        bulk_g2s(st + t * b_term, Q.B[t] + (long long)kb * A.Np * KB + (long long)n0 * KB, b_term,
+                 &bfull[s]);
       last_b[s] = kb;
     };
     bool ok = true;
@@ -292,33 +367,40 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
     for (int kb = 0; kb < nkb && ok; ++kb) {
       const int s = kb % STAGES;
       const uint32_t par = (uint32_t)(kb / STAGES) & 1u;
-      if (!mbar_wait(&bfull[s], par) || !mbar_wait(&afull[s], par)) {
+      const int c = kb / kChunk;
+      const bool first = (kb % kChunk) == 0;
+      const bool last = (kb % kChunk) == kChunk - 1 || kb == nkb - 1;
+      if (first && c >= 2 && !mbar_wait(&hempty[c & 1], (uint32_t)((c >> 1) - 1) & 1u, spin)) {
+        ok = false;
+        break;
+      }
+      if (!mbar_wait(&bfull[s], par, spin) || !mbar_wait(&afull[s], par, spin)) {
         ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       unsigned char *st = smem + (size_t)s * stage_bytes;
-      // term pairs (i, j) with i + j <= 2, smallest terms first
-      const int pi[6] = {2, 1, 0, 1, 0, 0}, pj[6] = {0, 1, 2, 0, 1, 0};
+      const uint32_t dH = tmem + (uint32_t)((c & 1) * tnc), dL = tmem + colL;
+      // term pairs (i, j): (0, 0) into H, the others into L
+      const int pi[6] = {0, 2, 1, 0, 1, 0}, pj[6] = {0, 0, 1, 2, 0, 1};
 #pragma unroll
       for (int q = 0; q < 6; ++q) {
 #pragma unroll
         for (int ks = 0; ks < KB / 16; ++ks) {
           const uint64_t bd = smem_desc(st + kABytes + pj[q] * b_term + ks * 256, 128, (KB / 8) * 128);
-#pragma unroll
-          for (int hh = 0; hh < NH; ++hh) {
-            const uint64_t ad =
-                smem_desc(st + pi[q] * kATermBytes + hh * kAHalfBytes + ks * 256, 128, (KB / 8) * 128);
-            umma_bf16(tmem + (uint32_t)(hh * A.Np), ad, bd, idesc,
-                      (kb > 0 || q > 0 || ks > 0) ? 1u : 0u);
-          }
+          const uint64_t ad = smem_desc(st + pi[q] * kATermBytes + ks * 256, 128, (KB / 8) * 128);
+          if (q == 0)
+            umma_bf16(dH, ad, bd, idesc, (first && ks == 0) ? 0u : 1u);
+          else
+            umma_bf16(dL, ad, bd, idesc, (kb == 0 && q == 1 && ks == 0) ? 0u : 1u);
         }
       }
       umma_commit(&empty[s]);
+      if (last) umma_commit(&hfull[c & 1]);
       // refill the stage of the previous step once its MMAs have drained
       if (kb >= 1 && kb - 1 + STAGES < nkb) {
         const int sp = (kb - 1) % STAGES;
-        if (!mbar_wait(&empty[sp], (uint32_t)((kb - 1) / STAGES) & 1u)) {
+        if (!mbar_wait(&empty[sp], (uint32_t)((kb - 1) / STAGES) & 1u, spin)) {
           ok = false;
           break;
         }
@@ -327,106 +409,80 @@ __global__ void __launch_bounds__(TileCfg<NH>::kThreads, 1) umma_kernel(const __
     }
     umma_commit(&done);
     if (!ok) {
-      fail = 1;
+      *vfail = 1;
       atomicCAS(&g_umma_error, 0, 1);
       // let the bulk copies already issued land before the CTA exits
       for (int s = 0; s < STAGES; ++s)
-        if (last_b[s] >= 0) mbar_wait(&bfull[s], (uint32_t)(last_b[s] / STAGES) & 1u);
+        if (last_b[s] >= 0) mbar_wait(&bfull[s], (uint32_t)(last_b[s] / STAGES) & 1u, kSpinLimit);
     }
   }
   __syncthreads();
-  // all MMAs complete before the accumulators are read (bounded wait)
-  const bool drained = mbar_wait(&done, 0);
+  // all MMAs complete before the L accumulator is read and the stages are
+  // reused (the full limit: this wait must not leave MMAs in flight)
+  const bool drained = mbar_wait(&done, 0, kSpinLimit);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const bool use = __syncthreads_and(drained && !fail);
   if (!drained && threadIdx.x == 0) atomicCAS(&g_umma_error, 0, 2);
-  // factor epilogue: the tile's factor block (TM/2 x-rows x N columns, one
+  // factor epilogue: the tile's factor block (64 x-rows x tnc columns, one
   // contiguous run per column, started towards L2 during the K loop) is
-  // copied into the drained stages with 16-byte loads, all threads at once,
-  // instead of a dependent global load per column group
-  const int nxr = TM / 2, xr0 = mt * (TM / 2);
+  // copied into the drained stages with 16-byte loads, all threads at once
+  constexpr int nxr = TH / 2;
+  const int xr0 = mt * nxr;
   const float *facs = reinterpret_cast<const float *>(smem);
   bool fac_smem = false;
   if (EPI == TC_EPI_SHIFT_FAC && use && A.fac_staged) {
     const int rows = min(nxr, (A.M >> 1) - xr0);  // a multiple of 4 (host check)
-    const int nq = nxr / 4, total = nq * A.N;       // float4 per column, in the block
+    constexpr int nq = nxr / 4;
+    const int total = nq * tnc;  // float4 per column, in the block
     float4 *dst = reinterpret_cast<float4 *>(smem);
     constexpr int kBatch = 13;
     for (int t0 = threadIdx.x; t0 < total; t0 += kBatch * (int)blockDim.x) {
-      float4 v[kBatch];
+      float4 vv[kBatch];
 #pragma unroll
       for (int b = 0; b < kBatch; ++b) {
         const int t = t0 + b * (int)blockDim.x;
         const int n = t / nq, q = t - n * nq;
-        v[b] = (t < total && 4 * q < rows)
-                   ? __ldg(reinterpret_cast<const float4 *>(Q.fac + xr0 + (long long)(A.M >> 1) * n) + q)
-                   : make_float4(1.f, 1.f, 1.f, 1.f);
+        vv[b] = (t < total && 4 * q < rows && n0 + n < A.N)
+                    ? __ldg(reinterpret_cast<const float4 *>(Q.fac + xr0 + (long long)(A.M >> 1) * (n0 + n)) + q)
+                    : make_float4(1.f, 1.f, 1.f, 1.f);
       }
 #pragma unroll
       for (int b = 0; b < kBatch; ++b) {
         const int t = t0 + b * (int)blockDim.x;
-        if (t < total) dst[t] = v[b];
+        if (t < total) dst[t] = vv[b];
       }
     }
     __syncthreads();
     fac_smem = true;
   }
   if (use && threadIdx.x < kProducers) {
-    const int qd = warp & 3, hh = warp >> 2;       // TMEM lane quarter, row half
-    const int row = hh * TH + qd * 32 + lane;      // row of the tile
-    const long long gm = (long long)mt * TM + row;
+    tmem_add_row(acc, tmem_lane, colL, tnc);  // + the correction pairs
+    const int row = threadIdx.x;
+    const long long gm = (long long)mt * TH + row;
     float2 sh = make_float2(1.f, 0.f);
     if (EPI != TC_EPI_STORE && gm < A.M) sh = A.shift[gm >> 1];
     float *C = Q.C;
     const float *fac = Q.fac;
     const bool rok = gm < A.M;
-    // 16-column groups in pairs: both accumulator loads issued before one wait
-    auto tmem_ld16 = [&](uint32_t (&v)[16], int c0) {
-      const uint32_t taddr = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(hh * A.Np + c0);
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-            "=r"(v[14]), "=r"(v[15])
-          : "r"(taddr));
-    };
-    auto finish16 = [&](const uint32_t (&v)[16], int c0) {
-      // factors of the 16 columns
-      float fv[16];
-      if (EPI == TC_EPI_SHIFT_FAC) {
-        if (fac_smem) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) fv[j] = facs[(c0 + j) * nxr + (row >> 1)];
-        } else {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int n = c0 + j;
-            fv[j] = (rok && n < A.N) ? __ldg(fac + (gm >> 1) + (long long)(A.M >> 1) * n) : 1.0f;
-          }
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        float x = __uint_as_float(v[j]);
-        const int n = c0 + j;
+    for (int j = 0; j < TH; ++j) {
+      if (j < tnc) {
+        float x = acc[j];
+        const int n = n0 + j;
         if (EPI != TC_EPI_STORE) {
           // rows 2x (re) and 2x+1 (im) sit in adjacent lanes
           const float other = __shfl_xor_sync(0xffffffffu, x, 1);
           const float re = (row & 1) ? other : x, im = (row & 1) ? x : other;
           x = (row & 1) ? (re * sh.y + im * sh.x) : (re * sh.x - im * sh.y);
-          if (EPI == TC_EPI_SHIFT_FAC) x *= fv[j];
+          if (EPI == TC_EPI_SHIFT_FAC) {
+            const float f = fac_smem ? facs[j * nxr + (row >> 1)]
+                                     : ((rok && n < A.N) ? __ldg(fac + (gm >> 1) + (long long)(A.M >> 1) * n)
+                                                         : 1.0f);
+            x *= f;
+          }
         }
         if (rok && n < A.N) C[gm + (long long)n * A.M] = x;
       }
-    };
-    for (int c0 = 0; c0 < A.Np; c0 += 32) {
-      uint32_t va[16], vb[16];
-      const bool two = c0 + 16 < A.Np;
-      tmem_ld16(va, c0);
-      if (two) tmem_ld16(vb, c0 + 16);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      finish16(va, c0);
-      if (two) finish16(vb, c0 + 16);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -445,9 +501,9 @@ namespace chm {
 
 int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, const float2 *shift,
                    cudaStream_t st) {
-  const int Np = (int)rup(N, 16), Kp = (int)rup(K, KB);
-  if (Np > 256) {
-    set_error("umma: N must be <= 256");
+  const int tnc = tc_tile_cols(N), ntn = tc_col_tiles(N), Np = tc_np(N), Kp = (int)rup(K, KB);
+  if (tnc > TH || tnc % 16) {
+    set_error("umma: bad column tile %d", tnc);
     return CHM_ERR_RANGE;
   }
   if (M % 2) {
@@ -459,42 +515,30 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
       set_error("umma: problem %d has no prepared %dx%d operator", i, K, N);
       return CHM_ERR_ARG;
     }
-  // 128-row tiles (one accumulator per CTA, a deeper K pipeline) when all
-  // of them run in one wave, else 256-row tiles (two accumulators per CTA:
-  // the same number of waves of twice the work, half the B traffic)
-  const bool two = 2LL * count * ((M + 255) / 256) > sm_count();
-  const int NH = two ? 2 : 1;
-  const int TM = NH * TH, STAGES = two ? TileCfg<2>::STAGES : TileCfg<1>::STAGES;
-  const uint32_t kABytes = two ? TileCfg<2>::kABytes : TileCfg<1>::kABytes;
-  const int threads = two ? TileCfg<2>::kThreads : TileCfg<1>::kThreads;
-  const int mt = (int)((M + TM - 1) / TM);
-  const uint32_t b_term = (uint32_t)Np * KB * 2;
-  const size_t smem = (size_t)STAGES * (kABytes + 3 * b_term) + 1024;
-  void (*kern)(const UmmaBatch, UmmaArgs);
-  if (two)
-    kern = epi == TC_EPI_STORE ? umma_kernel<TC_EPI_STORE, 2>
-                               : (epi == TC_EPI_SHIFT ? umma_kernel<TC_EPI_SHIFT, 2>
-                                                      : umma_kernel<TC_EPI_SHIFT_FAC, 2>);
-  else
-    kern = epi == TC_EPI_STORE ? umma_kernel<TC_EPI_STORE, 1>
-                               : (epi == TC_EPI_SHIFT ? umma_kernel<TC_EPI_SHIFT, 1>
-                                                      : umma_kernel<TC_EPI_SHIFT_FAC, 1>);
+  const int mt = (int)((M + TH - 1) / TH);
+  const uint32_t b_term = (uint32_t)tnc * KB * 2;
+  const size_t stage_bytes = kABytes + 3 * (size_t)b_term;
+  const size_t smem = (size_t)STAGES * stage_bytes + 1024;
+  void (*kern)(const UmmaBatch, UmmaArgs) =
+      epi == TC_EPI_STORE ? umma_kernel<TC_EPI_STORE>
+                          : (epi == TC_EPI_SHIFT ? umma_kernel<TC_EPI_SHIFT> : umma_kernel<TC_EPI_SHIFT_FAC>);
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   uint32_t cols = 32;
-  while (cols < (uint32_t)(NH * Np)) cols <<= 1;
+  while (cols < (uint32_t)(3 * tnc)) cols <<= 1;  // H0, H1 and L
   UmmaArgs ua{};
   ua.M = M;
   ua.N = N;
   ua.Np = Np;
   ua.K = K;
   ua.Kp = Kp;
+  ua.tnc = tnc;
   ua.shift = shift;
-  ua.epi = epi;
   ua.tmem_cols = cols;
+  ua.spin = g_spin_limit;
   // the staged factor block is read with 16-byte loads: M/2 a multiple of 4
-  // and 16-byte aligned factor planes; it (TM/2 x Np FP32) fits in the stages
+  // and 16-byte aligned factor planes; it (64 x tnc FP32) fits in the stages
   ua.fac_staged = (epi == TC_EPI_SHIFT_FAC && (M / 2) % 4 == 0 &&
-                 (size_t)(TM / 2) * Np * 4 <= (size_t)STAGES * (kABytes + 3 * b_term)) ? 1 : 0;
+                   (size_t)(TH / 2) * tnc * 4 <= (size_t)STAGES * stage_bytes) ? 1 : 0;
   for (int i = 0; i < count && ua.fac_staged; ++i)
     if (!p[i].fac || (reinterpret_cast<uintptr_t>(p[i].fac) & 15)) ua.fac_staged = 0;
   for (int c0 = 0; c0 < count; c0 += kMaxBatch) {
@@ -508,7 +552,7 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
                           reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[2])},
                          q.reflect};
     }
-    kern<<<dim3(mt, cnt), threads, smem, st>>>(ub, ua);
+    kern<<<dim3(mt, ntn, cnt), kThreads, smem, st>>>(ub, ua);
     count_launch();
   }
   cudaError_t e = cudaGetLastError();
@@ -522,7 +566,14 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
 }  // namespace chm
 
 extern "C" int chm_sp_umma_status(void) {
-  int v = 0;
+  int v = 0, z = 0;
   cudaMemcpyFromSymbol(&v, g_umma_error, sizeof(int));
+  if (v) cudaMemcpyToSymbol(g_umma_error, &z, sizeof(int));
   return v;
+}
+
+extern "C" int64_t chm_sp_set_umma_spin_limit(int64_t polls) {
+  const long long prev = g_spin_limit;
+  g_spin_limit = polls < 0 ? kSpinLimit : polls;
+  return prev;
 }

@@ -444,6 +444,22 @@ int chm_sp_gather_push(int32_t *ix, float *fx, float *y, float *z, float *px,
                        float win_f, float dr_inv, const void *eb_c64, int nx,
                        int nr, int nm, float dtq, void *stream);
 
+/* The same two operations with the per-particle kernels for every nm (each
+ * value rounded separately): the reference the cell-run kernels (nm <= 3)
+ * are tested against.  The entry points above use the cell-run kernels for
+ * nm <= 3 and these kernels beyond. */
+int chm_sp_push_deposit_generic(int32_t *ix, float *fx, float *y, float *z,
+                                float *px, float *py, float *pz, float *w,
+                                int64_t n, int win_k, float win_f, float dx_inv,
+                                float dr_inv, float dt, int nx, int nr, int nm,
+                                int push, uint64_t *accJ, const double *scaleJ,
+                                uint64_t *accR, const double *scaleR, void *stream);
+int chm_sp_gather_push_generic(int32_t *ix, float *fx, float *y, float *z,
+                               float *px, float *py, float *pz, float *w,
+                               int64_t n, int win_k, float win_f, float dr_inv,
+                               const void *eb_c64, int nx, int nr, int nm,
+                               float dtq, void *stream);
+
 /* FP64 (3,n)/(n) particle arrays (particle order) <-> split layout; from_f64
  * writes particles offset .. offset+n-1 and clears their dead flags (dead
  * may be NULL). */
@@ -520,8 +536,16 @@ int chm_sp_psatd(void *eg_c64, const void *j_c64, const void *gprv_c64,
 int64_t chm_sp_gemm_ws_bytes(int64_t M, int64_t K, int64_t count);
 int chm_sp_gemm(float *C, const float *A, const chm_sp_ops *ops, int64_t mode,
                 int64_t M, int engine, void *ws, int64_t ws_bytes, void *stream);
-/* Nonzero if a tensor-core GEMM CTA hit a wait limit since load. */
+/* Nonzero if a tensor-core GEMM CTA hit a wait limit since the last call
+ * (then reset): 1 or 3 the operand pipeline, 4 an accumulator hand-over,
+ * 2 the final drain.  The CTA that gave up wrote no output. */
 int chm_sp_umma_status(void);
+/* Iteration limit of the tensor-core GEMM's pipeline waits for launches
+ * after this call (polls of mbarrier.try_wait; < 0 restores the default
+ * 2^20); returns the previous limit.  A test hook: with 0 every pipeline
+ * wait gives up at once, and the kernel must report it and free its tensor
+ * memory (its clean-up waits keep the default limit). */
+int64_t chm_sp_set_umma_spin_limit(int64_t polls);
 /* Deposit cells of the split-form run kernels that fell outside their
  * block's box while inside the grid since the last call (then reset).  The
  * block plan bounds every finite particle's deposit cells, so this is 0
