@@ -1,29 +1,37 @@
 """Benchmark of the CHIMERA PIC step on GB300: particle*steps/s.
 
-Workload (the laser-wakefield configuration the headline metric is quoted
-on): Nx = 2048 (dx = 0.04), Nr = 256 (dr = 0.4), azimuthal modes m = 0, 1,
-FixedCell (2, 2, 8) electrons filling the box (~16.7M) over still ions
-(SpaceCharge + StillAsBackground), density 0.003 n_c with a 20 lambda0
-linear up-ramp, Gaussian laser a0 = 2, w0 = 12, FWHM 10 lambda0/c, moving
-window at c, x-chunked deposition (16 chunks, 10 guard cells).  Inputs are
-synthetic (seeded numpy), of this shape.
+Workload (default --size cfg3, the largest configuration that fits one
+GPU): the laser-wakefield set-up Nx = 4096 (dx = 0.04), Nr = 512 (dr = 0.4),
+azimuthal modes m = 0..2, FixedCell (2, 2, 12) electrons at 0.002 n_c in the
+x > 0 half of the box (~50.3M) over still ions (SpaceCharge +
+StillAsBackground), Gaussian laser a0 = 3, w0 = 15, FWHM 10 lambda0/c
+focused at the plasma entrance, moving window at c
+(chimera_gb300/workloads.py; --size cfg2 is the 2048 x 256 x 2-mode set-up).
+Inputs are synthetic (seeded numpy) of this shape.
 
-  value  particle*steps/s of ChimeraRun.make_step with all state resident on
-         the GPU (moving species only, as the metric counts them)
-  e2e    the same through the public API with the window's plasma
+  value  particle*steps/s of the split-precision form (SplitRun.make_step)
+         with all state resident on the GPU (moving species only, as the
+         metric counts them); --form fp64 makes the plain FP64 form the value
+  fp64_gpu  the plain FP64 form (ChimeraRun.make_step) on the same workload
+         in the same run, and split_over_fp64 the ratio of the two
+  transform_errors  relative L2 of every split transform against the FP64
+         kernels on the run's own fields after the timed steps
+  e2e    the split form through the public API with the window's plasma
          injection (AddPlasma + AbsorbLayer + IonsOnTop, as in the
          reference's lpa-testrun.py): the generator's host data copied
          host->device every step, and the laser a0 read back every step
   roofline  the dominant stage's algorithmic bytes (or FLOPs) over its live
-         CUDA-event time against MEASURED_PEAKS.json, with the ncu DRAM
-         traffic of the deposit kernels scaled by particle count
+         CUDA-event time against MEASURED_PEAKS.json
   cpu_baseline  the oracle's C/OpenMP step on all host cores, a bounded
          sample of the e2e workload
   clocks  nvidia-smi SM clock and throttle reasons sampled through the run
+  device_flags  the split form's device error flags after the run (a
+         tensor-core CTA that gave up on a wait; deposit cells outside their
+         block box); the run fails when either is set
 
 --impl reference runs the oracle's CPU step driver (the reference's step
 loop over the C restatement of its Fortran kernels, OpenMP on every host
-core) on the same configuration.
+core) on the e2e workload, from the same laser field.
 """
 from __future__ import annotations
 
@@ -40,80 +48,24 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from chimera_gb300 import workloads  # noqa: E402
+
 METRIC = "particle*steps/s"
-WORKLOAD_SIZE = "cfg2"
-WORKLOAD = "lwfa_nx2048_nr256_m2_ppc2x2x8"
+WORKLOAD_SIZE = "cfg3"
 
 
-SIZES = {  # name: (nx, nkr, ppc)
-    "cfg2": (2048, 256, (2, 2, 8)),
-    # quarter radius: 4.2M electrons (134 MB of split-form particle state,
-    # above the 129 MB L2) and ~3 GB on the device, for ncu captures
-    "prof": (2048, 64, (2, 2, 8)),
-    # the cfg2 grid with 1 particle per cell (0.5M electrons, small particle
-    # state), for ncu captures of the spectral kernels at their full size
-    "spec": (2048, 256, (1, 1, 1)),
-    "small": (512, 64, (2, 2, 4)),
-}
-
-
-def workload_config(nchunks=16):
-    nx, nkr, ppc = SIZES[WORKLOAD_SIZE]
-    dx, dr = 0.04, 0.4
-    xmin = -80.0 if nx == 2048 else -(nx * dx) + 1.92
-    xmax = xmin + nx * dx
-    grid = (xmin, xmax, nkr * dr, dx, dr)
-    ramp = 20.0
-
-    def prof(x):
-        return np.interp(x, [xmin, xmin + ramp, 1e9], [0.0, 1.0, 1.0])
-
-    fwhm = 10.0
-    Lx = fwhm / (2 * np.sqrt(np.log(2) / 2))
-    return dict(
-        solver={"Grid": grid, "TimeStep": dx, "MaxAzimuthMode": 1,
-                "Xchunked": (nchunks, 10), "Features": ("SpaceCharge", "StillAsBackground")},
-        laser={"a0": 2.0, "k0": 1.0, "x0": -30.0, "x_foc": -30.0 + 20.0, "Lx": Lx, "LR": 12.0},
-        electrons={"Grid": grid, "TimeStep": dx, "Density": 0.003, "FixedCell": ppc,
-                   "Xchunked": (nchunks, 10), "Features": ("NoSorting",)},
-        domain=(xmin + 1.5 * dx, xmax, 0.0, nkr * dr),  # Xgrid starts at xmin + dx
-        profile=prof, dx=dx)
-
-
-def build_run(device_kind, window, seed=1002):
-    """Solver + electrons + still ions + ChimeraRun (GPU) or CpuRun (oracle)."""
-    from copy import deepcopy
-
-    from chimera_gb300.messages import msg
-    msg.quiet = True
-    cfg = workload_config()
-    np.random.seed(seed)
+def build_run(device_kind, window, seed=1003):
+    """ChimeraRun of the workload (GPU) or the oracle's CpuRun inputs."""
     if device_kind == "gpu":
-        from chimera_gb300 import ChimeraRun, Solver, Specie
-        solver = Solver(deepcopy(cfg["solver"]))
-        solver.add_gauss_beam(cfg["laser"])
-        dev = None
-    else:
-        from chimera_gb300.solvers import Solver
-        from chimera_gb300.species import Specie
-        solver = Solver(deepcopy(cfg["solver"]), device="cpu")
-        dev = "cpu"
-    el_in = deepcopy(cfg["electrons"])
-    io_in = deepcopy(cfg["electrons"])
-    io_in["Charge"], io_in["Mass"], io_in["Features"] = 1.0, 1836.0, ("Still", "NoSorting")
-    kw = {} if dev is None else {"device": dev}
-    el, io = Specie(el_in, **kw), Specie(io_in, **kw)
-    parts = el.gen_parts(Domain=cfg["domain"], ProfileFunc=cfg["profile"])
-    el.add_particles(*parts)
-    parts[-1] = parts[-1] * -1
-    io.add_particles(*parts)
-    wind = {"TimeStep": cfg["dx"], "Steps": 1, "Velocity": 1.0}
-    if window == "inject":
-        wind.update({"AbsorbLayer": 64, "AddPlasma": cfg["profile"], "Features": ("IonsOnTop",)})
-    if device_kind == "gpu":
-        run = ChimeraRun({"Solvers": (solver,), "Particles": (el, io), "MovingFrames": (wind,)})
-        return run, solver, el
-    return solver, el, io, wind
+        from chimera_gb300 import ChimeraRun
+        comps = workloads.components(WORKLOAD_SIZE, window, seed)
+        run = ChimeraRun(comps)
+        return run, comps["Solvers"][0], comps["Particles"][0]
+    from oracle.step import add_gauss_beam
+    comps = workloads.components(WORKLOAD_SIZE, window, seed, device="cpu")
+    solver = comps["Solvers"][0]
+    add_gauss_beam(solver, workloads.config(WORKLOAD_SIZE)["laser"])
+    return solver, comps["Particles"][0], comps["Particles"][1], comps["MovingFrames"][0]
 
 
 class ClockSampler:
@@ -201,10 +153,11 @@ SPLIT_BYTES = {"push_electrons": 32 + 16,  # read ix,fx,y,z,p,w; write ix,fx,y,z
 FP64_BYTES = {"push_velocs": 48 + 48 + 24, "push_coords": 24 + 24 + 24 + 24,
               "dep_curr": 24 + 24 + 8, "dep_dens": 24 + 8, "proj_fld": 24 + 8 + 48 + 48}
 # DRAM bytes (read + write) per particle of the dominant split-form stage,
-# from one ncu --set full capture of the quarter-radius case (--size prof,
-# 4.13M particles per species; traffic grows with the particle count):
-# electrons (push + J + rho) 179.5 MB, still ions (rho) 89.5 MB
-SPLIT_TRAFFIC = {"push_electrons": 179.90e6 / 4128768, "deposit_still": 87.29e6 / 4128768}
+# by the number of stored modes, from one ncu capture of a quarter-radius
+# case (traffic grows with the particle count): 2 modes from --size prof
+# (4.13M particles per species: electrons (push + J + rho) 179.9 MB, still
+# ions (rho) 87.3 MB)
+SPLIT_TRAFFIC = {2: {"push_electrons": 179.90e6 / 4128768, "deposit_still": 87.29e6 / 4128768}}
 GEMM_STAGES = ("chm_fb_graddiv", "chm_fb_rot", "chm_fb_grad", "chm_fb_div", "chm_fb_in",
                "chm_fb_out", "chm_fb_eb_out", "chm_sp_poisson", "chm_sp_fb_in_acc",
                "chm_sp_fb_eb_out", "chm_sp_rot_b", "chm_sp_fb_grad")
@@ -251,8 +204,9 @@ def stage_roofline(form, prof, nprof, n_e, n_i, peaks, peak_kind):
     top = dict(rows[0]) if rows else {"stage": None}
     top["kernel"] = top.pop("stage")
     top["traffic"] = None
-    if form == "split" and top.get("kernel") == "chm_sp_push_deposit":
-        top["traffic"] = n_e * SPLIT_TRAFFIC["push_electrons"] + n_i * SPLIT_TRAFFIC["deposit_still"]
+    tr = SPLIT_TRAFFIC.get(workloads.SIZES[WORKLOAD_SIZE].modes)
+    if form == "split" and top.get("kernel") == "chm_sp_push_deposit" and tr:
+        top["traffic"] = n_e * tr["push_electrons"] + n_i * tr["deposit_still"]
         top["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
                                  "quarter-radius case, scaled by particle count")
     top["peak_source"] = f"MEASURED_PEAKS.json ({peak_kind})" if top.get("bound") != "fp64" else \
@@ -296,13 +250,9 @@ def max_over_ranks(world, v):
 
 def cpu_step_time(nsteps, warmup=0, window="none"):
     """Wall time per step and moving particles per step of the oracle's CPU
-    step driver on this workload."""
+    step driver on this workload (from the same laser field as the GPU arm)."""
     from oracle.step import CpuRun, CpuSpecies
-    import torch
     solver, el, io, wind = build_run("cpu", window)
-    # the reference initialises the laser in spectral space with the same
-    # kernels; the CPU arm starts from a zero field (same cost per step)
-    solver.Data["EG_fb"] = torch.zeros(tuple(solver.Data["EG_fb"].shape), dtype=torch.complex128)
     run = CpuRun(solver, [CpuSpecies(el), CpuSpecies(io)], wind)
     for i in range(1, warmup + 1):
         run.make_step(i)
@@ -315,6 +265,10 @@ def cpu_step_time(nsteps, warmup=0, window="none"):
     return dt, psteps / nsteps
 
 
+def workload_name(window="none"):
+    return workloads.SIZES[WORKLOAD_SIZE].name + ("_window_inject" if window == "inject" else "")
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -322,17 +276,27 @@ def run_reference(args):
         return 0
     cores = len(os.sched_getaffinity(0))
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    steps = max(1, min(args.steps, args.ref_max_steps))
+    # one warm-up step: the CPU step has no lazy initialisation after the first
     warm = min(args.warmup, 1)
+    steps = args.steps
+    clamp = None
+    if args.ref_max_steps is not None and steps > args.ref_max_steps:
+        steps = args.ref_max_steps
+        clamp = f"steps clamped from {args.steps} to {steps} (--ref-max-steps)"
     t_step, n = cpu_step_time(steps, warm, window="inject")
     value = n / t_step
+    W = workloads.SIZES[WORKLOAD_SIZE]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * t_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD + "_window_inject", "particles": n, "cpu_threads": cores,
+        "config": {"workload": workload_name("inject"), "particles": n, "cpu_threads": cores,
+                   "nx": W.nx, "nr": W.nkr + 1, "modes": W.modes,
                    "window": "AbsorbLayer=64, AddPlasma, IonsOnTop, moving at c (the e2e "
-                             "workload of the gb300 arm)"},
+                             "workload of the gb300 arm), from the same laser field",
+                   "warmup_note": f"warm-up {warm} of {args.warmup}: the CPU step has no lazy "
+                                  "initialisation after its first step",
+                   "steps_note": clamp},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
                          "sample": f"{steps} full steps of the workload (after {warm} warm-up) "
                                    "with the oracle's C/OpenMP restatement of the reference "
@@ -343,64 +307,103 @@ def run_reference(args):
     return 0
 
 
-def run_gb300(args):
+def time_steps(run, first, count, nmov, stream):
+    """CUDA-event time (ms) of `count` make_step calls from step `first`, and
+    the moving particles summed over them."""
     import torch
-
-    from chimera_gb300 import _lib, fimera
-
-    world, rank, local = dist_setup()
-    lib = _lib.load()
-    run, solver, el = build_run("gpu", "none", seed=1002 + rank)
-    if args.form == "split":
-        from chimera_gb300.split import SplitRun
-        run = SplitRun(None, fp64_run=run)
-
-        def nmov():
-            return run.num_moving
-    else:
-        def nmov():
-            return el.num_particles
-    n_moving = nmov()
-    stream = torch.cuda.current_stream()
-    # the clock sampler starts before the warm-up (its start-up stays out of
-    # the timed region) and samples through warm-up and timed steps
-    clocks = ClockSampler(local)
-    clocks.start()
-    for i in range(1, args.warmup + 1):
-        run.make_step(i)
-    torch.cuda.synchronize()
-    # L2: the particle state (0.53 GB per species in the split form, 1.9 GB
-    # in the FP64 form) is far larger than the 129 MB L2, so every step
-    # streams from HBM.
-    barrier(world)
-    torch.cuda.synchronize()
-    launches0 = lib.chm_launch_count()
-    flops0 = lib.chm_gemm_flops()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    t0 = time.perf_counter()
     psteps = 0
-    for i in range(args.warmup + 1, args.warmup + args.steps + 1):
+    for i in range(first, first + count):
         run.make_step(i)
         psteps += nmov()
     ev1.record(stream)
     torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+    return ev0.elapsed_time(ev1), psteps
+
+
+def run_gb300(args):
+    import torch
+
+    from chimera_gb300 import _lib, fimera
+    from chimera_gb300.split import SplitRun, transform_errors
+
+    world, rank, local = dist_setup()
+    lib = _lib.load()
+    W = workloads.SIZES[WORKLOAD_SIZE]
+    stream = torch.cuda.current_stream()
+    fp, solver, el = build_run("gpu", "none", seed=1003 + rank)
+    # the clock sampler starts before the warm-up (its start-up stays out of
+    # the timed region) and samples through warm-up and timed steps
+    clocks = ClockSampler(local)
+    clocks.start()
+    step = 0
+    # the plain FP64 form on the same workload: its own warm-up and steps
+    fp64 = None
+    if args.fp64_steps > 0 or args.form == "fp64":
+        nsteps = args.steps if args.form == "fp64" else args.fp64_steps
+        nwarm = args.warmup if args.form == "fp64" else 1
+        for _ in range(nwarm):
+            step += 1
+            fp.make_step(step)
+        torch.cuda.synchronize()
+        barrier(world)
+        ms64, ps64 = time_steps(fp, step + 1, nsteps, lambda: el.num_particles, stream)
+        step += nsteps
+        ms64 = max_over_ranks(world, ms64)
+        fp64 = {"value": world * ps64 / (ms64 / 1e3), "unit": METRIC, "steps": nsteps,
+                "warmup": nwarm, "ms_per_step": ms64 / nsteps, "dtype": "f64",
+                "what": "ChimeraRun.make_step (the plain FP64 form: FP64 particles, complex128 "
+                        "fields, FP64 products) on the same workload, device resident"}
+    if args.form == "split":
+        # the split form continues from the FP64 run's state
+        run = SplitRun(None, fp64_run=fp)
+        nmov = lambda: run.num_moving  # noqa: E731
+    else:
+        run = fp
+        nmov = lambda: el.num_particles  # noqa: E731
+    n_moving = nmov()
+    if args.form == "split":
+        for _ in range(args.warmup):
+            step += 1
+            run.make_step(step)
+        torch.cuda.synchronize()
+        # L2: the particle state (1.6 GB per species in the split form at
+        # cfg3) is far larger than the 129 MB L2, so every step streams from HBM
+        barrier(world)
+        torch.cuda.synchronize()
+        launches0 = lib.chm_launch_count()
+        flops0 = lib.chm_gemm_flops()
+        t0 = time.perf_counter()
+        ms, psteps = time_steps(run, step + 1, args.steps, nmov, stream)
+        wall = time.perf_counter() - t0
+        step += args.steps
+        launches = lib.chm_launch_count() - launches0
+        gemm_flops = lib.chm_gemm_flops() - flops0
+        ms_max = max_over_ranks(world, ms)
+        value = world * psteps / (ms_max / 1e3)
+    else:
+        ms_max = fp64["ms_per_step"] * fp64["steps"]
+        value = fp64["value"]
+        wall, launches, gemm_flops = None, None, 0.0
     barrier(world)
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    ms_max = max_over_ranks(world, ms)
-    launches = lib.chm_launch_count() - launches0
-    gemm_flops = lib.chm_gemm_flops() - flops0
-    value = world * (psteps / args.steps) * args.steps / (ms_max / 1e3)
+
+    # device error flags of the split form (must be clear)
+    flags = {"umma_status": int(lib.chm_sp_umma_status()),
+             "deposit_cells_dropped": int(lib.chm_sp_deposit_dropped())}
+    # split transforms against the FP64 kernels on this run's own fields
+    terr = None
+    if args.form == "split" and not args.no_errors:
+        terr = transform_errors(run)
 
     # stage profile of a few more steps (events around every C-ABI call)
     _lib.profile_begin()
     nprof = max(2, min(3, args.steps))
-    base = args.warmup + args.steps
-    for i in range(base + 1, base + nprof + 1):
+    for i in range(step + 1, step + nprof + 1):
         run.make_step(i)
+    step += nprof
     prof = _lib.profile_end()
     tot = sum(v[1] for v in prof.values())
     stages = {k.replace("chm_", ""): {"calls": c / nprof, "ms_per_step": t / nprof,
@@ -410,16 +413,17 @@ def run_gb300(args):
     peaks, peak_kind = load_peaks()
     roofline = stage_roofline(args.form, prof, nprof, n_moving, still_count(run, args.form),
                               peaks, peak_kind)
-    roofline["algorithmic_gemm_gflop_per_step"] = gemm_flops / args.steps / 1e9
+    roofline["algorithmic_gemm_gflop_per_step"] = gemm_flops / max(1, args.steps) / 1e9
+    del run, fp, solver, el
+    torch.cuda.empty_cache()
 
     # end to end through the public API with per-step host I/O
     e2e = None
     if not args.no_e2e:
-        run2, solver2, el2 = build_run("gpu", "inject", seed=2002 + rank)
+        run2, solver2, el2 = build_run("gpu", "inject", seed=2003 + rank)
         eb2 = lambda: solver2.Data["EB"]  # noqa: E731
         cnt2 = lambda: el2.num_particles  # noqa: E731
         if args.form == "split":
-            from chimera_gb300.split import SplitRun
             run2 = SplitRun(None, fp64_run=run2)
             eb2 = lambda: run2.EB  # noqa: E731
             cnt2 = lambda: run2.num_moving  # noqa: E731
@@ -466,14 +470,16 @@ def run_gb300(args):
         d2h = (fimera.io_bytes["d2h"] - d0) / args.steps + slots[0].element_size()
         if args.form == "split":
             d2h += 8 / args.steps  # the live-count read
+            run2.check_status()
         e2e = {"value": world * ps2 / t_e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "laser_a0_last": a0,
+               "d2h_bytes_per_step": d2h, "laser_a0_last": a0, "workload": workload_name("inject"),
                "what": "make_step with AddPlasma+AbsorbLayer window (the injected plasma's "
                        "host data copied H2D each step: random numbers and pattern tables in "
                        "the split form, the generated particles in the FP64 form) and a "
                        "laser-a0 read back each step (asynchronous copy to pinned memory, "
                        "consumed one step later)"}
         del run2, solver2, el2
+        torch.cuda.empty_cache()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -482,23 +488,29 @@ def run_gb300(args):
         t_cpu, n_cpu = cpu_step_time(args.cpu_steps, 0, window="inject")
         cpu = {"value": n_cpu / t_cpu, "unit": METRIC, "cores": cores, "kind": "port",
                "sample": f"{args.cpu_steps} full step(s) of the e2e workload (window with "
-                         "injection and absorption) with the oracle's C/OpenMP restatement of "
-                         "the reference kernels and step loop"}
+                         "injection and absorption, from the same laser field) with the "
+                         "oracle's C/OpenMP restatement of the reference kernels and step loop"}
 
+    split = args.form == "split"
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.form == "fp64" else "f32 (bf16x3 split tensor-core GEMMs)",
+        "dtype": "f32 (bf16x3 split tensor-core GEMMs)" if split else "f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": args.form, "particles_moving": n_moving,
-                   "particles_still": n_moving, "nx": SIZES[WORKLOAD_SIZE][0],
-                   "nr": SIZES[WORKLOAD_SIZE][1] + 1, "modes": 2,
+        "config": {"workload": workload_name(), "form": args.form, "particles_moving": n_moving,
+                   "particles_still": n_moving, "nx": W.nx, "nr": W.nkr + 1, "modes": W.modes,
+                   "ppc": list(W.ppc),
                    "parallelism": f"replicas{world}" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (particle state %s per species)"
-                         % ("0.53 GB" if args.form == "split" else "1.9 GB")},
+                   "l2": "inputs larger than L2 (particle state %.2f GB per species)"
+                         % (n_moving * (32 if split else 80) / 1e9)},
         "wall_s_timed": wall,
         "gpu_launches": launches,
+        "fp64_gpu": fp64,
+        "split_over_fp64": (value / fp64["value"]) if (split and fp64) else None,
+        "max_transform_err": max(terr.values()) if terr else None,
+        "transform_errors": terr,
+        "device_flags": flags,
         "roofline": roofline,
         "stages": stages,
         "clocks": clk,
@@ -512,6 +524,9 @@ def run_gb300(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+    if flags["umma_status"] or flags["deposit_cells_dropped"]:
+        print(f"device error flags set: {flags}", file=sys.stderr)
+        return 1
     return 0
 
 
@@ -581,25 +596,27 @@ def run_batched(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=1)
-    ap.add_argument("--ref-max-steps", type=int, default=5)
+    ap.add_argument("--ref-max-steps", type=int, default=None,
+                    help="reference arm: at most this many timed steps (recorded in the line)")
+    ap.add_argument("--fp64-steps", type=int, default=2,
+                    help="timed steps of the plain FP64 form in the same run (0: skip)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-errors", action="store_true")
     ap.add_argument("--form", default="split", choices=["fp64", "split"],
                     help="fp64 = plain FP64 form; split = split-precision form")
     ap.add_argument("--batched", type=int, default=0,
                     help="run the batched workload with this many instances instead")
-    ap.add_argument("--size", default="cfg2", choices=sorted(SIZES),
-                    help="cfg2 = the benchmark workload; prof, small = reduced cases for profiling")
+    ap.add_argument("--size", default="cfg3", choices=sorted(workloads.SIZES),
+                    help="cfg3 = the benchmark workload; cfg2, cfg1 the smaller configurations; "
+                         "prof3, prof, spec, small = reduced cases for profiling")
     args = ap.parse_args()
-    global WORKLOAD_SIZE, WORKLOAD
+    global WORKLOAD_SIZE
     WORKLOAD_SIZE = args.size
-    if args.size != "cfg2":
-        nx, nkr, ppc = SIZES[args.size]
-        WORKLOAD = f"lwfa_nx{nx}_nr{nkr}_m2_ppc{ppc[0]}x{ppc[1]}x{ppc[2]}"
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":

@@ -281,6 +281,11 @@ class SplitRun:
         # (chimera_main.py:277-284); it starts empty, as the reference's
         self.have_bg = False
         self._inject_order = {}  # particle order of injected batches, per shape
+        # the device error flags (a tensor-core CTA that gave up on a wait, a
+        # deposit cell outside its block box) are read every this many steps
+        # and by check_status(); either raises
+        self.check_every = 64
+        self._steps = 0
 
     # ------------------------------------------------------------------
     def _moving(self):
@@ -436,6 +441,21 @@ class SplitRun:
         self._project_fields_and_push()
         for spc, P in self._moving():
             _lib.call("chm_sp_count_live", P.counters.data_ptr(), P.n, st)
+        self._steps += 1
+        if self.check_every and self._steps % self.check_every == 0:
+            self.check_status()
+
+    def check_status(self):
+        """Raise if a device error flag is set: a tensor-core product CTA
+        that gave up on a bounded wait (its tile was not written) or deposit
+        cells dropped outside their block box (corrupt positions).  Reading
+        the flags waits for the work queued so far."""
+        lib = _lib.load()
+        umma = lib.chm_sp_umma_status()
+        dropped = lib.chm_sp_deposit_dropped()
+        if umma or dropped:
+            raise _lib.ChimeraError(
+                f"split form: tensor-core status {umma}, {dropped} deposit cells dropped")
 
     def _project_fields_and_push(self):
         A = self.solver.Args
@@ -594,6 +614,7 @@ class SplitRun:
 
     def to_fp64(self):
         """Write the split state into the FP64 Data of the solver and species."""
+        self.check_status()
         D = self.solver.Data
         D["EG_fb"].copy_(self.EG)
         D["EB"].copy_(self.EB)
@@ -613,3 +634,86 @@ class SplitRun:
                       d["momenta"].stride(1), d["weights"].data_ptr(), d["weights"].stride(0),
                       self.X0, self.dx, _stream())
         return self
+
+
+def transform_errors(run: SplitRun) -> dict:
+    """Relative L2 error of each split transform against the FP64 kernels on
+    the run's own current data (converted exactly to FP64): fb_in of the last
+    current deposit (the int64 accumulators, with DepFact), fb_grad of the
+    charge spectrum, the 3-iteration Poisson correction of J_fb, curl +
+    PoissFact of G and fb_eb_out with eb_correction of E and B.  Leaves the
+    run's state unchanged."""
+    S, A = run.solver, run.solver.Args
+    nx, nr, nkr, nm = run.nx, run.nr, run.nkr, run.nm
+    st = _stream()
+    ws, wsb = run.ws.data_ptr(), run.ws.numel()
+    dev = run.device
+    c128 = lambda t: t.to(torch.complex128)  # noqa: E731
+    rel = lambda a, b: float(torch.linalg.vector_norm(a.to(torch.complex128) - b)  # noqa: E731
+                             / torch.linalg.vector_norm(b))
+    errs = {}
+    leftX = float(A["leftX"])
+    # fb_in of the current accumulators
+    acc = run.accJ.view(3, nm, nr, nx, 2).permute(3, 2, 1, 0, 4)  # (nx, nr, nm, 3, {re, im})
+    J = torch.complex(acc[..., 0].to(torch.float64), acc[..., 1].to(torch.float64))
+    J = J / run.scaleJ[0]
+    J[:, 1] -= J[:, 0]
+    J[:, 0] = 0
+    Jf = chimera.fortran_empty(tuple(J.shape), torch.complex128, dev)
+    Jf.copy_(J)
+    del J
+    out = chimera.fortran_zeros((nx, nkr, nm, 3), torch.complex64, dev)
+    _lib.call("chm_sp_fb_in_acc", out.data_ptr(), run.accJ.data_ptr(), run.scaleJ.data_ptr(), None,
+              None, leftX, run.kx64.data_ptr(), C.addressof(run.ops["InCurr"]),
+              run.depfact.data_ptr(), nx, nr, nkr, nm, 3, ws, wsb, st)
+    ref = chimera._fb_in(chimera.fortran_zeros((nx, nkr, nm, 3), device=dev), Jf, leftX,
+                         *A["FBCurrIn"], 3, fact=S.dev["DepFact"])
+    errs["fb_in"] = rel(out, ref)
+    del Jf, ref
+    FBD = (A["DpS2S"], A["DmS2S"], A["kx"])
+    if run.space_charge:
+        g = chimera.fortran_zeros((nx, nkr, nm, 3), torch.complex64, dev)
+        _lib.call("chm_sp_fb_grad", g.data_ptr(), run.Rfb.data_ptr(), C.addressof(run.ops["Dp"]),
+                  C.addressof(run.ops["Dm"]), run.kx32.data_ptr(), nx, nkr, nm, ws, wsb, st)
+        ref = chimera.fb_grad(chimera.fortran_zeros((nx, nkr, nm, 3), device=dev), c128(run.Rfb),
+                              *FBD)
+        errs["fb_grad"] = rel(g, ref)
+        del g, ref
+    if run.poisson:
+        Js = run.Jfb.clone(memory_format=torch.preserve_format)
+        sc = run.space_charge
+        _lib.call("chm_sp_poisson", Js.data_ptr(), run.gprv.data_ptr() if sc else None,
+                  run.gnxt.data_ptr() if sc else None, run.pf.data_ptr(), float(A["dt_inv"]),
+                  C.addressof(run.ops["Dp"]), C.addressof(run.ops["Dm"]), run.kx32.data_ptr(),
+                  nx, nkr, nm, 3, int(sc), ws, wsb, st)
+        Jd = c128(run.Jfb)
+        for _ in range(3):
+            v = Jd.clone(memory_format=torch.preserve_format)
+            v = chimera.fb_graddiv(v, *FBD)
+            if sc:
+                Jd = chimera.poiss_corr(Jd, v, c128(run.gprv), c128(run.gnxt), A["dt_inv"],
+                                        S.dev["PoissFact"])
+            else:
+                Jd = chimera.omp_add_vec(Jd, chimera.omp_mult_vec(v, S.dev["PoissFact"]))
+        errs["poisson"] = rel(Js, Jd)
+        del Js, Jd, v
+    G = run.EG[:, :, :, 3:]
+    Bs = chimera.fortran_zeros((nx, nkr, nm, 3), torch.complex64, dev)
+    _lib.call("chm_sp_rot_b", Bs.data_ptr(), G.data_ptr(), run.pf.data_ptr(),
+              C.addressof(run.ops["Dp"]), C.addressof(run.ops["Dm"]), run.kx32.data_ptr(), nx, nkr,
+              nm, ws, wsb, st)
+    Gd = chimera.fortran_empty((nx, nkr, nm, 3), torch.complex128, dev)
+    Gd.copy_(G)
+    ref = chimera.fb_rot(chimera.fortran_zeros((nx, nkr, nm, 3), device=dev), Gd, *FBD)
+    ref = chimera.omp_mult_vec(ref, S.dev["PoissFact"])
+    errs["rot_b"] = rel(Bs, ref)
+    del Gd, ref
+    EB = chimera.fortran_zeros((nx, nr, nm, 6), torch.complex64, dev)
+    _lib.call("chm_sp_fb_eb_out", EB.data_ptr(), run.EG.data_ptr(), Bs.data_ptr(), leftX,
+              run.kx64.data_ptr(), C.addressof(run.ops["Out"]), nx, nr, nkr, nm, ws, wsb, st)
+    ref = chimera.fb_eb_out(chimera.fortran_zeros((nx, nr, nm, 6), device=dev), c128(run.EG),
+                            c128(Bs), leftX, A["kx"], A["Out"], eb_mode=1)
+    errs["fb_eb_out"] = rel(EB, ref)
+    del EB, ref, Bs
+    run.check_status()
+    return errs

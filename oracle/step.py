@@ -299,3 +299,45 @@ class CpuRun:
         self.update_fields()
         self.project_fields()
         self.push_velocs()
+
+
+def add_gauss_beam(solver, S):
+    """Gaussian laser pulse added to solver.Data["EG_fb"] in spectral space,
+    for the plain (non-envelope) solver, with the oracle's kernels: the
+    reference's Solver.add_gauss_beam (moduls/solvers.py:555-610) restated on
+    numpy.  solver: a Solver built on the CPU; S: the laser dict."""
+    A = solver.Args
+    k0, a0 = 2 * np.pi * S["k0"], 2 * np.pi * S["a0"]
+    Xf = S["x0"] - S["x_foc"]
+    nx, nkr, nm = A["Nx"], A["Nkr"], A["Mtot"]
+    X, R = A["Xgrid"][:, None], A["Rgrid"][None, :]
+    prof = (a0 * np.cos(k0 * (X - S["x0"])) * np.exp(-(X - S["x0"]) ** 2 / S["Lx"] ** 2
+                                                     - R ** 2 / S["LR"] ** 2)
+            * (abs(R) < 3.5 * S["LR"]) * (abs(X - S["x0"]) < 3.5 * S["Lx"]))
+    prof[:, 0] = 0.0
+    scl = np.zeros((nx, A["Nr"], nm), complex, order="F")
+    scl[:, :, 0] = prof
+    scl_fb = orc.fb_scl_in(np.zeros((nx, nkr, nm), complex, order="F"), scl, A["leftX"], A["kx"],
+                           A["In"])
+    EE = np.zeros((nx, nkr, nm, 3), complex, order="F")
+    EE[:, :, :, 2] = scl_fb / nx
+    # div_clean (solvers.py:644-650): EE + PoissFact grad(div(EE))
+    v = orc.fb_graddiv(EE.copy(order="F"), A["DpS2S"], A["DmS2S"], A["kx"])
+    v = orc.omp_mult_vec(v, A["PoissFact"])
+    EE = orc.omp_add_vec(EE, v)
+    kx_g = A["kx_g"][:, :, None, None]
+    w4 = A["w"][:, :, :, None]
+    DT = -1.j * w4 * np.sign(kx_g + (kx_g == 0))
+    GG = DT * EE
+    cw, sw = np.cos(w4 * Xf), np.sin(w4 * Xf)
+    E1 = cw * EE + sw / w4 * GG
+    G1 = -w4 * sw * EE + cw * GG
+    ph = np.exp(1.j * kx_g * Xf)
+    eg = solver.Data["EG_fb"]
+    eg[:, :, :, :3] += torch_from(E1 * ph)
+    eg[:, :, :, 3:] += torch_from(G1 * ph)
+
+
+def torch_from(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a))

@@ -49,3 +49,14 @@ def test_cpu_step_driver_matches_reference_step_loop(golden, tag, window):
         assert rel_l2(run.D[k], golden[f"{tag}/solver/{k}"]) < 1e-13, k
     for k in ("coords", "momenta", "weights"):
         assert rel_l2(el.Data[k], golden[f"{tag}/electrons/{k}"]) < 1e-13, k
+
+
+def test_cpu_laser_init_matches_reference(golden):
+    """oracle.step.add_gauss_beam (the benchmark's CPU arm) reproduces the
+    reference's spectral laser initialisation (solvers.py:555-610)."""
+    import torch
+    from oracle.step import add_gauss_beam
+    solver, *_ = _lpa(False)
+    solver.Data["EG_fb"] = torch.zeros(tuple(solver.Data["EG_fb"].shape), dtype=torch.complex128)
+    add_gauss_beam(solver, {"a0": 1.0, "k0": 1.0, "x0": -2.5, "x_foc": 2.0, "Lx": 1.5, "LR": 2.5})
+    assert rel_l2(solver.Data["EG_fb"].numpy(), golden["lpa/EG_fb_init"]) < 1e-12
