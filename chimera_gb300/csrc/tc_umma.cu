@@ -19,11 +19,14 @@
 //
 // One CTA computes a 128-row x TNC-column tile (TNC <= 128, a multiple of
 // 16) of one problem of a batch; grid = (row tiles, column tiles, problems):
-//   - warps 0..3 (one thread per row) load the FP32 A block of every 32-wide
-//     K step, split it into the three BF16 terms, store them into the stage
-//     in the tensor-core operand layout (K-major core matrices of 8 rows x 16
-//     bytes), drain the H chunks into their registers and write the tile;
-//   - warp 4's lane 0 streams the prepared B terms of the step with bulk-copy
+//   - warps 0..7 are the row threads: warp w takes rows 32 (w % 4) .. +31
+//     (the TMEM lanes its quarter may access) and half w / 4 of every 32-wide
+//     K step and of the tile's columns.  Each thread loads its 16 FP32 A
+//     values of the step, splits them into the three BF16 terms, stores them
+//     into the stage in the tensor-core operand layout (K-major core
+//     matrices of 8 rows x 16 bytes), drains its 64 columns of the H chunks
+//     into registers and writes them;
+//   - warp 8's lane 0 streams the prepared B terms of the step with bulk-copy
 //     TMA (cp.async.bulk, completion on an mbarrier) and issues the 12
 //     tcgen05.mma of the step (6 term pairs x 2 K halves), releasing the
 //     stage with tcgen05.commit.
@@ -44,8 +47,10 @@ constexpr int TH = 128;                 // rows per tile (UMMA M)
 constexpr int KB = 32;                  // K step (elements)
 constexpr int kChunk = 2;               // K steps per H accumulator chunk
 constexpr int STAGES = 4;
-constexpr int kProducers = TH;          // one thread per row
+constexpr int kProducers = 2 * TH;      // two threads per row (K and column halves)
 constexpr int kThreads = kProducers + 32;
+constexpr int KH = KB / 2;              // K values of a step per row thread
+constexpr int CH = TH / 2;              // tile columns per row thread
 constexpr int kMaxBatch = 64;
 constexpr long long kSpinLimit = 1LL << 20;  // try_wait polls; each may block briefly
 constexpr uint32_t kATermBytes = TH * KB * 2;  // one BF16 term of the A block
@@ -157,14 +162,14 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// acc[0 .. tnc) += the tnc accumulator columns starting at column `col`
-// (tnc a multiple of 16, at most 128; loads issued in pairs before one wait)
-__device__ __forceinline__ void tmem_add_row(float (&acc)[TH], uint32_t tmem_lane, uint32_t col, int tnc) {
+// acc[0 .. nc) += the nc accumulator columns starting at column `col`
+// (nc a multiple of 16, at most 64; loads issued in pairs before one wait)
+__device__ __forceinline__ void tmem_add_row(float (&acc)[CH], uint32_t tmem_lane, uint32_t col, int nc) {
 #pragma unroll
-  for (int c0 = 0; c0 < TH; c0 += 32) {
-    if (c0 < tnc) {
+  for (int c0 = 0; c0 < CH; c0 += 32) {
+    if (c0 < nc) {
       uint32_t va[16], vb[16];
-      const bool two = c0 + 16 < tnc;
+      const bool two = c0 + 16 < nc;
       tmem_ld16(va, tmem_lane + col + (uint32_t)c0);
       if (two) tmem_ld16(vb, tmem_lane + col + (uint32_t)(c0 + 16));
       tmem_wait_ld();
@@ -246,15 +251,19 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
   const uint32_t tmem = tmem_base;
   const uint32_t colL = 2u * (uint32_t)tnc;  // the correction-pair accumulator
 
-  float acc[TH];  // this row's sum of the drained H chunks (producer threads)
+  // row threads: rows 32 (warp % 4) + lane, K half and column half warp / 4
+  const int half = (warp >> 2) & 1;
+  const int col0 = half * CH;                                  // first tile column of this thread
+  const int ncol = max(0, min(CH, tnc - col0));                // its columns (multiple of 16)
+  float acc[CH];  // this thread's sum of the drained H chunks
 #pragma unroll
-  for (int j = 0; j < TH; ++j) acc[j] = 0.0f;
+  for (int j = 0; j < CH; ++j) acc[j] = 0.0f;
   const uint32_t tmem_lane = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   volatile int *vfail = &fail;
 
   if (threadIdx.x < kProducers) {
-    // ---- producers: FP32 A row -> three BF16 terms in the stage; drain H
-    const int r = threadIdx.x;
+    // ---- row threads: FP32 A -> three BF16 terms in the stage; drain H
+    const int r = (warp & 3) * 32 + (threadIdx.x & 31);
     const long long gm = (long long)mt * TH + r;
     const bool row_ok = gm < A.M;
     long long src = gm;
@@ -265,11 +274,11 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
       if ((gm & 1) == 0) neg = 0x80008000u;
     }
     const float *Arow = Q.A + src;
-    float v[KB];
+    float v[KH];
     auto load = [&](int kb) {
 #pragma unroll
-      for (int k = 0; k < KB; ++k) {
-        const int gk = kb * KB + k;
+      for (int k = 0; k < KH; ++k) {
+        const int gk = kb * KB + half * KH + k;
         v[k] = (row_ok && gk < A.K) ? Arow[(long long)gk * A.M] : 0.0f;
       }
     };
@@ -282,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
         atomicCAS(&g_umma_error, 0, 4);
       } else {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        tmem_add_row(acc, tmem_lane, (uint32_t)(b * tnc), tnc);
+        tmem_add_row(acc, tmem_lane, (uint32_t)(b * tnc + col0), ncol);
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       }
       mbar_arrive(&hempty[b]);
@@ -300,14 +309,15 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
         unsigned char *st = smem + (size_t)s * stage_bytes;
         const int rr = r;
 #pragma unroll
-        for (int kg = 0; kg < KB / 8; ++kg) {
+        for (int kh = 0; kh < KH / 8; ++kh) {
+          const int kg = half * (KH / 8) + kh;  // 8-wide K group of the step
           uint32_t w0[4], w1[4], w2[4];
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             uint32_t t0[2], t1[2], t2[2];
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
-              const float x = v[kg * 8 + 2 * q + e];
+              const float x = v[kh * 8 + 2 * q + e];
               const __nv_bfloat16 b0 = __float2bfloat16_rn(x);
               const float r1 = x - __bfloat162float(b0);
               const __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
@@ -456,8 +466,8 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
     fac_smem = true;
   }
   if (use && threadIdx.x < kProducers) {
-    tmem_add_row(acc, tmem_lane, colL, tnc);  // + the correction pairs
-    const int row = threadIdx.x;
+    tmem_add_row(acc, tmem_lane, colL + (uint32_t)col0, ncol);  // + the correction pairs
+    const int row = (warp & 3) * 32 + (threadIdx.x & 31);
     const long long gm = (long long)mt * TH + row;
     float2 sh = make_float2(1.f, 0.f);
     if (EPI != TC_EPI_STORE && gm < A.M) sh = A.shift[gm >> 1];
@@ -465,10 +475,10 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
     const float *fac = Q.fac;
     const bool rok = gm < A.M;
 #pragma unroll
-    for (int j = 0; j < TH; ++j) {
-      if (j < tnc) {
-        float x = acc[j];
-        const int n = n0 + j;
+    for (int jj = 0; jj < CH; ++jj) {
+      if (jj < ncol) {
+        float x = acc[jj];
+        const int j = col0 + jj, n = n0 + j;
         if (EPI != TC_EPI_STORE) {
           // rows 2x (re) and 2x+1 (im) sit in adjacent lanes
           const float other = __shfl_xor_sync(0xffffffffu, x, 1);
