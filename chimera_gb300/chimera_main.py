@@ -4,6 +4,11 @@ The control flow, the order of the kernel calls and the moving-window logic
 follow the reference; every kernel is a CUDA launch on the current torch
 stream, so a step issues no host synchronisation except where particles are
 absorbed or injected (the new particle count is read back).
+
+This module restates the reference's GPLv3-licensed Python layer
+(hightower8083/chimera) statement by statement to keep its API as a
+drop-in; it is a derivative of that code and is distributed under the GNU
+General Public License, version 3 or later, as the reference is.
 """
 from __future__ import annotations
 

@@ -542,12 +542,21 @@ extern "C" int chm_dep_curr_noalloc(const double *coord, int64_t x_cs, int64_t x
                                     double leftX, const double *rgrid, double dx_inv,
                                     double dr_inv, int64_t np, int64_t nx, int64_t nr, int64_t nm,
                                     void *stream) {
-  const int64_t need = chm_dep_ws_bytes(nx, nr, nm, 3, np);
-  if (need > kNoAllocScratchBytes || nx <= 0 || nr <= 0 || nm <= 0) {
-    set_error("dep_curr_noalloc: a (%lld, %lld, %lld, 3) grid needs %lld bytes of scratch, more "
-              "than the %lld-byte static array; use chm_dep_curr with a workspace",
-              (long long)nx, (long long)nr, (long long)nm, (long long)need,
-              (long long)kNoAllocScratchBytes);
+  // the grid's own rules first (as chm_dep_curr checks them), then its size
+  // against the static array, without an overflowing product
+  if (nx <= 1 || nr <= 1 || nm < 1) {
+    set_error("dep_curr_noalloc: bad grid (%lld, %lld, %lld): nx > 1, nr > 1 and nm >= 1 are "
+              "required", (long long)nx, (long long)nr, (long long)nm);
+    return CHM_ERR_ARG;
+  }
+  int64_t nodes = 0, need = 0;
+  const bool big = __builtin_mul_overflow(nx, nr, &nodes) || __builtin_mul_overflow(nodes, nm, &nodes) ||
+                   nodes > (kNoAllocScratchBytes - 8 * kRedBlocks - 256) / 48;
+  if (!big) need = chm_dep_ws_bytes(nx, nr, nm, 3, np);
+  if (big || need > kNoAllocScratchBytes) {
+    set_error("dep_curr_noalloc: a (%lld, %lld, %lld, 3) grid needs more scratch than the "
+              "%lld-byte static array; use chm_dep_curr with a workspace",
+              (long long)nx, (long long)nr, (long long)nm, (long long)kNoAllocScratchBytes);
     return CHM_ERR_RANGE;
   }
   void *scratch = nullptr;

@@ -16,6 +16,11 @@ kilobytes, come to the host.  Field-like returns (Fields, FieldsFB,
 Density, Particles) are device tensors, as the ``Data`` entries they copy;
 the energy and power profiles are numpy arrays, as the reference writes them
 to text files.
+
+This module restates the reference's GPLv3-licensed Python layer
+(hightower8083/chimera) statement by statement to keep its API as a
+drop-in; it is a derivative of that code and is distributed under the GNU
+General Public License, version 3 or later, as the reference is.
 """
 from __future__ import annotations
 

@@ -2,6 +2,11 @@
 
 The report texts are kept identical to the reference's so that logs of a run
 read the same; every printed line is also appended to ``msg.log``.
+
+This module restates the reference's GPLv3-licensed Python layer
+(hightower8083/chimera) statement by statement to keep its API as a
+drop-in; it is a derivative of that code and is distributed under the GNU
+General Public License, version 3 or later, as the reference is.
 """
 from __future__ import annotations
 

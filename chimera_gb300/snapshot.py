@@ -14,6 +14,11 @@ Reading restores every stored key of the run's current ``Data`` / ``Args``:
 grids are copied into the existing device tensors (their Fortran layout is
 kept), particle stores are resized to the stored particle count, arrays and
 scalars of ``Args`` are replaced.
+
+This module restates the reference's GPLv3-licensed Python layer
+(hightower8083/chimera) statement by statement to keep its API as a
+drop-in; it is a derivative of that code and is distributed under the GNU
+General Public License, version 3 or later, as the reference is.
 """
 from __future__ import annotations
 

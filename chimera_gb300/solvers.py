@@ -10,6 +10,11 @@ order and every per-step operation calls the CUDA kernels through
 argument packs the kernels are called with (``FBDiff``, ``DepProj``,
 ``FBCurrIn``, ``FBIn``, ``FBout``, ``FBoutFull``) hold device copies, so
 ``fimera.fb_vec_in(J_fb, J, leftX, *Args['FBCurrIn'])`` reads no host memory.
+
+This module restates the reference's GPLv3-licensed Python layer
+(hightower8083/chimera) statement by statement to keep its API as a
+drop-in; it is a derivative of that code and is distributed under the GNU
+General Public License, version 3 or later, as the reference is.
 """
 from __future__ import annotations
 

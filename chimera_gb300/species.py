@@ -7,6 +7,11 @@ Generation (``gen_parts``) runs on the host in numpy with the reference's
 random-number call sequence, so a seeded ``np.random`` gives the same
 particles as the reference; pushing, sorting, absorption and compaction run
 as CUDA kernels through ``chimera_gb300.fimera``.
+
+This module restates the reference's GPLv3-licensed Python layer
+(hightower8083/chimera) statement by statement to keep its API as a
+drop-in; it is a derivative of that code and is distributed under the GNU
+General Public License, version 3 or later, as the reference is.
 """
 from __future__ import annotations
 

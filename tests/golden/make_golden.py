@@ -1,9 +1,10 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a container that has the reference checkout (default
-``/root/reference``; override with CHIMERA_REFERENCE):
+Run where a checkout of the reference is available, naming it:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <path-to-reference-checkout>
+
+(or set CHIMERA_REFERENCE to that path).
 
 The reference's own Python layer (moduls/solvers.py, species.py,
 chimera_main.py) is imported unmodified as the package ``chimera``.  Its
@@ -34,7 +35,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("CHIMERA_REFERENCE", "/root/reference")
+REF = os.environ.get("CHIMERA_REFERENCE")
+if len(sys.argv) > 1:
+    REF = sys.argv[1]
 
 
 def import_reference():
@@ -232,4 +235,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(REF):
+        sys.exit("usage: make_golden.py <path-to-reference-checkout> (or set CHIMERA_REFERENCE)")
     main()

@@ -64,3 +64,17 @@ def test_no_alloc_deposit_rejects_oversized_grid(cuda):
                                   4096, 513, 3, None)
     assert rc == 5  # CHM_ERR_RANGE
     assert b"static array" in lib.chm_last_error()
+
+
+def test_no_alloc_deposit_rejects_bad_and_overflowing_dims(cuda):
+    from chimera_gb300 import _lib
+    lib = _lib.load()
+    # dimensions whose product wraps a 64-bit integer are rejected as too large
+    rc = lib.chm_dep_curr_noalloc(None, 1, 3, None, 1, 3, None, 1, None, 0.0, None, 1.0, 1.0, 0,
+                                  1 << 40, 1 << 20, 1 << 10, None)
+    assert rc == 5 and b"static array" in lib.chm_last_error()
+    # grids the deposit does not accept get their own message
+    for dims in ((0, 33, 2), (256, 1, 2), (256, 33, 0), (-5, 33, 2)):
+        rc = lib.chm_dep_curr_noalloc(None, 1, 3, None, 1, 3, None, 1, None, 0.0, None, 1.0, 1.0,
+                                      0, *dims, None)
+        assert rc == 1 and b"bad grid" in lib.chm_last_error(), dims
