@@ -724,9 +724,11 @@ struct Batch32 {
   }
 };
 
-int gemm32(const Batch32 &b, int M, int N, int K, int epi, const float2 *shift, cudaStream_t st) {
+// W: the caller's remaining workspace (by value: the split A planes live
+// there only while the product runs, stream-ordered before later kernels)
+int gemm32(const Batch32 &b, int M, int N, int K, int epi, const float2 *shift, Ws W, cudaStream_t st) {
   if (b.count == 0) return CHM_OK;
-  return tc_gemm_launch(b.p, b.count, M, N, K, epi, shift, st);
+  return tc_gemm_launch(b.p, b.count, M, N, K, epi, shift, W.p, W.left, st);
 }
 
 struct Fb32 {
@@ -747,7 +749,11 @@ extern "C" {
 int64_t chm_sp_fb_ws_bytes(int64_t nx, int64_t nr, int64_t nkr, int64_t nm) {
   const i64 rows = nr - 1 > nkr ? nr - 1 : nkr;
   const i64 plane = 8 * nx * (rows > nkr ? rows : nkr);
-  return 4 * r256(8 * nx) + r256(plane * nm * 6) + 8 * r256(plane * (nm + 2)) + 8192;
+  // + the BF16 split of the A planes of the largest product batch (6 nm
+  // planes in fb_eb_out and the curl, 4 (nm + 1) in the Poisson correction)
+  const i64 most = 6 * nm > 4 * (nm + 1) ? 6 * nm : 4 * (nm + 1);
+  return 4 * r256(8 * nx) + r256(plane * nm * 6) + 8 * r256(plane * (nm + 2)) + 8192 +
+         tc_split_bytes((int)(2 * nx), (int)rows, (int)most);
 }
 
 // fb_vec_in / fb_scl_in of a deposit accumulator (ncomp 3 or 1), with
@@ -790,7 +796,7 @@ int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, con
     for (i64 l = 0; l < ncomp; ++l)
       b.add(tmp + nx * nrr * (m + nm * l), reinterpret_cast<float2 *>(out_c64) + nx * nkr * (m + nm * l),
             fact + nx * nkr * m, In.mode[m]);
-  return gemm32(b, (int)(2 * nx), (int)nkr, (int)nrr, TC_EPI_SHIFT_FAC, shift, st);
+  return gemm32(b, (int)(2 * nx), (int)nkr, (int)nrr, TC_EPI_SHIFT_FAC, shift, W, st);
 }
 
 // fb_eb_out + eb_correction (fb_io.f90:182-228, grid_deps.f90:219-266)
@@ -818,7 +824,7 @@ int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double 
                                  : reinterpret_cast<const float2 *>(b_c64) + nx * nkr * (m + nm * (l - 3)));
       b.add(src, tmp + nx * nrr * (m + nm * l), nullptr, Out.mode[m]);
     }
-  int rc = gemm32(b, (int)(2 * nx), (int)nrr, (int)nkr, TC_EPI_SHIFT, shift, st);
+  int rc = gemm32(b, (int)(2 * nx), (int)nrr, (int)nkr, TC_EPI_SHIFT, shift, W, st);
   if (rc) return rc;
   Lines32 L{};
   L.in = tmp;
@@ -892,7 +898,7 @@ int neighbours32(Fb32 &F, const float2 *in, i64 cs, int ncomp, int nin, int nout
       }
     }
   }
-  return gemm32(b, (int)(2 * F.nx), (int)F.nk, (int)F.nk, TC_EPI_STORE, nullptr, F.st);
+  return gemm32(b, (int)(2 * F.nx), (int)F.nk, (int)F.nk, TC_EPI_STORE, nullptr, F.ws, F.st);
 }
 
 }  // namespace
@@ -1001,7 +1007,7 @@ int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, cons
       }
       bg.add(scl + plane * (m + 1), up[0] + plane * m, nullptr, F.Dp.mode[m]);
     }
-    rc = gemm32(bg, (int)(2 * nx), (int)nkr, (int)nkr, TC_EPI_STORE, nullptr, F.st);
+    rc = gemm32(bg, (int)(2 * nx), (int)nkr, (int)nkr, TC_EPI_STORE, nullptr, F.ws, F.st);
     if (rc) return rc;
     GradArgs A{};
     A.nx = nx;

@@ -134,15 +134,15 @@ inline i64 rup(i64 a, i64 b) { return (a + b - 1) / b * b; }
 namespace chm {
 
 int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, const float2 *shift,
-                   cudaStream_t st);
+                   void *ws, long long ws_bytes, cudaStream_t st);
 
 // engine 1: tensor cores (every product of the split form); 0: the FP32 SIMT
 // kernel, reached only through chm_sp_gemm as the tests' accuracy reference
 static int launch(const TcProblem *p, int count, int M, int N, int K, int epi, const float2 *shift,
-                  cudaStream_t st, int engine) {
+                  void *ws, long long ws_bytes, cudaStream_t st, int engine) {
   if (count <= 0) return CHM_OK;
   count_gemm_flops((double)count * 2.0 * M * N * K);
-  if (engine == 1) return tc_umma_launch(p, count, M, N, K, epi, shift, st);
+  if (engine == 1) return tc_umma_launch(p, count, M, N, K, epi, shift, ws, ws_bytes, st);
   for (int c0 = 0; c0 < count; c0 += kMaxProb) {
     Prob32 b{};
     b.count = count - c0 < kMaxProb ? count - c0 : kMaxProb;
@@ -162,8 +162,8 @@ static int launch(const TcProblem *p, int count, int M, int N, int K, int epi, c
 }
 
 int tc_gemm_launch(const TcProblem *p, int count, int M, int N, int K, int epi, const float2 *shift,
-                   cudaStream_t st) {
-  return launch(p, count, M, N, K, epi, shift, st, 1);
+                   void *ws, long long ws_bytes, cudaStream_t st) {
+  return launch(p, count, M, N, K, epi, shift, ws, ws_bytes, st, 1);
 }
 
 TcMatrices tc_matrices(const chm_sp_ops *ops) {
@@ -220,10 +220,8 @@ int chm_sp_prepare_ops(chm_sp_ops *ops, const double *mats, int64_t K, int64_t N
 }
 
 int64_t chm_sp_gemm_ws_bytes(int64_t M, int64_t K, int64_t count) {
-  (void)M;
-  (void)K;
-  (void)count;
-  return 256;  // the tensor-core path splits A on chip; nothing is staged
+  // the BF16 split of the A planes of the tensor-core path
+  return tc_split_bytes((int)M, (int)K, (int)(count > 0 ? count : 1));
 }
 
 int chm_sp_gemm(float *C, const float *A, const chm_sp_ops *ops, int64_t mode, int64_t M, int engine,
@@ -231,11 +229,10 @@ int chm_sp_gemm(float *C, const float *A, const chm_sp_ops *ops, int64_t mode, i
   CHM_REQUIRE(C && A && ops && mode >= 0 && mode < ops->nmodes && M > 0 && M % 2 == 0,
               "sp_gemm: bad args");
   CHM_REQUIRE(engine == 0 || engine == 1, "sp_gemm: engine must be 0 (SIMT) or 1 (tensor cores)");
-  (void)ws;
-  (void)ws_bytes;
   TcMatrices T = tc_matrices(ops);
   TcProblem p{A, C, nullptr, T.mode[mode], 0};
-  return launch(&p, 1, (int)M, p.B.N, p.B.K, TC_EPI_STORE, nullptr, as_stream(stream), engine);
+  return launch(&p, 1, (int)M, p.B.N, p.B.K, TC_EPI_STORE, nullptr, ws, ws_bytes, as_stream(stream),
+                engine);
 }
 
 }  // extern "C"

@@ -44,9 +44,12 @@ struct TcProblem {
 
 enum { TC_EPI_STORE = 0, TC_EPI_SHIFT = 1, TC_EPI_SHIFT_FAC = 2 };
 
-// Batched product; no scratch (the split of A happens inside the kernel).
+// Batched product.  ws holds the BF16 split of every distinct A plane of
+// the batch (at most tc_split_bytes(M, K, count) bytes), in use until the
+// product completes on the stream.
 int tc_gemm_launch(const TcProblem *p, int count, int M, int N, int K, int epi,
-                   const float2 *shift, cudaStream_t st);
+                   const float2 *shift, void *ws, long long ws_bytes, cudaStream_t st);
+long long tc_split_bytes(int M, int K, int count);
 
 // Host view of a prepared operator set (chm_sp_ops) as per-mode operands.
 TcMatrices tc_matrices(const chm_sp_ops *ops);

@@ -4,6 +4,14 @@
 //   operator mode; computed as sum_{i+j<=2} A_i B_j with A = A0+A1+A2 and
 //   B = B0+B1+B2 the 3-term BF16 splits.
 //
+// Two kernels per batch:
+//   split_a_kernel  each distinct A plane (plane pointer + reflection) -> its
+//                   three BF16 terms in the tensor-core operand layout, one
+//                   8 KB block per (128-row tile, 32-wide K step) and term,
+//                   so the product kernel loads A like B, with bulk copies;
+//   umma_kernel     persistent: one CTA per SM walks the batch's output tiles
+//                   (128 rows x TNC columns, TNC <= 128 a multiple of 16).
+//
 // Accumulation.  The tensor core's FP32 accumulation is not round-to-nearest:
 // with all six term pairs summed into one TMEM accumulator the error grows
 // about linearly with the number of MMAs per accumulator (measured on GB300:
@@ -14,26 +22,27 @@
 //     row threads drain a finished chunk into FP32 registers (one
 //     round-to-nearest add per chunk) while the tensor core fills the other;
 //   - the five correction pairs (2^-8 and smaller relative to the result)
-//     go into a third accumulator L over the whole K range; its error is
-//     scaled by the same 2^-8.
+//     go into an accumulator L over the tile's whole K range (error scaled by
+//     the same 2^-8); L0 / L1 take turns over tiles, so the next tile's MMAs
+//     start while the row threads finish the previous tile.
+// TMEM: H0, H1, L0, L1 of TNC columns each (512 columns at TNC = 128).
 //
-// One CTA computes a 128-row x TNC-column tile (TNC <= 128, a multiple of
-// 16) of one problem of a batch; grid = (row tiles, column tiles, problems):
-//   - warps 0..7 are the row threads: warp w takes rows 32 (w % 4) .. +31
-//     (the TMEM lanes its quarter may access) and half w / 4 of every 32-wide
-//     K step and of the tile's columns.  Each thread loads its 16 FP32 A
-//     values of the step, splits them into the three BF16 terms, stores them
-//     into the stage in the tensor-core operand layout (K-major core
-//     matrices of 8 rows x 16 bytes), drains its 64 columns of the H chunks
-//     into registers and writes them;
-//   - warp 8's lane 0 streams the prepared B terms of the step with bulk-copy
-//     TMA (cp.async.bulk, completion on an mbarrier) and issues the 12
-//     tcgen05.mma of the step (6 term pairs x 2 K halves), releasing the
-//     stage with tcgen05.commit.
+// Roles in umma_kernel (320 threads):
+//   - warps 0..7, the row threads: warp w takes rows 32 (w % 4) .. +31 (the
+//     TMEM lanes its quarter may access) and column half w / 4 of the tile;
+//     they drain the H chunks and the L accumulator into registers and write
+//     the tile (complex shift and factor epilogues; the factor block of a
+//     tile is staged in shared memory after the stage ring);
+//   - warp 8, lane 0: issues the 12 tcgen05.mma of every K step (6 term
+//     pairs x 2 K halves) and the commits that release stages and
+//     accumulators;
+//   - warp 9, lane 0: streams the A and B terms of every K step into a
+//     4-stage ring with bulk-copy TMA (cp.async.bulk, mbarrier completion).
 // Every mbarrier wait has an iteration limit.  The pipeline waits use a limit
 // set from the host (chm_sp_set_umma_spin_limit, so that a test can make
-// them run out); on a timeout the CTA records an error, waits with the full
-// limit for its own bulk copies and MMAs, frees its TMEM and returns.
+// them run out); on a timeout the CTA records an error, stops issuing work,
+// waits with the full limit for its own bulk copies and MMAs, frees its TMEM
+// and returns.
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -47,14 +56,16 @@ constexpr int TH = 128;                 // rows per tile (UMMA M)
 constexpr int KB = 32;                  // K step (elements)
 constexpr int kChunk = 2;               // K steps per H accumulator chunk
 constexpr int STAGES = 4;
-constexpr int kProducers = 2 * TH;      // two threads per row (K and column halves)
-constexpr int kThreads = kProducers + 32;
-constexpr int KH = KB / 2;              // K values of a step per row thread
+constexpr int kRowThreads = 2 * TH;     // two threads per row (column halves)
+constexpr int kMmaThread = kRowThreads;         // warp 8, lane 0
+constexpr int kLoadThread = kRowThreads + 32;   // warp 9, lane 0
+constexpr int kThreads = kRowThreads + 64;
 constexpr int CH = TH / 2;              // tile columns per row thread
 constexpr int kMaxBatch = 64;
 constexpr long long kSpinLimit = 1LL << 20;  // try_wait polls; each may block briefly
-constexpr uint32_t kATermBytes = TH * KB * 2;  // one BF16 term of the A block
+constexpr uint32_t kATermBytes = TH * KB * 2;  // one BF16 term of an A block (8 KB)
 constexpr uint32_t kABytes = 3 * kATermBytes;
+constexpr int kSplitBlock = TH * KB;           // elements of one A block and term
 
 __device__ int g_umma_error;  // first failing CTA records a code here
 long long g_spin_limit = kSpinLimit;
@@ -99,21 +110,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long l
   return false;
 }
 
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
       : "memory");
 }
 
-__device__ __forceinline__ uint64_t smem_desc(const void *p, uint32_t lbo, uint32_t sbo) {
-  const uint64_t a = (smem_u32(p) & 0x3FFFFu) >> 4;
-  uint64_t d = a;
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+// shared-memory matrix descriptor (SWIZZLE_NONE, K-major core matrices of 8
+// rows x 16 bytes: LBO = 128 B between K groups, SBO = 512 B between row
+// groups); the start address sits in bits 0..13 (address >> 4), so adding
+// (offset >> 4) to a descriptor moves it by offset bytes
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(128u >> 4) << 16;
+  d |= (uint64_t)(((KB / 8) * 128u) >> 4) << 32;
   d |= (uint64_t)1 << 46;  // descriptor version for tcgen05
-  // base offset 0, lbo mode 0, layout SWIZZLE_NONE (0)
   return d;
 }
 
@@ -142,10 +155,6 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
-}
-
-__device__ __forceinline__ uint32_t bf16_bits(__nv_bfloat16 b) {
-  return (uint32_t)__bfloat16_as_ushort(b);
 }
 
 // 16 consecutive FP32 accumulator columns of this warp's 32 TMEM lanes
@@ -183,15 +192,91 @@ __device__ __forceinline__ void tmem_add_row(float (&acc)[CH], uint32_t tmem_lan
   }
 }
 
+// AND of v over the row threads (named barrier 1, warps 0..7): their loop
+// exits stay uniform, so the named barriers of the factor epilogue never
+// wait for a thread that has left
+__device__ __forceinline__ bool row_threads_all(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n"
+      ".reg .pred p, q;\n"
+      "setp.ne.u32 q, %1, 0;\n"
+      "bar.red.and.pred p, 1, %2, q;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "n"(kRowThreads)
+      : "memory");
+  return r != 0;
+}
+
+// ----------------------------------------------------------------------
+// A split: FP32 plane -> three BF16 terms in the operand layout
+// ----------------------------------------------------------------------
+struct SplitJobs {
+  const float *A[kMaxBatch];
+  __nv_bfloat16 *T[kMaxBatch];  // term 0; term t at + t * term_stride
+  int reflect[kMaxBatch];
+};
+
+// x ~ t0 + t1 + t2 for two values at a time: each term the round-to-nearest
+// BF16 of the remainder (the pair conversions pack two values per register)
+__device__ __forceinline__ void split_pair(float x0, float x1, uint32_t &t0, uint32_t &t1, uint32_t &t2) {
+  const __nv_bfloat162 b0 = __floats2bfloat162_rn(x0, x1);
+  const float2 f0 = __bfloat1622float2(b0);
+  const float r0 = x0 - f0.x, r1 = x1 - f0.y;
+  const __nv_bfloat162 b1 = __floats2bfloat162_rn(r0, r1);
+  const float2 f1 = __bfloat1622float2(b1);
+  const __nv_bfloat162 b2 = __floats2bfloat162_rn(r0 - f1.x, r1 - f1.y);
+  t0 = *reinterpret_cast<const uint32_t *>(&b0);
+  t1 = *reinterpret_cast<const uint32_t *>(&b1);
+  t2 = *reinterpret_cast<const uint32_t *>(&b2);
+}
+
+// blockIdx = (row tile, K step, job); thread = row of the tile.  Element
+// (r, k) of a block sits at ((r / 8) * 4 + k / 8) * 64 + (r % 8) * 8 + k % 8;
+// rows past M and K values past K are zero.  A reflected plane: row (x, c)
+// is (c ? 1 : -1) * row ((M/2 - x) mod M/2, c) of the stored plane.
+__global__ void __launch_bounds__(TH) split_a_kernel(const __grid_constant__ SplitJobs J, int M, int K,
+                                                    int nkb, long long term_stride) {
+  const int r = threadIdx.x, mt = blockIdx.x, kb = blockIdx.y, job = blockIdx.z;
+  const long long gm = (long long)mt * TH + r;
+  const bool row_ok = gm < M;
+  long long src = gm;
+  float sgn = 1.0f;
+  if (J.reflect[job] && row_ok) {
+    const long long x = gm >> 1, nxh = M >> 1;
+    src = 2 * (x == 0 ? 0 : nxh - x) + (gm & 1);
+    if ((gm & 1) == 0) sgn = -1.0f;
+  }
+  const float *Arow = J.A[job] + src;
+  float v[KB];
+#pragma unroll
+  for (int k = 0; k < KB; ++k) {
+    const int gk = kb * KB + k;
+    v[k] = (row_ok && gk < K) ? sgn * __ldg(Arow + (long long)gk * M) : 0.0f;
+  }
+  __nv_bfloat16 *T = J.T[job] + ((long long)mt * nkb + kb) * kSplitBlock;
+#pragma unroll
+  for (int kg = 0; kg < KB / 8; ++kg) {
+    uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) split_pair(v[kg * 8 + 2 * q], v[kg * 8 + 2 * q + 1], w0[q], w1[q], w2[q]);
+    const int off = ((r >> 3) * (KB / 8) + kg) * 64 + (r & 7) * 8;
+    *reinterpret_cast<uint4 *>(T + off) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+    *reinterpret_cast<uint4 *>(T + term_stride + off) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+    *reinterpret_cast<uint4 *>(T + 2 * term_stride + off) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+  }
+}
+
 // ----------------------------------------------------------------------
 // MMA kernel
 // ----------------------------------------------------------------------
 struct UmmaProb {
-  const float *A;
+  const __nv_bfloat16 *A;  // split A, term 0 (terms at + a_term_stride)
   float *C;
   const float *fac;
   const __nv_bfloat16 *B[3];  // split B terms of this problem's mode
-  int reflect;                // read A reflected (see TcProblem)
 };
 
 struct UmmaBatch {
@@ -199,46 +284,48 @@ struct UmmaBatch {
 };
 
 struct UmmaArgs {
-  int M, N, Np, K, Kp;
-  int tnc;            // columns per tile (multiple of 16, <= 128)
+  int M, N, Np, nkb;
+  int tnc, ntn, nmt, ntiles;  // tile columns, column tiles, row tiles, tiles of the batch
+  long long a_term_stride;    // elements between the split terms of one A plane
   const float2 *shift;
-  int fac_staged;     // factor block staged in shared memory for the epilogue
   uint32_t tmem_cols;
-  long long spin;     // iteration limit of the pipeline waits
+  long long spin;             // iteration limit of the pipeline waits
 };
 
 template <int EPI>
 __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant__ UmmaBatch P, UmmaArgs A) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t afull[STAGES], bfull[STAGES], empty[STAGES], hfull[2], hempty[2],
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], hfull[2], hempty[2], lfull[2], lempty[2],
       done;
   __shared__ uint32_t tmem_base;
   __shared__ int fail;
-  const int prob = blockIdx.z, nt = blockIdx.y, mt = blockIdx.x;
   const int warp = threadIdx.x >> 5;
-  const int tnc = A.tnc, n0 = nt * tnc;
+  const int tnc = A.tnc, nkb = A.nkb;
+  const int nchunk = (nkb + kChunk - 1) / kChunk;
   const uint32_t b_term = (uint32_t)tnc * KB * 2;  // one B term of a stage
   const uint32_t stage_bytes = kABytes + 3 * b_term;
-  const int nkb = A.Kp / KB;
-  const int nchunk = (nkb + kChunk - 1) / kChunk;
-  const UmmaProb &Q = P.p[prob];
   const long long spin = A.spin;
+  volatile int *vfail = &fail;
+  // this CTA's tiles: blockIdx.x, blockIdx.x + gridDim.x, ...; the column
+  // tile varies fastest, so the CTAs running at once share A rows in L2
+  const int my_tiles = A.ntiles > (int)blockIdx.x ? (A.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
-      mbar_init(&afull[s], kProducers);
-      mbar_init(&bfull[s], 1);
+      mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&hfull[b], 1);
-      mbar_init(&hempty[b], kProducers);
+      mbar_init(&hempty[b], kRowThreads);
+      mbar_init(&lfull[b], 1);
+      mbar_init(&lempty[b], kRowThreads);
     }
     mbar_init(&done, 1);
     fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == kProducers / 32) {
+  if (warp == kMmaThread / 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base)),
                  "r"(A.tmem_cols)
@@ -249,255 +336,175 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
-  const uint32_t colL = 2u * (uint32_t)tnc;  // the correction-pair accumulator
+  const uint32_t smem0 = smem_u32(smem);
+  float *facs = reinterpret_cast<float *>(smem + (size_t)STAGES * stage_bytes);  // factor epilogue
 
-  // row threads: rows 32 (warp % 4) + lane, K half and column half warp / 4
-  const int half = (warp >> 2) & 1;
-  const int col0 = half * CH;                                  // first tile column of this thread
-  const int ncol = max(0, min(CH, tnc - col0));                // its columns (multiple of 16)
-  float acc[CH];  // this thread's sum of the drained H chunks
-#pragma unroll
-  for (int j = 0; j < CH; ++j) acc[j] = 0.0f;
-  const uint32_t tmem_lane = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-  volatile int *vfail = &fail;
-
-  if (threadIdx.x < kProducers) {
-    // ---- row threads: FP32 A -> three BF16 terms in the stage; drain H
-    const int r = (warp & 3) * 32 + (threadIdx.x & 31);
-    const long long gm = (long long)mt * TH + r;
-    const bool row_ok = gm < A.M;
-    long long src = gm;
-    uint32_t neg = 0;  // sign flip of the BF16 terms (reflected real part)
-    if (Q.reflect && row_ok) {
-      const long long x = gm >> 1, nxh = A.M >> 1;
-      src = 2 * (x == 0 ? 0 : nxh - x) + (gm & 1);
-      if ((gm & 1) == 0) neg = 0x80008000u;
-    }
-    const float *Arow = Q.A + src;
-    float v[KH];
-    auto load = [&](int kb) {
-#pragma unroll
-      for (int k = 0; k < KH; ++k) {
-        const int gk = kb * KB + half * KH + k;
-        v[k] = (row_ok && gk < A.K) ? Arow[(long long)gk * A.M] : 0.0f;
-      }
-    };
-    // drain chunk c (H accumulator c & 1) into acc, then hand it back
-    auto drain = [&](int c) {
-      const int b = c & 1;
-      bool ok = !*vfail && mbar_wait(&hfull[b], (uint32_t)(c >> 1) & 1u, spin);
-      if (!ok) {
-        *vfail = 1;
-        atomicCAS(&g_umma_error, 0, 4);
-      } else {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        tmem_add_row(acc, tmem_lane, (uint32_t)(b * tnc + col0), ncol);
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      }
-      mbar_arrive(&hempty[b]);
-    };
-    int drained = 0;
-    load(0);
-    for (int kb = 0; kb < nkb; ++kb) {
-      const int s = kb % STAGES;
-      bool ok = true;
-      if (kb >= STAGES) ok = !*vfail && mbar_wait(&empty[s], (uint32_t)(kb / STAGES - 1) & 1u, spin);
-      if (!ok) {
-        *vfail = 1;
-        atomicCAS(&g_umma_error, 0, 3);
-      } else {
-        unsigned char *st = smem + (size_t)s * stage_bytes;
-        const int rr = r;
-#pragma unroll
-        for (int kh = 0; kh < KH / 8; ++kh) {
-          const int kg = half * (KH / 8) + kh;  // 8-wide K group of the step
-          uint32_t w0[4], w1[4], w2[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            uint32_t t0[2], t1[2], t2[2];
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-              const float x = v[kh * 8 + 2 * q + e];
-              const __nv_bfloat16 b0 = __float2bfloat16_rn(x);
-              const float r1 = x - __bfloat162float(b0);
-              const __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
-              const float r2 = r1 - __bfloat162float(b1);
-              t0[e] = bf16_bits(b0);
-              t1[e] = bf16_bits(b1);
-              t2[e] = bf16_bits(__float2bfloat16_rn(r2));
-            }
-            w0[q] = (t0[0] | (t0[1] << 16)) ^ neg;
-            w1[q] = (t1[0] | (t1[1] << 16)) ^ neg;
-            w2[q] = (t2[0] | (t2[1] << 16)) ^ neg;
-          }
-          // element (rr, k) of a 128 x 32 term block at ((rr/8)*4 + k/8)*64 + (rr%8)*8 + k%8
-          const uint32_t off = (((rr >> 3) * (KB / 8) + kg) * 64 + (rr & 7) * 8) * 2;
-          *reinterpret_cast<uint4 *>(st + off) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
-          *reinterpret_cast<uint4 *>(st + kATermBytes + off) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
-          *reinterpret_cast<uint4 *>(st + 2 * kATermBytes + off) =
-              make_uint4(w2[0], w2[1], w2[2], w2[3]);
-        }
-      }
-      // generic-proxy stores -> visible to the tensor core (async proxy)
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(&afull[s]);
-      if (kb + 1 < nkb) load(kb + 1);
-      // chunk c is drained once the stages of chunk c + 1 are written, so the
-      // tensor core has the next chunk's operands while the rows drain
-      const int c_ready = (kb + 1) / kChunk - 2;
-      while (drained <= c_ready) drain(drained++);
-    }
-    while (drained < nchunk) drain(drained++);
-  } else if (EPI == TC_EPI_SHIFT_FAC && A.fac_staged && threadIdx.x > kProducers) {
-    // idle lanes of the MMA warp: start the tile's factor block (read by the
-    // epilogue) towards L2, one or two 128-byte lines per column
-    const int xr0p = mt * (TH / 2);
-    const int rows = min(TH / 2, (A.M >> 1) - xr0p);
-    for (int t = threadIdx.x - kProducers - 1; t < 2 * tnc; t += 31) {
-      const int n = n0 + (t >> 1), part = t & 1;
-      if (part * 32 < rows && n < A.N)
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(Q.fac + xr0p + part * 32 + (long long)(A.M >> 1) * n));
-    }
-  } else if (threadIdx.x == kProducers) {
-    // ---- B streaming and MMA issue
-    const uint32_t idesc = idesc_bf16(TH, tnc);
-    int last_b[STAGES];
-    for (int s = 0; s < STAGES; ++s) last_b[s] = -1;
-    auto load_b = [&](int kb) {
-      const int s = kb % STAGES;
-      unsigned char *st = smem + (size_t)s * stage_bytes + kABytes;
-      mbar_expect_tx(&bfull[s], 3 * b_term);
-      for (int t = 0; t < 3; ++t)
-        bulk_g2s(st + t * b_term, Q.B[t] + (long long)kb * A.Np * KB + (long long)n0 * KB, b_term,
-                 &bfull[s]);
-      last_b[s] = kb;
-    };
+  if (threadIdx.x == kLoadThread) {
+    // ---- bulk copies of the A and B terms of every K step
+    int last[STAGES];
+    for (int s = 0; s < STAGES; ++s) last[s] = -1;
+    long long g = 0;
     bool ok = true;
-    for (int kb = 0; kb < STAGES && kb < nkb; ++kb) load_b(kb);
-    for (int kb = 0; kb < nkb && ok; ++kb) {
-      const int s = kb % STAGES;
-      const uint32_t par = (uint32_t)(kb / STAGES) & 1u;
-      const int c = kb / kChunk;
-      const bool first = (kb % kChunk) == 0;
-      const bool last = (kb % kChunk) == kChunk - 1 || kb == nkb - 1;
-      if (first && c >= 2 && !mbar_wait(&hempty[c & 1], (uint32_t)((c >> 1) - 1) & 1u, spin)) {
-        ok = false;
-        break;
-      }
-      if (!mbar_wait(&bfull[s], par, spin) || !mbar_wait(&afull[s], par, spin)) {
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      unsigned char *st = smem + (size_t)s * stage_bytes;
-      const uint32_t dH = tmem + (uint32_t)((c & 1) * tnc), dL = tmem + colL;
-      // term pairs (i, j): (0, 0) into H, the others into L
-      const int pi[6] = {0, 2, 1, 0, 1, 0}, pj[6] = {0, 0, 1, 2, 0, 1};
-#pragma unroll
-      for (int q = 0; q < 6; ++q) {
-#pragma unroll
-        for (int ks = 0; ks < KB / 16; ++ks) {
-          const uint64_t bd = smem_desc(st + kABytes + pj[q] * b_term + ks * 256, 128, (KB / 8) * 128);
-          const uint64_t ad = smem_desc(st + pi[q] * kATermBytes + ks * 256, 128, (KB / 8) * 128);
-          if (q == 0)
-            umma_bf16(dH, ad, bd, idesc, (first && ks == 0) ? 0u : 1u);
-          else
-            umma_bf16(dL, ad, bd, idesc, (kb == 0 && q == 1 && ks == 0) ? 0u : 1u);
-        }
-      }
-      umma_commit(&empty[s]);
-      if (last) umma_commit(&hfull[c & 1]);
-      // refill the stage of the previous step once its MMAs have drained
-      if (kb >= 1 && kb - 1 + STAGES < nkb) {
-        const int sp = (kb - 1) % STAGES;
-        if (!mbar_wait(&empty[sp], (uint32_t)((kb - 1) / STAGES) & 1u, spin)) {
+    for (int i = 0; i < my_tiles && ok && !*vfail; ++i) {
+      const int t = (int)blockIdx.x + i * (int)gridDim.x;
+      const int rest = t % (A.nmt * A.ntn), prob = t / (A.nmt * A.ntn);
+      const int mt = rest / A.ntn, nt = rest % A.ntn;
+      const UmmaProb &Q = P.p[prob];
+      const __nv_bfloat16 *Ab = Q.A + (long long)mt * nkb * kSplitBlock;
+      for (int kb = 0; kb < nkb; ++kb, ++g) {
+        const int s = (int)(g % STAGES);
+        if (g >= STAGES && !mbar_wait(&empty[s], (uint32_t)(g / STAGES - 1) & 1u, spin)) {
+          *vfail = 1;
+          atomicCAS(&g_umma_error, 0, 3);
           ok = false;
           break;
         }
-        load_b(kb - 1 + STAGES);
+        const uint32_t st = smem0 + (uint32_t)s * stage_bytes, bar = smem_u32(&full[s]);
+        mbar_expect_tx(&full[s], kABytes + 3 * b_term);
+        for (int tt = 0; tt < 3; ++tt) {
+          bulk_g2s(st + tt * kATermBytes, Ab + tt * A.a_term_stride + (long long)kb * kSplitBlock,
+                   kATermBytes, bar);
+          bulk_g2s(st + kABytes + tt * b_term, Q.B[tt] + (long long)kb * A.Np * KB + (long long)nt * tnc * KB,
+                   b_term, bar);
+        }
+        last[s] = (int)(g / STAGES);
+      }
+    }
+    // the copies issued last on every stage land before the CTA goes on
+    for (int s = 0; s < STAGES; ++s)
+      if (last[s] >= 0 && !mbar_wait(&full[s], (uint32_t)last[s] & 1u, kSpinLimit))
+        atomicCAS(&g_umma_error, 0, 5);
+  } else if (threadIdx.x == kMmaThread) {
+    // ---- MMA issue
+    const uint32_t idesc = idesc_bf16(TH, tnc);
+    long long g = 0;
+    bool ok = true;
+    for (int i = 0; i < my_tiles && ok; ++i) {
+      const int lb = i & 1;
+      for (int kb = 0; kb < nkb; ++kb, ++g) {
+        const int s = (int)(g % STAGES);
+        const long long c = (long long)i * nchunk + kb / kChunk;
+        const bool first = (kb % kChunk) == 0;
+        const bool last = (kb % kChunk) == kChunk - 1 || kb == nkb - 1;
+        if (first && c >= 2 && !mbar_wait(&hempty[c & 1], (uint32_t)((c >> 1) - 1) & 1u, spin)) ok = false;
+        if (ok && kb == 0 && i >= 2 && !mbar_wait(&lempty[lb], (uint32_t)((i >> 1) - 1) & 1u, spin))
+          ok = false;
+        if (ok && !mbar_wait(&full[s], (uint32_t)(g / STAGES) & 1u, spin)) ok = false;
+        if (!ok || *vfail) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = smem0 + (uint32_t)s * stage_bytes;
+        const uint64_t a0 = smem_desc(st), b0 = smem_desc(st + kABytes);
+        const uint32_t dH = tmem + (uint32_t)((c & 1) * tnc), dL = tmem + (uint32_t)((2 + lb) * tnc);
+        // term pairs (i, j): (0, 0) into H, the others into L
+        const int pi[6] = {0, 2, 1, 0, 1, 0}, pj[6] = {0, 0, 1, 2, 0, 1};
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+#pragma unroll
+          for (int ks = 0; ks < KB / 16; ++ks) {
+            const uint64_t ad = a0 + ((pi[q] * kATermBytes + ks * 256) >> 4);
+            const uint64_t bd = b0 + ((pj[q] * b_term + ks * 256) >> 4);
+            if (q == 0)
+              umma_bf16(dH, ad, bd, idesc, (first && ks == 0) ? 0u : 1u);
+            else
+              umma_bf16(dL, ad, bd, idesc, (kb == 0 && q == 1 && ks == 0) ? 0u : 1u);
+          }
+        }
+        umma_commit(&empty[s]);
+        if (last) umma_commit(&hfull[c & 1]);
+        if (kb == nkb - 1) umma_commit(&lfull[lb]);
       }
     }
     umma_commit(&done);
     if (!ok) {
       *vfail = 1;
       atomicCAS(&g_umma_error, 0, 1);
-      // let the bulk copies already issued land before the CTA exits
-      for (int s = 0; s < STAGES; ++s)
-        if (last_b[s] >= 0) mbar_wait(&bfull[s], (uint32_t)(last_b[s] / STAGES) & 1u, kSpinLimit);
     }
-  }
-  __syncthreads();
-  // all MMAs complete before the L accumulator is read and the stages are
-  // reused (the full limit: this wait must not leave MMAs in flight)
-  const bool drained = mbar_wait(&done, 0, kSpinLimit);
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const bool use = __syncthreads_and(drained && !fail);
-  if (!drained && threadIdx.x == 0) atomicCAS(&g_umma_error, 0, 2);
-  // factor epilogue: the tile's factor block (64 x-rows x tnc columns, one
-  // contiguous run per column, started towards L2 during the K loop) is
-  // copied into the drained stages with 16-byte loads, all threads at once
-  constexpr int nxr = TH / 2;
-  const int xr0 = mt * nxr;
-  const float *facs = reinterpret_cast<const float *>(smem);
-  bool fac_smem = false;
-  if (EPI == TC_EPI_SHIFT_FAC && use && A.fac_staged) {
-    const int rows = min(nxr, (A.M >> 1) - xr0);  // a multiple of 4 (host check)
-    constexpr int nq = nxr / 4;
-    const int total = nq * tnc;  // float4 per column, in the block
-    float4 *dst = reinterpret_cast<float4 *>(smem);
-    constexpr int kBatch = 13;
-    for (int t0 = threadIdx.x; t0 < total; t0 += kBatch * (int)blockDim.x) {
-      float4 vv[kBatch];
-#pragma unroll
-      for (int b = 0; b < kBatch; ++b) {
-        const int t = t0 + b * (int)blockDim.x;
-        const int n = t / nq, q = t - n * nq;
-        vv[b] = (t < total && 4 * q < rows && n0 + n < A.N)
-                    ? __ldg(reinterpret_cast<const float4 *>(Q.fac + xr0 + (long long)(A.M >> 1) * (n0 + n)) + q)
-                    : make_float4(1.f, 1.f, 1.f, 1.f);
-      }
-#pragma unroll
-      for (int b = 0; b < kBatch; ++b) {
-        const int t = t0 + b * (int)blockDim.x;
-        if (t < total) dst[t] = vv[b];
-      }
-    }
-    __syncthreads();
-    fac_smem = true;
-  }
-  if (use && threadIdx.x < kProducers) {
-    tmem_add_row(acc, tmem_lane, colL + (uint32_t)col0, ncol);  // + the correction pairs
+  } else if (threadIdx.x < kRowThreads) {
+    // ---- row threads: drain the accumulators, write the tiles
+    const int half = warp >> 2;
+    const int col0 = half * CH;
+    const int ncol = max(0, min(CH, tnc - col0));  // a multiple of 16
+    const uint32_t tmem_lane = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const int row = (warp & 3) * 32 + (threadIdx.x & 31);
-    const long long gm = (long long)mt * TH + row;
-    float2 sh = make_float2(1.f, 0.f);
-    if (EPI != TC_EPI_STORE && gm < A.M) sh = A.shift[gm >> 1];
-    float *C = Q.C;
-    const float *fac = Q.fac;
-    const bool rok = gm < A.M;
+    float acc[CH];
+    for (int i = 0; i < my_tiles; ++i) {
+      const int t = (int)blockIdx.x + i * (int)gridDim.x;
+      const int rest = t % (A.nmt * A.ntn), prob = t / (A.nmt * A.ntn);
+      const int mt = rest / A.ntn, nt = rest % A.ntn;
+      const int lb = i & 1;
+      const UmmaProb &Q = P.p[prob];
+      const long long gm = (long long)mt * TH + row;
+      const bool rok = gm < A.M;
 #pragma unroll
-    for (int jj = 0; jj < CH; ++jj) {
-      if (jj < ncol) {
-        float x = acc[jj];
-        const int j = col0 + jj, n = n0 + j;
-        if (EPI != TC_EPI_STORE) {
-          // rows 2x (re) and 2x+1 (im) sit in adjacent lanes
-          const float other = __shfl_xor_sync(0xffffffffu, x, 1);
-          const float re = (row & 1) ? other : x, im = (row & 1) ? x : other;
-          x = (row & 1) ? (re * sh.y + im * sh.x) : (re * sh.x - im * sh.y);
-          if (EPI == TC_EPI_SHIFT_FAC) {
-            const float f = fac_smem ? facs[j * nxr + (row >> 1)]
-                                     : ((rok && n < A.N) ? __ldg(fac + (gm >> 1) + (long long)(A.M >> 1) * n)
-                                                         : 1.0f);
-            x *= f;
-          }
+      for (int j = 0; j < CH; ++j) acc[j] = 0.0f;
+      if (EPI == TC_EPI_SHIFT_FAC) {
+        // the tile's factor block (64 x-rows x tnc columns) into shared
+        // memory before the accumulator waits, so that its load latency is
+        // hidden; the row threads meet before (the previous tile's epilogue
+        // has read the block) and after writing it
+        asm volatile("bar.sync 1, %0;" ::"n"(kRowThreads) : "memory");
+        const long long xr0 = (long long)mt * (TH / 2);
+        const long long rows = min((long long)(TH / 2), (long long)(A.M >> 1) - xr0);
+        for (int e = threadIdx.x; e < (TH / 2) * tnc; e += kRowThreads) {
+          const int col = e / (TH / 2), xx = e % (TH / 2), n = nt * tnc + col;
+          facs[e] = (xx < rows && n < A.N) ? __ldg(Q.fac + xr0 + xx + (long long)(A.M >> 1) * n) : 1.0f;
         }
-        if (rok && n < A.N) C[gm + (long long)n * A.M] = x;
+        asm volatile("bar.sync 1, %0;" ::"n"(kRowThreads) : "memory");
+      }
+      bool ok = true;
+      for (int cc = 0; cc < nchunk; ++cc) {
+        const long long c = (long long)i * nchunk + cc;
+        const int b = (int)(c & 1);
+        ok = ok && !*vfail && mbar_wait(&hfull[b], (uint32_t)(c >> 1) & 1u, spin);
+        if (ok) {
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          tmem_add_row(acc, tmem_lane, (uint32_t)(b * tnc + col0), ncol);
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        }
+        mbar_arrive(&hempty[b]);
+      }
+      ok = ok && !*vfail && mbar_wait(&lfull[lb], (uint32_t)(i >> 1) & 1u, spin);
+      if (ok) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        tmem_add_row(acc, tmem_lane, (uint32_t)((2 + lb) * tnc + col0), ncol);
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      }
+      mbar_arrive(&lempty[lb]);
+      if (!ok) atomicCAS(&g_umma_error, 0, 4);
+      if (!row_threads_all(ok && !*vfail)) {
+        *vfail = 1;
+        break;
+      }
+      // epilogue from registers, while the tensor core runs the next tile
+      float2 sh = make_float2(1.f, 0.f);
+      if (EPI != TC_EPI_STORE && rok) sh = A.shift[gm >> 1];
+#pragma unroll
+      for (int jj = 0; jj < CH; ++jj) {
+        if (jj < ncol) {
+          float x = acc[jj];
+          const int n = nt * tnc + col0 + jj;
+          if (EPI != TC_EPI_STORE) {
+            // rows 2x (re) and 2x+1 (im) sit in adjacent lanes
+            const float other = __shfl_xor_sync(0xffffffffu, x, 1);
+            const float re = (row & 1) ? other : x, im = (row & 1) ? x : other;
+            x = (row & 1) ? (re * sh.y + im * sh.x) : (re * sh.x - im * sh.y);
+            if (EPI == TC_EPI_SHIFT_FAC) x *= facs[(col0 + jj) * (TH / 2) + (row >> 1)];
+          }
+          if (rok && n < A.N) Q.C[gm + (long long)n * A.M] = x;
+        }
       }
     }
   }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == kProducers / 32) {
+  // every MMA complete before the TMEM is freed (the full limit: this wait
+  // must not leave MMAs in flight)
+  if (!mbar_wait(&done, 0, kSpinLimit) && threadIdx.x == 0) atomicCAS(&g_umma_error, 0, 2);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == kMmaThread / 32) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(A.tmem_cols)
                  : "memory");
   }
@@ -509,9 +516,14 @@ inline long long rup(long long a, long long b) { return (a + b - 1) / b * b; }
 
 namespace chm {
 
+long long tc_split_bytes(int M, int K, int count) {
+  return (long long)count * 6 * rup(M, TH) * rup(K, KB) + 256;
+}
+
 int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, const float2 *shift,
-                   cudaStream_t st) {
-  const int tnc = tc_tile_cols(N), ntn = tc_col_tiles(N), Np = tc_np(N), Kp = (int)rup(K, KB);
+                   void *ws, long long ws_bytes, cudaStream_t st) {
+  const int tnc = tc_tile_cols(N), ntn = tc_col_tiles(N), Np = tc_np(N);
+  const int nkb = (int)(rup(K, KB) / KB), nmt = (int)((M + TH - 1) / TH);
   if (tnc > TH || tnc % 16) {
     set_error("umma: bad column tile %d", tnc);
     return CHM_ERR_RANGE;
@@ -525,44 +537,62 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
       set_error("umma: problem %d has no prepared %dx%d operator", i, K, N);
       return CHM_ERR_ARG;
     }
-  const int mt = (int)((M + TH - 1) / TH);
+  const long long term_stride = (long long)nmt * nkb * kSplitBlock;  // elements
+  const long long split_one = 3 * term_stride * 2;                     // bytes per A plane
+  char *wsp = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(ws) + 255) & ~(uintptr_t)255);
+  const long long avail = ws ? ws_bytes - (wsp - reinterpret_cast<char *>(ws)) : 0;
   const uint32_t b_term = (uint32_t)tnc * KB * 2;
-  const size_t stage_bytes = kABytes + 3 * (size_t)b_term;
-  const size_t smem = (size_t)STAGES * stage_bytes + 1024;
+  const size_t smem = (size_t)STAGES * (kABytes + 3 * (size_t)b_term) + 1024 +
+                     (epi == TC_EPI_SHIFT_FAC ? (size_t)(TH / 2) * tnc * 4 : 0);
   void (*kern)(const UmmaBatch, UmmaArgs) =
       epi == TC_EPI_STORE ? umma_kernel<TC_EPI_STORE>
                           : (epi == TC_EPI_SHIFT ? umma_kernel<TC_EPI_SHIFT> : umma_kernel<TC_EPI_SHIFT_FAC>);
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   uint32_t cols = 32;
-  while (cols < (uint32_t)(3 * tnc)) cols <<= 1;  // H0, H1 and L
-  UmmaArgs ua{};
-  ua.M = M;
-  ua.N = N;
-  ua.Np = Np;
-  ua.K = K;
-  ua.Kp = Kp;
-  ua.tnc = tnc;
-  ua.shift = shift;
-  ua.tmem_cols = cols;
-  ua.spin = g_spin_limit;
-  // the staged factor block is read with 16-byte loads: M/2 a multiple of 4
-  // and 16-byte aligned factor planes; it (64 x tnc FP32) fits in the stages
-  ua.fac_staged = (epi == TC_EPI_SHIFT_FAC && (M / 2) % 4 == 0 &&
-                   (size_t)(TH / 2) * tnc * 4 <= (size_t)STAGES * stage_bytes) ? 1 : 0;
-  for (int i = 0; i < count && ua.fac_staged; ++i)
-    if (!p[i].fac || (reinterpret_cast<uintptr_t>(p[i].fac) & 15)) ua.fac_staged = 0;
+  while (cols < (uint32_t)(4 * tnc)) cols <<= 1;  // H0, H1, L0, L1
   for (int c0 = 0; c0 < count; c0 += kMaxBatch) {
     const int cnt = count - c0 < kMaxBatch ? count - c0 : kMaxBatch;
+    // split every distinct A plane (pointer and reflection) once
+    SplitJobs J;
+    int njobs = 0;
     UmmaBatch ub;
     for (int i = 0; i < cnt; ++i) {
       const TcProblem &q = p[c0 + i];
-      ub.p[i] = UmmaProb{q.A, q.C, q.fac,
+      int j = 0;
+      while (j < njobs && !(J.A[j] == q.A && J.reflect[j] == q.reflect)) ++j;
+      if (j == njobs) {
+        if ((long long)(njobs + 1) * split_one > avail) {
+          set_error("umma: workspace of %lld bytes holds no room for %d split A planes", ws_bytes,
+                    njobs + 1);
+          return CHM_ERR_WS;
+        }
+        J.A[j] = q.A;
+        J.reflect[j] = q.reflect;
+        J.T[j] = reinterpret_cast<__nv_bfloat16 *>(wsp + (long long)j * split_one);
+        ++njobs;
+      }
+      ub.p[i] = UmmaProb{J.T[j], q.C, q.fac,
                          {reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[0]),
                           reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[1]),
-                          reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[2])},
-                         q.reflect};
+                          reinterpret_cast<const __nv_bfloat16 *>(q.B.bf[2])}};
     }
-    kern<<<dim3(mt, ntn, cnt), kThreads, smem, st>>>(ub, ua);
+    split_a_kernel<<<dim3(nmt, nkb, njobs), TH, 0, st>>>(J, M, K, nkb, term_stride);
+    count_launch();
+    UmmaArgs ua{};
+    ua.M = M;
+    ua.N = N;
+    ua.Np = Np;
+    ua.nkb = nkb;
+    ua.tnc = tnc;
+    ua.ntn = ntn;
+    ua.nmt = nmt;
+    ua.ntiles = cnt * nmt * ntn;
+    ua.a_term_stride = term_stride;
+    ua.shift = shift;
+    ua.tmem_cols = cols;
+    ua.spin = g_spin_limit;
+    const int grid = ua.ntiles < sm_count() ? ua.ntiles : sm_count();
+    kern<<<grid, kThreads, smem, st>>>(ub, ua);
     count_launch();
   }
   cudaError_t e = cudaGetLastError();
