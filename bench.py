@@ -357,8 +357,10 @@ def run_gb300(args):
                 "what": "ChimeraRun.make_step (the plain FP64 form: FP64 particles, complex128 "
                         "fields, FP64 products) on the same workload, device resident"}
     if args.form == "split":
-        # the split form continues from the FP64 run's state
+        # the split form continues from the FP64 run's state; its re-sort by
+        # deposit cell runs at the cadence the run-time tuner picks
         run = SplitRun(None, fp64_run=fp)
+        run.sort_every = "auto"
         nmov = lambda: run.num_moving  # noqa: E731
     else:
         run = fp
@@ -410,6 +412,25 @@ def run_gb300(args):
                                       "share": t / tot if tot else None,
                                       "gemm_gflop_per_step": f / nprof / 1e9}
               for k, (c, t, f) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+    # long-run decay: the same run continued to step decay_steps; the last
+    # 20 steps timed against the first window (re-sorts included)
+    decay = None
+    if args.form == "split" and args.decay_steps > step + 20:
+        first = (args.warmup + 1 + (args.fp64_steps + 1 if args.fp64_steps > 0 else 0))
+        while step < args.decay_steps - 20:
+            step += 1
+            run.make_step(step)
+        torch.cuda.synchronize()
+        ms_late, _ = time_steps(run, step + 1, 20, nmov, stream)
+        step += 20
+        decay = {"early_steps": [first, first + args.steps - 1],
+                 "early_ms_per_step": ms_max / args.steps,
+                 "late_steps": [step - 19, step], "late_ms_per_step": ms_late / 20,
+                 "late_over_early": (ms_late / 20) / (ms_max / args.steps),
+                 "sort": {"mode": "auto (SortCadence)",
+                          "history": [{"step": h[0], "cadence": h[1], "sort_ms": h[2],
+                                       "slope_ms_per_step": h[3]} for h in run.sorter.history]}}
+        run.check_status()
     peaks, peak_kind = load_peaks()
     roofline = stage_roofline(args.form, prof, nprof, n_moving, still_count(run, args.form),
                               peaks, peak_kind)
@@ -511,6 +532,7 @@ def run_gb300(args):
         "max_transform_err": max(terr.values()) if terr else None,
         "transform_errors": terr,
         "device_flags": flags,
+        "decay": decay,
         "roofline": roofline,
         "stages": stages,
         "clocks": clk,
@@ -604,6 +626,8 @@ def main():
                     help="reference arm: at most this many timed steps (recorded in the line)")
     ap.add_argument("--fp64-steps", type=int, default=2,
                     help="timed steps of the plain FP64 form in the same run (0: skip)")
+    ap.add_argument("--decay-steps", type=int, default=500,
+                    help="continue the timed split run to this step and time its last 20 steps")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-errors", action="store_true")

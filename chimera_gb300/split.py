@@ -171,6 +171,26 @@ class _SpParticles:
                   tw.data_ptr(), tw.stride(0), float(X0), float(dx), m, _stream())
         self.n += m
 
+    def sort_cells(self, win_k, nx, nr, dr_inv):
+        """Re-sort the particles by deposit cell (chm_sp_sort_cells), dropping
+        the dead ones; one device->host read (the live count)."""
+        if self.n == 0:
+            return
+        if self.spare is None:
+            self.spare = self._alloc(self.cap)
+        ws = chimera.workspace(_lib.query("chm_sp_sort_ws_bytes", self.n), self.device)
+        n_out = torch.empty(1, dtype=torch.int64, device=self.device)
+        _lib.call("chm_sp_sort_cells", *self.ptrs(), self.dead.data_ptr(), self.n, int(win_k),
+                  int(nx), int(nr), float(dr_inv), *self.ptrs(self.spare), n_out.data_ptr(),
+                  ws.data_ptr(), ws.numel(), _stream())
+        n = int(n_out.item())
+        chimera.io_bytes["d2h"] += 8
+        self.buf, self.spare = self.spare, self.buf
+        self.n = n
+        self.dead[:_slots(n)].zero_()
+        self.counters[0].zero_()
+        self.moves = 0
+
     def compact(self):
         """Drop the dead particles (stable order); one device->host read."""
         if self.n == 0:
@@ -192,6 +212,48 @@ class _SpParticles:
 
 def _stream():
     return torch.cuda.current_stream().cuda_stream
+
+
+class SortCadence:
+    """Run-time choice of the re-sort cadence (steps between two sorts by
+    deposit cell).  As particles drift, the cell runs of the deposit and
+    gather kernels break up and those kernels slow down; a sort costs a
+    fixed time S.  With the particle kernels' time growing by g per step
+    after a sort, sorting every c steps costs S / c + g c / 2 per step,
+    least at c = sqrt(2 S / g).  Both S and g are measured with CUDA events
+    (read back only at the next sort, so no step waits for them) and the
+    cadence is refreshed after every interval; ``history`` keeps
+    (step, cadence, sort ms, slope ms/step) for the record."""
+
+    def __init__(self, start=32, lo=8, hi=512):
+        self.cadence, self.lo, self.hi = start, lo, hi
+        self.history = []
+        self._events = []      # (steps since sort, start, end) of the particle kernels
+        self._sort_ev = None   # (start, end) of the last sort
+
+    def step_events(self, since):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        self._events.append((since, a, b))
+        return a, b
+
+    def sort_events(self):
+        self._sort_ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        return self._sort_ev
+
+    def update(self, step):
+        """After a sort (the stream has been synchronised by its count read)."""
+        t = [(s, a.elapsed_time(b)) for s, a, b in self._events if a.query() and b.query()]
+        self._events = []
+        S = self._sort_ev[0].elapsed_time(self._sort_ev[1]) if self._sort_ev else None
+        g = None
+        if len(t) >= 4 and S is not None:
+            x = np.array([u for u, _ in t], dtype=float)
+            y = np.array([v for _, v in t], dtype=float)
+            if x.std() > 0:
+                g = float(np.polyfit(x, y, 1)[0])
+                c = self.hi if g <= 0 else int(np.sqrt(2.0 * S / g))
+                self.cadence = int(min(self.hi, max(self.lo, c)))
+        self.history.append((int(step), int(self.cadence), S, g))
 
 
 class SplitRun:
@@ -286,6 +348,14 @@ class SplitRun:
         # and by check_status(); either raises
         self.check_every = 64
         self._steps = 0
+        # re-sort by deposit cell every this many steps (0: never), or "auto":
+        # SortCadence picks the cadence from measured times.  A sort changes
+        # the order of the FP32 run sums of the deposit, so a fixed cadence
+        # keeps runs bitwise reproducible; "auto" makes the sort steps (and
+        # so the last bits of the fields) depend on timing.
+        self.sort_every = 64
+        self.sorter = SortCadence()
+        self._since_sort = 0
 
     # ------------------------------------------------------------------
     def _moving(self):
@@ -390,8 +460,13 @@ class SplitRun:
                 self._deposit_background()
             # the reference's dep_dens here (postframe_corr) is overwritten by
             # project_density before any use; it is not repeated
+        self._maybe_sort(istep)
         if not self._scales_valid:
             self._refresh_scales()
+        ev = None
+        if self.sort_every == "auto":
+            ev = self.sorter.step_events(self._since_sort)
+            ev[0].record()
         # push_coords + J (half step) [+ rho (new position), fused unless a
         # staged frame moves between the two deposits]
         self.accJ.zero_()
@@ -439,11 +514,34 @@ class SplitRun:
                   self.gnxt.data_ptr() if self.space_charge else None, self.c1.data_ptr(),
                   self.c2.data_ptr(), int(self.nterm), P_, st)
         self._project_fields_and_push()
+        if ev is not None:
+            ev[1].record()
         for spc, P in self._moving():
             _lib.call("chm_sp_count_live", P.counters.data_ptr(), P.n, st)
         self._steps += 1
+        self._since_sort += 1
         if self.check_every and self._steps % self.check_every == 0:
             self.check_status()
+
+    def _maybe_sort(self, istep):
+        every = self.sorter.cadence if self.sort_every == "auto" else int(self.sort_every or 0)
+        if every and self._since_sort >= every:
+            self.resort(istep)
+
+    def resort(self, istep=None):
+        """Re-sort every species by deposit cell (dead particles dropped)."""
+        k, _ = self._win()
+        auto = self.sort_every == "auto"
+        if auto:
+            ev = self.sorter.sort_events()
+            ev[0].record()
+        for spc, P in zip(self.fp.Particles, self.parts):
+            P.sort_cells(k, self.nx, self.nr, float(self.solver.Args["dr_inv"]))
+        if auto:
+            ev[1].record()
+            ev[1].synchronize()
+            self.sorter.update(self._steps if istep is None else istep)
+        self._since_sort = 0
 
     def check_status(self):
         """Raise if a device error flag is set: a tensor-core product CTA
@@ -577,6 +675,7 @@ class SplitRun:
         arrays["split/scaleBG"] = self.scaleBG.cpu().numpy()
         arrays["split/scales_valid"] = np.asarray(self._scales_valid)
         arrays["split/have_bg"] = np.asarray(self.have_bg)
+        arrays["split/since_sort"] = np.asarray(self._since_sort)
         arrays["split/accBG"] = self.accBG.cpu().numpy()
         return snapshot.write(snapshot.snap_name(fname), arrays)
 
@@ -605,6 +704,8 @@ class SplitRun:
                     t.copy_(torch.from_numpy(np.ascontiguousarray(f["split/" + k])))
                 self._scales_valid = bool(f["split/scales_valid"])
                 self.have_bg = bool(f["split/have_bg"])
+                if "split/since_sort" in f.files:
+                    self._since_sort = int(f["split/since_sort"])
             else:
                 self._scales_valid = False
                 self.have_bg = False

@@ -326,6 +326,59 @@ def test_absorb_and_compact(mods):
         assert np.array_equal(_gather(Q[key].cpu().numpy(), m), exp), key
 
 
+def _logical(q):
+    q = np.asarray(q, dtype=np.int64)
+    return (q & ~511) | ((q & 31) << 4) | ((q >> 5) & 15)
+
+
+def test_sort_by_cell_matches_host(mods):
+    """chm_sp_sort_cells: the stable order of the documented deposit-cell key
+    (host restatement with the same FP32 arithmetic), dead particles dropped,
+    the live count returned, every particle moved whole."""
+    torch, _lib, fm, split = mods
+    n, nx, nr, dr = 70000 + 123, 96, 40, 0.5
+    P = _sp_particles(torch, n, nx, nr, dr, 21, runs=False)
+    names = ("ix", "fx", "y", "z", "px", "py", "pz", "w")
+    cap = P["w"].numel()
+    rng = np.random.default_rng(4)
+    dead_h = np.zeros(cap, np.uint8)
+    dead_h[_slots(n)[rng.random(n) < 0.05]] = 1
+    dead = torch.from_numpy(dead_h).cuda()
+    win_k = 100
+    st = _st(torch)
+    Q = {k: torch.full_like(v, 7) for k, v in P.items()}
+    ws = torch.empty(_lib.query("chm_sp_sort_ws_bytes", n), dtype=torch.uint8, device="cuda")
+    n_out = torch.zeros(1, dtype=torch.int64, device="cuda")
+    _lib.call("chm_sp_sort_cells", *[P[k].data_ptr() for k in names], dead.data_ptr(), n, win_k, nx,
+              nr, np.float32(1 / dr), *[Q[k].data_ptr() for k in names], n_out.data_ptr(),
+              ws.data_ptr(), ws.numel(), st)
+    torch.cuda.synchronize()
+    h = {k: v.cpu().numpy() for k, v in P.items()}
+    q = np.arange(cap)
+    live = (_logical(q) < n) & (dead_h == 0)
+    f32 = np.float32
+    y, z = h["y"], h["z"]
+    sv = np.sqrt(y * y + z * z).astype(f32) * f32(1 / dr)
+    grf = np.floor(sv)
+    half = ((sv - grf) >= f32(0.5)).astype(np.uint64)
+    gr = np.minimum(np.maximum(grf.astype(np.int64), 0), nr + 4).astype(np.uint64)
+    gx = np.minimum(np.maximum(h["ix"].astype(np.int64) - win_k + 8, 0), nx + 24).astype(np.uint64)
+    npx = np.uint64((nx + 24) // 4 + 1)
+    px, lx, pr, lr = gx >> 2, gx & 3, gr >> 2, gr & 3
+    pxs = np.where(pr & 1, npx - 1 - px, px)
+    lxs = np.where(lr & 1, 3 - lx, lx)
+    key = ((((pr * npx + pxs) * 4 + lr) * 4 + lxs) << 1) | half
+    key = np.where(live, key, 0xffffffff).astype(np.uint64)
+    order = np.argsort(key, kind="stable")
+    nlive = int(live.sum())
+    assert int(n_out.item()) == nlive
+    src = order[:nlive]  # source slots in sorted order
+    for k in names:
+        got = _gather(Q[k].cpu().numpy(), nlive)
+        assert np.array_equal(got, h[k][src]), k
+    assert np.all(np.diff(key[src].astype(np.int64)) >= 0)
+
+
 def test_tile_slot_map(mods):
     """chm_sp_slot / chm_sp_capacity follow the documented tile layout."""
     torch, _lib, fm, split = mods
@@ -345,15 +398,18 @@ def _window_comps(seed):
     return comps
 
 
-def test_split_window_with_injection_tracks_fp64_form(mods):
+@pytest.mark.parametrize("sort_every", [64, 2])
+def test_split_window_with_injection_tracks_fp64_form(mods, sort_every):
     """Moving window with absorption and plasma injection (the demos'
     AbsorbLayer + AddPlasma + IonsOnTop): same particle counts as the FP64
-    form and fields within 1e-4 after 8 steps, with compactions in between."""
+    form and fields within 1e-4 after 8 steps, with compactions in between
+    (and re-sorts by deposit cell every 2 steps)."""
     torch, _lib, fm, split = mods
     from chimera_gb300 import ChimeraRun
     ref = ChimeraRun(_window_comps(2024))
     run = split.SplitRun(_window_comps(2024))
     run.compact_every = 3
+    run.sort_every = sort_every
     live = 0
     for i in range(1, 9):
         np.random.seed(500 + i)  # the same injected plasma in both runs
