@@ -159,7 +159,8 @@ FP64_BYTES = {"push_velocs": 48 + 48 + 24, "push_coords": 24 + 24 + 24 + 24,
 # ions (rho) 87.3 MB)
 SPLIT_TRAFFIC = {2: {"push_electrons": 179.90e6 / 4128768, "deposit_still": 87.29e6 / 4128768}}
 GEMM_STAGES = ("chm_fb_graddiv", "chm_fb_rot", "chm_fb_grad", "chm_fb_div", "chm_fb_in",
-               "chm_fb_out", "chm_fb_eb_out", "chm_sp_poisson", "chm_sp_fb_in_acc",
+               "chm_fb_out", "chm_fb_eb_out", "chm_sp_poisson", "chm_sp_poisson_psatd",
+               "chm_sp_fb_in_acc",
                "chm_sp_fb_eb_out", "chm_sp_rot_b", "chm_sp_fb_grad")
 
 

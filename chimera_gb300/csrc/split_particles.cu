@@ -47,8 +47,6 @@ constexpr int kSpBoxBytes = 40 * 1024;             // 10240 int32 values
 // rho-only run kernel (still species): a smaller box (a block's box holds
 // 2 nm - 1 values per node) and fewer registers, for more resident blocks
 constexpr int kRhoBoxBytes = 16 * 1024;
-constexpr int kRhoMinBlocks = 8;
-constexpr int kRhoGroup = 1;  // particles loaded ahead per lane
 
 // deposit cells dropped outside a block box while inside the grid (corrupt
 // positions); read and reset by chm_sp_deposit_dropped
@@ -61,29 +59,13 @@ __host__ __device__ __forceinline__ i64 phys_of(i64 i) {
 __host__ __device__ __forceinline__ i64 logical_of(i64 p) {
   return (p & ~(i64)(kTile - 1)) | ((p & (kTileRuns - 1)) << 4) | ((p >> 5) & (kRunLen - 1));
 }
-inline i64 tiles_of(i64 n) { return (n + kTile - 1) / kTile; }
+__host__ __device__ inline i64 tiles_of(i64 n) { return (n + kTile - 1) / kTile; }
 
 struct SpParts {
   int32_t *ix;
   float *fx, *y, *z, *px, *py, *pz, *w;
   i64 n;
 };
-
-// Starts the particle data of one tile (512 slots; 16 rows of 32
-// consecutive slots per array) towards L2: one prefetch per 128-byte row,
-// the warp's lanes taking rows in turn.  The arrays are read slot by slot
-// afterwards, so this turns their DRAM latency into L2 latency.  Tiles past
-// the last particle are not touched (the arrays hold whole tiles up to n).
-__device__ __forceinline__ void prefetch_tile(const SpParts &P, i64 tile, int lane, bool momenta) {
-  if (tile >= P.n) return;
-  const int narr = momenta ? 8 : 5;
-  for (int k = lane; k < kRunLen * narr; k += 32) {
-    const int row = k & (kRunLen - 1), arr = k >> 4;
-    const float *b = arr == 0 ? P.w : arr == 1 ? (const float *)P.ix : arr == 2 ? P.fx
-                   : arr == 3 ? P.y : arr == 4 ? P.z : arr == 5 ? P.px : arr == 6 ? P.py : P.pz;
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(b + tile + (i64)row * kTileRuns));
-  }
-}
 
 struct SpGrid {
   int win_k;      // window origin, whole cells from X0
@@ -321,6 +303,52 @@ __device__ __forceinline__ Pushed push_one(const PushDepArgs &A, i64 i) {
   return push_vals(A, P.ix[i], P.fx[i], P.y[i], P.z[i], P.px[i], P.py[i], P.pz[i], P.w[i]);
 }
 
+// ----------------------------------------------------------------------
+// Shared-memory staging of a block's particles: the run kernels first copy
+// the block's 2048 slots of every array they read into shared memory with
+// 16-byte asynchronous copies (cp.async, only the tiles that exist), then
+// plan and walk the runs from there, so no particle load of the main loops
+// waits on L2 or DRAM.  Arrays in the stage: w, ix, fx, y, z, px, py, pz.
+// ----------------------------------------------------------------------
+constexpr int kStageArrays = 8;
+
+struct StageView {  // particle values by slot (global arrays or the stage)
+  const int32_t *ix;
+  const float *fx, *y, *z, *px, *py, *pz, *w;
+};
+
+__device__ __forceinline__ StageView global_view(const SpParts &P, i64 base) {
+  return StageView{P.ix + base, P.fx + base, P.y + base, P.z + base,
+                   P.px + base, P.py + base, P.pz + base, P.w + base};
+}
+
+__device__ __forceinline__ StageView stage_view(const unsigned char *sm) {
+  const float *f = reinterpret_cast<const float *>(sm);
+  return StageView{reinterpret_cast<const int32_t *>(f + kDepBlock), f + 2 * kDepBlock,
+                   f + 3 * kDepBlock, f + 4 * kDepBlock, f + 5 * kDepBlock, f + 6 * kDepBlock,
+                   f + 7 * kDepBlock, f};
+}
+
+// copies the block's slots [base, base + 2048) of the first narr arrays
+// (5: w, ix, fx, y, z; 8: and the momenta) into sm; slots of tiles past the
+// last particle are not copied (and are never read)
+__device__ __forceinline__ void stage_block(const SpParts &P, i64 base, int narr, unsigned char *sm) {
+  const i64 ntiles = tiles_of(P.n);
+  const int tiles = (int)max((i64)0, min((i64)(kDepBlock / kTile), ntiles - base / kTile));
+  const int nchunk = tiles * kTile / 4;  // 16-byte chunks per array
+  const uint32_t s0 = static_cast<uint32_t>(__cvta_generic_to_shared(sm));
+  for (int c = threadIdx.x; c < narr * nchunk; c += blockDim.x) {
+    const int a = c / nchunk, k = c - a * nchunk;
+    const float *src = a == 0 ? P.w : a == 1 ? reinterpret_cast<const float *>(P.ix) : a == 2 ? P.fx
+                     : a == 3 ? P.y : a == 4 ? P.z : a == 5 ? P.px : a == 6 ? P.py : P.pz;
+    const uint32_t dst = s0 + (uint32_t)((a * kDepBlock + 4 * k) * 4);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src + base + 4 * k)
+                 : "memory");
+  }
+  asm volatile("cp.async.commit_group;\ncp.async.wait_all;" ::: "memory");
+  __syncthreads();
+}
+
 // Block plan shared by the deposit kernels: the box of nodes the block's
 // deposits can touch, from every particle of its 2048 slots.  The box is
 // bounded without pushing: a particle moves less than c dt, so its deposit
@@ -337,7 +365,8 @@ struct BlockPlan {
   float sJ, sR;    // global scales 2^eJ, 2^eR (path without a box)
 };
 
-__device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box_bytes) {
+__device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box_bytes,
+                                const StageView &V) {
   __shared__ float wsm[2][kDepThreads / 32];
   if (threadIdx.x == 0) {
     bb[0] = INT_MAX;
@@ -353,14 +382,15 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box
   for (int s = threadIdx.x; s < kDepBlock; s += blockDim.x) {
     const i64 p = base + s;
     const bool valid = logical_of(p) < A.P.n;
-    const i64 q = valid ? p : base;  // slot 0 of the block always holds a particle
-    const float w = A.P.w[q];
-    if (!A.push && !A.dep_j) asm volatile("prefetch.global.L2 [%0];" ::"l"(A.P.fx + q));
-    const int ix = A.P.ix[q];
-    const float y = A.P.y[q], z = A.P.z[q];
+    const int q = valid ? s : 0;  // slot 0 of the block always holds a particle
+    const float w = V.w[q];
+    // (the rho-only pass reads global memory: its fx starts towards L2 here)
+    if (!A.push && !A.dep_j) asm volatile("prefetch.global.L2 [%0];" ::"l"(V.fx + q));
+    const int ix = V.ix[q];
+    const float y = V.y[q], z = V.z[q];
     float pp = 0.0f;
     if (A.dep_j) {
-      const float px = A.P.px[q], py = A.P.py[q], pz = A.P.pz[q];
+      const float px = V.px[q], py = V.py[q], pz = V.pz[q];
       // max_l |v_l| = max_l |p_l| / gamma
       pp = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz))) *
            rsqrtf(1.0f + (px * px + py * py + pz * pz));
@@ -448,7 +478,7 @@ __global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A
   extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
   const i64 base = (i64)blockIdx.x * kDepBlock;
-  const BlockPlan Pl = plan_block(A, base, bb, kSpBoxBytes);
+  const BlockPlan Pl = plan_block(A, base, bb, kSpBoxBytes, global_view(A.P, base));
   if (Pl.use_box)
     for (long long t = threadIdx.x; t < Pl.nvals; t += kDepThreads) box[t] = 0;
   __syncthreads();
@@ -602,51 +632,52 @@ __device__ __forceinline__ void acc_add(CellAcc<NM, NC> &c, const Loc &L, const 
   }
 }
 
-// resident blocks per SM the register budget is set for: three modes carry
-// 5 instead of 3 mode parts per accumulated component
-template <int NM, bool DJ>
-constexpr int dep_min_blocks() { return DJ ? (NM >= 3 ? 3 : 4) : (NM >= 3 ? 6 : kRhoMinBlocks); }
+// The moving species' pass (push, J, rho) stages the block's particles in
+// shared memory (64 KB) ahead of its box: 2 resident blocks per SM.  The
+// still species' rho-only pass reads 20 B per particle once and runs more
+// blocks per SM instead (measured faster unstaged: 118 against 157 us for
+// 12.6M ions of the 4096 x 128 x 3-mode case).
+constexpr int kRhoMinBlocks = 8;
 
 template <int NM, bool PUSH, bool DJ, bool DR>
-__global__ void __launch_bounds__(kDepThreads, dep_min_blocks<NM, DJ>())
+__global__ void __launch_bounds__(kDepThreads, (PUSH || DJ) ? 2 : kRhoMinBlocks)
     push_deposit_run_kernel(PushDepArgs A) {
-  extern __shared__ __align__(16) int box[];
+  extern __shared__ __align__(16) unsigned char dsm[];
+  constexpr bool STAGE = PUSH || DJ;
+  int *box = reinterpret_cast<int *>(dsm + (STAGE ? (size_t)kStageArrays * kDepBlock * 4 : 0));
   __shared__ int bb[4];
-  // slot indices: 32-bit in the rho-only kernel (measured faster there; the
-  // host launches it for n < 2^31 only), 64-bit otherwise
-  using Idx = typename std::conditional<DJ, i64, unsigned>::type;
-  const Idx base = (Idx)blockIdx.x * kDepBlock;
-  // (the rho-only pass starts only fx towards L2, in the plan: measured
-  // faster there than the whole tile)
-  if (PUSH || DJ) prefetch_tile(A.P, (i64)base + (threadIdx.x >> 5) * kTile, threadIdx.x & 31, true);
-  const BlockPlan Pl = plan_block(A, base, bb, DJ ? kSpBoxBytes : kRhoBoxBytes);
+  const i64 base = (i64)blockIdx.x * kDepBlock;
+  if (STAGE) stage_block(A.P, base, kStageArrays, dsm);
+  const StageView V = STAGE ? stage_view(dsm) : global_view(A.P, base);
+  const BlockPlan Pl = plan_block(A, base, bb, DJ ? kSpBoxBytes : kRhoBoxBytes, V);
   if (Pl.use_box)
     for (int t = threadIdx.x; t < (int)Pl.nvals; t += kDepThreads) box[t] = 0;
   __syncthreads();
   const BoxGeo geo = make_geo(box, Pl, A);
   const int lane = threadIdx.x & 31;
-  const Idx tile = base + (Idx)(threadIdx.x >> 5) * kTile;
-  const Idx first = tile + (Idx)lane * kRunLen;  // this lane's run, in particle order
+  const int ltile = (threadIdx.x >> 5) * kTile;  // this warp's tile, local slots
+  const i64 first = base + ltile + (i64)lane * kRunLen;  // this lane's run, in particle order
   CellAcc<NM, 3> cj;
   CellAcc<NM, 1> cr;
   cj.live = false;
   cr.live = false;
-  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - (i64)first));
+  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - first));
   if (!Pl.use_box) {
     // a block whose nodes do not fit a box (a wide footprint): each particle
     // straight to the global accumulators at the global scales, apart from
     // the main loop so that the loop does not carry this path's registers
     for (int j = 0; j < cnt; ++j) {
-      const Idx p = tile + (Idx)j * kTileRuns + lane;
-      const float w = A.P.w[p];
+      const int ls = ltile + j * kTileRuns + lane;
+      const i64 p = base + ls;
+      const float w = V.w[ls];
       Pushed u;
       if (PUSH || DJ) {
-        u = push_one(A, p);
+        u = push_vals(A, V.ix[ls], V.fx[ls], V.y[ls], V.z[ls], V.px[ls], V.py[ls], V.pz[ls], w);
       } else {
-        u.ixh = u.ixn = A.P.ix[p];
-        u.fxh = u.fxn = A.P.fx[p];
-        u.yh = u.yn = A.P.y[p];
-        u.zh = u.zn = A.P.z[p];
+        u.ixh = u.ixn = V.ix[ls];
+        u.fxh = u.fxn = V.fx[ls];
+        u.yh = u.yn = V.y[ls];
+        u.zh = u.zn = V.z[ls];
       }
       if (PUSH) {
         A.P.ix[p] = u.ixn;
@@ -678,74 +709,62 @@ __global__ void __launch_bounds__(kDepThreads, dep_min_blocks<NM, DJ>())
     }
     return;
   }
-  // software pipeline: the next group of particles is loaded before this
-  // group's results are stored (the stores could alias the loads
-  // otherwise); G particles per group (kRhoGroup for the rho-only pass:
-  // one measured best at its 64-register budget)
-  constexpr int G = DJ ? 1 : kRhoGroup;
+  // lane r walks run r of its warp's tile (local slot ltile + 32 j + r:
+  // the warp's 32 lanes read 32 consecutive words, one bank each when
+  // staged); the next particle is loaded before this one is processed
   struct Part {
     int ix;
     float fx, y, z, px, py, pz, w;
   };
   auto load = [&](int j) {
     Part q;
-    const Idx p = tile + (Idx)j * kTileRuns + lane;
-    q.w = A.P.w[p];
-    q.ix = A.P.ix[p];
-    q.fx = A.P.fx[p];
-    q.y = A.P.y[p];
-    q.z = A.P.z[p];
+    const int ls = ltile + j * kTileRuns + lane;
+    q.w = V.w[ls];
+    q.ix = V.ix[ls];
+    q.fx = V.fx[ls];
+    q.y = V.y[ls];
+    q.z = V.z[ls];
     if (PUSH || DJ) {
-      q.px = A.P.px[p];
-      q.py = A.P.py[p];
-      q.pz = A.P.pz[p];
+      q.px = V.px[ls];
+      q.py = V.py[ls];
+      q.pz = V.pz[ls];
     }
     return q;
   };
-  Part cur[G], nxt[G];
-#pragma unroll
-  for (int g = 0; g < G; ++g)
-    if (g < cnt) cur[g] = load(g);
-  for (int j0 = 0; j0 < cnt; j0 += G) {
-#pragma unroll
-    for (int g = 0; g < G; ++g)
-      if (j0 + G + g < cnt) nxt[g] = load(j0 + G + g);
-#pragma unroll
-    for (int g = 0; g < G; ++g) {
-      const int j = j0 + g;
-      if (j >= cnt) break;
-      const Part &c = cur[g];
-      const Idx p = tile + (Idx)j * kTileRuns + lane;
-      const float w = c.w;
-      Pushed u;
-      if (PUSH || DJ) {
-        u = push_vals(A, c.ix, c.fx, c.y, c.z, c.px, c.py, c.pz, w);
-      } else {
-        u.ixh = u.ixn = c.ix;
-        u.fxh = u.fxn = c.fx;
-        u.yh = u.yn = c.y;
-        u.zh = u.zn = c.z;
-      }
-      if (PUSH) {
-        A.P.ix[p] = u.ixn;
-        A.P.fx[p] = u.fxn;
-        A.P.y[p] = u.yn;
-        A.P.z[p] = u.zn;
-      }
-      if (w == 0.0f) continue;
-      if (DJ && u.moving) {  // grid_deps.f90:42: no current from particles at rest
-        const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, A.G);
-        const float vs[3] = {u.vj[0] * Pl.lJ, u.vj[1] * Pl.lJ, u.vj[2] * Pl.lJ};
-        acc_add(cj, L, vs, 0, A.G, geo);
-      }
-      if (DR) {
-        const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, A.G);
-        const float ws[1] = {w * Pl.lR};
-        acc_add(cr, L, ws, 3 * NM, A.G, geo);
-      }
+  Part cur, nxt;
+  if (cnt > 0) cur = load(0);
+  for (int j = 0; j < cnt; ++j) {
+    if (j + 1 < cnt) nxt = load(j + 1);
+    const int ls = ltile + j * kTileRuns + lane;
+    const float w = cur.w;
+    Pushed u;
+    if (PUSH || DJ) {
+      u = push_vals(A, cur.ix, cur.fx, cur.y, cur.z, cur.px, cur.py, cur.pz, w);
+    } else {
+      u.ixh = u.ixn = cur.ix;
+      u.fxh = u.fxn = cur.fx;
+      u.yh = u.yn = cur.y;
+      u.zh = u.zn = cur.z;
     }
-#pragma unroll
-    for (int g = 0; g < G; ++g) cur[g] = nxt[g];
+    cur = nxt;
+    if (PUSH) {
+      const i64 p = base + ls;
+      A.P.ix[p] = u.ixn;
+      A.P.fx[p] = u.fxn;
+      A.P.y[p] = u.yn;
+      A.P.z[p] = u.zn;
+    }
+    if (w == 0.0f) continue;
+    if (DJ && u.moving) {  // grid_deps.f90:42: no current from particles at rest
+      const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, A.G);
+      const float vs[3] = {u.vj[0] * Pl.lJ, u.vj[1] * Pl.lJ, u.vj[2] * Pl.lJ};
+      acc_add(cj, L, vs, 0, A.G, geo);
+    }
+    if (DR) {
+      const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, A.G);
+      const float ws[1] = {w * Pl.lR};
+      acc_add(cr, L, ws, 3 * NM, A.G, geo);
+    }
   }
   if (DJ) acc_flush(cj, 0, A.G, geo);
   if (DR) acc_flush(cr, 3 * NM, A.G, geo);
@@ -956,11 +975,16 @@ __global__ void __launch_bounds__(256) gather_push_kernel(GatherArgs A, i64 nphy
 // (mode 0: real parts; modes >= 1: complex), reloading them only when the
 // cell changes.  Same interpolation and rotation as gather_push_kernel.
 template <int NM>
-__global__ void __launch_bounds__(kDepThreads, NM >= 3 ? 3 : 4) gather_push_run_kernel(GatherArgs A) {
+__global__ void __launch_bounds__(kDepThreads, 3) gather_push_run_kernel(GatherArgs A) {
+  extern __shared__ __align__(16) unsigned char gsm[];
   const SpGrid &G = A.G;
   const i64 plane = (i64)G.nx * G.nr;
   const int lane = threadIdx.x & 31;
-  const i64 tile = (i64)blockIdx.x * kDepBlock + (i64)(threadIdx.x >> 5) * kTile;
+  const i64 base = (i64)blockIdx.x * kDepBlock;
+  stage_block(A.P, base, kStageArrays, gsm);
+  const StageView V = stage_view(gsm);
+  const int ltile = (threadIdx.x >> 5) * kTile;  // this warp's tile, local slots
+  const i64 tile = base + ltile;
   const i64 first = tile + (i64)lane * kRunLen;
   int ccx = INT_MIN, ccr = INT_MIN;
   float f0[6][4];
@@ -972,18 +996,17 @@ __global__ void __launch_bounds__(kDepThreads, NM >= 3 ? 3 : 4) gather_push_run_
   };
   auto load = [&](int j) {
     Part q;
-    const i64 p = tile + (i64)j * kTileRuns + lane;
-    q.w = A.P.w[p];
-    q.ix = A.P.ix[p];
-    q.fx = A.P.fx[p];
-    q.y = A.P.y[p];
-    q.z = A.P.z[p];
-    q.px = A.P.px[p];
-    q.py = A.P.py[p];
-    q.pz = A.P.pz[p];
+    const int ls = ltile + j * kTileRuns + lane;
+    q.w = V.w[ls];
+    q.ix = V.ix[ls];
+    q.fx = V.fx[ls];
+    q.y = V.y[ls];
+    q.z = V.z[ls];
+    q.px = V.px[ls];
+    q.py = V.py[ls];
+    q.pz = V.pz[ls];
     return q;
   };
-  prefetch_tile(A.P, tile, lane, true);
   Part cur;
   if (cnt > 0) cur = load(0);
   for (int j = 0; j < cnt; ++j) {
@@ -1270,8 +1293,12 @@ int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *p
                      : push_deposit_run_kernel<3, false, false, true>;
   }
   int box_bytes = kSpBoxBytes;
-  if (!kern) kern = push_deposit_kernel;
-  else if (!A.dep_j) box_bytes = kRhoBoxBytes;
+  if (!kern) {
+    kern = push_deposit_kernel;
+  } else {
+    // the moving species' run kernels stage the block's particles ahead of the box
+    box_bytes = (push || A.dep_j) ? kStageArrays * kDepBlock * 4 + kSpBoxBytes : kRhoBoxBytes;
+  }
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, box_bytes);
   kern<<<blocks, kDepThreads, box_bytes, st>>>(A);
   chm::count_launch();
@@ -1293,12 +1320,12 @@ int gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, float *py
   cudaStream_t st = as_stream(stream);
   if (!generic && nm >= 1 && nm <= 3) {
     const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
-    if (nm == 1)
-      gather_push_run_kernel<1><<<blocks, kDepThreads, 0, st>>>(A);
-    else if (nm == 2)
-      gather_push_run_kernel<2><<<blocks, kDepThreads, 0, st>>>(A);
-    else
-      gather_push_run_kernel<3><<<blocks, kDepThreads, 0, st>>>(A);
+    // each block stages its 2048 slots of the eight particle arrays
+    const int sm = kStageArrays * kDepBlock * 4;
+    void (*kern)(GatherArgs) =
+        nm == 1 ? gather_push_run_kernel<1> : nm == 2 ? gather_push_run_kernel<2> : gather_push_run_kernel<3>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    kern<<<blocks, kDepThreads, sm, st>>>(A);
   } else {
     const i64 nphys = tiles_of(n) * kTile;
     gather_push_kernel<<<grid_for(nphys, 256, 16), 256, 0, st>>>(A, nphys);

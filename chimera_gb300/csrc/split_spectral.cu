@@ -587,7 +587,39 @@ struct GradArgs {
   float dt_inv;
   int up_from;            // modes m < up_to have an upper product
   int up_to;
+  // PSATD fused into the J update (maxwell_solvers.f90:18-96): with eg set,
+  // the element's E and G advance with the new J (real FP32 coefficients
+  // c1, c2 of nterm terms, planes of pstride elements)
+  float2 *eg;
+  const float *c1, *c2;
+  int nterm;
+  i64 pstride;
 };
+
+// the PSATD update of one spectral element from its new current jn
+__device__ __forceinline__ void psatd_elem(float2 *__restrict__ eg, const float *__restrict__ c1,
+                                           const float *__restrict__ c2, int nterm, i64 P, i64 i,
+                                           const float2 *jn, const float2 *ga, const float2 *gb) {
+  float a[5], b[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    a[k] = k < nterm ? c1[i + k * P] : 0.f;
+    b[k] = k < nterm ? c2[i + k * P] : 0.f;
+  }
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    const float2 e = eg[i + P * l], g = eg[i + P * (3 + l)], jj = jn[l];
+    float2 en = fadd(fadd(fscl(e, a[0]), fscl(g, a[1])), fscl(jj, a[2]));
+    float2 gn = fadd(fadd(fscl(e, b[0]), fscl(g, b[1])), fscl(jj, b[2]));
+    if (nterm == 5) {
+      const float2 x = ga[l], y = gb[l];
+      en = fadd(en, fadd(fscl(x, a[3]), fscl(y, a[4])));
+      gn = fadd(gn, fadd(fscl(x, b[3]), fscl(y, b[4])));
+    }
+    eg[i + P * (3 + l)] = gn;
+    eg[i + P * l] = en;
+  }
+}
 
 // The elementwise kernels below take one x line per block: blockIdx.x = kr,
 // blockIdx.y = mode, threads along x (no index division per element).
@@ -610,15 +642,19 @@ __global__ void grad32_kernel(GradArgs A) {
       for (int c = 0; c < 3; ++c) A.out[t + c * A.cs] = g[c];
     } else {
       const float f = A.pf[t];
+      float2 jn[3], ga[3], gb[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         float2 v = g[c];
         if (A.poiss == 1) {
-          float2 d = fsub(A.gnxt[t + c * A.cs], A.gprv[t + c * A.cs]);
-          v = fadd(v, fscl(d, A.dt_inv));
+          ga[c] = A.gprv[t + c * A.cs];
+          gb[c] = A.gnxt[t + c * A.cs];
+          v = fadd(v, fscl(fsub(gb[c], ga[c]), A.dt_inv));
         }
-        A.out[t + c * A.cs] = fadd(A.out[t + c * A.cs], fscl(v, f));
+        jn[c] = fadd(A.out[t + c * A.cs], fscl(v, f));
+        A.out[t + c * A.cs] = jn[c];
       }
+      if (A.eg) psatd_elem(A.eg, A.c1, A.c2, A.nterm, A.pstride, t, jn, ga, gb);
     }
   }
 }
@@ -946,10 +982,15 @@ int chm_sp_fb_grad(void *out_c64, const void *scl_c64, const void *Dp_ops, const
 //   v = grad(div(J)) (fb_graddiv, fb_math.f90:201-293)
 //   J += (v + (gnxt - gprv) dt_inv) PF      (space charge)
 //   J += v PF                               (otherwise)
-int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, const float *pf,
-                   float dt_inv, const void *Dp_ops, const void *Dm_ops, const float *kx,
-                   int64_t nx, int64_t nkr, int64_t nm, int iters, int space_charge, void *ws,
-                   int64_t ws_bytes, void *stream) {
+}  // extern "C"
+
+namespace {
+
+int poisson_impl(void *J_c64, const void *gprv_c64, const void *gnxt_c64, const float *pf,
+                 float dt_inv, const void *Dp_ops, const void *Dm_ops, const float *kx, int64_t nx,
+                 int64_t nkr, int64_t nm, int iters, int space_charge, void *eg_c64,
+                 const float *c1, const float *c2, int nterm, void *ws, int64_t ws_bytes,
+                 void *stream) {
   CHM_REQUIRE(J_c64 && pf && Dp_ops && Dm_ops && kx && nm <= 14, "sp_poisson: bad args");
   CHM_REQUIRE(!space_charge || (gprv_c64 && gnxt_c64), "sp_poisson: missing charge gradients");
   CHM_REQUIRE(ws && ws_bytes >= chm_sp_fb_ws_bytes(nx, nkr + 1, nkr, nm), "sp_poisson: workspace");
@@ -1026,10 +1067,42 @@ int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, cons
     A.pf = pf;
     A.dt_inv = dt_inv;
     A.up_to = (int)nm;
+    if (eg_c64 && it == iters - 1) {
+      A.eg = reinterpret_cast<float2 *>(eg_c64);
+      A.c1 = c1;
+      A.c2 = c2;
+      A.nterm = nterm;
+      A.pstride = cs;
+    }
     grad32_kernel<<<dim3((unsigned)nkr, (unsigned)nm), 256, 0, F.st>>>(A); chm::count_launch();
   }
   CHM_CHECK_LAUNCH();
   return CHM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64, const float *pf,
+                   float dt_inv, const void *Dp_ops, const void *Dm_ops, const float *kx,
+                   int64_t nx, int64_t nkr, int64_t nm, int iters, int space_charge, void *ws,
+                   int64_t ws_bytes, void *stream) {
+  return poisson_impl(J_c64, gprv_c64, gnxt_c64, pf, dt_inv, Dp_ops, Dm_ops, kx, nx, nkr, nm, iters,
+                      space_charge, nullptr, nullptr, nullptr, 0, ws, ws_bytes, stream);
+}
+
+// the Poisson correction with the PSATD update fused into its last J update
+int chm_sp_poisson_psatd(void *J_c64, const void *gprv_c64, const void *gnxt_c64, const float *pf,
+                         float dt_inv, const void *Dp_ops, const void *Dm_ops, const float *kx,
+                         int64_t nx, int64_t nkr, int64_t nm, int iters, int space_charge,
+                         void *eg_c64, const float *c1, const float *c2, int nterm, void *ws,
+                         int64_t ws_bytes, void *stream) {
+  CHM_REQUIRE(eg_c64 && c1 && c2 && iters >= 1, "sp_poisson_psatd: bad args");
+  CHM_REQUIRE((space_charge && nterm == 5) || (!space_charge && nterm == 3),
+              "sp_poisson_psatd: 5 PSATD terms with space charge, 3 without");
+  return poisson_impl(J_c64, gprv_c64, gnxt_c64, pf, dt_inv, Dp_ops, Dm_ops, kx, nx, nkr, nm, iters,
+                      space_charge, eg_c64, c1, c2, nterm, ws, ws_bytes, stream);
 }
 
 // B = rot(G) * PoissFact (solvers.py:536-553)

@@ -500,19 +500,22 @@ class SplitRun:
             _lib.call("chm_sp_fb_grad", self.gnxt.data_ptr(), self.Rfb.data_ptr(),
                       C.addressof(self.ops["Dp"]), C.addressof(self.ops["Dm"]),
                       self.kx32.data_ptr(), self.nx, self.nkr, self.nm, ws, wsb, st)
-        # fields
+        # fields: the Poisson correction (solvers.py:301-331) with the PSATD
+        # update (solvers.py:281-299) fused into its last J update
         if self.poisson:
-            _lib.call("chm_sp_poisson", self.Jfb.data_ptr(),
+            _lib.call("chm_sp_poisson_psatd", self.Jfb.data_ptr(),
                       self.gprv.data_ptr() if self.space_charge else None,
                       self.gnxt.data_ptr() if self.space_charge else None, self.pf.data_ptr(),
                       float(A["dt_inv"]), C.addressof(self.ops["Dp"]), C.addressof(self.ops["Dm"]),
                       self.kx32.data_ptr(), self.nx, self.nkr, self.nm, 3, int(self.space_charge),
+                      self.EG.data_ptr(), self.c1.data_ptr(), self.c2.data_ptr(), int(self.nterm),
                       ws, wsb, st)
-        P_ = self.nx * self.nkr * self.nm
-        _lib.call("chm_sp_psatd", self.EG.data_ptr(), self.Jfb.data_ptr(),
-                  self.gprv.data_ptr() if self.space_charge else None,
-                  self.gnxt.data_ptr() if self.space_charge else None, self.c1.data_ptr(),
-                  self.c2.data_ptr(), int(self.nterm), P_, st)
+        else:
+            P_ = self.nx * self.nkr * self.nm
+            _lib.call("chm_sp_psatd", self.EG.data_ptr(), self.Jfb.data_ptr(),
+                      self.gprv.data_ptr() if self.space_charge else None,
+                      self.gnxt.data_ptr() if self.space_charge else None, self.c1.data_ptr(),
+                      self.c2.data_ptr(), int(self.nterm), P_, st)
         self._project_fields_and_push()
         if ev is not None:
             ev[1].record()

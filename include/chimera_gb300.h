@@ -547,6 +547,17 @@ int chm_sp_poisson(void *J_c64, const void *gprv_c64, const void *gnxt_c64,
                    const void *Dm_ops, const float *kx, int64_t nx,
                    int64_t nkr, int64_t nm, int iters, int space_charge,
                    void *ws, int64_t ws_bytes, void *stream);
+/* chm_sp_poisson followed by chm_sp_psatd (maxwell_push_with_spchrg /
+ * maxwell_push_wo_spchrg, maxwell_solvers.f90:18-96) in one pass: the last
+ * J update of the correction also advances E and G of eg_c64 (nx, nkr, nm,
+ * 6) with the FP32 coefficients c1, c2 (nx, nkr, nm, nterm); nterm 5 with
+ * space charge, 3 without.  Bitwise the two calls' result. */
+int chm_sp_poisson_psatd(void *J_c64, const void *gprv_c64, const void *gnxt_c64,
+                         const float *pf, float dt_inv, const void *Dp_ops,
+                         const void *Dm_ops, const float *kx, int64_t nx,
+                         int64_t nkr, int64_t nm, int iters, int space_charge,
+                         void *eg_c64, const float *c1, const float *c2, int nterm,
+                         void *ws, int64_t ws_bytes, void *stream);
 int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf,
                  const void *Dp_ops, const void *Dm_ops, const float *kx,
                  int64_t nx, int64_t nkr, int64_t nm, void *ws,

@@ -134,6 +134,40 @@ def test_split_spectral_operators_match_fp64(mods, lpa):
     assert rel_l2(EBs.cpu().numpy(), EBd.cpu().numpy()) < TOL_T
 
 
+@pytest.mark.parametrize("space_charge", [1, 0])
+def test_poisson_with_fused_psatd_equals_two_calls(mods, lpa, space_charge):
+    """chm_sp_poisson_psatd (PSATD fused into the correction's last J
+    update) gives bitwise the J and E/G of chm_sp_poisson + chm_sp_psatd."""
+    torch, _lib, fm, split = mods
+    g, o, ws, (nx, nr, nkr, nm) = lpa
+    st = _st(torch)
+    kx32 = _c(g["kx"], torch).to(torch.float32)
+    pf32 = _c(g["PoissFact"].astype(np.float32), torch)
+    nterm = 5 if space_charge else 3
+    rng = np.random.default_rng(8)
+    c1 = _c(rng.standard_normal((nx, nkr, nm, nterm)).astype(np.float32), torch)
+    c2 = _c(rng.standard_normal((nx, nkr, nm, nterm)).astype(np.float32), torch)
+    J0 = _c(_rand((nx, nkr, nm, 3), 2).astype(np.complex64), torch)
+    EG0 = _c(_rand((nx, nkr, nm, 6), 3).astype(np.complex64), torch)
+    gp = _c((0.1 * _rand((nx, nkr, nm, 3), 4)).astype(np.complex64), torch)
+    gn = _c((0.1 * _rand((nx, nkr, nm, 3), 5)).astype(np.complex64), torch)
+    sc_args = (gp.data_ptr(), gn.data_ptr()) if space_charge else (None, None)
+    Ja, EGa = J0.clone(memory_format=torch.preserve_format), EG0.clone(memory_format=torch.preserve_format)
+    _lib.call("chm_sp_poisson", Ja.data_ptr(), *sc_args, pf32.data_ptr(), 10.0,
+              C.addressof(o["Dp"][0]), C.addressof(o["Dm"][0]), kx32.data_ptr(), nx, nkr, nm, 3,
+              space_charge, ws.data_ptr(), ws.numel(), st)
+    _lib.call("chm_sp_psatd", EGa.data_ptr(), Ja.data_ptr(), *sc_args, c1.data_ptr(),
+              c2.data_ptr(), nterm, nx * nkr * nm, st)
+    Jb, EGb = J0.clone(memory_format=torch.preserve_format), EG0.clone(memory_format=torch.preserve_format)
+    _lib.call("chm_sp_poisson_psatd", Jb.data_ptr(), *sc_args, pf32.data_ptr(), 10.0,
+              C.addressof(o["Dp"][0]), C.addressof(o["Dm"][0]), kx32.data_ptr(), nx, nkr, nm, 3,
+              space_charge, EGb.data_ptr(), c1.data_ptr(), c2.data_ptr(), nterm, ws.data_ptr(),
+              ws.numel(), st)
+    torch.cuda.synchronize()
+    assert torch.equal(Ja, Jb) and torch.equal(EGa, EGb)
+    assert not torch.equal(EGa, EG0)
+
+
 def _lpa_comps(seed, xchunked=False, max_mode=1):
     from chimera_gb300 import Solver, Specie
     from chimera_gb300.messages import msg
