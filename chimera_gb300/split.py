@@ -171,7 +171,7 @@ class _SpParticles:
                   tw.data_ptr(), tw.stride(0), float(X0), float(dx), m, _stream())
         self.n += m
 
-    def sort_cells(self, win_k, nx, nr, dr_inv):
+    def sort_cells(self, win_k, win_f, nx, nr, dr_inv):
         """Re-sort the particles by deposit cell (chm_sp_sort_cells), dropping
         the dead ones; one device->host read (the live count)."""
         if self.n == 0:
@@ -181,7 +181,8 @@ class _SpParticles:
         ws = chimera.workspace(_lib.query("chm_sp_sort_ws_bytes", self.n), self.device)
         n_out = torch.empty(1, dtype=torch.int64, device=self.device)
         _lib.call("chm_sp_sort_cells", *self.ptrs(), self.dead.data_ptr(), self.n, int(win_k),
-                  int(nx), int(nr), float(dr_inv), *self.ptrs(self.spare), n_out.data_ptr(),
+                  float(win_f), int(nx), int(nr), float(dr_inv), *self.ptrs(self.spare),
+                  n_out.data_ptr(),
                   ws.data_ptr(), ws.numel(), _stream())
         n = int(n_out.item())
         chimera.io_bytes["d2h"] += 8
@@ -217,19 +218,27 @@ def _stream():
 class SortCadence:
     """Run-time choice of the re-sort cadence (steps between two sorts by
     deposit cell).  As particles drift, the cell runs of the deposit and
-    gather kernels break up and those kernels slow down; a sort costs a
-    fixed time S.  With the particle kernels' time growing by g per step
-    after a sort, sorting every c steps costs S / c + g c / 2 per step,
-    least at c = sqrt(2 S / g).  Both S and g are measured with CUDA events
-    (read back only at the next sort, so no step waits for them) and the
-    cadence is refreshed after every interval; ``history`` keeps
-    (step, cadence, sort ms, slope ms/step) for the record."""
+    gather kernels break up and those kernels slow down by g per step; a
+    sort costs a fixed time S and recovers what the drift cost.  Sorting
+    every c steps then costs S / c + g c / 2 per step, least at
+    c = sqrt(2 S / g).  S is timed directly; g is the time a sort recovers
+    (the step time of the last steps before a sort minus that of the first
+    steps after it) over the steps since the previous sort, so that the
+    physical growth of the work (more particles moving as the laser enters
+    the plasma) is not mistaken for disorder.  When a sort recovers nothing
+    the cadence goes to its maximum.  The step times come from CUDA events
+    read back at the next sort, so no step waits for them; ``history`` keeps
+    (step, cadence, sort ms, recovered ms per step) for the record."""
+
+    NAVG = 4  # steps averaged on each side of a sort
 
     def __init__(self, start=32, lo=8, hi=512):
         self.cadence, self.lo, self.hi = start, lo, hi
         self.history = []
-        self._events = []      # (steps since sort, start, end) of the particle kernels
+        self._events = []      # (steps since sort, start, end) of the interval's steps
         self._sort_ev = None   # (start, end) of the last sort
+        self._tail = None      # mean step ms of the last steps before the last sort
+        self._last_len = None  # steps of the interval that ended with the last sort
 
     def step_events(self, since):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -242,17 +251,19 @@ class SortCadence:
 
     def update(self, step):
         """After a sort (the stream has been synchronised by its count read)."""
-        t = [(s, a.elapsed_time(b)) for s, a, b in self._events if a.query() and b.query()]
+        t = [v for _, v in sorted((s, a.elapsed_time(b)) for s, a, b in self._events
+                                  if a.query() and b.query())]
         self._events = []
         S = self._sort_ev[0].elapsed_time(self._sort_ev[1]) if self._sort_ev else None
         g = None
-        if len(t) >= 4 and S is not None:
-            x = np.array([u for u, _ in t], dtype=float)
-            y = np.array([v for _, v in t], dtype=float)
-            if x.std() > 0:
-                g = float(np.polyfit(x, y, 1)[0])
+        if len(t) >= 2 * self.NAVG:
+            head = float(np.mean(t[:self.NAVG]))
+            if self._tail is not None and self._last_len and S is not None:
+                g = (self._tail - head) / self._last_len
                 c = self.hi if g <= 0 else int(np.sqrt(2.0 * S / g))
                 self.cadence = int(min(self.hi, max(self.lo, c)))
+            self._tail = float(np.mean(t[-self.NAVG:]))
+        self._last_len = len(t)
         self.history.append((int(step), int(self.cadence), S, g))
 
 
@@ -533,13 +544,13 @@ class SplitRun:
 
     def resort(self, istep=None):
         """Re-sort every species by deposit cell (dead particles dropped)."""
-        k, _ = self._win()
+        k, f = self._win()
         auto = self.sort_every == "auto"
         if auto:
             ev = self.sorter.sort_events()
             ev[0].record()
         for spc, P in zip(self.fp.Particles, self.parts):
-            P.sort_cells(k, self.nx, self.nr, float(self.solver.Args["dr_inv"]))
+            P.sort_cells(k, f, self.nx, self.nr, float(self.solver.Args["dr_inv"]))
         if auto:
             ev[1].record()
             ev[1].synchronize()

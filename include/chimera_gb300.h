@@ -508,18 +508,21 @@ int chm_sp_compact(const int32_t *ix, const float *fx, const float *y,
  * then the lower or upper deposit cell of the generation cell -- written in
  * tile layout to the *_out arrays (the capacity of the input); dead
  * particles are dropped and *n_out (device int64) receives the live count.
- * The key of a particle is ((((pr P + px') 4 + lr) 4 + lx') 2 + half with
- * gx = min(max(ix - win_k + 8, 0), nx + 24), gr = min(floor(s), nr + 4),
- * s = sqrt(y y + z z) dr_inv (each operation rounded in FP32), half =
- * (s - floor(s) >= 0.5), px = gx / 4, lx = gx % 4, pr = gr / 4, lr = gr % 4,
+ * The key of a particle is (((((pr P + px') 4 + lr) 4 + lx') 2 + half) 16
+ * + 4 qx + qr with gx = min(max(ix - win_k + 8, 0), nx + 24), gr =
+ * min(floor(s), nr + 4), s = sqrt(y y + z z) dr_inv, fr = s - floor(s),
+ * half = (fr >= 0.5), px = gx / 4, lx = gx % 4, pr = gr / 4, lr = gr % 4,
  * P = (nx + 24) / 4 + 1, px' = pr odd ? P - 1 - px : px, lx' = lr odd ?
- * 3 - lx : lx; ties keep the slot order.  n < 2^31. */
+ * 3 - lx : lx, and the quarter of the deposit cell qx = min(3, floor(4 sx)),
+ * qr = min(3, floor(4 sr)) with d = fx - win_f, sx = d - floor(d), sr =
+ * half ? fr - 1/2 : fr + 1/2 (each operation rounded in FP32); ties keep the
+ * slot order.  n < 2^31. */
 int64_t chm_sp_sort_ws_bytes(int64_t n);
 int chm_sp_sort_cells(const int32_t *ix, const float *fx, const float *y,
                       const float *z, const float *px, const float *py,
                       const float *pz, const float *w, const uint8_t *dead,
-                      int64_t n, int win_k, int nx, int nr, float dr_inv,
-                      int32_t *ix_out, float *fx_out, float *y_out, float *z_out,
+                      int64_t n, int win_k, float win_f, int nx, int nr,
+                      float dr_inv, int32_t *ix_out, float *fx_out, float *y_out, float *z_out,
                       float *px_out, float *py_out, float *pz_out, float *w_out,
                       int64_t *n_out, void *ws, int64_t ws_bytes, void *stream);
 

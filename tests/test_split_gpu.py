@@ -378,13 +378,14 @@ def test_sort_by_cell_matches_host(mods):
     dead_h = np.zeros(cap, np.uint8)
     dead_h[_slots(n)[rng.random(n) < 0.05]] = 1
     dead = torch.from_numpy(dead_h).cuda()
-    win_k = 100
+    win_k, win_f = 100, np.float32(0.375)
     st = _st(torch)
     Q = {k: torch.full_like(v, 7) for k, v in P.items()}
     ws = torch.empty(_lib.query("chm_sp_sort_ws_bytes", n), dtype=torch.uint8, device="cuda")
     n_out = torch.zeros(1, dtype=torch.int64, device="cuda")
-    _lib.call("chm_sp_sort_cells", *[P[k].data_ptr() for k in names], dead.data_ptr(), n, win_k, nx,
-              nr, np.float32(1 / dr), *[Q[k].data_ptr() for k in names], n_out.data_ptr(),
+    _lib.call("chm_sp_sort_cells", *[P[k].data_ptr() for k in names], dead.data_ptr(), n, win_k,
+              float(win_f), nx, nr, np.float32(1 / dr), *[Q[k].data_ptr() for k in names],
+              n_out.data_ptr(),
               ws.data_ptr(), ws.numel(), st)
     torch.cuda.synchronize()
     h = {k: v.cpu().numpy() for k, v in P.items()}
@@ -394,14 +395,20 @@ def test_sort_by_cell_matches_host(mods):
     y, z = h["y"], h["z"]
     sv = np.sqrt(y * y + z * z).astype(f32) * f32(1 / dr)
     grf = np.floor(sv)
-    half = ((sv - grf) >= f32(0.5)).astype(np.uint64)
+    fr = (sv - grf).astype(f32)
+    half = (fr >= f32(0.5)).astype(np.uint64)
+    dxf = (h["fx"] - win_f).astype(f32)
+    sx = (dxf - np.floor(dxf)).astype(f32)
+    sr = np.where(half == 1, fr - f32(0.5), fr + f32(0.5)).astype(f32)
+    qx = np.minimum(3, np.floor(sx * f32(4)).astype(np.int64)).astype(np.uint64)
+    qr = np.minimum(3, np.floor(sr * f32(4)).astype(np.int64)).astype(np.uint64)
     gr = np.minimum(np.maximum(grf.astype(np.int64), 0), nr + 4).astype(np.uint64)
     gx = np.minimum(np.maximum(h["ix"].astype(np.int64) - win_k + 8, 0), nx + 24).astype(np.uint64)
     npx = np.uint64((nx + 24) // 4 + 1)
     px, lx, pr, lr = gx >> 2, gx & 3, gr >> 2, gr & 3
     pxs = np.where(pr & 1, npx - 1 - px, px)
     lxs = np.where(lr & 1, 3 - lx, lx)
-    key = ((((pr * npx + pxs) * 4 + lr) * 4 + lxs) << 1) | half
+    key = ((((((pr * npx + pxs) * 4 + lr) * 4 + lxs) * 2 + half) << 4) | (qx << 2) | qr)
     key = np.where(live, key, 0xffffffff).astype(np.uint64)
     order = np.argsort(key, kind="stable")
     nlive = int(live.sum())
