@@ -156,8 +156,10 @@ FP64_BYTES = {"push_velocs": 48 + 48 + 24, "push_coords": 24 + 24 + 24 + 24,
 # by the number of stored modes, from one ncu capture of a quarter-radius
 # case (traffic grows with the particle count): 2 modes from --size prof
 # (4.13M particles per species: electrons (push + J + rho) 179.9 MB, still
-# ions (rho) 87.3 MB)
-SPLIT_TRAFFIC = {2: {"push_electrons": 179.90e6 / 4128768, "deposit_still": 87.29e6 / 4128768}}
+# ions (rho) 87.3 MB); 3 modes from --size prof3 (12.49M per species:
+# electrons 637.8 MB, still ions 273.1 MB)
+SPLIT_TRAFFIC = {2: {"push_electrons": 179.90e6 / 4128768, "deposit_still": 87.29e6 / 4128768},
+                 3: {"push_electrons": 637.78e6 / 12490704, "deposit_still": 273.07e6 / 12490704}}
 GEMM_STAGES = ("chm_fb_graddiv", "chm_fb_rot", "chm_fb_grad", "chm_fb_div", "chm_fb_in",
                "chm_fb_out", "chm_fb_eb_out", "chm_sp_poisson", "chm_sp_poisson_psatd",
                "chm_sp_fb_in_acc",
@@ -616,6 +618,88 @@ def run_batched(args):
     return 0
 
 
+def run_spectral(args):
+    """The split form's spectral stages alone on the workload's grid (random
+    complex64 fields, no particles), each timed with CUDA events: the case
+    the tensor-core product kernel is profiled on.  --spectral-stages picks
+    the stages (poisson, eb_out, fb_in, rot_b)."""
+    import ctypes as C
+
+    import torch
+
+    from chimera_gb300 import _lib
+    from chimera_gb300 import fimera as fm
+    from chimera_gb300 import split
+    from chimera_gb300.messages import msg
+    from chimera_gb300.solvers import Solver
+    msg.quiet = True
+    S = Solver(dict(workloads.config(WORKLOAD_SIZE)["solver"]))
+    A = S.Args
+    nx, nr, nkr, nm = A["Nx"], A["Nr"], A["Nkr"], A["Mtot"]
+    dev = torch.device("cuda")
+    o = {k: split._prepare_ops(A[key], dev) for k, key in
+         (("InCurr", "InCurr"), ("Out", "Out"), ("Dp", "DpS2S"), ("Dm", "DmS2S"))}
+    ws = torch.empty(_lib.query("chm_sp_fb_ws_bytes", nx, nr, nkr, nm), dtype=torch.uint8,
+                     device=dev)
+    st = torch.cuda.current_stream().cuda_stream
+    kx64 = S.dev["kx"]
+    kx32 = kx64.to(torch.float32)
+    pf32 = torch.from_numpy(np.asfortranarray(A["PoissFact"].astype(np.float32))).cuda()
+    depf = torch.from_numpy(np.asfortranarray(A["DepFact"].astype(np.float32))).cuda()
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(7)
+
+    def rnd(shape):
+        t = fm.fortran_zeros(shape, torch.complex64)
+        t.real.normal_(generator=gen)
+        t.imag.normal_(generator=gen)
+        return t
+    J, gp, gn = rnd((nx, nkr, nm, 3)), rnd((nx, nkr, nm, 3)), rnd((nx, nkr, nm, 3))
+    EG, Bf = rnd((nx, nkr, nm, 6)), rnd((nx, nkr, nm, 3))
+    G = EG[:, :, :, 3:]
+    EB = fm.fortran_zeros((nx, nr, nm, 6), torch.complex64)
+    acc = torch.randint(-2 ** 40, 2 ** 40, (nx * nr * nm * 3 * 2,), dtype=torch.int64, device=dev,
+                        generator=gen)
+    sc = torch.tensor([2.0 ** 40, 1.0], dtype=torch.float64, device=dev)
+    lib = _lib.load()
+    P = lambda name: C.addressof(o[name][0])  # noqa: E731
+    stages = {
+        "poisson": lambda: _lib.call("chm_sp_poisson", J.data_ptr(), gp.data_ptr(), gn.data_ptr(),
+                                     pf32.data_ptr(), 10.0, P("Dp"), P("Dm"), kx32.data_ptr(), nx,
+                                     nkr, nm, 3, 1, ws.data_ptr(), ws.numel(), st),
+        "eb_out": lambda: _lib.call("chm_sp_fb_eb_out", EB.data_ptr(), EG.data_ptr(), Bf.data_ptr(),
+                                    1.0, kx64.data_ptr(), P("Out"), nx, nr, nkr, nm, ws.data_ptr(),
+                                    ws.numel(), st),
+        "fb_in": lambda: _lib.call("chm_sp_fb_in_acc", J.data_ptr(), acc.data_ptr(), sc.data_ptr(),
+                                   None, None, 1.0, kx64.data_ptr(), P("InCurr"), depf.data_ptr(), nx,
+                                   nr, nkr, nm, 3, ws.data_ptr(), ws.numel(), st),
+        "rot_b": lambda: _lib.call("chm_sp_rot_b", Bf.data_ptr(), G.data_ptr(), pf32.data_ptr(),
+                                   P("Dp"), P("Dm"), kx32.data_ptr(), nx, nkr, nm, ws.data_ptr(),
+                                   ws.numel(), st),
+    }
+    peaks, peak_kind = load_peaks()
+    out = {}
+    for name in args.spectral_stages.split(","):
+        f = stages[name]
+        f()
+        torch.cuda.synchronize()
+        f0 = lib.chm_gemm_flops()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            f()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        fl = (lib.chm_gemm_flops() - f0) / args.steps
+        out[name] = {"ms": ms, "algorithmic_tflops": fl / ms / 1e9,
+                     "executed_tflops": 6 * fl / ms / 1e9,
+                     "executed_frac": 6 * fl / ms / 1e9 / float(peaks.get("bf16_tflops", 1900.0))}
+    print(json.dumps({"spectral_stages": out, "workload": workloads.SIZES[WORKLOAD_SIZE].name,
+                      "umma_status": int(lib.chm_sp_umma_status()), "peaks": peak_kind}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -636,6 +720,9 @@ def main():
                     help="fp64 = plain FP64 form; split = split-precision form")
     ap.add_argument("--batched", type=int, default=0,
                     help="run the batched workload with this many instances instead")
+    ap.add_argument("--spectral", action="store_true",
+                    help="time the split form's spectral stages alone on the grid (profiling)")
+    ap.add_argument("--spectral-stages", default="poisson,eb_out,fb_in,rot_b")
     ap.add_argument("--size", default="cfg3", choices=sorted(workloads.SIZES),
                     help="cfg3 = the benchmark workload; cfg2, cfg1 the smaller configurations; "
                          "prof3, prof, spec, small = reduced cases for profiling")
@@ -648,6 +735,8 @@ def main():
         return run_reference(args)
     if args.batched:
         return run_batched(args)
+    if args.spectral:
+        return run_spectral(args)
     return run_gb300(args)
 
 
