@@ -669,10 +669,10 @@ def run_spectral(args):
                                      nkr, nm, 3, 1, ws.data_ptr(), ws.numel(), st),
         "eb_out": lambda: _lib.call("chm_sp_fb_eb_out", EB.data_ptr(), EG.data_ptr(), Bf.data_ptr(),
                                     1.0, kx64.data_ptr(), P("Out"), nx, nr, nkr, nm, ws.data_ptr(),
-                                    ws.numel(), st),
+                                    ws.numel(), st, None),
         "fb_in": lambda: _lib.call("chm_sp_fb_in_acc", J.data_ptr(), acc.data_ptr(), sc.data_ptr(),
                                    None, None, 1.0, kx64.data_ptr(), P("InCurr"), depf.data_ptr(), nx,
-                                   nr, nkr, nm, 3, ws.data_ptr(), ws.numel(), st),
+                                   nr, nkr, nm, 3, ws.data_ptr(), ws.numel(), st, None),
         "rot_b": lambda: _lib.call("chm_sp_rot_b", Bf.data_ptr(), G.data_ptr(), pf32.data_ptr(),
                                    P("Dp"), P("Dm"), kx32.data_ptr(), nx, nkr, nm, ws.data_ptr(),
                                    ws.numel(), st),

@@ -3,7 +3,8 @@
 Every instance is a ``SplitRun`` (split-precision form) with its own CUDA
 stream.  ``BatchedRun.make_step(istep)`` issues each instance's step on its
 stream, so the kernels of small instances, which fill only part of the GPU
-alone, run concurrently.  Instances share nothing: each result is bitwise
+alone, run concurrently; ``graph_step(istep)`` replays all the instances'
+steps from one CUDA graph (one launch per step from the host).  Instances share nothing: each result is bitwise
 the one the instance gives when advanced alone (the step is deterministic and
 has no cross-instance state).
 
@@ -46,6 +47,54 @@ class BatchedRun:
         for run, s in zip(self.runs, self.streams):
             with torch.cuda.stream(s):
                 run.make_step(istep)
+
+    def graph_step(self, istep: int) -> None:
+        """make_step with every instance's step in one CUDA graph: the
+        instances' device work is captured on their own streams (forked from
+        the capture stream and joined back), so one replay per step runs them
+        all, concurrently where they fit.  Captured on first use and again
+        when an instance's particle arrays change; host-side window
+        bookkeeping, re-sorts and error-flag reads run outside the graph.
+        Falls back to make_step when a step is not capturable
+        (SplitRun.graph_capturable)."""
+        if self.form != "split" or not all(r.graph_capturable() for r in self.runs):
+            return self.make_step(istep)
+        cur = torch.cuda.current_stream()
+        for r, s in zip(self.runs, self.streams):
+            s.wait_stream(cur)
+            with torch.cuda.stream(s):
+                r._maybe_sort(istep)
+                if not r._scales_valid:
+                    r._refresh_scales()
+            cur.wait_stream(s)
+        key = tuple(r._layout_key() for r in self.runs)
+        graphs = getattr(self, "_graphs", None)
+        layout = tuple(k[:-1] for k in key)
+        if graphs is None or graphs[0] != layout:
+            graphs = self._graphs = [layout, {}]  # per gradient-buffer assignment
+        self._graph = graphs[1].get(tuple(k[-1] for k in key))
+        if self._graph is None:
+            from . import _lib
+            lib = _lib.load()
+            g = torch.cuda.CUDAGraph()
+            n0 = lib.chm_launch_count()
+            with torch.cuda.graph(g):
+                cap = torch.cuda.current_stream()
+                for r, s in zip(self.runs, self.streams):
+                    s.wait_stream(cap)
+                    with torch.cuda.stream(s):
+                        r._step_body(istep)
+                for s in self.streams:
+                    cap.wait_stream(s)
+            self.graph_launches = lib.chm_launch_count() - n0  # kernels per replay
+            self._graph = graphs[1][tuple(k[-1] for k in key)] = g
+            self.graph_captures = getattr(self, "graph_captures", 0) + 1
+        else:
+            for r in self.runs:
+                r._host_effects(istep)
+        self._graph.replay()
+        for r in self.runs:
+            r._after_step()
 
     def synchronize(self) -> None:
         for s in self.streams:

@@ -74,6 +74,15 @@ struct SpGrid {
   int nx, nr, nm;  // spatial grid
 };
 
+// the window origin from the device record when there is one
+__device__ __forceinline__ SpGrid window_grid(SpGrid G, const chm_sp_window *w) {
+  if (w) {
+    G.win_k = w->k;
+    G.win_f = w->f;
+  }
+  return G;
+}
+
 // ceil(log2 v) of a positive finite float, and the exponent of a power of
 // two held in a double (from its bits): the per-block plan stays off the
 // FP64 pipe
@@ -175,6 +184,7 @@ struct PushDepArgs {
   unsigned long long *accJ;  // (nx, nr, nm, 3) x {re, im}
   unsigned long long *accR;  // (nx, nr, nm) x {re, im}
   const double *scaleJ, *scaleR;  // global scales 2^e
+  const chm_sp_window *win;       // device window origin (or null: G's)
 };
 
 // Block box: 32-bit fixed-point values at the block's own scales 2^elJ,
@@ -474,7 +484,9 @@ __device__ __forceinline__ BoxGeo make_geo(int *box, const BlockPlan &P, const P
 // Generic push + deposit (any nm): one particle per thread and slot, each
 // value rounded to the block quantum and added to the box (or, without a
 // box, to the global quantum and added to the global accumulator).
-__global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A) {
+__global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A_) {
+  PushDepArgs A = A_;
+  A.G = window_grid(A_.G, A_.win);
   extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
   const i64 base = (i64)blockIdx.x * kDepBlock;
@@ -641,7 +653,9 @@ constexpr int kRhoMinBlocks = 8;
 
 template <int NM, bool PUSH, bool DJ, bool DR>
 __global__ void __launch_bounds__(kDepThreads, (PUSH || DJ) ? 2 : kRhoMinBlocks)
-    push_deposit_run_kernel(PushDepArgs A) {
+    push_deposit_run_kernel(PushDepArgs A_) {
+  PushDepArgs A = A_;
+  A.G = window_grid(A_.G, A_.win);
   extern __shared__ __align__(16) unsigned char dsm[];
   constexpr bool STAGE = PUSH || DJ;
   int *box = reinterpret_cast<int *>(dsm + (STAGE ? (size_t)kStageArrays * kDepBlock * 4 : 0));
@@ -918,11 +932,12 @@ struct GatherArgs {
   SpGrid G;
   const float2 *eb;  // (nx, nr, nm, 6) complex64, Fortran order
   float dtq;          // push_fact * dt
+  const chm_sp_window *win;  // device window origin (or null: G's)
 };
 
 // generic gather (any nm), one particle per thread and slot
 __global__ void __launch_bounds__(256) gather_push_kernel(GatherArgs A, i64 nphys) {
-  const SpGrid &G = A.G;
+  const SpGrid G = window_grid(A.G, A.win);
   const i64 plane = (i64)G.nx * G.nr;
   for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < nphys;
        p += (i64)gridDim.x * blockDim.x) {
@@ -977,7 +992,7 @@ __global__ void __launch_bounds__(256) gather_push_kernel(GatherArgs A, i64 nphy
 template <int NM>
 __global__ void __launch_bounds__(kDepThreads, 3) gather_push_run_kernel(GatherArgs A) {
   extern __shared__ __align__(16) unsigned char gsm[];
-  const SpGrid &G = A.G;
+  const SpGrid G = window_grid(A.G, A.win);
   const i64 plane = (i64)G.nx * G.nr;
   const int lane = threadIdx.x & 31;
   const i64 base = (i64)blockIdx.x * kDepBlock;
@@ -1256,7 +1271,8 @@ namespace {
 int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,
                  float *w, int64_t n, int win_k, float win_f, float dx_inv, float dr_inv, float dt,
                  int nx, int nr, int nm, int push, uint64_t *accJ, const double *scaleJ,
-                 uint64_t *accR, const double *scaleR, void *stream, bool generic) {
+                 uint64_t *accR, const double *scaleR, void *stream, bool generic,
+                 const chm_sp_window *win) {
   CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && nm >= 1 && nm <= 8, "sp_push_deposit: bad dims");
   if (n == 0) return CHM_OK;
   CHM_REQUIRE(ix && fx && y && z && px && py && pz && w, "sp_push_deposit: null particle array");
@@ -1274,6 +1290,7 @@ int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *p
   A.accR = reinterpret_cast<unsigned long long *>(accR);
   A.scaleJ = scaleJ;
   A.scaleR = scaleR;
+  A.win = win;
   const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
   cudaStream_t st = as_stream(stream);
   // run kernels for nm 1..3 and the three uses: moving species (push, J,
@@ -1308,7 +1325,7 @@ int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *p
 
 int gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,
                 float *w, int64_t n, int win_k, float win_f, float dr_inv, const void *eb_c64, int nx,
-                int nr, int nm, float dtq, void *stream, bool generic) {
+                int nr, int nm, float dtq, void *stream, bool generic, const chm_sp_window *win) {
   CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && nm >= 1, "sp_gather_push: bad dims");
   if (n == 0) return CHM_OK;
   CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && eb_c64, "sp_gather_push: null pointer");
@@ -1317,6 +1334,7 @@ int gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, float *py
   A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
   A.eb = reinterpret_cast<const float2 *>(eb_c64);
   A.dtq = dtq;
+  A.win = win;
   cudaStream_t st = as_stream(stream);
   if (!generic && nm >= 1 && nm <= 3) {
     const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
@@ -1343,18 +1361,18 @@ int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, f
                         float *pz, float *w, int64_t n, int win_k, float win_f, float dx_inv,
                         float dr_inv, float dt, int nx, int nr, int nm, int push,
                         uint64_t *accJ, const double *scaleJ, uint64_t *accR,
-                        const double *scaleR, void *stream) {
+                        const double *scaleR, void *stream, const chm_sp_window *win) {
   return push_deposit(ix, fx, y, z, px, py, pz, w, n, win_k, win_f, dx_inv, dr_inv, dt, nx, nr, nm,
-                      push, accJ, scaleJ, accR, scaleR, stream, false);
+                      push, accJ, scaleJ, accR, scaleR, stream, false, win);
 }
 
 int chm_sp_push_deposit_generic(int32_t *ix, float *fx, float *y, float *z, float *px, float *py,
                                 float *pz, float *w, int64_t n, int win_k, float win_f,
                                 float dx_inv, float dr_inv, float dt, int nx, int nr, int nm,
                                 int push, uint64_t *accJ, const double *scaleJ, uint64_t *accR,
-                                const double *scaleR, void *stream) {
+                                const double *scaleR, void *stream, const chm_sp_window *win) {
   return push_deposit(ix, fx, y, z, px, py, pz, w, n, win_k, win_f, dx_inv, dr_inv, dt, nx, nr, nm,
-                      push, accJ, scaleJ, accR, scaleR, stream, true);
+                      push, accJ, scaleJ, accR, scaleR, stream, true, win);
 }
 
 int64_t chm_sp_deposit_dropped(void) {
@@ -1366,17 +1384,18 @@ int64_t chm_sp_deposit_dropped(void) {
 
 int chm_sp_gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,
                        float *w, int64_t n, int win_k, float win_f, float dr_inv,
-                       const void *eb_c64, int nx, int nr, int nm, float dtq, void *stream) {
+                       const void *eb_c64, int nx, int nr, int nm, float dtq, void *stream,
+                       const chm_sp_window *win) {
   return gather_push(ix, fx, y, z, px, py, pz, w, n, win_k, win_f, dr_inv, eb_c64, nx, nr, nm, dtq,
-                     stream, false);
+                     stream, false, win);
 }
 
 int chm_sp_gather_push_generic(int32_t *ix, float *fx, float *y, float *z, float *px, float *py,
                                float *pz, float *w, int64_t n, int win_k, float win_f,
                                float dr_inv, const void *eb_c64, int nx, int nr, int nm, float dtq,
-                               void *stream) {
+                               void *stream, const chm_sp_window *win) {
   return gather_push(ix, fx, y, z, px, py, pz, w, n, win_k, win_f, dr_inv, eb_c64, nx, nr, nm, dtq,
-                     stream, true);
+                     stream, true, win);
 }
 
 int chm_sp_from_f64(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,

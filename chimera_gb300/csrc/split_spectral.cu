@@ -81,8 +81,10 @@ __global__ void twiddle32_kernel(float2 *tw, int n) {
 // FP32; with tw, also the FFT twiddles exp(-2 pi i t / nx) (as twiddle32_kernel).
 // Launched with warp-sized blocks: the FP64 trigonometry spreads over as
 // many SMs as there are warps of work.
+// (win: the device window origin, when given, instead of leftX)
 __global__ void shift32_kernel(float2 *shift, const double *kx, double leftX, int sign, i64 nx,
-                               float2 *tw) {
+                               float2 *tw, const chm_sp_window *win = nullptr) {
+  if (win) leftX = win->leftX;
   for (i64 x = blockIdx.x * (i64)blockDim.x + threadIdx.x; x < nx; x += (i64)gridDim.x * blockDim.x) {
     double s, c;
     sincos(leftX * kx[x], &s, &c);
@@ -92,6 +94,23 @@ __global__ void shift32_kernel(float2 *shift, const double *kx, double leftX, in
       tw[x] = make_float2((float)c, (float)-s);
     }
   }
+}
+
+// the window record: k = floor((leftX - X0) / dx), f = the rest (FP64)
+__global__ void window_kernel(chm_sp_window *w, int set, double leftX, double X0, double dx,
+                              double shift) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (set) {
+    w->leftX = leftX;
+    w->X0 = X0;
+    w->dx = dx;
+  } else {
+    w->leftX = w->leftX + shift;
+  }
+  const double sv = (w->leftX - w->X0) / w->dx;
+  const double k = floor(sv);
+  w->k = (int32_t)k;
+  w->f = (float)(sv - k);
 }
 
 __device__ __forceinline__ float2 tw32(const float2 *tw, int t, int sign) {
@@ -797,7 +816,8 @@ int64_t chm_sp_fb_ws_bytes(int64_t nx, int64_t nr, int64_t nkr, int64_t nm) {
 int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, const int64_t *acc2,
                      const double *scale2, double leftX, const double *kx, const void *In_ops,
                      const float *fact, int64_t nx, int64_t nr, int64_t nkr, int64_t nm,
-                     int64_t ncomp, void *ws, int64_t ws_bytes, void *stream) {
+                     int64_t ncomp, void *ws, int64_t ws_bytes, void *stream,
+                     const chm_sp_window *win) {
   CHM_REQUIRE(out_c64 && acc && scale && kx && In_ops && fact, "sp_fb_in_acc: null pointer");
   CHM_REQUIRE(ws && ws_bytes >= chm_sp_fb_ws_bytes(nx, nr, nkr, nm), "sp_fb_in_acc: workspace");
   cudaStream_t st = as_stream(stream);
@@ -810,7 +830,7 @@ int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, con
     set_error("sp_fb_in_acc: workspace exhausted");
     return CHM_ERR_WS;
   }
-  shift32_kernel<<<grid_for(nx, 32), 32, 0, st>>>(shift, kx, leftX, -1, nx, tw); chm::count_launch();
+  shift32_kernel<<<grid_for(nx, 32), 32, 0, st>>>(shift, kx, leftX, -1, nx, tw, win); chm::count_launch();
   Lines32 L{};
   L.acc = reinterpret_cast<const long long *>(acc);
   L.acc_scale = scale;
@@ -838,7 +858,7 @@ int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, con
 // fb_eb_out + eb_correction (fb_io.f90:182-228, grid_deps.f90:219-266)
 int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double leftX,
                      const double *kx, const void *Out_ops, int64_t nx, int64_t nr, int64_t nkr,
-                     int64_t nm, void *ws, int64_t ws_bytes, void *stream) {
+                     int64_t nm, void *ws, int64_t ws_bytes, void *stream, const chm_sp_window *win) {
   CHM_REQUIRE(eb_c64 && e_c64 && b_c64 && kx && Out_ops, "sp_fb_eb_out: null pointer");
   CHM_REQUIRE(ws && ws_bytes >= chm_sp_fb_ws_bytes(nx, nr, nkr, nm), "sp_fb_eb_out: workspace");
   cudaStream_t st = as_stream(stream);
@@ -851,7 +871,7 @@ int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double 
     set_error("sp_fb_eb_out: workspace exhausted");
     return CHM_ERR_WS;
   }
-  shift32_kernel<<<grid_for(nx, 32), 32, 0, st>>>(shift, kx, leftX, +1, nx, tw); chm::count_launch();
+  shift32_kernel<<<grid_for(nx, 32), 32, 0, st>>>(shift, kx, leftX, +1, nx, tw, win); chm::count_launch();
   const TcMatrices Out = tc_matrices(reinterpret_cast<const chm_sp_ops *>(Out_ops));
   Batch32 b{};  // every mode and component in one launch
   for (i64 m = 0; m < nm; ++m)
@@ -879,7 +899,8 @@ int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double 
 // fb_filtr on complex64 planes (fb_io.f90:230-308)
 int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx, const float *filtr,
                     int64_t nxfilt, int modefilt, int64_t nx, int64_t nkr, int64_t nm,
-                    int64_t ncomp, void *ws, int64_t ws_bytes, void *stream) {
+                    int64_t ncomp, void *ws, int64_t ws_bytes, void *stream,
+                    const chm_sp_window *win) {
   CHM_REQUIRE(vec_c64 && kx && (nxfilt == 0 || filtr) && modefilt >= 0 && modefilt <= 2,
               "sp_fb_filtr: bad args");
   CHM_REQUIRE(ws && ws_bytes >= 2 * r256(8 * nx), "sp_fb_filtr: workspace");
@@ -887,7 +908,7 @@ int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx, const float *
   Ws W{(char *)ws, ws_bytes};
   float2 *tw = W.take<float2>(nx);
   float2 *shift = W.take<float2>(nx);
-  shift32_kernel<<<grid_for(nx, 32), 32, 0, st>>>(shift, kx, leftX, +1, nx, tw); chm::count_launch();
+  shift32_kernel<<<grid_for(nx, 32), 32, 0, st>>>(shift, kx, leftX, +1, nx, tw, win); chm::count_launch();
   Lines32 L{};
   L.in = reinterpret_cast<const float2 *>(vec_c64);
   L.out = reinterpret_cast<float2 *>(vec_c64);
@@ -1154,6 +1175,26 @@ int chm_sp_psatd(void *eg_c64, const void *j_c64, const void *gprv_c64, const vo
   psatd32_kernel<<<grid_for(P, 256), 256, 0, as_stream(stream)>>>(
       (float2 *)eg_c64, (const float2 *)j_c64, (const float2 *)gprv_c64, (const float2 *)gnxt_c64,
       c1, c2, nterm, P); chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int chm_sp_window_set(chm_sp_window *win, double leftX, double X0, double dx, void *stream) {
+  CHM_REQUIRE(win && dx > 0, "sp_window_set: bad args");
+  window_kernel<<<1, 32, 0, as_stream(stream)>>>(win, 1, leftX, X0, dx, 0.0);
+  chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+int chm_sp_window_advance(chm_sp_window *win, double shift, void *stream) {
+  CHM_REQUIRE(win, "sp_window_advance: bad args");
+  window_kernel<<<1, 32, 0, as_stream(stream)>>>(win, 0, 0.0, 0.0, 0.0, shift);
+  chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }

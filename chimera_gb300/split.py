@@ -288,6 +288,12 @@ class SplitRun:
         self.nx, self.nr, self.nkr, self.nm = A["Nx"], A["Nr"], A["Nkr"], A["Mtot"]
         self.dx, self.dt = A["dx"], A["TimeStep"]
         self.X0 = float(A["Xgrid"][0])  # fixed origin of the particle cell index
+        # the window origin on the device (chm_sp_window: leftX, X0, dx, k, f),
+        # advanced on the stream at every window move, so the step's kernels
+        # read the current origin also when the step replays as a CUDA graph
+        self.win = torch.zeros(32, dtype=torch.uint8, device=S.device)
+        _lib.call("chm_sp_window_set", self.win.data_ptr(), float(A["leftX"]), self.X0,
+                  float(A["dx"]), _stream())
         # operators (FP64 host build -> FP32 copy + split BF16)
         self._keep = []
         self.ops = {}
@@ -418,7 +424,7 @@ class SplitRun:
                   int(push), accJ.data_ptr() if accJ is not None else None,
                   scaleJ.data_ptr() if scaleJ is not None else None,
                   accR.data_ptr() if accR is not None else None,
-                  scaleR.data_ptr() if scaleR is not None else None, _stream())
+                  scaleR.data_ptr() if scaleR is not None else None, _stream(), self.win.data_ptr())
 
     def _deposit_background(self):
         if not self._scales_valid:
@@ -435,11 +441,89 @@ class SplitRun:
                   scale2.data_ptr() if scale2 is not None else None, float(A["leftX"]),
                   self.kx64.data_ptr(), C.addressof(self.ops["InCurr"]), self.depfact.data_ptr(),
                   self.nx, self.nr, self.nkr, self.nm, ncomp, self.ws.data_ptr(), self.ws.numel(),
-                  _stream())
+                  _stream(), self.win.data_ptr())
 
     # ------------------------------------------------------------------
     def make_step(self, istep):
         """chimera_main.py:82-92 in the split precision."""
+        self._maybe_sort(istep)
+        self._step_body(istep)
+        self._after_step()
+
+    # ------------------------------------------------------------------
+    # CUDA-graph replay of a step
+    def graph_capturable(self) -> bool:
+        """A step is captured when its host side is the same every step: a
+        window without plasma injection or absorbing layer (those draw host
+        random numbers or read counts back) and a fixed re-sort cadence."""
+        for wind in self.fp.MovingFrames:
+            if "AddPlasma" in wind or wind.get("AbsorbLayer", 0) > 0:
+                return False
+        return self.sort_every != "auto"
+
+    def _layout_key(self):
+        # the particle arrays and counts, and which charge-gradient buffer
+        # holds the previous step's gradient (the step swaps the two)
+        gp = self.gprv.data_ptr() if self.space_charge else 0
+        return tuple((P.n, P.cap, *P.ptrs()) for P in self.parts) + (gp,)
+
+    def graph_step(self, istep):
+        """make_step(istep) with the step's kernels replayed from a CUDA graph.
+        The graph holds the device work of one step (window origin advance,
+        deposits, spectral stage, gather and push); it is captured on first
+        use and again whenever the particle arrays change (a re-sort,
+        compaction or growth).  The host side (window bookkeeping, re-sorts,
+        error-flag reads) runs outside the graph.  Same results as
+        make_step, bitwise.  Falls back to make_step when the step is not
+        capturable (see graph_capturable)."""
+        if not self.graph_capturable():
+            return self.make_step(istep)
+        self._maybe_sort(istep)
+        if not self._scales_valid:
+            self._refresh_scales()
+        key = self._layout_key()
+        graphs = getattr(self, "_graphs", None)
+        if graphs is None or graphs[0] != key[:-1]:
+            graphs = self._graphs = [key[:-1], {}]  # per gradient-buffer assignment
+        self._graph = graphs[1].get(key[-1])
+        if self._graph is None:
+            lib = _lib.load()
+            g = torch.cuda.CUDAGraph()
+            n0 = lib.chm_launch_count()
+            with torch.cuda.graph(g):
+                self._step_body(istep)
+            self.graph_launches = lib.chm_launch_count() - n0  # kernels per replay
+            self._graph = graphs[1][key[-1]] = g
+            self.graph_captures = getattr(self, "graph_captures", 0) + 1
+        else:
+            self._host_effects(istep)
+        self._graph.replay()
+        self.graph_replays = getattr(self, "graph_replays", 0) + 1
+        self._after_step()
+
+    def _host_effects(self, istep):
+        """The host side of a replayed step: the window moves' Xgrid / leftX /
+        rightX bookkeeping (chimera_main.py:286-304) and the swap of the two
+        charge-gradient buffers."""
+        if self.space_charge:
+            self.gprv, self.gnxt = self.gnxt, self.gprv
+        fp = self.fp
+        for wind in fp.MovingFrames:
+            if istep < wind["TimeActive"][0] or istep > wind["TimeActive"][1]:
+                continue
+            if np.mod(istep - wind["TimeActive"][0], wind["Steps"]) != 0:
+                continue
+            fp.move_frame(wind)
+            if "Staged" in wind["Features"]:
+                fp.move_frame(wind)
+
+    def _after_step(self):
+        self._steps += 1
+        self._since_sort += 1
+        if self.check_every and self._steps % self.check_every == 0:
+            self.check_status()
+
+    def _step_body(self, istep):
         fp = self.fp
         A = self.solver.Args
         st = _stream()
@@ -461,8 +545,9 @@ class SplitRun:
                                                else A["damp_profile"], self.device)
                 _lib.call("chm_sp_fb_filtr", self.EG.data_ptr(), float(A["leftX"]),
                           self.kx64.data_ptr(), prof.data_ptr(), prof.numel(), 0, self.nx,
-                          self.nkr, self.nm, 6, ws, wsb, st)
+                          self.nkr, self.nm, 6, ws, wsb, st, self.win.data_ptr())
             fp.move_frame(wind)
+            _lib.call("chm_sp_window_advance", self.win.data_ptr(), float(wind["shiftX"]), st)
             if "AddPlasma" in wind:
                 self._add_plasma(wind)
             if "AbsorbLayer" in wind:
@@ -471,7 +556,6 @@ class SplitRun:
                 self._deposit_background()
             # the reference's dep_dens here (postframe_corr) is overwritten by
             # project_density before any use; it is not repeated
-        self._maybe_sort(istep)
         if not self._scales_valid:
             self._refresh_scales()
         ev = None
@@ -499,6 +583,7 @@ class SplitRun:
                 continue
             if "Staged" in wind["Features"]:
                 fp.move_frame(wind)
+                _lib.call("chm_sp_window_advance", self.win.data_ptr(), float(wind["shiftX"]), st)
         # density
         if self.space_charge:
             if not fuse_rho:
@@ -532,10 +617,6 @@ class SplitRun:
             ev[1].record()
         for spc, P in self._moving():
             _lib.call("chm_sp_count_live", P.counters.data_ptr(), P.n, st)
-        self._steps += 1
-        self._since_sort += 1
-        if self.check_every and self._steps % self.check_every == 0:
-            self.check_status()
 
     def _maybe_sort(self, istep):
         every = self.sorter.cadence if self.sort_every == "auto" else int(self.sort_every or 0)
@@ -582,12 +663,12 @@ class SplitRun:
                   self.nx, self.nkr, self.nm, ws, wsb, st)
         _lib.call("chm_sp_fb_eb_out", self.EB.data_ptr(), self.EG.data_ptr(), self.Bfb.data_ptr(),
                   float(A["leftX"]), self.kx64.data_ptr(), C.addressof(self.ops["Out"]), self.nx,
-                  self.nr, self.nkr, self.nm, ws, wsb, st)
+                  self.nr, self.nkr, self.nm, ws, wsb, st, self.win.data_ptr())
         k, f = self._win()
         for spc, P in self._moving():
             dtq = spc.Args["push_fact"] * spc.Args["TimeStep"]
             _lib.call("chm_sp_gather_push", *P.ptrs(), P.n, k, f, float(A["dr_inv"]),
-                      self.EB.data_ptr(), self.nx, self.nr, self.nm, float(dtq), st)
+                      self.EB.data_ptr(), self.nx, self.nr, self.nm, float(dtq), st, self.win.data_ptr())
 
     def _add_plasma(self, wind):
         fp = self.fp
@@ -702,6 +783,8 @@ class SplitRun:
         with np.load(fname, allow_pickle=False) as f:
             snapshot.read_into(f, self.fp.Solvers, self.fp.Particles, verbose)
             D = self.solver.Data
+            _lib.call("chm_sp_window_set", self.win.data_ptr(), float(self.solver.Args["leftX"]),
+                      self.X0, float(self.dx), _stream())
             self.EG.copy_(D["EG_fb"])
             if self.space_charge:
                 self.gprv.copy_(D["gradRho_fb_prv"])
@@ -780,7 +863,7 @@ def transform_errors(run: SplitRun) -> dict:
     out = chimera.fortran_zeros((nx, nkr, nm, 3), torch.complex64, dev)
     _lib.call("chm_sp_fb_in_acc", out.data_ptr(), run.accJ.data_ptr(), run.scaleJ.data_ptr(), None,
               None, leftX, run.kx64.data_ptr(), C.addressof(run.ops["InCurr"]),
-              run.depfact.data_ptr(), nx, nr, nkr, nm, 3, ws, wsb, st)
+              run.depfact.data_ptr(), nx, nr, nkr, nm, 3, ws, wsb, st, None)
     ref = chimera._fb_in(chimera.fortran_zeros((nx, nkr, nm, 3), device=dev), Jf, leftX,
                          *A["FBCurrIn"], 3, fact=S.dev["DepFact"])
     errs["fb_in"] = rel(out, ref)
@@ -825,7 +908,7 @@ def transform_errors(run: SplitRun) -> dict:
     del Gd, ref
     EB = chimera.fortran_zeros((nx, nr, nm, 6), torch.complex64, dev)
     _lib.call("chm_sp_fb_eb_out", EB.data_ptr(), run.EG.data_ptr(), Bs.data_ptr(), leftX,
-              run.kx64.data_ptr(), C.addressof(run.ops["Out"]), nx, nr, nkr, nm, ws, wsb, st)
+              run.kx64.data_ptr(), C.addressof(run.ops["Out"]), nx, nr, nkr, nm, ws, wsb, st, None)
     ref = chimera.fb_eb_out(chimera.fortran_zeros((nx, nr, nm, 6), device=dev), c128(run.EG),
                             c128(Bs), leftX, A["kx"], A["Out"], eb_mode=1)
     errs["fb_eb_out"] = rel(EB, ref)

@@ -418,6 +418,23 @@ int chm_sp_prepare_ops(chm_sp_ops *ops, const double *mats, int64_t K, int64_t N
 int64_t chm_sp_capacity(int64_t n);
 int64_t chm_sp_slot(int64_t i);
 
+/* The moving window's origin in device memory, for the split-form entry
+ * points below that take `win`: leftX = X0 + (k + f) dx with k = floor((leftX
+ * - X0) / dx) and f = (leftX - X0) / dx - k, evaluated in FP64 on the device.
+ * chm_sp_window_set writes it, chm_sp_window_advance adds a shift to leftX
+ * (leftX + shift in FP64, as the window moves: chimera_main.py:286-290) and
+ * re-evaluates k and f, so a step captured in a CUDA graph replays with the
+ * current origin.  With win == NULL the entry points use their scalar
+ * arguments (win_k, win_f, leftX). */
+typedef struct {
+  double leftX, X0, dx;
+  int32_t k;
+  float f;
+} chm_sp_window;
+int chm_sp_window_set(chm_sp_window *win, double leftX, double X0, double dx,
+                      void *stream);
+int chm_sp_window_advance(chm_sp_window *win, double shift, void *stream);
+
 /* Deterministic global deposit scale: scale2[0] = 2^min(61 - ceil(log2 B),
  * 120), scale2[1] = B = sum |w| (device doubles). */
 int64_t chm_sp_scale_ws_bytes(void);
@@ -435,14 +452,16 @@ int chm_sp_push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px,
                         float win_f, float dx_inv, float dr_inv, float dt,
                         int nx, int nr, int nm, int push, uint64_t *accJ,
                         const double *scaleJ, uint64_t *accR,
-                        const double *scaleR, void *stream);
+                        const double *scaleR, void *stream,
+                        const chm_sp_window *win);
 
 /* proj_fld + push_velocs fused (grid_deps.f90:149-217,
  * particle_tools.f90:18-56): gather from the complex64 EB grid and Boris. */
 int chm_sp_gather_push(int32_t *ix, float *fx, float *y, float *z, float *px,
                        float *py, float *pz, float *w, int64_t n, int win_k,
                        float win_f, float dr_inv, const void *eb_c64, int nx,
-                       int nr, int nm, float dtq, void *stream);
+                       int nr, int nm, float dtq, void *stream,
+                        const chm_sp_window *win);
 
 /* The same two operations with the per-particle kernels for every nm (each
  * value rounded separately): the reference the cell-run kernels (nm <= 3)
@@ -453,12 +472,14 @@ int chm_sp_push_deposit_generic(int32_t *ix, float *fx, float *y, float *z,
                                 int64_t n, int win_k, float win_f, float dx_inv,
                                 float dr_inv, float dt, int nx, int nr, int nm,
                                 int push, uint64_t *accJ, const double *scaleJ,
-                                uint64_t *accR, const double *scaleR, void *stream);
+                                uint64_t *accR, const double *scaleR, void *stream,
+                        const chm_sp_window *win);
 int chm_sp_gather_push_generic(int32_t *ix, float *fx, float *y, float *z,
                                float *px, float *py, float *pz, float *w,
                                int64_t n, int win_k, float win_f, float dr_inv,
                                const void *eb_c64, int nx, int nr, int nm,
-                               float dtq, void *stream);
+                               float dtq, void *stream,
+                        const chm_sp_window *win);
 
 /* FP64 (3,n)/(n) particle arrays (particle order) <-> split layout; from_f64
  * writes particles offset .. offset+n-1 and clears their dead flags (dead
@@ -532,15 +553,18 @@ int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale,
                      const int64_t *acc2, const double *scale2, double leftX,
                      const double *kx, const void *In_ops, const float *fact,
                      int64_t nx, int64_t nr, int64_t nkr, int64_t nm,
-                     int64_t ncomp, void *ws, int64_t ws_bytes, void *stream);
+                     int64_t ncomp, void *ws, int64_t ws_bytes, void *stream,
+                        const chm_sp_window *win);
 int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64,
                      double leftX, const double *kx, const void *Out_ops,
                      int64_t nx, int64_t nr, int64_t nkr, int64_t nm, void *ws,
-                     int64_t ws_bytes, void *stream);
+                     int64_t ws_bytes, void *stream,
+                        const chm_sp_window *win);
 int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx,
                     const float *filtr, int64_t nxfilt, int modefilt,
                     int64_t nx, int64_t nkr, int64_t nm, int64_t ncomp,
-                    void *ws, int64_t ws_bytes, void *stream);
+                    void *ws, int64_t ws_bytes, void *stream,
+                        const chm_sp_window *win);
 int chm_sp_fb_grad(void *out_c64, const void *scl_c64, const void *Dp_ops,
                    const void *Dm_ops, const float *kx, int64_t nx,
                    int64_t nkr, int64_t nm, void *ws, int64_t ws_bytes,

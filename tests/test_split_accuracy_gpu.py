@@ -141,7 +141,7 @@ def test_split_transforms_at_config_sizes(mods, grid):
     Jfb = fm.fortran_zeros((nx, nkr, nm, 3), torch.complex64)
     _lib.call("chm_sp_fb_in_acc", Jfb.data_ptr(), accd.data_ptr(), scd.data_ptr(), None, None,
               leftX, kx64.data_ptr(), C.addressof(o["InCurr"][0]), depf.data_ptr(), nx, nr, nkr, nm,
-              3, ws.data_ptr(), ws.numel(), st)
+              3, ws.data_ptr(), ws.numel(), st, None)
     Jsp = (acc[0] + 1j * acc[1]) / scale
     Jsp[:, 1] -= Jsp[:, 0]  # the ghost-row fold of the deposit
     Jsp[:, 0] = 0
@@ -194,7 +194,7 @@ def test_split_transforms_at_config_sizes(mods, grid):
     EBs = fm.fortran_zeros((nx, nr, nm, 6), torch.complex64)
     _lib.call("chm_sp_fb_eb_out", EBs.data_ptr(), Ed.data_ptr(), Bqd.data_ptr(), leftX,
               kx64.data_ptr(), C.addressof(o["Out"][0]), nx, nr, nkr, nm, ws.data_ptr(), ws.numel(),
-              st)
+              st, None)
     EBd = fm.fb_eb_out(fm.fortran_zeros((nx, nr, nm, 6)), _c(E.astype(np.complex128), torch),
                        _c(Bq.astype(np.complex128), torch), leftX, A["kx"], A["Out"], eb_mode=1)
     errs["fb_eb_out"] = rel_l2(EBs.cpu().numpy(), EBd.cpu().numpy())

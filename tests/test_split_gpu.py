@@ -128,7 +128,7 @@ def test_split_spectral_operators_match_fp64(mods, lpa):
     Ed, Bqd = _c(E, torch), _c(Bq, torch)
     _lib.call("chm_sp_fb_eb_out", EBs.data_ptr(), Ed.data_ptr(), Bqd.data_ptr(),
               leftX, kx64.data_ptr(), C.addressof(o["Out"][0]), nx, nr, nkr, nm, ws.data_ptr(),
-              ws.numel(), st)
+              ws.numel(), st, None)
     EBd = fm.fb_eb_out(fm.fortran_zeros((nx, nr, nm, 6)), _c(E.astype(np.complex128), torch),
                        _c(Bq.astype(np.complex128), torch), leftX, g["kx"], g["Out"], eb_mode=1)
     assert rel_l2(EBs.cpu().numpy(), EBd.cpu().numpy()) < TOL_T
@@ -290,7 +290,7 @@ def test_cell_run_deposit_equals_generic_kernel(mods, nm, runs, push):
         _lib.call(entry, *[P[k].data_ptr() for k in names], n, 100, 0.25,
                   1 / 0.1, 1 / dr, 0.1, nx, nr, nm, push,
                   accJ.data_ptr() if push else None, scale.data_ptr() if push else None,
-                  accR.data_ptr(), scale.data_ptr(), st)
+                  accR.data_ptr(), scale.data_ptr(), st, None)
         torch.cuda.synchronize()
         out[variant] = (accJ.cpu().numpy(), accR.cpu().numpy(),
                         {k: P[k].cpu().numpy() for k in names})
@@ -484,7 +484,7 @@ def test_cell_run_gather_matches_generic_kernel(mods, nm, runs):
         entry = "chm_sp_gather_push" + ("_generic" if variant == "generic" else "")
         P = {k: v.clone() for k, v in P0.items()}
         _lib.call(entry, *[P[k].data_ptr() for k in names], n, 100, 0.25, 1 / dr,
-                  ebd.data_ptr(), nx, nr, nm, 0.05, _st(torch))
+                  ebd.data_ptr(), nx, nr, nm, 0.05, _st(torch), None)
         torch.cuda.synchronize()
         out[variant] = np.stack([P[k].cpu().numpy() for k in ("px", "py", "pz")])
     p0 = np.stack([P0[k].cpu().numpy() for k in ("px", "py", "pz")])
@@ -517,6 +517,53 @@ def test_batched_instances_match_single_runs(mods):
     assert batch.num_moving == sum(r.num_moving for r in batch.runs) > 0
     assert _lib.load().chm_sp_umma_status() == 0
     assert _lib.load().chm_sp_deposit_dropped() == 0  # every deposit cell inside its box
+
+
+def test_graph_step_equals_make_step(mods):
+    """SplitRun.graph_step (the step's kernels replayed from a CUDA graph,
+    re-captured after each re-sort) gives bitwise the fields and particles of
+    make_step."""
+    torch, _lib, fm, split = mods
+    runs = [split.SplitRun(_lpa_comps(1001)), split.SplitRun(_lpa_comps(1001))]
+    for r in runs:
+        r.sort_every = 3
+    for i in range(1, 8):
+        runs[0].make_step(i)
+        runs[1].graph_step(i)
+    torch.cuda.synchronize()
+    a, b = runs
+    assert b.graph_captures >= 2 and b.graph_replays == 7 and b.graph_launches > 10
+    assert a.solver.Args["leftX"] == b.solver.Args["leftX"]
+    assert torch.equal(a.EG, b.EG) and torch.equal(a.EB, b.EB)
+    for Pa, Pb in zip(a.parts, b.parts):
+        assert Pa.n == Pb.n
+        for k in Pa.NAMES:
+            assert torch.equal(Pa.buf[k][: Pa.n], Pb.buf[k][: Pb.n]), k
+    b.check_status()
+
+
+def test_batched_graph_step_matches_single_runs(mods):
+    """BatchedRun.graph_step (every instance's step in one CUDA graph) gives
+    bitwise what each instance gives alone."""
+    torch, _lib, fm, split = mods
+    from chimera_gb300.batched import BatchedRun, draw_instances, lwfa_instance
+    from chimera_gb300.messages import msg
+    msg.quiet = True
+    params = [dict(p, nx=min(p["nx"], 256), nr=min(p["nr"], 32)) for p in draw_instances(3, 9)]
+    batch = BatchedRun([lwfa_instance(**p) for p in params])
+    for i in range(1, 5):
+        batch.graph_step(i)
+    batch.synchronize()
+    assert batch.graph_captures == 2  # even and odd steps (the gradient buffers swap)
+    for p, run in zip(params, batch.runs):
+        alone = split.SplitRun(lwfa_instance(**p))
+        for i in range(1, 5):
+            alone.make_step(i)
+        torch.cuda.synchronize()
+        assert torch.equal(alone.EG, run.EG) and torch.equal(alone.EB, run.EB)
+        for Pa, Pb in zip(alone.parts, run.parts):
+            for k in Pa.NAMES:
+                assert torch.equal(Pa.buf[k][: Pa.n], Pb.buf[k][: Pb.n]), k
 
 
 @pytest.mark.parametrize("spreads,with_profile", [((0.0, 0.0, 0.0), True), ((0.1, 0.05, 0.05), False)])
