@@ -310,16 +310,17 @@ def run_reference(args):
     return 0
 
 
-def time_steps(run, first, count, nmov, stream):
-    """CUDA-event time (ms) of `count` make_step calls from step `first`, and
-    the moving particles summed over them."""
+def time_steps(run, first, count, nmov, stream, stepper=None):
+    """CUDA-event time (ms) of `count` steps from step `first` (make_step, or
+    `stepper`), and the moving particles summed over them."""
     import torch
+    stepper = stepper or run.make_step
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     psteps = 0
     for i in range(first, first + count):
-        run.make_step(i)
+        stepper(i)
         psteps += nmov()
     ev1.record(stream)
     torch.cuda.synchronize()
@@ -363,16 +364,17 @@ def run_gb300(args):
         # the split form continues from the FP64 run's state; its re-sort by
         # deposit cell runs at the cadence the run-time tuner picks
         run = SplitRun(None, fp64_run=fp)
-        run.sort_every = "auto"
         nmov = lambda: run.num_moving  # noqa: E731
     else:
         run = fp
         nmov = lambda: el.num_particles  # noqa: E731
     n_moving = nmov()
     if args.form == "split":
+        # each step's kernels replay from a CUDA graph (SplitRun.graph_step)
+        stepper = run.graph_step
         for _ in range(args.warmup):
             step += 1
-            run.make_step(step)
+            stepper(step)
         torch.cuda.synchronize()
         # L2: the particle state (1.6 GB per species in the split form at
         # cfg3) is far larger than the 129 MB L2, so every step streams from HBM
@@ -381,10 +383,13 @@ def run_gb300(args):
         launches0 = lib.chm_launch_count()
         flops0 = lib.chm_gemm_flops()
         t0 = time.perf_counter()
-        ms, psteps = time_steps(run, step + 1, args.steps, nmov, stream)
+        replays0 = getattr(run, "graph_replays", 0)
+        ms, psteps = time_steps(run, step + 1, args.steps, nmov, stream, stepper)
         wall = time.perf_counter() - t0
         step += args.steps
-        launches = lib.chm_launch_count() - launches0
+        # kernels launched by the library, plus those replayed in graphs
+        launches = lib.chm_launch_count() - launches0 + \
+            (getattr(run, "graph_replays", 0) - replays0) * getattr(run, "graph_launches", 0)
         gemm_flops = lib.chm_gemm_flops() - flops0
         ms_max = max_over_ranks(world, ms)
         value = world * psteps / (ms_max / 1e3)
@@ -419,6 +424,7 @@ def run_gb300(args):
     # 20 steps timed against the first window (re-sorts included)
     decay = None
     if args.form == "split" and args.decay_steps > step + 20:
+        run.sort_every = "auto"
         first = (args.warmup + 1 + (args.fp64_steps + 1 if args.fp64_steps > 0 else 0))
         while step < args.decay_steps - 20:
             step += 1
@@ -527,7 +533,9 @@ def run_gb300(args):
                    "ppc": list(W.ppc),
                    "parallelism": f"replicas{world}" if world > 1 else "single",
                    "l2": "inputs larger than L2 (particle state %.2f GB per species)"
-                         % (n_moving * (32 if split else 80) / 1e9)},
+                         % (n_moving * (32 if split else 80) / 1e9),
+                   "step": "kernels replayed from a CUDA graph per step (SplitRun.graph_step)"
+                           if split else "ChimeraRun.make_step"},
         "wall_s_timed": wall,
         "gpu_launches": launches,
         "fp64_gpu": fp64,
@@ -570,19 +578,21 @@ def run_batched(args):
     params = draw_instances(args.batched, 1005)
     batch = BatchedRun([lwfa_instance(**p) for p in params])
     for i in range(1, args.warmup + 1):
-        batch.make_step(i)
+        batch.graph_step(i)
     batch.synchronize()
     torch.cuda.synchronize()
     launches0 = lib.chm_launch_count()
+    captures0 = getattr(batch, "graph_captures", 0)
     t0 = time.perf_counter()
     psteps = 0
     for i in range(args.warmup + 1, args.warmup + args.steps + 1):
-        batch.make_step(i)
+        batch.graph_step(i)
         psteps += batch.num_moving
     batch.synchronize()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
-    launches = lib.chm_launch_count() - launches0
+    # kernels: those launched (captures), plus the replays' graph kernels
+    launches = lib.chm_launch_count() - launches0 + args.steps * getattr(batch, "graph_launches", 0)
     value = psteps / wall
     # the same instances one by one in the plain FP64 form (their FP64 runs,
     # two steps each after one warm-up step)
@@ -608,7 +618,10 @@ def run_batched(args):
                    "particles_moving": psteps // args.steps,
                    "nx": sorted({p["nx"] for p in params}), "nr": sorted({p["nr"] for p in params}),
                    "modes": sorted({p["max_mode"] + 1 for p in params}),
-                   "streams": len(batch.streams), "timing": "host wall clock, all streams synced"},
+                   "streams": len(batch.streams), "timing": "host wall clock, all streams synced",
+                   "step": "every instance's kernels in one CUDA graph per step (BatchedRun.graph_step)",
+                   "graph_kernels_per_step": getattr(batch, "graph_launches", None),
+                   "graph_captures_timed": getattr(batch, "graph_captures", 0) - captures0},
         "gpu_launches": launches,
         "fp64_one_by_one": {"value": fp_value, "unit": METRIC,
                             "what": "each instance's plain FP64 step alone, summed over instances"},
