@@ -67,6 +67,20 @@ struct SpParts {
   i64 n;
 };
 
+// Starts the particle data of one tile (512 slots; 16 rows of 32
+// consecutive slots per array) towards L2: one prefetch per 128-byte row,
+// the warp's lanes taking rows in turn (the unstaged run kernels).
+__device__ __forceinline__ void prefetch_tile(const SpParts &P, i64 tile, int lane, bool momenta) {
+  if (tile >= P.n) return;
+  const int narr = momenta ? 8 : 5;
+  for (int k = lane; k < kRunLen * narr; k += 32) {
+    const int row = k & (kRunLen - 1), arr = k >> 4;
+    const float *b = arr == 0 ? P.w : arr == 1 ? (const float *)P.ix : arr == 2 ? P.fx
+                   : arr == 3 ? P.y : arr == 4 ? P.z : arr == 5 ? P.px : arr == 6 ? P.py : P.pz;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(b + tile + (i64)row * kTileRuns));
+  }
+}
+
 struct SpGrid {
   int win_k;      // window origin, whole cells from X0
   float win_f;    // window origin, fraction of a cell
@@ -375,8 +389,9 @@ struct BlockPlan {
   float sJ, sR;    // global scales 2^eJ, 2^eR (path without a box)
 };
 
-__device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box_bytes,
-                                const StageView &V) {
+template <bool STAGED>
+__device__ BlockPlan plan_block(const PushDepArgs &A, const SpGrid &G, i64 base, int *bb,
+                                int box_bytes, const StageView &V) {
   __shared__ float wsm[2][kDepThreads / 32];
   if (threadIdx.x == 0) {
     bb[0] = INT_MAX;
@@ -392,15 +407,18 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box
   for (int s = threadIdx.x; s < kDepBlock; s += blockDim.x) {
     const i64 p = base + s;
     const bool valid = logical_of(p) < A.P.n;
-    const int q = valid ? s : 0;  // slot 0 of the block always holds a particle
-    const float w = V.w[q];
+    // (V: the block's stage when STAGED, else the arguments' arrays)
+    const int qs = valid ? s : 0;  // slot 0 of the block always holds a particle
+    const i64 q = base + qs;
+    const float w = STAGED ? V.w[qs] : A.P.w[q];
     // (the rho-only pass reads global memory: its fx starts towards L2 here)
-    if (!A.push && !A.dep_j) asm volatile("prefetch.global.L2 [%0];" ::"l"(V.fx + q));
-    const int ix = V.ix[q];
-    const float y = V.y[q], z = V.z[q];
+    if (!STAGED && !A.push && !A.dep_j) asm volatile("prefetch.global.L2 [%0];" ::"l"(A.P.fx + q));
+    const int ix = STAGED ? V.ix[qs] : A.P.ix[q];
+    const float y = STAGED ? V.y[qs] : A.P.y[q], z = STAGED ? V.z[qs] : A.P.z[q];
     float pp = 0.0f;
     if (A.dep_j) {
-      const float px = V.px[q], py = V.py[q], pz = V.pz[q];
+      const float px = STAGED ? V.px[qs] : A.P.px[q], py = STAGED ? V.py[qs] : A.P.py[q],
+                  pz = STAGED ? V.pz[qs] : A.P.pz[q];
       // max_l |v_l| = max_l |p_l| / gamma
       pp = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz))) *
            rsqrtf(1.0f + (px * px + py * py + pz * pz));
@@ -420,10 +438,10 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box
   if (xlo <= xhi) {
     const int D = A.push ? (int)ceilf(A.dt * A.dx_inv) : 0;
     const float drc = A.push ? A.dt : 0.0f;
-    x0 = xlo - A.G.win_k - 1 - D;
-    x1 = xhi - A.G.win_k + 1 + D;
-    r0 = max(0, (int)floorf((sqrtf(r2lo) - drc) * A.G.dr_inv + 0.5f) - 1);
-    r1 = (int)floorf((sqrtf(r2hi) + drc) * A.G.dr_inv + 0.5f) + 2;
+    x0 = xlo - G.win_k - 1 - D;
+    x1 = xhi - G.win_k + 1 + D;
+    r0 = max(0, (int)floorf((sqrtf(r2lo) - drc) * G.dr_inv + 0.5f) - 1);
+    r1 = (int)floorf((sqrtf(r2hi) + drc) * G.dr_inv + 0.5f) + 2;
   }
   x0 = __reduce_min_sync(0xffffffffu, x0);
   x1 = __reduce_max_sync(0xffffffffu, x1);
@@ -453,11 +471,11 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, i64 base, int *bb, int box
   // flush, as the reference drops them)
   P.bx0 = max(bb[0], -1);
   P.br0 = max(bb[2], 0);
-  const int bx1 = min(bb[1], A.G.nx), br1 = min(bb[3], A.G.nr - 1);
+  const int bx1 = min(bb[1], G.nx), br1 = min(bb[3], G.nr - 1);
   P.bnx = bx1 - P.bx0 + 1;
   P.bnr = br1 - P.br0 + 1;
   // deposited components (J_x, J_y, J_z and/or rho) x mode parts
-  const int per_node = (3 * (A.dep_j ? 1 : 0) + (A.dep_rho ? 1 : 0)) * (2 * A.G.nm - 1);
+  const int per_node = (3 * (A.dep_j ? 1 : 0) + (A.dep_rho ? 1 : 0)) * (2 * G.nm - 1);
   P.c0 = A.dep_j ? 0 : 3;
   P.nvals = (bb[0] <= bb[1] && P.bnx > 0 && P.bnr > 0) ? (long long)P.bnx * P.bnr * per_node : 0;
   P.use_box = P.nvals > 0 && P.nvals * 4 <= box_bytes && Bl > 0.0f && isfinite(Bl);
@@ -484,13 +502,12 @@ __device__ __forceinline__ BoxGeo make_geo(int *box, const BlockPlan &P, const P
 // Generic push + deposit (any nm): one particle per thread and slot, each
 // value rounded to the block quantum and added to the box (or, without a
 // box, to the global quantum and added to the global accumulator).
-__global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A_) {
-  PushDepArgs A = A_;
-  A.G = window_grid(A_.G, A_.win);
+__global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A) {
+  const SpGrid G = window_grid(A.G, A.win);
   extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
   const i64 base = (i64)blockIdx.x * kDepBlock;
-  const BlockPlan Pl = plan_block(A, base, bb, kSpBoxBytes, global_view(A.P, base));
+  const BlockPlan Pl = plan_block<false>(A, G, base, bb, kSpBoxBytes, StageView{});
   if (Pl.use_box)
     for (long long t = threadIdx.x; t < Pl.nvals; t += kDepThreads) box[t] = 0;
   __syncthreads();
@@ -502,31 +519,31 @@ __global__ void __launch_bounds__(kDepThreads) push_deposit_kernel(PushDepArgs A
     const Pushed q = push_one(A, p);
     if (w != 0.0f) {
       if (A.dep_j) {
-        const Loc L = locate(q.ixh, q.fxh, q.yh, q.zh, A.G);
-        deposit_at(L, q.vj, 3, 0, A.G, [&](int plane, int r, int x, float re, float im) {
+        const Loc L = locate(q.ixh, q.fxh, q.yh, q.zh, G);
+        deposit_at(L, q.vj, 3, 0, G, [&](int plane, int r, int x, float re, float im) {
           if (Pl.use_box) {
             const int qr = __float2int_rn(re * Pl.lJ), qi = __float2int_rn(im * Pl.lJ);
             if (qr) box_put(geo, plane, r, x, 0, qr);
             if (qi) box_put(geo, plane, r, x, 1, qi);
           } else {
             const long long qr = f2ll(re * Pl.sJ), qi = f2ll(im * Pl.sJ);
-            const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
+            const i64 e = ((i64)plane * G.nr + r) * G.nx + x;
             if (qr) atomicAdd(&A.accJ[2 * e], (unsigned long long)qr);
             if (qi) atomicAdd(&A.accJ[2 * e + 1], (unsigned long long)qi);
           }
         });
       }
       if (A.dep_rho) {
-        const Loc L = locate(q.ixn, q.fxn, q.yn, q.zn, A.G);
+        const Loc L = locate(q.ixn, q.fxn, q.yn, q.zn, G);
         const float wv[1] = {w};
-        deposit_at(L, wv, 1, 3 * A.G.nm, A.G, [&](int plane, int r, int x, float re, float im) {
+        deposit_at(L, wv, 1, 3 * G.nm, G, [&](int plane, int r, int x, float re, float im) {
           if (Pl.use_box) {
             const int qr = __float2int_rn(re * Pl.lR), qi = __float2int_rn(im * Pl.lR);
             if (qr) box_put(geo, plane, r, x, 0, qr);
             if (qi) box_put(geo, plane, r, x, 1, qi);
           } else {
             const long long qr = f2ll(re * Pl.sR), qi = f2ll(im * Pl.sR);
-            const i64 e = ((i64)(plane - 3 * A.G.nm) * A.G.nr + r) * A.G.nx + x;
+            const i64 e = ((i64)(plane - 3 * G.nm) * G.nr + r) * G.nx + x;
             if (qr) atomicAdd(&A.accR[2 * e], (unsigned long long)qr);
             if (qi) atomicAdd(&A.accR[2 * e + 1], (unsigned long long)qi);
           }
@@ -644,54 +661,124 @@ __device__ __forceinline__ void acc_add(CellAcc<NM, NC> &c, const Loc &L, const 
   }
 }
 
-// The moving species' pass (push, J, rho) stages the block's particles in
-// shared memory (64 KB) ahead of its box: 2 resident blocks per SM.  The
-// still species' rho-only pass reads 20 B per particle once and runs more
-// blocks per SM instead (measured faster unstaged: 118 against 157 us for
-// 12.6M ions of the 4096 x 128 x 3-mode case).
+// A particle's values in a run kernel's registers.
+struct RunPart {
+  int ix;
+  float fx, y, z, px, py, pz, w;
+};
+
+// One particle of a run kernel's main loop: push (store(u) writes the new
+// coordinates), then its J at the half step and rho at the new position
+// into the lane's cell sums at the block scale.
+template <int NM, bool PUSH, bool DJ, bool DR, typename Store>
+__device__ __forceinline__ void run_particle(const PushDepArgs &A, const SpGrid &G,
+                                             const BlockPlan &Pl, const BoxGeo &geo,
+                                             const RunPart &c, CellAcc<NM, 3> &cj,
+                                             CellAcc<NM, 1> &cr, Store store) {
+  const float w = c.w;
+  Pushed u;
+  if (PUSH || DJ) {
+    u = push_vals(A, c.ix, c.fx, c.y, c.z, c.px, c.py, c.pz, w);
+  } else {
+    u.ixh = u.ixn = c.ix;
+    u.fxh = u.fxn = c.fx;
+    u.yh = u.yn = c.y;
+    u.zh = u.zn = c.z;
+  }
+  if (PUSH) store(u);
+  if (w == 0.0f) return;
+  if (DJ && u.moving) {  // grid_deps.f90:42: no current from particles at rest
+    const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, G);
+    const float vs[3] = {u.vj[0] * Pl.lJ, u.vj[1] * Pl.lJ, u.vj[2] * Pl.lJ};
+    acc_add(cj, L, vs, 0, G, geo);
+  }
+  if (DR) {
+    const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, G);
+    const float ws[1] = {w * Pl.lR};
+    acc_add(cr, L, ws, 3 * NM, G, geo);
+  }
+}
+
+// A particle of a block without a box: its values straight to the global
+// accumulators at the global scales.
+template <bool DJ, bool DR>
+__device__ __forceinline__ void deposit_global(const PushDepArgs &A, const SpGrid &G,
+                                               const BlockPlan &Pl, const Pushed &u, float w) {
+  if (DJ && u.moving) {
+    const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, G);
+    const float vs[3] = {u.vj[0] * Pl.sJ, u.vj[1] * Pl.sJ, u.vj[2] * Pl.sJ};
+    deposit_at(L, vs, 3, 0, G, [&](int plane, int r, int x, float re, float im) {
+      const i64 e = ((i64)plane * G.nr + r) * G.nx + x;
+      const long long qr = f2ll(re), qi = f2ll(im);
+      if (qr) atomicAdd(&A.accJ[2 * e], (unsigned long long)qr);
+      if (qi) atomicAdd(&A.accJ[2 * e + 1], (unsigned long long)qi);
+    });
+  }
+  if (DR) {
+    const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, G);
+    const float ws[1] = {w * Pl.sR};
+    deposit_at(L, ws, 1, 0, G, [&](int plane, int r, int x, float re, float im) {
+      const i64 e = ((i64)plane * G.nr + r) * G.nx + x;
+      const long long qr = f2ll(re), qi = f2ll(im);
+      if (qr) atomicAdd(&A.accR[2 * e], (unsigned long long)qr);
+      if (qi) atomicAdd(&A.accR[2 * e + 1], (unsigned long long)qi);
+    });
+  }
+}
+
+// Run kernels of the moving species with one or two modes and of the still
+// species' rho-only pass: unstaged, the warp's tile started towards L2 first
+// (measured faster than staged at 2048 x 256 x 2 modes), 4 blocks per SM at
+// 128 registers (moving) or 8 at 64 (rho-only: 20 B per particle read once;
+// 6 with three modes, whose sums spill at 64).
 constexpr int kRhoMinBlocks = 8;
+constexpr int kRhoGroup = 1;  // particles loaded ahead per lane (rho-only pass)
 
 template <int NM, bool PUSH, bool DJ, bool DR>
-__global__ void __launch_bounds__(kDepThreads, (PUSH || DJ) ? 2 : kRhoMinBlocks)
-    push_deposit_run_kernel(PushDepArgs A_) {
-  PushDepArgs A = A_;
-  A.G = window_grid(A_.G, A_.win);
-  extern __shared__ __align__(16) unsigned char dsm[];
-  constexpr bool STAGE = PUSH || DJ;
-  int *box = reinterpret_cast<int *>(dsm + (STAGE ? (size_t)kStageArrays * kDepBlock * 4 : 0));
+__global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
+    push_deposit_run_kernel(PushDepArgs A) {
+  if (A.win) {  // the window origin from the device record
+    A.G.win_k = A.win->k;
+    A.G.win_f = A.win->f;
+  }
+  extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
-  const i64 base = (i64)blockIdx.x * kDepBlock;
-  if (STAGE) stage_block(A.P, base, kStageArrays, dsm);
-  const StageView V = STAGE ? stage_view(dsm) : global_view(A.P, base);
-  const BlockPlan Pl = plan_block(A, base, bb, DJ ? kSpBoxBytes : kRhoBoxBytes, V);
+  // slot indices: 32-bit in the rho-only kernel (measured faster there; the
+  // host launches it for n < 2^31 only), 64-bit otherwise
+  using Idx = typename std::conditional<DJ, i64, unsigned>::type;
+  const Idx base = (Idx)blockIdx.x * kDepBlock;
+  // (the rho-only pass starts only fx towards L2, in the plan: measured
+  // faster there than the whole tile)
+  if (PUSH || DJ) prefetch_tile(A.P, (i64)base + (threadIdx.x >> 5) * kTile, threadIdx.x & 31, true);
+  const BlockPlan Pl = plan_block<false>(A, A.G, (i64)base, bb, DJ ? kSpBoxBytes : kRhoBoxBytes,
+                                         StageView{});
   if (Pl.use_box)
     for (int t = threadIdx.x; t < (int)Pl.nvals; t += kDepThreads) box[t] = 0;
   __syncthreads();
   const BoxGeo geo = make_geo(box, Pl, A);
   const int lane = threadIdx.x & 31;
-  const int ltile = (threadIdx.x >> 5) * kTile;  // this warp's tile, local slots
-  const i64 first = base + ltile + (i64)lane * kRunLen;  // this lane's run, in particle order
+  const Idx tile = base + (Idx)(threadIdx.x >> 5) * kTile;
+  const Idx first = tile + (Idx)lane * kRunLen;  // this lane's run, in particle order
   CellAcc<NM, 3> cj;
   CellAcc<NM, 1> cr;
   cj.live = false;
   cr.live = false;
-  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - first));
+  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - (i64)first));
   if (!Pl.use_box) {
     // a block whose nodes do not fit a box (a wide footprint): each particle
     // straight to the global accumulators at the global scales, apart from
     // the main loop so that the loop does not carry this path's registers
     for (int j = 0; j < cnt; ++j) {
-      const int ls = ltile + j * kTileRuns + lane;
-      const i64 p = base + ls;
-      const float w = V.w[ls];
+      const Idx p = tile + (Idx)j * kTileRuns + lane;
+      const float w = A.P.w[p];
       Pushed u;
       if (PUSH || DJ) {
-        u = push_vals(A, V.ix[ls], V.fx[ls], V.y[ls], V.z[ls], V.px[ls], V.py[ls], V.pz[ls], w);
+        u = push_one(A, p);
       } else {
-        u.ixh = u.ixn = V.ix[ls];
-        u.fxh = u.fxn = V.fx[ls];
-        u.yh = u.yn = V.y[ls];
-        u.zh = u.zn = V.z[ls];
+        u.ixh = u.ixn = A.P.ix[p];
+        u.fxh = u.fxn = A.P.fx[p];
+        u.yh = u.yn = A.P.y[p];
+        u.zh = u.zn = A.P.z[p];
       }
       if (PUSH) {
         A.P.ix[p] = u.ixn;
@@ -723,65 +810,157 @@ __global__ void __launch_bounds__(kDepThreads, (PUSH || DJ) ? 2 : kRhoMinBlocks)
     }
     return;
   }
-  // lane r walks run r of its warp's tile (local slot ltile + 32 j + r:
-  // the warp's 32 lanes read 32 consecutive words, one bank each when
-  // staged); the next particle is loaded before this one is processed
+  // software pipeline: the next group of particles is loaded before this
+  // group's results are stored (the stores could alias the loads
+  // otherwise); G particles per group (kRhoGroup for the rho-only pass:
+  // one measured best at its 64-register budget)
+  constexpr int G = DJ ? 1 : kRhoGroup;
   struct Part {
     int ix;
     float fx, y, z, px, py, pz, w;
   };
   auto load = [&](int j) {
     Part q;
+    const Idx p = tile + (Idx)j * kTileRuns + lane;
+    q.w = A.P.w[p];
+    q.ix = A.P.ix[p];
+    q.fx = A.P.fx[p];
+    q.y = A.P.y[p];
+    q.z = A.P.z[p];
+    if (PUSH || DJ) {
+      q.px = A.P.px[p];
+      q.py = A.P.py[p];
+      q.pz = A.P.pz[p];
+    }
+    return q;
+  };
+  Part cur[G], nxt[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g)
+    if (g < cnt) cur[g] = load(g);
+  for (int j0 = 0; j0 < cnt; j0 += G) {
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+      if (j0 + G + g < cnt) nxt[g] = load(j0 + G + g);
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int j = j0 + g;
+      if (j >= cnt) break;
+      const Part &c = cur[g];
+      const Idx p = tile + (Idx)j * kTileRuns + lane;
+      const float w = c.w;
+      Pushed u;
+      if (PUSH || DJ) {
+        u = push_vals(A, c.ix, c.fx, c.y, c.z, c.px, c.py, c.pz, w);
+      } else {
+        u.ixh = u.ixn = c.ix;
+        u.fxh = u.fxn = c.fx;
+        u.yh = u.yn = c.y;
+        u.zh = u.zn = c.z;
+      }
+      if (PUSH) {
+        A.P.ix[p] = u.ixn;
+        A.P.fx[p] = u.fxn;
+        A.P.y[p] = u.yn;
+        A.P.z[p] = u.zn;
+      }
+      if (w == 0.0f) continue;
+      if (DJ && u.moving) {  // grid_deps.f90:42: no current from particles at rest
+        const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, A.G);
+        const float vs[3] = {u.vj[0] * Pl.lJ, u.vj[1] * Pl.lJ, u.vj[2] * Pl.lJ};
+        acc_add(cj, L, vs, 0, A.G, geo);
+      }
+      if (DR) {
+        const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, A.G);
+        const float ws[1] = {w * Pl.lR};
+        acc_add(cr, L, ws, 3 * NM, A.G, geo);
+      }
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g) cur[g] = nxt[g];
+  }
+  if (DJ) acc_flush(cj, 0, A.G, geo);
+  if (DR) acc_flush(cr, 3 * NM, A.G, geo);
+  __syncthreads();
+  flush_box(geo, Pl.nvals);
+}
+
+// Staged run kernel of the moving species with three modes: the block's
+// particles are copied into shared memory (64 KB) ahead of its box, 2
+// resident blocks per SM with room for the registers (measured 500 against
+// 523 us for 12.5M electrons of the 4096 x 128 x 3-mode case, where the
+// unstaged kernel spills).
+template <int NM, bool PUSH, bool DR>
+__global__ void __launch_bounds__(kDepThreads, 2) push_deposit_staged_kernel(PushDepArgs A) {
+  constexpr bool DJ = true;
+  const SpGrid G = window_grid(A.G, A.win);
+  extern __shared__ __align__(16) unsigned char dsm[];
+  int *box = reinterpret_cast<int *>(dsm + (size_t)kStageArrays * kDepBlock * 4);
+  __shared__ int bb[4];
+  const i64 base = (i64)blockIdx.x * kDepBlock;
+  stage_block(A.P, base, kStageArrays, dsm);
+  const StageView V = stage_view(dsm);
+  const BlockPlan Pl = plan_block<true>(A, G, base, bb, kSpBoxBytes, V);
+  if (Pl.use_box)
+    for (int t = threadIdx.x; t < (int)Pl.nvals; t += kDepThreads) box[t] = 0;
+  __syncthreads();
+  const BoxGeo geo = make_geo(box, Pl, A);
+  const int lane = threadIdx.x & 31;
+  const int ltile = (threadIdx.x >> 5) * kTile;  // this warp's tile, local slots
+  const i64 first = base + ltile + (i64)lane * kRunLen;  // this lane's run, in particle order
+  CellAcc<NM, 3> cj;
+  CellAcc<NM, 1> cr;
+  cj.live = false;
+  cr.live = false;
+  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - first));
+  // lane r walks run r of its warp's tile (local slot ltile + 32 j + r: the
+  // warp's 32 lanes read 32 consecutive words, one bank each)
+  auto load = [&](int j) {
+    RunPart q;
     const int ls = ltile + j * kTileRuns + lane;
     q.w = V.w[ls];
     q.ix = V.ix[ls];
     q.fx = V.fx[ls];
     q.y = V.y[ls];
     q.z = V.z[ls];
-    if (PUSH || DJ) {
-      q.px = V.px[ls];
-      q.py = V.py[ls];
-      q.pz = V.pz[ls];
-    }
+    q.px = V.px[ls];
+    q.py = V.py[ls];
+    q.pz = V.pz[ls];
     return q;
   };
-  Part cur, nxt;
+  if (!Pl.use_box) {
+    // a block whose nodes do not fit a box: each particle straight to the
+    // global accumulators at the global scales
+    for (int j = 0; j < cnt; ++j) {
+      const RunPart q = load(j);
+      const Pushed u = push_vals(A, q.ix, q.fx, q.y, q.z, q.px, q.py, q.pz, q.w);
+      if (PUSH) {
+        const i64 p = base + ltile + j * kTileRuns + lane;
+        A.P.ix[p] = u.ixn;
+        A.P.fx[p] = u.fxn;
+        A.P.y[p] = u.yn;
+        A.P.z[p] = u.zn;
+      }
+      if (q.w == 0.0f) continue;
+      deposit_global<DJ, DR>(A, G, Pl, u, q.w);
+    }
+    return;
+  }
+  RunPart cur, nxt;
   if (cnt > 0) cur = load(0);
   for (int j = 0; j < cnt; ++j) {
     if (j + 1 < cnt) nxt = load(j + 1);
-    const int ls = ltile + j * kTileRuns + lane;
-    const float w = cur.w;
-    Pushed u;
-    if (PUSH || DJ) {
-      u = push_vals(A, cur.ix, cur.fx, cur.y, cur.z, cur.px, cur.py, cur.pz, w);
-    } else {
-      u.ixh = u.ixn = cur.ix;
-      u.fxh = u.fxn = cur.fx;
-      u.yh = u.yn = cur.y;
-      u.zh = u.zn = cur.z;
-    }
-    cur = nxt;
-    if (PUSH) {
-      const i64 p = base + ls;
+    const i64 p = base + ltile + j * kTileRuns + lane;
+    run_particle<NM, PUSH, DJ, DR>(A, G, Pl, geo, cur, cj, cr, [&](const Pushed &u) {
       A.P.ix[p] = u.ixn;
       A.P.fx[p] = u.fxn;
       A.P.y[p] = u.yn;
       A.P.z[p] = u.zn;
-    }
-    if (w == 0.0f) continue;
-    if (DJ && u.moving) {  // grid_deps.f90:42: no current from particles at rest
-      const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, A.G);
-      const float vs[3] = {u.vj[0] * Pl.lJ, u.vj[1] * Pl.lJ, u.vj[2] * Pl.lJ};
-      acc_add(cj, L, vs, 0, A.G, geo);
-    }
-    if (DR) {
-      const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, A.G);
-      const float ws[1] = {w * Pl.lR};
-      acc_add(cr, L, ws, 3 * NM, A.G, geo);
-    }
+    });
+    cur = nxt;
   }
-  if (DJ) acc_flush(cj, 0, A.G, geo);
-  if (DR) acc_flush(cr, 3 * NM, A.G, geo);
+  acc_flush(cj, 0, G, geo);
+  if (DR) acc_flush(cr, 3 * NM, G, geo);
   __syncthreads();
   flush_box(geo, Pl.nvals);
 }
@@ -989,15 +1168,18 @@ __global__ void __launch_bounds__(256) gather_push_kernel(GatherArgs A, i64 nphy
 // and keeps the fields of the 4 nodes of the current cell in registers
 // (mode 0: real parts; modes >= 1: complex), reloading them only when the
 // cell changes.  Same interpolation and rotation as gather_push_kernel.
+// (staged in shared memory with three modes, as the deposit; unstaged with
+// its tile started towards L2 and 4 blocks per SM otherwise)
 template <int NM>
-__global__ void __launch_bounds__(kDepThreads, 3) gather_push_run_kernel(GatherArgs A) {
+__global__ void __launch_bounds__(kDepThreads, NM >= 3 ? 3 : 4) gather_push_run_kernel(GatherArgs A) {
   extern __shared__ __align__(16) unsigned char gsm[];
   const SpGrid G = window_grid(A.G, A.win);
   const i64 plane = (i64)G.nx * G.nr;
   const int lane = threadIdx.x & 31;
   const i64 base = (i64)blockIdx.x * kDepBlock;
-  stage_block(A.P, base, kStageArrays, gsm);
-  const StageView V = stage_view(gsm);
+  if (NM >= 3) stage_block(A.P, base, kStageArrays, gsm);
+  else prefetch_tile(A.P, base + (threadIdx.x >> 5) * kTile, lane, true);
+  const StageView V = NM >= 3 ? stage_view(gsm) : global_view(A.P, base);
   const int ltile = (threadIdx.x >> 5) * kTile;  // this warp's tile, local slots
   const i64 tile = base + ltile;
   const i64 first = tile + (i64)lane * kRunLen;
@@ -1012,14 +1194,26 @@ __global__ void __launch_bounds__(kDepThreads, 3) gather_push_run_kernel(GatherA
   auto load = [&](int j) {
     Part q;
     const int ls = ltile + j * kTileRuns + lane;
-    q.w = V.w[ls];
-    q.ix = V.ix[ls];
-    q.fx = V.fx[ls];
-    q.y = V.y[ls];
-    q.z = V.z[ls];
-    q.px = V.px[ls];
-    q.py = V.py[ls];
-    q.pz = V.pz[ls];
+    if (NM >= 3) {
+      q.w = V.w[ls];
+      q.ix = V.ix[ls];
+      q.fx = V.fx[ls];
+      q.y = V.y[ls];
+      q.z = V.z[ls];
+      q.px = V.px[ls];
+      q.py = V.py[ls];
+      q.pz = V.pz[ls];
+    } else {  // straight from the arguments' arrays
+      const i64 p = base + ls;
+      q.w = A.P.w[p];
+      q.ix = A.P.ix[p];
+      q.fx = A.P.fx[p];
+      q.y = A.P.y[p];
+      q.z = A.P.z[p];
+      q.px = A.P.px[p];
+      q.py = A.P.py[p];
+      q.pz = A.P.pz[p];
+    }
     return q;
   };
   Part cur;
@@ -1300,10 +1494,10 @@ int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *p
     const int mode = (push ? 4 : 0) | (A.dep_j ? 2 : 0) | (A.dep_rho ? 1 : 0);
     if (mode == 7) kern = nm == 1 ? push_deposit_run_kernel<1, true, true, true>
                         : nm == 2 ? push_deposit_run_kernel<2, true, true, true>
-                                  : push_deposit_run_kernel<3, true, true, true>;
+                                  : push_deposit_staged_kernel<3, true, true>;
     if (mode == 6) kern = nm == 1 ? push_deposit_run_kernel<1, true, true, false>
                         : nm == 2 ? push_deposit_run_kernel<2, true, true, false>
-                                  : push_deposit_run_kernel<3, true, true, false>;
+                                  : push_deposit_staged_kernel<3, true, false>;
     if (mode == 1 && n < (i64)INT32_MAX - kDepBlock)
       kern = nm == 1 ? push_deposit_run_kernel<1, false, false, true>
            : nm == 2 ? push_deposit_run_kernel<2, false, false, true>
@@ -1313,8 +1507,10 @@ int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *p
   if (!kern) {
     kern = push_deposit_kernel;
   } else {
-    // the moving species' run kernels stage the block's particles ahead of the box
-    box_bytes = (push || A.dep_j) ? kStageArrays * kDepBlock * 4 + kSpBoxBytes : kRhoBoxBytes;
+    // the three-mode moving species' kernels stage the block's particles
+    // ahead of the box
+    box_bytes = !A.dep_j ? kRhoBoxBytes
+              : (nm >= 3 ? kStageArrays * kDepBlock * 4 + kSpBoxBytes : kSpBoxBytes);
   }
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, box_bytes);
   kern<<<blocks, kDepThreads, box_bytes, st>>>(A);
@@ -1338,8 +1534,8 @@ int gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, float *py
   cudaStream_t st = as_stream(stream);
   if (!generic && nm >= 1 && nm <= 3) {
     const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
-    // each block stages its 2048 slots of the eight particle arrays
-    const int sm = kStageArrays * kDepBlock * 4;
+    // with three modes each block stages its 2048 slots of the eight particle arrays
+    const int sm = nm >= 3 ? kStageArrays * kDepBlock * 4 : 0;
     void (*kern)(GatherArgs) =
         nm == 1 ? gather_push_run_kernel<1> : nm == 2 ? gather_push_run_kernel<2> : gather_push_run_kernel<3>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
