@@ -141,6 +141,16 @@ def load_peaks():
 FP64_PEAK_TFLOPS = 1.20
 
 
+def umma_tuned(lib):
+    """The tensor-core products' tuned column-tile widths: one record
+    [M, N, K, batch count, epilogue, width] per product shape."""
+    import ctypes
+    n = lib.chm_sp_umma_tuned(None, 0)
+    buf = (ctypes.c_int32 * (6 * max(n, 1)))()
+    lib.chm_sp_umma_tuned(buf, n)
+    return [list(buf[6 * i: 6 * i + 6]) for i in range(n)]
+
+
 def still_count(run, form):
     parts = run.fp.Particles if form == "split" else run.Particles
     return sum(p.num_particles for p in parts if "Still" in p.Args["Features"])
@@ -544,6 +554,11 @@ def run_gb300(args):
         "transform_errors": terr,
         "device_flags": flags,
         "decay": decay,
+        "tuning": {"umma_cols": umma_tuned(lib) if split else None,
+                   "umma_cols_fields": "M, N, K, batch count, epilogue, column-tile width "
+                                       "(timed on each shape's first launch)",
+                   "sort": "every 64 steps in the timed steps; SortCadence picks it in the "
+                           "decay run" if split else None},
         "roofline": roofline,
         "stages": stages,
         "clocks": clk,
@@ -626,6 +641,8 @@ def run_batched(args):
         "fp64_one_by_one": {"value": fp_value, "unit": METRIC,
                             "what": "each instance's plain FP64 step alone, summed over instances"},
         "batched_over_fp64": value / fp_value,
+        "tuning": {"umma_cols": umma_tuned(_lib.load()),
+                   "umma_cols_fields": "M, N, K, batch count, epilogue, column-tile width"},
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -52,12 +52,18 @@ class BatchedRun:
         """make_step with every instance's step in one CUDA graph: the
         instances' device work is captured on their own streams (forked from
         the capture stream and joined back), so one replay per step runs them
-        all, concurrently where they fit.  Captured on first use and again
-        when an instance's particle arrays change; host-side window
+        all, concurrently where they fit.  Captured on the second call (the
+        first step runs eagerly) and again when an instance's particle arrays
+        change; host-side window
         bookkeeping, re-sorts and error-flag reads run outside the graph.
         Falls back to make_step when a step is not capturable
         (SplitRun.graph_capturable)."""
         if self.form != "split" or not all(r.graph_capturable() for r in self.runs):
+            return self.make_step(istep)
+        if not getattr(self, "_eager_done", False):
+            # the first step runs eagerly: the tensor-core products time their
+            # column-tile widths on a shape's first launch, which a capture cannot
+            self._eager_done = True
             return self.make_step(istep)
         cur = torch.cuda.current_stream()
         for r, s in zip(self.runs, self.streams):

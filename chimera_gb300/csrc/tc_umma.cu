@@ -46,6 +46,11 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
 #include "tc_gemm.cuh"
 
 using namespace chm;
@@ -512,6 +517,35 @@ __global__ void __launch_bounds__(kThreads, 1) umma_kernel(const __grid_constant
 
 inline long long rup(long long a, long long b) { return (a + b - 1) / b * b; }
 
+// Column-tile width of the products.  Every multiple of 16 that divides
+// Np = tc_np(N) and is at most 128 gives the same output bitwise: each
+// output element's K sum runs through the same MMAs and chunk drains in the
+// same order whatever the width, which changes only the number of tiles,
+// the B bytes per stage and the TMEM columns.  The width for a shape
+// (M, N, K, batch count, epilogue) is picked by timing: the first launch of
+// the shape outside stream capture runs every candidate width (one warm-up
+// and three timed launches each, CUDA events on the launch stream) and
+// keeps the fastest.  g_cols_mode: -1 tune (the default), 0 the default
+// width tc_tile_cols(N), > 0 that width where it is a candidate.
+int g_cols_mode = -1;
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int, int>, int> g_tuned;  // shape -> width
+
+// the default width tc_tile_cols(N) first, then the narrower multiples of
+// 16 (32 and up) that divide Np
+std::vector<int> col_candidates(int N) {
+  const int Np = tc_np(N), w0 = tc_tile_cols(N);
+  std::vector<int> c{w0};
+  for (int w = w0 - 16; w >= 32; w -= 16)
+    if (Np % w == 0) c.push_back(w);
+  return c;
+}
+
+size_t umma_smem(int tnc, int epi) {
+  return (size_t)STAGES * (kABytes + 3 * (size_t)tnc * KB * 2) + 1024 +
+         (epi == TC_EPI_SHIFT_FAC ? (size_t)(TH / 2) * tnc * 4 : 0);
+}
+
 }  // namespace
 
 namespace chm {
@@ -522,10 +556,11 @@ long long tc_split_bytes(int M, int K, int count) {
 
 int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, const float2 *shift,
                    void *ws, long long ws_bytes, cudaStream_t st) {
-  const int tnc = tc_tile_cols(N), ntn = tc_col_tiles(N), Np = tc_np(N);
+  const int Np = tc_np(N);
   const int nkb = (int)(rup(K, KB) / KB), nmt = (int)((M + TH - 1) / TH);
-  if (tnc > TH || tnc % 16) {
-    set_error("umma: bad column tile %d", tnc);
+  const std::vector<int> cands = col_candidates(N);
+  if (cands.empty() || cands[0] > TH) {
+    set_error("umma: no column tile for N = %d", N);
     return CHM_ERR_RANGE;
   }
   if (M % 2) {
@@ -541,15 +576,24 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
   const long long split_one = 3 * term_stride * 2;                     // bytes per A plane
   char *wsp = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(ws) + 255) & ~(uintptr_t)255);
   const long long avail = ws ? ws_bytes - (wsp - reinterpret_cast<char *>(ws)) : 0;
-  const uint32_t b_term = (uint32_t)tnc * KB * 2;
-  const size_t smem = (size_t)STAGES * (kABytes + 3 * (size_t)b_term) + 1024 +
-                     (epi == TC_EPI_SHIFT_FAC ? (size_t)(TH / 2) * tnc * 4 : 0);
   void (*kern)(const UmmaBatch, UmmaArgs) =
       epi == TC_EPI_STORE ? umma_kernel<TC_EPI_STORE>
                           : (epi == TC_EPI_SHIFT ? umma_kernel<TC_EPI_SHIFT> : umma_kernel<TC_EPI_SHIFT_FAC>);
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  uint32_t cols = 32;
-  while (cols < (uint32_t)(4 * tnc)) cols <<= 1;  // H0, H1, L0, L1
+  // (the widest candidate needs the most shared memory)
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)umma_smem(cands[0], epi));
+  // one product launch of the batch chunk ub (cnt problems) at width tnc
+  auto launch = [&](const UmmaBatch &ub, const UmmaArgs &base, int cnt, int tnc) {
+    UmmaArgs ua = base;
+    ua.tnc = tnc;
+    ua.ntn = Np / tnc;
+    ua.ntiles = cnt * nmt * ua.ntn;
+    uint32_t cols = 32;
+    while (cols < (uint32_t)(4 * tnc)) cols <<= 1;  // H0, H1, L0, L1
+    ua.tmem_cols = cols;
+    const int grid = ua.ntiles < sm_count() ? ua.ntiles : sm_count();
+    kern<<<grid, kThreads, umma_smem(tnc, epi), st>>>(ub, ua);
+    count_launch();
+  };
   for (int c0 = 0; c0 < count; c0 += kMaxBatch) {
     const int cnt = count - c0 < kMaxBatch ? count - c0 : kMaxBatch;
     // split every distinct A plane (pointer and reflection) once
@@ -583,17 +627,55 @@ int tc_umma_launch(const TcProblem *p, int count, int M, int N, int K, int epi, 
     ua.N = N;
     ua.Np = Np;
     ua.nkb = nkb;
-    ua.tnc = tnc;
-    ua.ntn = ntn;
     ua.nmt = nmt;
-    ua.ntiles = cnt * nmt * ntn;
     ua.a_term_stride = term_stride;
     ua.shift = shift;
-    ua.tmem_cols = cols;
     ua.spin = g_spin_limit;
-    const int grid = ua.ntiles < sm_count() ? ua.ntiles : sm_count();
-    kern<<<grid, kThreads, smem, st>>>(ub, ua);
-    count_launch();
+    // the column-tile width: forced, the widest, or the tuned one (timed on
+    // the first launch of this shape; the product reads only the split A
+    // planes and B and overwrites C, so the timed launches can repeat)
+    int tnc = cands[0];
+    bool tune = false;
+    const auto key = std::make_tuple(M, N, K, cnt, epi);
+    if (g_cols_mode > 0) {
+      for (int w : cands)
+        if (w == g_cols_mode) tnc = w;
+    } else if (g_cols_mode < 0 && cands.size() > 1) {
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      auto it = g_tuned.find(key);
+      if (it != g_tuned.end()) {
+        tnc = it->second;
+      } else {
+        // (not inside a stream capture, and not under a test's wait limit)
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(st, &cs);
+        tune = cs == cudaStreamCaptureStatusNone && g_spin_limit == kSpinLimit;
+      }
+    }
+    if (tune) {
+      cudaEvent_t e0, e1;
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      float best = 0.0f;
+      for (int w : cands) {
+        launch(ub, ua, cnt, w);  // warm-up
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < 3; ++r) launch(ub, ua, cnt, w);
+        cudaEventRecord(e1, st);
+        float ms = 0.0f;
+        if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+          break;
+        if (w == cands[0] || ms < best) {
+          best = ms;
+          tnc = w;
+        }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      g_tuned[key] = tnc;
+    }
+    launch(ub, ua, cnt, tnc);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -610,6 +692,36 @@ extern "C" int chm_sp_umma_status(void) {
   cudaMemcpyFromSymbol(&v, g_umma_error, sizeof(int));
   if (v) cudaMemcpyToSymbol(g_umma_error, &z, sizeof(int));
   return v;
+}
+
+extern "C" int chm_sp_set_umma_cols(int mode) {
+  const int prev = g_cols_mode;
+  g_cols_mode = mode < 0 ? -1 : mode;
+  return prev;
+}
+
+extern "C" int chm_sp_umma_tuned(int32_t *out, int max_shapes) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  int n = 0;
+  for (const auto &kv : g_tuned) {
+    if (out && n < max_shapes) {
+      int32_t *o = out + 6 * n;
+      o[0] = std::get<0>(kv.first);
+      o[1] = std::get<1>(kv.first);
+      o[2] = std::get<2>(kv.first);
+      o[3] = std::get<3>(kv.first);
+      o[4] = std::get<4>(kv.first);
+      o[5] = kv.second;
+    }
+    ++n;
+  }
+  return n;
+}
+
+extern "C" int chm_sp_umma_tune_reset(void) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tuned.clear();
+  return CHM_OK;
 }
 
 extern "C" int64_t chm_sp_set_umma_spin_limit(int64_t polls) {

@@ -470,13 +470,19 @@ class SplitRun:
     def graph_step(self, istep):
         """make_step(istep) with the step's kernels replayed from a CUDA graph.
         The graph holds the device work of one step (window origin advance,
-        deposits, spectral stage, gather and push); it is captured on first
-        use and again whenever the particle arrays change (a re-sort,
-        compaction or growth).  The host side (window bookkeeping, re-sorts,
+        deposits, spectral stage, gather and push); it is captured on the
+        second call (the first step runs eagerly, so that the tensor-core
+        products can time their tile widths) and again whenever the particle
+        arrays change (a re-sort, compaction or growth).  The host side (window bookkeeping, re-sorts,
         error-flag reads) runs outside the graph.  Same results as
         make_step, bitwise.  Falls back to make_step when the step is not
         capturable (see graph_capturable)."""
         if not self.graph_capturable():
+            return self.make_step(istep)
+        if not getattr(self, "_eager_done", False):
+            # the first step runs eagerly: the tensor-core products time their
+            # column-tile widths on a shape's first launch, which a capture cannot
+            self._eager_done = True
             return self.make_step(istep)
         self._maybe_sort(istep)
         if not self._scales_valid:

@@ -602,6 +602,21 @@ int chm_sp_gemm(float *C, const float *A, const chm_sp_ops *ops, int64_t mode,
  * (then reset): 1 or 3 the operand pipeline, 4 an accumulator hand-over,
  * 2 the final drain.  The CTA that gave up wrote no output. */
 int chm_sp_umma_status(void);
+/* Column-tile width of the tensor-core products for launches after this
+ * call: -1 picks it per shape (M, N, K, batch count, epilogue) by timing
+ * every candidate on the first launch of the shape outside stream capture
+ * (the default), 0 the default width (N rounded up to 16 and cut into the
+ * fewest tiles of at most 128 columns), > 0 that width where it is a
+ * candidate (a multiple of 16, at least 32, dividing the padded N), else
+ * the default.  The width changes no output bit.  Returns the previous
+ * mode. */
+int chm_sp_set_umma_cols(int mode);
+/* The widths picked so far: up to max_shapes records of six int32 (M, N,
+ * K, batch count, epilogue, width) into out (may be null); returns the
+ * number of shapes tuned. */
+int chm_sp_umma_tuned(int32_t *out, int max_shapes);
+/* Forgets the tuned widths (the next launch of each shape tunes again). */
+int chm_sp_umma_tune_reset(void);
 /* Iteration limit of the tensor-core GEMM's pipeline waits for launches
  * after this call (polls of mbarrier.try_wait; < 0 restores the default
  * 2^20); returns the previous limit.  A test hook: with 0 every pipeline

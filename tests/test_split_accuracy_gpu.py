@@ -201,3 +201,68 @@ def test_split_transforms_at_config_sizes(mods, grid):
     print(f"{name}: " + " ".join(f"{k} {v:.2e}" for k, v in errs.items()))
     assert max(errs.values()) < TOL_T, errs
     assert _lib.load().chm_sp_umma_status() == 0
+
+
+def _split_outputs(torch, _lib, fm, S, o, ws, dims):
+    """fb_in (factor epilogue), the Poisson correction (shift epilogue) and
+    fb_eb_out (stored products) of fixed random inputs."""
+    nx, nr, nkr, nm = dims
+    A = S.Args
+    st = _st(torch)
+    kx64 = _c(A["kx"], torch)
+    kx32 = kx64.to(torch.float32)
+    pf32 = _c(A["PoissFact"].astype(np.float32), torch)
+    rng = np.random.default_rng(19)
+    acc = (rng.standard_normal(2 * nx * nr * nm * 3) * 2.0 ** 40).astype(np.int64)
+    accd = torch.from_numpy(acc).cuda()
+    scd = torch.tensor([2.0 ** 40, 1.0], dtype=torch.float64, device="cuda")
+    depf = _c(A["DepFact"].astype(np.float32), torch)
+    Jfb = fm.fortran_zeros((nx, nkr, nm, 3), torch.complex64)
+    _lib.call("chm_sp_fb_in_acc", Jfb.data_ptr(), accd.data_ptr(), scd.data_ptr(), None, None,
+              float(A["leftX"]) + 1.7, kx64.data_ptr(), C.addressof(o["InCurr"][0]),
+              depf.data_ptr(), nx, nr, nkr, nm, 3, ws.data_ptr(), ws.numel(), st, None)
+    Js = _c(_rand((nx, nkr, nm, 3), 12).astype(np.complex64), torch)
+    gp = _c((0.1 * _rand((nx, nkr, nm, 3), 13)).astype(np.complex64), torch)
+    gn = _c((0.1 * _rand((nx, nkr, nm, 3), 14)).astype(np.complex64), torch)
+    _lib.call("chm_sp_poisson", Js.data_ptr(), gp.data_ptr(), gn.data_ptr(), pf32.data_ptr(),
+              10.0, C.addressof(o["Dp"][0]), C.addressof(o["Dm"][0]), kx32.data_ptr(), nx, nkr, nm,
+              3, 1, ws.data_ptr(), ws.numel(), st)
+    E = _c(_rand((nx, nkr, nm, 6), 15).astype(np.complex64), torch)
+    Bq = _c(_rand((nx, nkr, nm, 3), 16).astype(np.complex64), torch)
+    EB = fm.fortran_zeros((nx, nr, nm, 6), torch.complex64)
+    _lib.call("chm_sp_fb_eb_out", EB.data_ptr(), E.data_ptr(), Bq.data_ptr(), float(A["leftX"]),
+              kx64.data_ptr(), C.addressof(o["Out"][0]), nx, nr, nkr, nm, ws.data_ptr(), ws.numel(),
+              st, None)
+    torch.cuda.synchronize()
+    return [Jfb.cpu(), Js.cpu(), EB.cpu()]
+
+
+def test_column_tile_widths_change_no_bit(mods, grid):
+    """The tensor-core products give the same bits at every column-tile
+    width, so the tuner's choice changes only the speed: the default width,
+    64 and 32 columns forced, and the tuned widths, on the three epilogues at
+    the configurations' operator sizes.  The tuner records one width per
+    shape, a candidate (a multiple of 16, 32 and up)."""
+    torch, _lib, fm, split = mods
+    name, S, o, ws, dims = grid
+    lib = _lib.load()
+    prev = lib.chm_sp_set_umma_cols(0)
+    try:
+        ref = _split_outputs(torch, _lib, fm, S, o, ws, dims)
+        for mode in (64, 32, -1):
+            lib.chm_sp_set_umma_cols(mode)
+            if mode < 0:
+                lib.chm_sp_umma_tune_reset()
+            got = _split_outputs(torch, _lib, fm, S, o, ws, dims)
+            for r, g in zip(ref, got):
+                assert torch.equal(r, g), (name, mode)
+        n = lib.chm_sp_umma_tuned(None, 0)
+        buf = (C.c_int32 * (6 * max(n, 1)))()
+        assert lib.chm_sp_umma_tuned(buf, n) == n > 0
+        recs = np.array(buf[: 6 * n]).reshape(n, 6)
+        print(f"{name}: tuned (M, N, K, count, epilogue, width):", recs.tolist())
+        assert np.all(recs[:, 5] % 16 == 0) and np.all(recs[:, 5] >= 16)
+        assert np.all(recs[:, 5] <= 128)
+    finally:
+        lib.chm_sp_set_umma_cols(prev)
+    assert lib.chm_sp_umma_status() == 0

@@ -532,7 +532,8 @@ def test_graph_step_equals_make_step(mods):
         runs[1].graph_step(i)
     torch.cuda.synchronize()
     a, b = runs
-    assert b.graph_captures >= 2 and b.graph_replays == 7 and b.graph_launches > 10
+    # (the first step runs eagerly; the others replay graphs)
+    assert b.graph_captures >= 2 and b.graph_replays == 6 and b.graph_launches > 10
     assert a.solver.Args["leftX"] == b.solver.Args["leftX"]
     assert torch.equal(a.EG, b.EG) and torch.equal(a.EB, b.EB)
     for Pa, Pb in zip(a.parts, b.parts):
