@@ -199,6 +199,11 @@ struct PushDepArgs {
   unsigned long long *accR;  // (nx, nr, nm) x {re, im}
   const double *scaleJ, *scaleR;  // global scales 2^e
   const chm_sp_window *win;       // device window origin (or null: G's)
+  // (envelope kernel) a light-speed step of D = c dt / dx cells, split
+  // exactly into whole cells and an FP32 fraction, for the full and the
+  // half step; far: D >= 2
+  int far, d_int, dh_int;
+  float d_frac, dh_frac, d_cells;
 };
 
 // Block box: 32-bit fixed-point values at the block's own scales 2^elJ,
@@ -325,6 +330,41 @@ __device__ __forceinline__ Pushed push_vals(const PushDepArgs &A, int ix, float 
 __device__ __forceinline__ Pushed push_one(const PushDepArgs &A, i64 i) {
   const SpParts &P = A.P;
   return push_vals(A, P.ix[i], P.fx[i], P.y[i], P.z[i], P.px[i], P.py[i], P.pz[i], P.w[i]);
+}
+
+// The same push for a species that moves many cells per step (a
+// relativistic beam, D = c dt / dx >> 1): the x displacement D v_x is
+// taken as D - D (1 - v_x), the light-speed part D added exactly in whole
+// cells plus its FP32 fraction, the slip D (1 - v_x) computed without
+// cancellation, (1 - v_x) = (1 + p_y^2 + p_z^2) / (gamma (gamma + p_x)) for
+// p_x >= 0 (1 - p_x / gamma otherwise).  An FP32 product p_x dt / gamma
+// would carry an error of the order of D 2^-24 cells per step instead.
+__device__ __forceinline__ Pushed push_vals_far(const PushDepArgs &A, int ix, float fx, float y,
+                                                float z, float px, float py, float pz, float w) {
+  Pushed o;
+  const float pt2 = py * py + pz * pz;
+  const float ig = rsqrtf(1.0f + (px * px + pt2));  // 1 / gamma
+  const float g = 1.0f / ig;
+  const float slip = px >= 0.0f ? (1.0f + pt2) / (g * (g + px)) : 1.0f - px * ig;
+  const float dtg = A.dt * ig;
+  float xh = fx + (A.dh_frac - 0.5f * A.d_cells * slip);
+  float xn = fx + (A.d_frac - A.d_cells * slip);
+  const float flh = floorf(xh), fln = floorf(xn);
+  o.ixh = ix + A.dh_int + (int)flh;
+  o.fxh = xh - flh;
+  o.ixn = ix + A.d_int + (int)fln;
+  o.fxn = xn - fln;
+  o.yh = y + 0.5f * py * dtg;
+  o.zh = z + 0.5f * pz * dtg;
+  o.yn = y + py * dtg;
+  o.zn = z + pz * dtg;
+  const bool moving = (fabsf(px) + fabsf(py) + fabsf(pz)) != 0.0f;
+  o.moving = moving;
+  const float wg = moving ? w * ig : 0.0f;
+  o.vj[0] = px * wg;
+  o.vj[1] = py * wg;
+  o.vj[2] = pz * wg;
+  return o;
 }
 
 // ----------------------------------------------------------------------
@@ -1284,6 +1324,222 @@ __global__ void __launch_bounds__(kDepThreads, NM >= 3 ? 3 : 4) gather_push_run_
   }
 }
 
+// ----------------------------------------------------------------------
+// Envelope (KxShift) solver: the beam's current deposit and its gather +
+// external undulator field + Boris push (grid_deps_env.f90:18-95, 164-238;
+// devices.f90:117-203).  The solver stores the modes -K..K at slots
+// 0..2K.  The carrier e^{-i kx0 x} of a position (ix, fx) is a per-cell
+// table value (built in FP64 for the window's cells, chm_sp_carrier) times
+// e^{-i kx0 dx fx} in FP32, so its phase error stays at the FP32 rounding
+// of kx0 dx fx instead of growing with kx0 x.
+// ----------------------------------------------------------------------
+struct EnvArgs {
+  const float2 *tab;  // e^{-i kx0 (X0 + (k + c - 2) dx)}, c = 0 .. nx + 3, k the window cell
+  float kdx;          // kx0 dx
+};
+
+__global__ void carrier_kernel(float2 *tab, int ntab, double kx0, double X0, double dx, int win_k,
+                               const chm_sp_window *win) {
+  const int k = win ? win->k : win_k;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ntab; c += gridDim.x * blockDim.x) {
+    double sv, cv;
+    sincos(kx0 * (X0 + (double)(k + c - 2) * dx), &sv, &cv);
+    tab[c] = make_float2((float)cv, (float)-sv);
+  }
+}
+
+// e^{-i kx0 x} at (ix, fx); zero outside the table (no node of such a
+// position lies in the grid: window-relative cells -1 .. nx keep c in
+// 1 .. nx + 2)
+__device__ __forceinline__ float2 env_carrier(const EnvArgs &E, const SpGrid &G, int ix, float fx) {
+  const int c = ix - G.win_k + 2;
+  if (c < 0 || c >= G.nx + 4) return make_float2(0.f, 0.f);
+  float sv, cv;
+  sincosf(E.kdx * fx, &sv, &cv);
+  const float2 t = E.tab[c];
+  return make_float2(t.x * cv + t.y * sv, t.y * cv - t.x * sv);  // t (cv - i sv)
+}
+
+__device__ __forceinline__ float2 cmf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// Push + J deposit of the envelope solver's moving species (NM = 2K + 1
+// stored modes): the coordinate push of push_coords, then at the half step
+// J_z only (grid_deps_env.f90:76 deposits the third component alone) with
+// value (p_z / gamma) w e^{-i kx0 x} e^{-+i m theta} at slot K +- m.  Lane r
+// walks run r of its tile (the tile layout) and sums its particles' node
+// values in FP32 registers while the deposit cell stays the same; the sums,
+// already at the global quantum, are rounded and added to the 64-bit
+// accumulator when the cell changes.
+template <int NM>
+__global__ void __launch_bounds__(kDepThreads) push_deposit_env_kernel(PushDepArgs A, EnvArgs E) {
+  constexpr int K = (NM - 1) / 2;
+  const SpGrid G = window_grid(A.G, A.win);
+  const float sJ = (float)A.scaleJ[0];
+  const int lane = threadIdx.x & 31;
+  const i64 tile = (i64)blockIdx.x * kDepBlock + (i64)(threadIdx.x >> 5) * kTile;
+  const i64 first = tile + (i64)lane * kRunLen;
+  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - first));
+  prefetch_tile(A.P, tile, lane, true);
+  int ccx = 0, ccr = 0;
+  bool live = false;
+  float v[NM][4][2];
+  auto flush = [&]() {
+    if (!live) return;
+#pragma unroll
+    for (int sl = 0; sl < NM; ++sl)
+#pragma unroll
+      for (int nd = 0; nd < 4; ++nd) {
+        const int gx = ccx + (nd & 1), r = ccr + (nd >> 1);
+        if (gx < 0 || gx >= G.nx) continue;
+        const i64 e = ((i64)(sl + NM * 2) * G.nr + r) * G.nx + gx;
+        const long long qr = f2ll(v[sl][nd][0]), qi = f2ll(v[sl][nd][1]);
+        if (qr) atomicAdd(&A.accJ[2 * e], (unsigned long long)qr);
+        if (qi) atomicAdd(&A.accJ[2 * e + 1], (unsigned long long)qi);
+      }
+    live = false;
+  };
+  for (int j = 0; j < cnt; ++j) {
+    const i64 p = tile + (i64)j * kTileRuns + lane;
+    const float w = A.P.w[p];
+    const Pushed u = A.far ? push_vals_far(A, A.P.ix[p], A.P.fx[p], A.P.y[p], A.P.z[p], A.P.px[p],
+                                           A.P.py[p], A.P.pz[p], w)
+                           : push_vals(A, A.P.ix[p], A.P.fx[p], A.P.y[p], A.P.z[p], A.P.px[p],
+                                       A.P.py[p], A.P.pz[p], w);
+    A.P.ix[p] = u.ixn;
+    A.P.fx[p] = u.fxn;
+    A.P.y[p] = u.yn;
+    A.P.z[p] = u.zn;
+    if (w == 0.0f || !u.moving) continue;
+    const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, G);
+    if (!L.ok) continue;
+    if (!live || L.cx != ccx || L.cr != ccr) {
+      flush();
+      ccx = L.cx;
+      ccr = L.cr;
+      live = true;
+#pragma unroll
+      for (int sl = 0; sl < NM; ++sl)
+#pragma unroll
+        for (int nd = 0; nd < 4; ++nd) v[sl][nd][0] = v[sl][nd][1] = 0.0f;
+    }
+    const float2 car = env_carrier(E, G, u.ixh, u.fxh);
+    const float a = u.vj[2] * sJ;  // p_z w / gamma at the global quantum
+    const float2 base = make_float2(car.x * a, car.y * a);
+    const float sx[2] = {1.0f - L.sx1, L.sx1};
+    const float sr[2] = {1.0f - L.sr1, L.sr1};
+    const float2 ph = make_float2(L.phr, -L.phi);  // e^{-i theta} (0 on the axis)
+    float2 phm = make_float2(1.0f, 0.0f);
+#pragma unroll
+    for (int mi = 0; mi <= K; ++mi) {
+      if (mi > 0) phm = cmf(phm, ph);
+#pragma unroll
+      for (int side = 0; side < (mi > 0 ? 2 : 1); ++side) {
+        const float2 pm = side ? make_float2(phm.x, -phm.y) : phm;
+        const int sl = side ? K - mi : K + mi;
+        const float2 val = cmf(pm, base);
+#pragma unroll
+        for (int nd = 0; nd < 4; ++nd) {
+          const float sh = sx[nd & 1] * sr[nd >> 1];
+          v[sl][nd][0] += val.x * sh;
+          v[sl][nd][1] += val.y * sh;
+        }
+      }
+    }
+  }
+  flush();
+}
+
+// undul_analytic / undul_analytic_taper (devices.f90:117-203) on a
+// particle at x - X0u = xr: B_y += a s cosh(ku y), B_x += a c sinh(ku y),
+// (s, c) = sincos(ku xr), a = a0 ramp(xr) [taper]; ramps of one period at
+// both ends of the undulator
+struct UndArgs {
+  int kind;          // 0 none, 1 undul_analytic, 2 undul_analytic_taper
+  float a0, lam, ku, len, taper;
+  double xo, dx;     // particles' origin X0 - undulator start X0u; cell size
+};
+
+__device__ __forceinline__ void undulator(float *F, int ix, float fx, float y, const UndArgs &U) {
+  const float xr = (float)(U.xo + (double)ix * U.dx) + fx * (float)U.dx;
+  float ampl;
+  if (xr <= 0.0f || xr >= U.len) ampl = 0.0f;
+  else if (xr < U.lam) ampl = xr / U.lam;
+  else if (xr > U.len - U.lam) ampl = (U.len - xr) / U.lam;
+  else ampl = 1.0f;
+  if (U.kind == 2) ampl *= 1.0f + U.taper * (xr - 0.5f * U.len) / (0.5f * U.len);
+  ampl *= U.a0;
+  float sv, cv;
+  sincosf(U.ku * xr, &sv, &cv);
+  F[4] += ampl * sv * coshf(U.ku * y);
+  F[3] += ampl * cv * sinhf(U.ku * y);
+}
+
+// Gather of the envelope fields (carrier e^{+i kx0 x}, phase e^{+-i m theta}
+// at slot K +- m, 1 on the axis), the undulator field, Boris push
+template <int NM>
+__global__ void __launch_bounds__(256) gather_push_env_kernel(GatherArgs A, EnvArgs E, UndArgs U,
+                                                              i64 nphys) {
+  constexpr int K = (NM - 1) / 2;
+  const SpGrid G = window_grid(A.G, A.win);
+  const i64 plane = (i64)G.nx * G.nr;
+  for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < nphys;
+       p += (i64)gridDim.x * blockDim.x) {
+    if (logical_of(p) >= A.P.n) continue;
+    float F[6] = {0, 0, 0, 0, 0, 0};
+    const float w = A.P.w[p];
+    const int ix = A.P.ix[p];
+    const float fx = A.P.fx[p], y = A.P.y[p], z = A.P.z[p];
+    if (w != 0.0f) {
+      const Loc L = locate(ix, fx, y, z, G);
+      if (L.ok) {
+        const float sx[2] = {1.0f - L.sx1, L.sx1};
+        const float sr[2] = {1.0f - L.sr1, L.sr1};
+        const bool okx0 = L.cx >= 0 && L.cx < G.nx, okx1 = L.cx + 1 >= 0 && L.cx + 1 < G.nx;
+        const float2 c0 = env_carrier(E, G, ix, fx);
+        const float2 car = make_float2(c0.x, -c0.y);  // e^{+i kx0 x}
+        const bool axis = !(y * y + z * z > 0.0f);
+        const float2 ph = axis ? make_float2(1.0f, 0.0f) : make_float2(L.phr, L.phi);
+        float2 phm = make_float2(1.0f, 0.0f);
+#pragma unroll
+        for (int mi = 0; mi <= K; ++mi) {
+          if (mi > 0) phm = cmf(phm, ph);
+#pragma unroll
+          for (int side = 0; side < (mi > 0 ? 2 : 1); ++side) {
+            const float2 pm = cmf(car, side ? make_float2(phm.x, -phm.y) : phm);
+            const int sl = side ? K - mi : K + mi;
+#pragma unroll
+            for (int l = 0; l < 6; ++l) {
+              const float2 *b = A.eb + (i64)(sl + NM * l) * plane + (i64)L.cr * G.nx + L.cx;
+              float acc = 0.0f;
+#pragma unroll
+              for (int jr = 0; jr < 2; ++jr) {
+                if (okx0) {
+                  const float2 f = b[jr * G.nx];
+                  acc += sr[jr] * sx[0] * (pm.x * f.x - pm.y * f.y);
+                }
+                if (okx1) {
+                  const float2 f = b[jr * G.nx + 1];
+                  acc += sr[jr] * sx[1] * (pm.x * f.x - pm.y * f.y);
+                }
+              }
+              F[l] += acc;
+            }
+          }
+        }
+      }
+    }
+    if (U.kind) undulator(F, ix, fx, y, U);
+    float px = A.P.px[p], py = A.P.py[p], pz = A.P.pz[p];
+    boris(px, py, pz, F, 0.5f * A.dtq);
+    A.P.px[p] = px;
+    A.P.py[p] = py;
+    A.P.pz[p] = pz;
+  }
+}
+
+
 // FP64 (3, n) strided particle arrays -> split layout, as particles off ..
 // off + n - 1 (their dead flags cleared)
 __global__ void from_f64_kernel(SpParts P, uint8_t *dead, i64 off, const double *__restrict__ x,
@@ -1592,6 +1848,96 @@ int chm_sp_gather_push_generic(int32_t *ix, float *fx, float *y, float *z, float
                                void *stream, const chm_sp_window *win) {
   return gather_push(ix, fx, y, z, px, py, pz, w, n, win_k, win_f, dr_inv, eb_c64, nx, nr, nm, dtq,
                      stream, true, win);
+}
+
+int chm_sp_carrier(void *tab_c64, int64_t ntab, double kx0, double X0, double dx, int win_k,
+                   void *stream, const chm_sp_window *win) {
+  CHM_REQUIRE(tab_c64 && ntab > 0 && ntab < (1 << 30), "sp_carrier: bad args");
+  carrier_kernel<<<grid_for(ntab, 128), 128, 0, as_stream(stream)>>>(
+      reinterpret_cast<float2 *>(tab_c64), (int)ntab, kx0, X0, dx, win_k, win);
+  chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+int chm_sp_push_deposit_env(int32_t *ix, float *fx, float *y, float *z, float *px, float *py,
+                            float *pz, float *w, int64_t n, int win_k, float win_f, float dx_inv,
+                            float dr_inv, double dt, double dx, int nx, int nr, int nm,
+                            uint64_t *accJ, const double *scaleJ, const void *carrier_c64,
+                            float kdx, void *stream, const chm_sp_window *win) {
+  CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && (nm == 1 || nm == 3 || nm == 5) && dt > 0.0 && dx > 0.0,
+              "sp_push_deposit_env: bad dims (the envelope modes -K..K, K <= 2)");
+  if (n == 0) return CHM_OK;
+  CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && accJ && scaleJ && carrier_c64,
+              "sp_push_deposit_env: null pointer");
+  PushDepArgs A{};
+  A.P = SpParts{ix, fx, y, z, px, py, pz, w, n};
+  A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
+  A.dt = (float)dt;
+  A.dx_inv = dx_inv;
+  A.push = 1;
+  A.dep_j = 1;
+  A.accJ = reinterpret_cast<unsigned long long *>(accJ);
+  A.scaleJ = scaleJ;
+  A.win = win;
+  // the light-speed step in cells, from FP64 dt and dx
+  const double D = dt / dx;
+  A.far = D >= 2.0;
+  A.d_cells = (float)D;
+  A.d_int = (int)floor(D);
+  A.d_frac = (float)(D - floor(D));
+  A.dh_int = (int)floor(0.5 * D);
+  A.dh_frac = (float)(0.5 * D - floor(0.5 * D));
+  const EnvArgs E{reinterpret_cast<const float2 *>(carrier_c64), kdx};
+  const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
+  cudaStream_t st = as_stream(stream);
+  if (nm == 1) push_deposit_env_kernel<1><<<blocks, kDepThreads, 0, st>>>(A, E);
+  else if (nm == 3) push_deposit_env_kernel<3><<<blocks, kDepThreads, 0, st>>>(A, E);
+  else push_deposit_env_kernel<5><<<blocks, kDepThreads, 0, st>>>(A, E);
+  chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z, float *px, float *py,
+                           float *pz, float *w, int64_t n, int win_k, float win_f, float dr_inv,
+                           const void *eb_c64, int nx, int nr, int nm, float dtq,
+                           const void *carrier_c64, float kdx, int und_kind, const double *und,
+                           double X0, double dx, void *stream, const chm_sp_window *win) {
+  CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && (nm == 1 || nm == 3 || nm == 5),
+              "sp_gather_push_env: bad dims (the envelope modes -K..K, K <= 2)");
+  CHM_REQUIRE(und_kind >= 0 && und_kind <= 2 && (und_kind == 0 || und), "sp_gather_push_env: bad undulator");
+  if (n == 0) return CHM_OK;
+  CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && eb_c64 && carrier_c64,
+              "sp_gather_push_env: null pointer");
+  GatherArgs A{};
+  A.P = SpParts{ix, fx, y, z, px, py, pz, w, n};
+  A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
+  A.eb = reinterpret_cast<const float2 *>(eb_c64);
+  A.dtq = dtq;
+  A.win = win;
+  const EnvArgs E{reinterpret_cast<const float2 *>(carrier_c64), kdx};
+  UndArgs U{};
+  U.kind = und_kind;
+  if (und_kind) {
+    // (a0, period, start, length[, taper]) as devices.f90 takes them
+    U.a0 = (float)und[0];
+    U.lam = (float)und[1];
+    U.ku = (float)(2.0 * 3.14159265358979323846 / und[1]);
+    U.len = (float)und[3];
+    U.taper = und_kind == 2 ? (float)und[4] : 0.0f;
+    U.xo = X0 - und[2];
+    U.dx = dx;
+  }
+  const i64 nphys = tiles_of(n) * kTile;
+  cudaStream_t st = as_stream(stream);
+  const unsigned g = grid_for(nphys, 256, 16);
+  if (nm == 1) gather_push_env_kernel<1><<<g, 256, 0, st>>>(A, E, U, nphys);
+  else if (nm == 3) gather_push_env_kernel<3><<<g, 256, 0, st>>>(A, E, U, nphys);
+  else gather_push_env_kernel<5><<<g, 256, 0, st>>>(A, E, U, nphys);
+  chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
 }
 
 int chm_sp_from_f64(int32_t *ix, float *fx, float *y, float *z, float *px, float *py, float *pz,

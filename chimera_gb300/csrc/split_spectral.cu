@@ -480,10 +480,15 @@ __global__ void __launch_bounds__(MODE == 2 ? 256 : 512, MODE == 2 ? 3 : 1)
   const i64 ob = line / L.out_rows, orow = line % L.out_rows;
   float2 *dstl = L.out + (ob * L.out_rows_tot + orow + L.out_row_off) * (i64)n;
   float fac = 1.0f, sg = 1.0f;
-  if (L.eb_mode) {
+  if (L.eb_mode == 1) {
     const int m = (int)(ob % L.nm);
     fac = (float)((m == 0) ? 0.5 / kPi : 1.0 / kPi);
     sg = (m == 0) ? 1.0f : -1.0f;
+  } else if (L.eb_mode == 2) {
+    // envelope modes (grid_deps_env.f90:240-283): 1 / pi for every mode,
+    // the ghost row mirrored with sign -1 unless a single mode is stored
+    fac = (float)(1.0 / kPi);
+    sg = L.nm == 1 ? 1.0f : -1.0f;
   }
   const bool ghost = L.eb_mode && orow == 0;
   float2 *gdst = L.out + (ob * L.out_rows_tot) * (i64)n;
@@ -709,6 +714,7 @@ __global__ void div32_kernel(DivArgs A) {
 struct RotArgs {
   i64 nx, nk;
   int nm;
+  int env;  // envelope curl (fb_math_env.f90): no lower-neighbour term in component 1
   const float2 *v;
   i64 cs;
   const float2 *lo[3], *up[3];
@@ -729,7 +735,7 @@ __global__ void rot32_kernel(RotArgs A) {
     const float2 p1 = hi ? A.up[0][t] : z, p2 = hi ? A.up[1][t] : z, p3 = hi ? A.up[2][t] : z;
     const float2 m1 = A.lo[0][t], m2 = A.lo[1][t], m3 = A.lo[2][t];
     float2 o1 = fsub(make_float2(0.f, 0.f), fsub(fmi(p2), p3));
-    o1 = fsub(o1, fadd(fmi(m2), m3));
+    if (!A.env) o1 = fsub(o1, fadd(fmi(m2), m3));
     float2 o2 = fadd(fscl(fmi(v3), -kxv), fadd(fmi(p1), fmi(m1)));
     float2 o3 = fadd(fscl(fmi(v2), kxv), fsub(m1, p1));
     const float f = A.pf[t];
@@ -761,6 +767,24 @@ __global__ void psatd32_kernel(float2 *__restrict__ eg, const float2 *__restrict
         en = fadd(en, fadd(fscl(x, a[3]), fscl(y, a[4])));
         gn = fadd(gn, fadd(fscl(x, b[3]), fscl(y, b[4])));
       }
+      eg[i + P * (3 + l)] = gn;
+      eg[i + P * l] = en;
+    }
+  }
+}
+
+// PSATD without space charge, complex FP32 coefficients (the envelope
+// solver's, maxwell_solvers.f90:62-96)
+__global__ void psatd32c_kernel(float2 *__restrict__ eg, const float2 *__restrict__ j,
+                                const float2 *__restrict__ c1, const float2 *__restrict__ c2, i64 P) {
+  for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < P; i += (i64)gridDim.x * blockDim.x) {
+    const float2 a0 = c1[i], a1 = c1[i + P], a2 = c1[i + 2 * P];
+    const float2 b0 = c2[i], b1 = c2[i + P], b2 = c2[i + 2 * P];
+#pragma unroll
+    for (int l = 0; l < 3; ++l) {
+      const float2 e = eg[i + P * l], g = eg[i + P * (3 + l)], jj = j[i + P * l];
+      const float2 en = fadd(fadd(fmul(a0, e), fmul(a1, g)), fmul(a2, jj));
+      const float2 gn = fadd(fadd(fmul(b0, e), fmul(b1, g)), fmul(b2, jj));
       eg[i + P * (3 + l)] = gn;
       eg[i + P * l] = en;
     }
@@ -855,10 +879,15 @@ int chm_sp_fb_in_acc(void *out_c64, const int64_t *acc, const double *scale, con
   return gemm32(b, (int)(2 * nx), (int)nkr, (int)nrr, TC_EPI_SHIFT_FAC, shift, W, st);
 }
 
-// fb_eb_out + eb_correction (fb_io.f90:182-228, grid_deps.f90:219-266)
-int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double leftX,
-                     const double *kx, const void *Out_ops, int64_t nx, int64_t nr, int64_t nkr,
-                     int64_t nm, void *ws, int64_t ws_bytes, void *stream, const chm_sp_window *win) {
+}  // extern "C"
+
+namespace {
+
+// fb_eb_out + eb_correction (fb_io.f90:182-228, grid_deps.f90:219-266;
+// eb_mode 2: grid_deps_env.f90:240-283)
+int eb_out_impl(void *eb_c64, const void *e_c64, const void *b_c64, double leftX, const double *kx,
+                const void *Out_ops, int64_t nx, int64_t nr, int64_t nkr, int64_t nm, void *ws,
+                int64_t ws_bytes, void *stream, const chm_sp_window *win, int eb_mode) {
   CHM_REQUIRE(eb_c64 && e_c64 && b_c64 && kx && Out_ops, "sp_fb_eb_out: null pointer");
   CHM_REQUIRE(ws && ws_bytes >= chm_sp_fb_ws_bytes(nx, nr, nkr, nm), "sp_fb_eb_out: workspace");
   cudaStream_t st = as_stream(stream);
@@ -890,10 +919,29 @@ int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double 
   L.out_rows_tot = (int)nr;
   L.out_row_off = 1;
   L.nm = (int)nm;
-  L.eb_mode = 1;
+  L.eb_mode = eb_mode;
   L.sign = +1;
   L.filt_mode = -1;
   return lines32_launch(L, (int)nx, nrr * nm * 6, tw, st, true);
+}
+
+}  // namespace
+
+extern "C" {
+
+int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64, double leftX,
+                     const double *kx, const void *Out_ops, int64_t nx, int64_t nr, int64_t nkr,
+                     int64_t nm, void *ws, int64_t ws_bytes, void *stream, const chm_sp_window *win) {
+  return eb_out_impl(eb_c64, e_c64, b_c64, leftX, kx, Out_ops, nx, nr, nkr, nm, ws, ws_bytes, stream,
+                     win, 1);
+}
+
+int chm_sp_fb_eb_out_env(void *eb_c64, const void *e_c64, const void *b_c64, double leftX,
+                         const double *kx, const void *Out_ops, int64_t nx, int64_t nr,
+                         int64_t nkr, int64_t nm, void *ws, int64_t ws_bytes, void *stream,
+                         const chm_sp_window *win) {
+  return eb_out_impl(eb_c64, e_c64, b_c64, leftX, kx, Out_ops, nx, nr, nkr, nm, ws, ws_bytes, stream,
+                     win, 2);
 }
 
 // fb_filtr on complex64 planes (fb_io.f90:230-308)
@@ -927,12 +975,13 @@ int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx, const float *
 namespace {
 
 // lower / upper neighbour products of `ncomp` components for output modes
-// 0..nout-1 (input mode m-1+shift / m+1+shift, D mode m).  The lower
+// 0..nout-1 (input mode m-1+shift / m+1+shift, D mode m + dshift: 1 for
+// the envelope solver, whose D operators start one mode below -K).  The lower
 // neighbour of input mode -1 is the m = 1 plane `refl[c]` read reflected by
 // the product; without one (a single mode) that product is zero.
 int neighbours32(Fb32 &F, const float2 *in, i64 cs, int ncomp, int nin, int nout, int shift,
                  const float2 *const *refl, float2 *lo[3], float2 *up[3], unsigned char *lo_ok,
-                 unsigned char *up_ok) {
+                 unsigned char *up_ok, int dshift = 0) {
   const i64 plane = F.nx * F.nk;
   Batch32 b{};  // every output mode, neighbour and component in one launch
   for (int m = 0; m < nout; ++m) {
@@ -940,17 +989,17 @@ int neighbours32(Fb32 &F, const float2 *in, i64 cs, int ncomp, int nin, int nout
     lo_ok[m] = up_ok[m] = 0;
     for (int c = 0; c < ncomp; ++c) {
       if (mlo >= 0 && mlo < nin) {
-        b.add(in + c * cs + plane * mlo, lo[c] + plane * m, nullptr, F.Dm.mode[m]);
+        b.add(in + c * cs + plane * mlo, lo[c] + plane * m, nullptr, F.Dm.mode[m + dshift]);
         lo_ok[m] = 1;
       } else if (mlo == -1 && refl) {
-        b.add(refl[c], lo[c] + plane * m, nullptr, F.Dm.mode[m], 1);
+        b.add(refl[c], lo[c] + plane * m, nullptr, F.Dm.mode[m + dshift], 1);
         lo_ok[m] = 1;
       } else if (mlo == -1) {
         zero32_kernel<<<grid_for(plane, 256), 256, 0, F.st>>>(lo[c] + plane * m, plane);
         chm::count_launch();
       }
       if (mhi >= 0 && mhi < nin) {
-        b.add(in + c * cs + plane * mhi, up[c] + plane * m, nullptr, F.Dp.mode[m]);
+        b.add(in + c * cs + plane * mhi, up[c] + plane * m, nullptr, F.Dp.mode[m + dshift]);
         up_ok[m] = 1;
       }
     }
@@ -1126,11 +1175,17 @@ int chm_sp_poisson_psatd(void *J_c64, const void *gprv_c64, const void *gnxt_c64
                       space_charge, eg_c64, c1, c2, nterm, ws, ws_bytes, stream);
 }
 
-// B = rot(G) * PoissFact (solvers.py:536-553)
-int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf, const void *Dp_ops,
-                 const void *Dm_ops, const float *kx, int64_t nx, int64_t nkr, int64_t nm, void *ws,
-                 int64_t ws_bytes, void *stream) {
+}  // extern "C"
+
+namespace {
+
+// B = rot(G) * PoissFact (solvers.py:536-553); env: the envelope curl
+// (fb_math_env.f90) on the stored modes -K..K, no reflected neighbour
+int rot_b_impl(void *B_c64, const void *G_c64, const float *pf, const void *Dp_ops,
+               const void *Dm_ops, const float *kx, int64_t nx, int64_t nkr, int64_t nm, void *ws,
+               int64_t ws_bytes, void *stream, int env) {
   CHM_REQUIRE(B_c64 && G_c64 && pf && Dp_ops && Dm_ops && kx && nm <= 14, "sp_rot_b: bad args");
+  CHM_REQUIRE(!env || nm % 2 == 1, "sp_rot_b_env: the envelope solver stores an odd mode count");
   CHM_REQUIRE(ws && ws_bytes >= chm_sp_fb_ws_bytes(nx, nkr + 1, nkr, nm), "sp_rot_b: workspace");
   Fb32 F{nx, nkr, nm, tc_matrices(reinterpret_cast<const chm_sp_ops *>(Dp_ops)),
          tc_matrices(reinterpret_cast<const chm_sp_ops *>(Dm_ops)), kx, as_stream(stream), Ws{(char *)ws, ws_bytes}};
@@ -1148,12 +1203,14 @@ int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf, const void *Dp
   }
   const float2 *refl[3] = {G + plane, G + cs + plane, G + 2 * cs + plane};
   unsigned char lok[16], uok[16];
-  int rc = neighbours32(F, G, cs, 3, (int)nm, (int)nm, 0, nm > 1 ? refl : nullptr, lo, up, lok, uok);
+  int rc = neighbours32(F, G, cs, 3, (int)nm, (int)nm, 0, (nm > 1 && !env) ? refl : nullptr, lo, up,
+                        lok, uok, env ? 1 : 0);
   if (rc) return rc;
   RotArgs A{};
   A.nx = nx;
   A.nk = nkr;
   A.nm = (int)nm;
+  A.env = env;
   A.v = G;
   A.cs = cs;
   for (int c = 0; c < 3; ++c) {
@@ -1164,6 +1221,33 @@ int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf, const void *Dp
   A.pf = pf;
   A.out = reinterpret_cast<float2 *>(B_c64);
   rot32_kernel<<<dim3((unsigned)nkr, (unsigned)nm), 256, 0, F.st>>>(A); chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf, const void *Dp_ops,
+                 const void *Dm_ops, const float *kx, int64_t nx, int64_t nkr, int64_t nm, void *ws,
+                 int64_t ws_bytes, void *stream) {
+  return rot_b_impl(B_c64, G_c64, pf, Dp_ops, Dm_ops, kx, nx, nkr, nm, ws, ws_bytes, stream, 0);
+}
+
+int chm_sp_rot_b_env(void *B_c64, const void *G_c64, const float *pf, const void *Dp_ops,
+                     const void *Dm_ops, const float *kx, int64_t nx, int64_t nkr, int64_t nm,
+                     void *ws, int64_t ws_bytes, void *stream) {
+  return rot_b_impl(B_c64, G_c64, pf, Dp_ops, Dm_ops, kx, nx, nkr, nm, ws, ws_bytes, stream, 1);
+}
+
+int chm_sp_psatd_c(void *eg_c64, const void *j_c64, const void *c1_c64, const void *c2_c64,
+                   int64_t P, void *stream) {
+  CHM_REQUIRE(eg_c64 && j_c64 && c1_c64 && c2_c64 && P >= 0, "sp_psatd_c: bad args");
+  if (P == 0) return CHM_OK;
+  psatd32c_kernel<<<grid_for(P, 256), 256, 0, as_stream(stream)>>>(
+      (float2 *)eg_c64, (const float2 *)j_c64, (const float2 *)c1_c64, (const float2 *)c2_c64, P);
+  chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
 }

@@ -215,6 +215,11 @@ def _stream():
     return torch.cuda.current_stream().cuda_stream
 
 
+# device functions of fimera the split form fuses into its gather + push
+# (chm_sp_gather_push_env und_kind)
+_UNDULATORS = {"undul_analytic": 1, "undul_analytic_taper": 2}
+
+
 class SortCadence:
     """Run-time choice of the re-sort cadence (steps between two sorts by
     deposit cell).  As particles drift, the cell runs of the deposit and
@@ -277,11 +282,28 @@ class SplitRun:
         self.solver = S = self.fp.Solvers[0]
         A = S.Args
         feats = A["Features"]
-        if "KxShift" in A or "StaticKick" in feats:
-            raise NotImplementedError("the split form covers the plain (non-envelope) solver")
+        if "StaticKick" in feats:
+            raise NotImplementedError("the split form covers the time-stepped solvers")
+        # envelope (KxShift) solver: modes -K..K, J_z deposit with the
+        # carrier e^{-i kx0 x}, complex PSATD coefficients
+        self.env = "KxShift" in A
+        if self.env and ("SpaceCharge" in feats or "StillAsBackground" in feats):
+            raise NotImplementedError("the envelope charge deposit is not in the split form")
+        # external fields: the analytic undulators, fused into the gather
+        self.undulators = []
         for sp in self.fp.Particles:
-            if sp.Devices:
-                raise NotImplementedError("external-field devices are not in the split form")
+            und = None
+            for d in sp.Devices:
+                kind = _UNDULATORS.get(getattr(d[0], "__name__", ""))
+                if kind is None or und is not None or len(d) != 2:
+                    raise NotImplementedError(
+                        "the split form fuses one analytic undulator (undul_analytic or "
+                        "undul_analytic_taper) per species into the push")
+                prm = np.asarray(d[1], dtype=np.float64).ravel()
+                und = (kind, prm)
+            self.undulators.append(und)
+        if any(self.undulators) and not self.env:
+            raise NotImplementedError("the split form fuses undulators into the envelope push only")
         dev = self.device = S.device
         self.space_charge = "SpaceCharge" in feats
         self.poisson = "NoPoissonCorrection" not in feats
@@ -301,21 +323,28 @@ class SplitRun:
             ops, buf, d = _prepare_ops(A[key], dev)
             self.ops[name] = ops
             self._keep += [buf, d]
+        # kx of the derivatives (kx0 + kx_env for the envelope solver) and of
+        # the transforms' shift (kx_env for the envelope solver)
         self.kx64 = S.dev["kx"]
         self.kx32 = self.kx64.to(torch.float32)
+        self.kxb64 = S.dev["kx_base"]
         self.depfact = _f32(A["DepFact"], dev)
         self.pf = _f32(A["PoissFact"], dev)
         CE, CG = S.Data["PSATD_E"], S.Data["PSATD_G"]
-        if CE.is_complex():
-            raise NotImplementedError("complex PSATD coefficients (envelope solver)")
+        self.complex_psatd = CE.is_complex()
         self.nterm = CE.shape[-1]
-        self.c1 = CE.to(torch.float32)
-        self.c2 = CG.to(torch.float32)
-        if not chimera.is_fortran(self.c1):
-            self.c1 = chimera.fortran_empty(tuple(CE.shape), torch.float32, dev)
-            self.c1.copy_(CE)
-            self.c2 = chimera.fortran_empty(tuple(CG.shape), torch.float32, dev)
-            self.c2.copy_(CG)
+        cdt = torch.complex64 if self.complex_psatd else torch.float32
+        self.c1 = chimera.fortran_empty(tuple(CE.shape), cdt, dev)
+        self.c1.copy_(CE)
+        self.c2 = chimera.fortran_empty(tuple(CG.shape), cdt, dev)
+        self.c2.copy_(CG)
+        if self.complex_psatd and (self.nterm != 3 or self.poisson):
+            raise NotImplementedError("complex PSATD coefficients without space charge and "
+                                      "without the Poisson correction")
+        if self.env:
+            # carrier table of the window's cells (chm_sp_carrier)
+            self.kx0 = float(A["kx0"])
+            self.carrier = torch.zeros(self.nx + 4, dtype=torch.complex64, device=dev)
         # fields
         D = S.Data
         fb = (self.nx, self.nkr, self.nm)
@@ -419,6 +448,14 @@ class SplitRun:
 
     def _deposit(self, P, push, accJ, accR, scaleJ, scaleR):
         k, f = self._win()
+        if self.env:
+            # (the envelope solver: push + J_z with the carrier; no charge)
+            _lib.call("chm_sp_push_deposit_env", *P.ptrs(), P.n, k, f, 1.0 / self.dx,
+                      float(self.solver.Args["dr_inv"]), float(self.dt), float(self.dx), self.nx,
+                      self.nr, self.nm,
+                      accJ.data_ptr(), scaleJ.data_ptr(), self.carrier.data_ptr(),
+                      float(self.kx0 * self.dx), _stream(), self.win.data_ptr())
+            return
         _lib.call("chm_sp_push_deposit", *P.ptrs(), P.n, k, f, 1.0 / self.dx,
                   float(self.solver.Args["dr_inv"]), float(self.dt), self.nx, self.nr, self.nm,
                   int(push), accJ.data_ptr() if accJ is not None else None,
@@ -439,7 +476,7 @@ class SplitRun:
         _lib.call("chm_sp_fb_in_acc", out.data_ptr(), acc.data_ptr(), scale.data_ptr(),
                   acc2.data_ptr() if acc2 is not None else None,
                   scale2.data_ptr() if scale2 is not None else None, float(A["leftX"]),
-                  self.kx64.data_ptr(), C.addressof(self.ops["InCurr"]), self.depfact.data_ptr(),
+                  self.kxb64.data_ptr(), C.addressof(self.ops["InCurr"]), self.depfact.data_ptr(),
                   self.nx, self.nr, self.nkr, self.nm, ncomp, self.ws.data_ptr(), self.ws.numel(),
                   _stream(), self.win.data_ptr())
 
@@ -574,6 +611,8 @@ class SplitRun:
         fuse_rho = self.space_charge and not staged_move
         if self.space_charge:
             self.accR.zero_()
+        if self.env:
+            self._carrier()
         for spc, P in self._moving():
             self._deposit(P, True, self.accJ, self.accR if fuse_rho else None, self.scaleJ,
                           self.scaleR if fuse_rho else None)
@@ -612,6 +651,10 @@ class SplitRun:
                       self.kx32.data_ptr(), self.nx, self.nkr, self.nm, 3, int(self.space_charge),
                       self.EG.data_ptr(), self.c1.data_ptr(), self.c2.data_ptr(), int(self.nterm),
                       ws, wsb, st)
+        elif self.complex_psatd:
+            # maxwell_push_wo_spchrg with the envelope solver's complex coefficients
+            _lib.call("chm_sp_psatd_c", self.EG.data_ptr(), self.Jfb.data_ptr(), self.c1.data_ptr(),
+                      self.c2.data_ptr(), self.nx * self.nkr * self.nm, st)
         else:
             P_ = self.nx * self.nkr * self.nm
             _lib.call("chm_sp_psatd", self.EG.data_ptr(), self.Jfb.data_ptr(),
@@ -664,17 +707,42 @@ class SplitRun:
             self.EB.zero_()
             return
         G = self.EG[:, :, :, 3:]
-        _lib.call("chm_sp_rot_b", self.Bfb.data_ptr(), G.data_ptr(), self.pf.data_ptr(),
+        env = "_env" if self.env else ""
+        _lib.call("chm_sp_rot_b" + env, self.Bfb.data_ptr(), G.data_ptr(), self.pf.data_ptr(),
                   C.addressof(self.ops["Dp"]), C.addressof(self.ops["Dm"]), self.kx32.data_ptr(),
                   self.nx, self.nkr, self.nm, ws, wsb, st)
-        _lib.call("chm_sp_fb_eb_out", self.EB.data_ptr(), self.EG.data_ptr(), self.Bfb.data_ptr(),
-                  float(A["leftX"]), self.kx64.data_ptr(), C.addressof(self.ops["Out"]), self.nx,
-                  self.nr, self.nkr, self.nm, ws, wsb, st, self.win.data_ptr())
+        _lib.call("chm_sp_fb_eb_out" + env, self.EB.data_ptr(), self.EG.data_ptr(),
+                  self.Bfb.data_ptr(), float(A["leftX"]), self.kxb64.data_ptr(),
+                  C.addressof(self.ops["Out"]), self.nx, self.nr, self.nkr, self.nm, ws, wsb, st,
+                  self.win.data_ptr())
         k, f = self._win()
-        for spc, P in self._moving():
+        if self.env:
+            self._carrier()  # (a staged frame moved since the deposit)
+        for i, (spc, P) in enumerate(zip(self.fp.Particles, self.parts)):
+            if "Still" in spc.Args["Features"]:
+                continue
             dtq = spc.Args["push_fact"] * spc.Args["TimeStep"]
-            _lib.call("chm_sp_gather_push", *P.ptrs(), P.n, k, f, float(A["dr_inv"]),
-                      self.EB.data_ptr(), self.nx, self.nr, self.nm, float(dtq), st, self.win.data_ptr())
+            if not self.env:
+                _lib.call("chm_sp_gather_push", *P.ptrs(), P.n, k, f, float(A["dr_inv"]),
+                          self.EB.data_ptr(), self.nx, self.nr, self.nm, float(dtq), st,
+                          self.win.data_ptr())
+                continue
+            und = self.undulators[i]
+            prm = np.zeros(5)
+            if und is not None:
+                prm[:min(5, und[1].size)] = und[1][:5]
+            _lib.call("chm_sp_gather_push_env", *P.ptrs(), P.n, k, f, float(A["dr_inv"]),
+                      self.EB.data_ptr(), self.nx, self.nr, self.nm, float(dtq),
+                      self.carrier.data_ptr(), float(self.kx0 * self.dx),
+                      0 if und is None else und[0], prm.ctypes.data, self.X0, float(self.dx), st,
+                      self.win.data_ptr())
+
+    def _carrier(self):
+        """The carrier table of the window's cells (chm_sp_carrier) from the
+        device window record."""
+        k, _ = self._win()
+        _lib.call("chm_sp_carrier", self.carrier.data_ptr(), self.carrier.numel(), self.kx0,
+                  self.X0, float(self.dx), k, _stream(), self.win.data_ptr())
 
     def _add_plasma(self, wind):
         fp = self.fp
@@ -868,7 +936,7 @@ def transform_errors(run: SplitRun) -> dict:
     del J
     out = chimera.fortran_zeros((nx, nkr, nm, 3), torch.complex64, dev)
     _lib.call("chm_sp_fb_in_acc", out.data_ptr(), run.accJ.data_ptr(), run.scaleJ.data_ptr(), None,
-              None, leftX, run.kx64.data_ptr(), C.addressof(run.ops["InCurr"]),
+              None, leftX, run.kxb64.data_ptr(), C.addressof(run.ops["InCurr"]),
               run.depfact.data_ptr(), nx, nr, nkr, nm, 3, ws, wsb, st, None)
     ref = chimera._fb_in(chimera.fortran_zeros((nx, nkr, nm, 3), device=dev), Jf, leftX,
                          *A["FBCurrIn"], 3, fact=S.dev["DepFact"])
@@ -902,21 +970,23 @@ def transform_errors(run: SplitRun) -> dict:
         errs["poisson"] = rel(Js, Jd)
         del Js, Jd, v
     G = run.EG[:, :, :, 3:]
+    env = "_env" if run.env else ""
     Bs = chimera.fortran_zeros((nx, nkr, nm, 3), torch.complex64, dev)
-    _lib.call("chm_sp_rot_b", Bs.data_ptr(), G.data_ptr(), run.pf.data_ptr(),
+    _lib.call("chm_sp_rot_b" + env, Bs.data_ptr(), G.data_ptr(), run.pf.data_ptr(),
               C.addressof(run.ops["Dp"]), C.addressof(run.ops["Dm"]), run.kx32.data_ptr(), nx, nkr,
               nm, ws, wsb, st)
     Gd = chimera.fortran_empty((nx, nkr, nm, 3), torch.complex128, dev)
     Gd.copy_(G)
-    ref = chimera.fb_rot(chimera.fortran_zeros((nx, nkr, nm, 3), device=dev), Gd, *FBD)
+    rot = chimera.fb_rot_env if run.env else chimera.fb_rot
+    ref = rot(chimera.fortran_zeros((nx, nkr, nm, 3), device=dev), Gd, *FBD)
     ref = chimera.omp_mult_vec(ref, S.dev["PoissFact"])
     errs["rot_b"] = rel(Bs, ref)
     del Gd, ref
     EB = chimera.fortran_zeros((nx, nr, nm, 6), torch.complex64, dev)
-    _lib.call("chm_sp_fb_eb_out", EB.data_ptr(), run.EG.data_ptr(), Bs.data_ptr(), leftX,
-              run.kx64.data_ptr(), C.addressof(run.ops["Out"]), nx, nr, nkr, nm, ws, wsb, st, None)
+    _lib.call("chm_sp_fb_eb_out" + env, EB.data_ptr(), run.EG.data_ptr(), Bs.data_ptr(), leftX,
+              run.kxb64.data_ptr(), C.addressof(run.ops["Out"]), nx, nr, nkr, nm, ws, wsb, st, None)
     ref = chimera.fb_eb_out(chimera.fortran_zeros((nx, nr, nm, 6), device=dev), c128(run.EG),
-                            c128(Bs), leftX, A["kx"], A["Out"], eb_mode=1)
+                            c128(Bs), leftX, *A["FBout"], eb_mode=2 if run.env else 1)
     errs["fb_eb_out"] = rel(EB, ref)
     del EB, ref, Bs
     run.check_status()

@@ -142,3 +142,74 @@ def components(size: str, kind: str = "none", seed: int = 1003, device=None) -> 
     parts[-1] = parts[-1] * -1
     io.add_particles(*parts)
     return {"Solvers": (solver,), "Particles": (el, io), "MovingFrames": (window(size, kind),)}
+
+
+# ----------------------------------------------------------------------
+# Free-electron-laser workloads: the reference's FEL set-up
+# (doc/tests/fel-testrun.py): envelope solver (KxShift at the resonant
+# wavenumber, CoPropagative at the beam velocity, NoPoissonCorrection), a
+# relativistic beam in a planar analytic undulator (undul_analytic, the
+# period as the length unit), a seed laser at the resonance and a Staged
+# window moving with the beam.  Lengths follow fel-testrun.py (box 200 um,
+# radius 1 mm cut at 0.7 mm, beam 80 um, undulator period 2.8 cm); the
+# beam energy and undulator strength, grid and particle count are the
+# workload's.
+@dataclass(frozen=True)
+class FelWorkload:
+    name: str
+    nx: int
+    nr: int
+    max_mode: int      # stored modes -max_mode .. max_mode
+    rand_cell: int     # particles per cell (RandCell)
+    gamma: float
+    K0: float
+    periods: float     # undulator length in periods
+    dt: float = 1.0 / 30
+    a0_seed: float = 0.15
+
+
+FEL = {
+    # 2048 x 128 grid, modes -1..1, ~8.4M beam particles
+    "fel4": FelWorkload("fel_2048x128_m3", nx=2048, nr=128, max_mode=1, rand_cell=80,
+                        gamma=200.0, K0=1.0, periods=80.0),
+    # the same set-up on a 256 x 32 grid (the long-run test's case)
+    "fel_small": FelWorkload("fel_256x32_m3", nx=256, nr=32, max_mode=1, rand_cell=16,
+                             gamma=200.0, K0=1.0, periods=80.0),
+}
+
+
+def fel_components(size: str, seed: int = 1004, device=None) -> dict:
+    """SimComps of an FEL workload (solver with its seed laser, the beam with
+    its undulator, the Staged window)."""
+    from . import fimera
+    from .messages import msg
+    from .solvers import Solver
+    from .species import Specie
+    msg.quiet = True
+    W = FEL[size]
+    lam0 = 2.8  # undulator period (cm), the length unit
+    g0 = W.gamma
+    gg = g0 / (1.0 + W.K0 ** 2 / 2) ** 0.5
+    k_res = 2 * gg ** 2
+    vb = (1.0 - gg ** -2) ** 0.5
+    Lgx, Rg, Rcut = 200e-4 / lam0, 1000e-4 / lam0, 700e-4 / lam0
+    lbx = lbr = 80e-4 / lam0
+    dens = 20e-12 / 1.6022e-19 / (np.pi * 80e-4 ** 3) / (1.1e21 / 2.8e4 ** 2)
+    np.random.seed(seed)
+    kw = {} if device is None else {"device": device}
+    solver = Solver({"Grid": (-0.5 * Lgx, 0.5 * Lgx, Rg, Lgx / W.nx, Rg / W.nr),
+                     "TimeStep": W.dt, "MaxAzimuthMode": W.max_mode, "KxShift": k_res,
+                     "Rcut": Rcut, "CoPropagative": vb,
+                     "Features": {"NoPoissonCorrection": True}}, **kw)
+    if device in (None, "cuda"):
+        solver.add_gauss_beam({"a0": W.a0_seed, "k0": k_res, "x0": -30e-4 / lam0,
+                               "x_foc": 70.0 / lam0, "Lx": 15e-4 / lam0, "LR": 180e-4 / lam0})
+    beam = Specie({"Grid": (-0.5 * Lgx, 0.5 * Lgx, Rg, Lgx / W.nx, lbr / W.nr),
+                   "TimeStep": W.dt, "Charge": -1.0, "Mass": 1.0, "Density": dens,
+                   "RandCell": W.rand_cell, "MomentaMeans": (g0, 0.0, 0.0),
+                   "MomentaSpreads": (1e-4 * g0, 2e-5 * g0, 2e-5 * g0),
+                   "Devices": ([fimera.undul_analytic, np.array([W.K0, 1.0, 1.0, W.periods])],)},
+                  **kw)
+    beam.add_particles(*beam.gen_parts(Domain=(-0.5 * lbx, 0.5 * lbx, 0.0, lbr)))
+    wind = {"TimeStep": W.dt, "Steps": 1, "Velocity": vb, "Features": ("Staged", "NoSorting")}
+    return {"Solvers": (solver,), "Particles": (beam,), "MovingFrames": (wind,)}

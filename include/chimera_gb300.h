@@ -481,6 +481,42 @@ int chm_sp_gather_push_generic(int32_t *ix, float *fx, float *y, float *z,
                                float dtq, void *stream,
                         const chm_sp_window *win);
 
+/* Envelope (KxShift) solver, nm = 2K + 1 stored modes -K..K (K <= 2).
+ * chm_sp_carrier fills tab (ntab >= nx + 4 complex64) with the carrier
+ * e^{-i kx0 (X0 + (k + c - 2) dx)} of the window's cells c (k = the window
+ * cell win->k, or win_k without a record), in FP64; the kernels below take
+ * a particle's carrier as tab[ix - k + 2] e^{-i kdx fx}, kdx = kx0 dx. */
+int chm_sp_carrier(void *tab_c64, int64_t ntab, double kx0, double X0, double dx,
+                   int win_k, void *stream, const chm_sp_window *win);
+/* push_coords + dep_curr_env (particle_tools.f90:58-82,
+ * grid_deps_env.f90:18-95): the coordinate push, then J_z only (the
+ * reference's envelope deposit writes the third component alone) with
+ * value (p_z / gamma) w e^{-i kx0 x} e^{-+i m theta} at mode slot K +- m,
+ * into accJ (nx,nr,nm,3) int64 {re, im} at the scale scaleJ.  When a step
+ * spans c dt / dx >= 2 cells (dt, dx in FP64), the x push takes the
+ * light-speed step exactly and the slip (1 - v_x) separately. */
+int chm_sp_push_deposit_env(int32_t *ix, float *fx, float *y, float *z,
+                            float *px, float *py, float *pz, float *w, int64_t n,
+                            int win_k, float win_f, float dx_inv, float dr_inv,
+                            double dt, double dx, int nx, int nr, int nm,
+                            uint64_t *accJ, const double *scaleJ,
+                            const void *carrier_c64, float kdx, void *stream,
+                            const chm_sp_window *win);
+/* proj_fld_env + an analytic undulator + push_velocs
+ * (grid_deps_env.f90:164-238, devices.f90:117-203, particle_tools.f90:18-56):
+ * gather with the carrier e^{+i kx0 x} and e^{+-i m theta} (1 on the axis),
+ * the undulator field of und_kind 1 (undul_analytic: und = a0, period,
+ * start, length) or 2 (undul_analytic_taper: und = a0, period, start,
+ * length, taper) at the particle's x = X0 + (ix + fx) dx, 0 for none, then
+ * the Boris push. */
+int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z,
+                           float *px, float *py, float *pz, float *w, int64_t n,
+                           int win_k, float win_f, float dr_inv,
+                           const void *eb_c64, int nx, int nr, int nm, float dtq,
+                           const void *carrier_c64, float kdx, int und_kind,
+                           const double *und, double X0, double dx,
+                           void *stream, const chm_sp_window *win);
+
 /* FP64 (3,n)/(n) particle arrays (particle order) <-> split layout; from_f64
  * writes particles offset .. offset+n-1 and clears their dead flags (dead
  * may be NULL). */
@@ -560,6 +596,14 @@ int chm_sp_fb_eb_out(void *eb_c64, const void *e_c64, const void *b_c64,
                      int64_t nx, int64_t nr, int64_t nkr, int64_t nm, void *ws,
                      int64_t ws_bytes, void *stream,
                         const chm_sp_window *win);
+/* fb_eb_out with the envelope solver's eb_correction
+ * (grid_deps_env.f90:240-283): 1/pi for every mode, the ghost row -1 times
+ * row 1 unless nm = 1.  kx: the envelope's kx_env. */
+int chm_sp_fb_eb_out_env(void *eb_c64, const void *e_c64, const void *b_c64,
+                         double leftX, const double *kx, const void *Out_ops,
+                         int64_t nx, int64_t nr, int64_t nkr, int64_t nm,
+                         void *ws, int64_t ws_bytes, void *stream,
+                         const chm_sp_window *win);
 int chm_sp_fb_filtr(void *vec_c64, double leftX, const double *kx,
                     const float *filtr, int64_t nxfilt, int modefilt,
                     int64_t nx, int64_t nkr, int64_t nm, int64_t ncomp,
@@ -592,6 +636,17 @@ int chm_sp_rot_b(void *B_c64, const void *G_c64, const float *pf,
 int chm_sp_psatd(void *eg_c64, const void *j_c64, const void *gprv_c64,
                  const void *gnxt_c64, const float *c1, const float *c2,
                  int nterm, int64_t P, void *stream);
+/* The envelope curl B = rot_env(G) * PoissFact (fb_math_env.f90 curl on
+ * the stored modes -K..K, Dp/Dm holding the modes -K-1..K+1; no
+ * lower-neighbour term in the first component) and the PSATD update without
+ * space charge with complex64 coefficients c1, c2 (nx, nkr, nm, 3)
+ * (maxwell_push_wo_spchrg, maxwell_solvers.f90:62-96). */
+int chm_sp_rot_b_env(void *B_c64, const void *G_c64, const float *pf,
+                     const void *Dp_ops, const void *Dm_ops, const float *kx,
+                     int64_t nx, int64_t nkr, int64_t nm, void *ws,
+                     int64_t ws_bytes, void *stream);
+int chm_sp_psatd_c(void *eg_c64, const void *j_c64, const void *c1_c64,
+                   const void *c2_c64, int64_t P, void *stream);
 /* Dense product C(M,N) = A(M,K) B(K,N) with B a prepared operator mode, on
  * the tensor cores (tcgen05, split-BF16) or, with engine = 0, on the FP32
  * SIMT path; for tests and tuning. */
