@@ -521,6 +521,8 @@ def run_gb300(args):
         del run2, solver2, el2
         torch.cuda.empty_cache()
 
+    fel = fel_leg(args, world) if (args.fel_steps > 0 and args.form == "split") else None
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
@@ -563,6 +565,7 @@ def run_gb300(args):
         "stages": stages,
         "clocks": clk,
         "e2e": e2e,
+        "fel": fel,
         "cpu_baseline": cpu,
         "peaks": {"source": peak_kind, "hbm_gbs": peaks.get("hbm_gbs"),
                   "bf16_tflops": peaks.get("bf16_tflops")},
@@ -576,6 +579,49 @@ def run_gb300(args):
         print(f"device error flags set: {flags}", file=sys.stderr)
         return 1
     return 0
+
+
+def fel_leg(args, world=1):
+    """The FEL workload (envelope solver, analytic undulator, Staged window;
+    2048 x 128 x 3 envelope modes, 8.4M beam particles): the plain FP64 form
+    and the split form (steps replayed from CUDA graphs) on the same run,
+    particle*steps/s of each from CUDA events on the launch stream."""
+    import torch
+
+    from chimera_gb300 import ChimeraRun
+    from chimera_gb300.split import SplitRun
+    stream = torch.cuda.current_stream()
+    fp = ChimeraRun(workloads.fel_components("fel4", seed=1004))
+    beam = fp.Particles[0]
+    step = 0
+    for _ in range(1):
+        step += 1
+        fp.make_step(step)
+    torch.cuda.synchronize()
+    n64 = max(1, args.fel_fp64_steps)
+    ms64, ps64 = time_steps(fp, step + 1, n64, lambda: beam.num_particles, stream)
+    step += n64
+    run = SplitRun(None, fp64_run=fp)
+    for _ in range(3):
+        step += 1
+        run.graph_step(step)
+    torch.cuda.synchronize()
+    ms, ps = time_steps(run, step + 1, args.fel_steps, lambda: run.num_moving, stream,
+                        run.graph_step)
+    run.check_status()
+    W = workloads.FEL["fel4"]
+    out = {"workload": W.name, "particles": beam.num_particles, "nx": W.nx,
+           "nr": int(run.nr), "nkr": int(run.nkr), "modes": int(run.nm),
+           "split": {"value": world * ps / (ms / 1e3), "unit": METRIC, "steps": args.fel_steps,
+                     "warmup": 3, "ms_per_step": ms / args.fel_steps},
+           "fp64_gpu": {"value": world * ps64 / (ms64 / 1e3), "unit": METRIC, "steps": n64,
+                        "warmup": 1, "ms_per_step": ms64 / n64},
+           "accuracy": "radiated energy within 1 % of the FP64 form over 2400 steps "
+                       "(tests/test_split_env_gpu.py, the 256 x 32 case)"}
+    out["split_over_fp64"] = out["split"]["value"] / out["fp64_gpu"]["value"]
+    del run, fp, beam
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_batched(args):
@@ -743,6 +789,10 @@ def main():
                     help="timed steps of the plain FP64 form in the same run (0: skip)")
     ap.add_argument("--decay-steps", type=int, default=500,
                     help="continue the timed split run to this step and time its last 20 steps")
+    ap.add_argument("--fel-steps", type=int, default=20,
+                    help="timed split steps of the FEL leg (0: skip)")
+    ap.add_argument("--fel-fp64-steps", type=int, default=3,
+                    help="timed FP64 steps of the FEL leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-errors", action="store_true")
