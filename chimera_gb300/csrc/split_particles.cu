@@ -432,7 +432,7 @@ struct BlockPlan {
 template <bool STAGED>
 __device__ BlockPlan plan_block(const PushDepArgs &A, const SpGrid &G, i64 base, int *bb,
                                 int box_bytes, const StageView &V) {
-  __shared__ float wsm[2][kDepThreads / 32];
+  __shared__ float wsm[2][8];  // per-warp partial sums (blocks of up to 8 warps)
   if (threadIdx.x == 0) {
     bb[0] = INT_MAX;
     bb[1] = INT_MIN;
@@ -502,7 +502,7 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, const SpGrid &G, i64 base,
   __syncthreads();
   BlockPlan P;
   float Bl = 0.0f, Bj = 0.0f;
-  for (int k = 0; k < kDepThreads / 32; ++k) {  // fixed order
+  for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {  // fixed order
     Bl += wsm[0][k];
     Bj += wsm[1][k];
   }
@@ -707,38 +707,6 @@ struct RunPart {
   float fx, y, z, px, py, pz, w;
 };
 
-// One particle of a run kernel's main loop: push (store(u) writes the new
-// coordinates), then its J at the half step and rho at the new position
-// into the lane's cell sums at the block scale.
-template <int NM, bool PUSH, bool DJ, bool DR, typename Store>
-__device__ __forceinline__ void run_particle(const PushDepArgs &A, const SpGrid &G,
-                                             const BlockPlan &Pl, const BoxGeo &geo,
-                                             const RunPart &c, CellAcc<NM, 3> &cj,
-                                             CellAcc<NM, 1> &cr, Store store) {
-  const float w = c.w;
-  Pushed u;
-  if (PUSH || DJ) {
-    u = push_vals(A, c.ix, c.fx, c.y, c.z, c.px, c.py, c.pz, w);
-  } else {
-    u.ixh = u.ixn = c.ix;
-    u.fxh = u.fxn = c.fx;
-    u.yh = u.yn = c.y;
-    u.zh = u.zn = c.z;
-  }
-  if (PUSH) store(u);
-  if (w == 0.0f) return;
-  if (DJ && u.moving) {  // grid_deps.f90:42: no current from particles at rest
-    const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, G);
-    const float vs[3] = {u.vj[0] * Pl.lJ, u.vj[1] * Pl.lJ, u.vj[2] * Pl.lJ};
-    acc_add(cj, L, vs, 0, G, geo);
-  }
-  if (DR) {
-    const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, G);
-    const float ws[1] = {w * Pl.lR};
-    acc_add(cr, L, ws, 3 * NM, G, geo);
-  }
-}
-
 // A particle of a block without a box: its values straight to the global
 // accumulators at the global scales.
 template <bool DJ, bool DR>
@@ -925,13 +893,18 @@ __global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
   flush_box(geo, Pl.nvals);
 }
 
-// Staged run kernel of the moving species with three modes: the block's
-// particles are copied into shared memory (64 KB) ahead of its box, 2
-// resident blocks per SM with room for the registers (measured 500 against
-// 523 us for 12.5M electrons of the 4096 x 128 x 3-mode case, where the
-// unstaged kernel spills).
+// Run kernel of the moving species with three modes: the block's 2048
+// slots of the eight particle arrays are first copied into shared memory
+// (cp.async, 64 KB) ahead of its box, and two warps take each tile of the
+// block (256 threads), both pushing the tile's particles: the even warp sums
+// J_x and J_y, the odd warp J_z and rho, 40 node values per lane instead of
+// 80, so the sums fit 128 registers and an SM holds 16 warps of the pass
+// (2 blocks; one warp per tile with all 80 sums took 213 registers, 8 warps
+// per SM, and ran 2.12 against 1.73 ms for 50.3M electrons of the 4096 x
+// 512 x 3-mode case, bitwise the same sums).  Only the even warp stores the
+// new positions.
 template <int NM, bool PUSH, bool DR>
-__global__ void __launch_bounds__(kDepThreads, 2) push_deposit_staged_kernel(PushDepArgs A) {
+__global__ void __launch_bounds__(2 * kDepThreads, 2) push_deposit_pair_kernel(PushDepArgs A) {
   constexpr bool DJ = true;
   const SpGrid G = window_grid(A.G, A.win);
   extern __shared__ __align__(16) unsigned char dsm[];
@@ -942,19 +915,14 @@ __global__ void __launch_bounds__(kDepThreads, 2) push_deposit_staged_kernel(Pus
   const StageView V = stage_view(dsm);
   const BlockPlan Pl = plan_block<true>(A, G, base, bb, kSpBoxBytes, V);
   if (Pl.use_box)
-    for (int t = threadIdx.x; t < (int)Pl.nvals; t += kDepThreads) box[t] = 0;
+    for (int t = threadIdx.x; t < (int)Pl.nvals; t += blockDim.x) box[t] = 0;
   __syncthreads();
   const BoxGeo geo = make_geo(box, Pl, A);
-  const int lane = threadIdx.x & 31;
-  const int ltile = (threadIdx.x >> 5) * kTile;  // this warp's tile, local slots
-  const i64 first = base + ltile + (i64)lane * kRunLen;  // this lane's run, in particle order
-  CellAcc<NM, 3> cj;
-  CellAcc<NM, 1> cr;
-  cj.live = false;
-  cr.live = false;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool second = warp & 1;  // J_z and rho (else J_x, J_y)
+  const int ltile = (warp >> 1) * kTile;  // this warp pair's tile, local slots
+  const i64 first = base + ltile + (i64)lane * kRunLen;
   const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - first));
-  // lane r walks run r of its warp's tile (local slot ltile + 32 j + r: the
-  // warp's 32 lanes read 32 consecutive words, one bank each)
   auto load = [&](int j) {
     RunPart q;
     const int ls = ltile + j * kTileRuns + lane;
@@ -968,39 +936,63 @@ __global__ void __launch_bounds__(kDepThreads, 2) push_deposit_staged_kernel(Pus
     q.pz = V.pz[ls];
     return q;
   };
-  if (!Pl.use_box) {
-    // a block whose nodes do not fit a box: each particle straight to the
-    // global accumulators at the global scales
-    for (int j = 0; j < cnt; ++j) {
-      const RunPart q = load(j);
-      const Pushed u = push_vals(A, q.ix, q.fx, q.y, q.z, q.px, q.py, q.pz, q.w);
-      if (PUSH) {
-        const i64 p = base + ltile + j * kTileRuns + lane;
-        A.P.ix[p] = u.ixn;
-        A.P.fx[p] = u.fxn;
-        A.P.y[p] = u.yn;
-        A.P.z[p] = u.zn;
-      }
-      if (q.w == 0.0f) continue;
-      deposit_global<DJ, DR>(A, G, Pl, u, q.w);
-    }
-    return;
-  }
-  RunPart cur, nxt;
-  if (cnt > 0) cur = load(0);
-  for (int j = 0; j < cnt; ++j) {
-    if (j + 1 < cnt) nxt = load(j + 1);
-    const i64 p = base + ltile + j * kTileRuns + lane;
-    run_particle<NM, PUSH, DJ, DR>(A, G, Pl, geo, cur, cj, cr, [&](const Pushed &u) {
+  auto store = [&](int j, const Pushed &u) {
+    if (PUSH && !second) {
+      const i64 p = base + ltile + j * kTileRuns + lane;
       A.P.ix[p] = u.ixn;
       A.P.fx[p] = u.fxn;
       A.P.y[p] = u.yn;
       A.P.z[p] = u.zn;
-    });
-    cur = nxt;
+    }
+  };
+  if (!Pl.use_box) {
+    // a block whose nodes do not fit a box: the even warps push and deposit
+    // every component straight to the global accumulators
+    if (!second)
+      for (int j = 0; j < cnt; ++j) {
+        const RunPart q = load(j);
+        const Pushed u = push_vals(A, q.ix, q.fx, q.y, q.z, q.px, q.py, q.pz, q.w);
+        store(j, u);
+        if (q.w == 0.0f) continue;
+        deposit_global<DJ, DR>(A, G, Pl, u, q.w);
+      }
+    return;
   }
-  acc_flush(cj, 0, G, geo);
-  if (DR) acc_flush(cr, 3 * NM, G, geo);
+  if (!second) {
+    CellAcc<NM, 2> cxy;
+    cxy.live = false;
+    for (int j = 0; j < cnt; ++j) {
+      const RunPart q = load(j);
+      const Pushed u = push_vals(A, q.ix, q.fx, q.y, q.z, q.px, q.py, q.pz, q.w);
+      store(j, u);
+      if (q.w == 0.0f || !u.moving) continue;  // grid_deps.f90:42
+      const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, G);
+      const float vs[2] = {u.vj[0] * Pl.lJ, u.vj[1] * Pl.lJ};
+      acc_add(cxy, L, vs, 0, G, geo);
+    }
+    acc_flush(cxy, 0, G, geo);
+  } else {
+    CellAcc<NM, 1> cz, cr;
+    cz.live = false;
+    cr.live = false;
+    for (int j = 0; j < cnt; ++j) {
+      const RunPart q = load(j);
+      const Pushed u = push_vals(A, q.ix, q.fx, q.y, q.z, q.px, q.py, q.pz, q.w);
+      if (q.w == 0.0f) continue;
+      if (u.moving) {
+        const Loc L = locate(u.ixh, u.fxh, u.yh, u.zh, G);
+        const float vs[1] = {u.vj[2] * Pl.lJ};
+        acc_add(cz, L, vs, 2 * NM, G, geo);
+      }
+      if (DR) {
+        const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, G);
+        const float ws[1] = {q.w * Pl.lR};
+        acc_add(cr, L, ws, 3 * NM, G, geo);
+      }
+    }
+    acc_flush(cz, 2 * NM, G, geo);
+    if (DR) acc_flush(cr, 3 * NM, G, geo);
+  }
   __syncthreads();
   flush_box(geo, Pl.nvals);
 }
@@ -1750,10 +1742,10 @@ int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *p
     const int mode = (push ? 4 : 0) | (A.dep_j ? 2 : 0) | (A.dep_rho ? 1 : 0);
     if (mode == 7) kern = nm == 1 ? push_deposit_run_kernel<1, true, true, true>
                         : nm == 2 ? push_deposit_run_kernel<2, true, true, true>
-                                  : push_deposit_staged_kernel<3, true, true>;
+                                  : push_deposit_pair_kernel<3, true, true>;
     if (mode == 6) kern = nm == 1 ? push_deposit_run_kernel<1, true, true, false>
                         : nm == 2 ? push_deposit_run_kernel<2, true, true, false>
-                                  : push_deposit_staged_kernel<3, true, false>;
+                                  : push_deposit_pair_kernel<3, true, false>;
     if (mode == 1 && n < (i64)INT32_MAX - kDepBlock)
       kern = nm == 1 ? push_deposit_run_kernel<1, false, false, true>
            : nm == 2 ? push_deposit_run_kernel<2, false, false, true>
@@ -1769,7 +1761,10 @@ int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *p
               : (nm >= 3 ? kStageArrays * kDepBlock * 4 + kSpBoxBytes : kSpBoxBytes);
   }
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, box_bytes);
-  kern<<<blocks, kDepThreads, box_bytes, st>>>(A);
+  // (the three-mode moving species' kernel runs two warps per tile)
+  const int threads = (kern != push_deposit_kernel && A.dep_j && nm >= 3) ? 2 * kDepThreads
+                                                                          : kDepThreads;
+  kern<<<blocks, threads, box_bytes, st>>>(A);
   chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
