@@ -1316,6 +1316,7 @@ __global__ void __launch_bounds__(kDepThreads, NM >= 3 ? 3 : 4) gather_push_run_
   }
 }
 
+
 // ----------------------------------------------------------------------
 // Envelope (KxShift) solver: the beam's current deposit and its gather +
 // external undulator field + Boris push (grid_deps_env.f90:18-95, 164-238;
@@ -1761,9 +1762,11 @@ int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *p
               : (nm >= 3 ? kStageArrays * kDepBlock * 4 + kSpBoxBytes : kSpBoxBytes);
   }
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, box_bytes);
-  // (the three-mode moving species' kernel runs two warps per tile)
-  const int threads = (kern != push_deposit_kernel && A.dep_j && nm >= 3) ? 2 * kDepThreads
-                                                                          : kDepThreads;
+  // (the three-mode moving species' kernel runs two warps per tile, 2 blocks
+  // of 104 KB per SM)
+  const bool pair = kern != push_deposit_kernel && A.dep_j && nm >= 3;
+  if (pair) cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  const int threads = pair ? 2 * kDepThreads : kDepThreads;
   kern<<<blocks, threads, box_bytes, st>>>(A);
   chm::count_launch();
   CHM_CHECK_LAUNCH();
@@ -1785,7 +1788,9 @@ int gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, float *py
   cudaStream_t st = as_stream(stream);
   if (!generic && nm >= 1 && nm <= 3) {
     const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
-    // with three modes each block stages its 2048 slots of the eight particle arrays
+    // with three modes each block stages its 2048 slots of the eight particle
+    // arrays (a two-warps-per-tile form with the E and B halves in separate
+    // warps measured 1.14 against 1.01 ms at 4096 x 512 x 3 modes)
     const int sm = nm >= 3 ? kStageArrays * kDepBlock * 4 : 0;
     void (*kern)(GatherArgs) =
         nm == 1 ? gather_push_run_kernel<1> : nm == 2 ? gather_push_run_kernel<2> : gather_push_run_kernel<3>;
