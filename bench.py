@@ -793,6 +793,12 @@ def main():
                     help="timed split steps of the FEL leg (0: skip)")
     ap.add_argument("--fel-fp64-steps", type=int, default=3,
                     help="timed FP64 steps of the FEL leg")
+    ap.add_argument("--umma-cols", type=int, default=-1,
+                    help="tensor-core product column-tile width: -1 tuned per shape (default), "
+                         "0 the default width, > 0 forced (for profiler runs, whose serialised "
+                         "launches would mislead the tuner)")
+    ap.add_argument("--fel", action="store_true",
+                    help="run the FEL leg alone (its own JSON line; profiling case)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-errors", action="store_true")
@@ -807,6 +813,9 @@ def main():
                     help="cfg3 = the benchmark workload; cfg2, cfg1 the smaller configurations; "
                          "prof3, prof, spec, small = reduced cases for profiling")
     args = ap.parse_args()
+    if args.umma_cols != -1:
+        from chimera_gb300 import _lib
+        _lib.load().chm_sp_set_umma_cols(args.umma_cols)
     global WORKLOAD_SIZE
     WORKLOAD_SIZE = args.size
     if args.warmup < 3 and args.impl == "gb300":
@@ -817,6 +826,14 @@ def main():
         return run_batched(args)
     if args.spectral:
         return run_spectral(args)
+    if args.fel:
+        out = fel_leg(args)
+        print(json.dumps({"metric": METRIC, "value": out["split"]["value"], "unit": METRIC,
+                          "n_gpus": 1, "steps": args.fel_steps, "warmup": 3,
+                          "ms_per_step": out["split"]["ms_per_step"], "higher_is_better": True,
+                          "dtype": "f32 (bf16x3 split tensor-core GEMMs)", "data": "synthetic",
+                          "config": {"workload": out["workload"]}, "fel": out}), flush=True)
+        return 0
     return run_gb300(args)
 
 

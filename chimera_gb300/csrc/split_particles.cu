@@ -1393,13 +1393,31 @@ __global__ void __launch_bounds__(kDepThreads) push_deposit_env_kernel(PushDepAr
       }
     live = false;
   };
-  for (int j = 0; j < cnt; ++j) {
+  // the next particle is loaded before this one is processed (its stores
+  // could alias the loads otherwise)
+  auto load = [&](int j) {
+    RunPart q;
     const i64 p = tile + (i64)j * kTileRuns + lane;
-    const float w = A.P.w[p];
-    const Pushed u = A.far ? push_vals_far(A, A.P.ix[p], A.P.fx[p], A.P.y[p], A.P.z[p], A.P.px[p],
-                                           A.P.py[p], A.P.pz[p], w)
-                           : push_vals(A, A.P.ix[p], A.P.fx[p], A.P.y[p], A.P.z[p], A.P.px[p],
-                                       A.P.py[p], A.P.pz[p], w);
+    q.w = A.P.w[p];
+    q.ix = A.P.ix[p];
+    q.fx = A.P.fx[p];
+    q.y = A.P.y[p];
+    q.z = A.P.z[p];
+    q.px = A.P.px[p];
+    q.py = A.P.py[p];
+    q.pz = A.P.pz[p];
+    return q;
+  };
+  RunPart cur, nxt;
+  if (cnt > 0) cur = load(0);
+  for (int j = 0; j < cnt; ++j) {
+    if (j + 1 < cnt) nxt = load(j + 1);
+    const RunPart q = cur;
+    cur = nxt;
+    const i64 p = tile + (i64)j * kTileRuns + lane;
+    const float w = q.w;
+    const Pushed u = A.far ? push_vals_far(A, q.ix, q.fx, q.y, q.z, q.px, q.py, q.pz, w)
+                           : push_vals(A, q.ix, q.fx, q.y, q.z, q.px, q.py, q.pz, w);
     A.P.ix[p] = u.ixn;
     A.P.fx[p] = u.fxn;
     A.P.y[p] = u.yn;
@@ -1472,27 +1490,48 @@ __device__ __forceinline__ void undulator(float *F, int ix, float fx, float y, c
 // Gather of the envelope fields (carrier e^{+i kx0 x}, phase e^{+-i m theta}
 // at slot K +- m, 1 on the axis), the undulator field, Boris push
 template <int NM>
-__global__ void __launch_bounds__(256) gather_push_env_kernel(GatherArgs A, EnvArgs E, UndArgs U,
-                                                              i64 nphys) {
+__global__ void __launch_bounds__(kDepThreads) gather_push_env_kernel(GatherArgs A, EnvArgs E,
+                                                                     UndArgs U) {
   constexpr int K = (NM - 1) / 2;
   const SpGrid G = window_grid(A.G, A.win);
   const i64 plane = (i64)G.nx * G.nr;
-  for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < nphys;
-       p += (i64)gridDim.x * blockDim.x) {
-    if (logical_of(p) >= A.P.n) continue;
+  // lane r walks run r of its tile (the tile layout), the next particle
+  // loaded before this one is processed
+  const int lane = threadIdx.x & 31;
+  const i64 tile = (i64)blockIdx.x * kDepBlock + (i64)(threadIdx.x >> 5) * kTile;
+  const i64 first = tile + (i64)lane * kRunLen;
+  const int cnt = (int)max((i64)0, min((i64)kRunLen, A.P.n - first));
+  prefetch_tile(A.P, tile, lane, true);
+  auto load = [&](int j) {
+    RunPart q;
+    const i64 p = tile + (i64)j * kTileRuns + lane;
+    q.w = A.P.w[p];
+    q.ix = A.P.ix[p];
+    q.fx = A.P.fx[p];
+    q.y = A.P.y[p];
+    q.z = A.P.z[p];
+    q.px = A.P.px[p];
+    q.py = A.P.py[p];
+    q.pz = A.P.pz[p];
+    return q;
+  };
+  RunPart cur, nxt;
+  if (cnt > 0) cur = load(0);
+  for (int j = 0; j < cnt; ++j) {
+    if (j + 1 < cnt) nxt = load(j + 1);
+    const RunPart q = cur;
+    cur = nxt;
+    const i64 p = tile + (i64)j * kTileRuns + lane;
     float F[6] = {0, 0, 0, 0, 0, 0};
-    const float w = A.P.w[p];
-    const int ix = A.P.ix[p];
-    const float fx = A.P.fx[p], y = A.P.y[p], z = A.P.z[p];
-    if (w != 0.0f) {
-      const Loc L = locate(ix, fx, y, z, G);
+    if (q.w != 0.0f) {
+      const Loc L = locate(q.ix, q.fx, q.y, q.z, G);
       if (L.ok) {
         const float sx[2] = {1.0f - L.sx1, L.sx1};
         const float sr[2] = {1.0f - L.sr1, L.sr1};
         const bool okx0 = L.cx >= 0 && L.cx < G.nx, okx1 = L.cx + 1 >= 0 && L.cx + 1 < G.nx;
-        const float2 c0 = env_carrier(E, G, ix, fx);
+        const float2 c0 = env_carrier(E, G, q.ix, q.fx);
         const float2 car = make_float2(c0.x, -c0.y);  // e^{+i kx0 x}
-        const bool axis = !(y * y + z * z > 0.0f);
+        const bool axis = !(q.y * q.y + q.z * q.z > 0.0f);
         const float2 ph = axis ? make_float2(1.0f, 0.0f) : make_float2(L.phr, L.phi);
         float2 phm = make_float2(1.0f, 0.0f);
 #pragma unroll
@@ -1523,8 +1562,8 @@ __global__ void __launch_bounds__(256) gather_push_env_kernel(GatherArgs A, EnvA
         }
       }
     }
-    if (U.kind) undulator(F, ix, fx, y, U);
-    float px = A.P.px[p], py = A.P.py[p], pz = A.P.pz[p];
+    if (U.kind) undulator(F, q.ix, q.fx, q.y, U);
+    float px = q.px, py = q.py, pz = q.pz;
     boris(px, py, pz, F, 0.5f * A.dtq);
     A.P.px[p] = px;
     A.P.py[p] = py;
@@ -1929,12 +1968,11 @@ int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z, float *px
     U.xo = X0 - und[2];
     U.dx = dx;
   }
-  const i64 nphys = tiles_of(n) * kTile;
+  const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
   cudaStream_t st = as_stream(stream);
-  const unsigned g = grid_for(nphys, 256, 16);
-  if (nm == 1) gather_push_env_kernel<1><<<g, 256, 0, st>>>(A, E, U, nphys);
-  else if (nm == 3) gather_push_env_kernel<3><<<g, 256, 0, st>>>(A, E, U, nphys);
-  else gather_push_env_kernel<5><<<g, 256, 0, st>>>(A, E, U, nphys);
+  if (nm == 1) gather_push_env_kernel<1><<<blocks, kDepThreads, 0, st>>>(A, E, U);
+  else if (nm == 3) gather_push_env_kernel<3><<<blocks, kDepThreads, 0, st>>>(A, E, U);
+  else gather_push_env_kernel<5><<<blocks, kDepThreads, 0, st>>>(A, E, U);
   chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;
