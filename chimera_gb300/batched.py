@@ -73,7 +73,7 @@ class BatchedRun:
                 if not r._scales_valid:
                     r._refresh_scales()
             cur.wait_stream(s)
-        key = tuple(r._layout_key() for r in self.runs)
+        key = tuple(r._layout_key(istep) for r in self.runs)
         graphs = getattr(self, "_graphs", None)
         layout = tuple(k[:-1] for k in key)
         if graphs is None or graphs[0] != layout:

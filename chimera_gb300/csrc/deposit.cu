@@ -342,7 +342,7 @@ int deposit_common(int kind, const double *coord, i64 x_cs, i64 x_ps, const doub
     wsum_partial_kernel<<<kRedBlocks, kDepThreads, 0, st>>>(wghts, w_ps, np, kind == DENS_ENV,
                                                             partial); chm::count_launch();
     wsum_final_kernel<<<1, 256, 0, st>>>(partial, kRedBlocks, scale); chm::count_launch();
-    DepArgs A;
+    DepArgs A{};
     A.x = coord;
     A.x_cs = x_cs;
     A.x_ps = x_ps;

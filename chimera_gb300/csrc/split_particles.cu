@@ -204,6 +204,13 @@ struct PushDepArgs {
   // half step; far: D >= 2
   int far, d_int, dh_int;
   float d_frac, dh_frac, d_cells;
+  // (still species' background pass) nodes x < gx_min are not written; a
+  // block records the x range of its live particles' cells (absolute cell
+  // indices) into ext_out, or skips itself when ext_in shows that its
+  // nodes cannot reach x >= gx_min
+  int gx_min;
+  int2 *ext_out;
+  const int2 *ext_in;
 };
 
 // Block box: 32-bit fixed-point values at the block's own scales 2^elJ,
@@ -221,6 +228,7 @@ struct BoxGeo {
   int elJ, elR, eJ, eR;          // local (J, rho) and global quantum exponents
   unsigned long long *gJ, *gR;   // global accumulators
   int nx, nr, nm;                // grid
+  int gx_min;                    // first grid column written (0: all)
 };
 
 // value at the local quantum 2^-el -> global quantum 2^-eg: an exact left
@@ -278,7 +286,7 @@ __device__ void flush_box(const BoxGeo &B, long long nvals) {
     const unsigned cp = div_small(t, mp), rem = t - cp * plane_n;
     const unsigned rr = div_small(rem, mx), xx = rem - rr * bnx;
     const int gx = B.bx0 + (int)xx;
-    if (gx < 0 || gx >= B.nx) continue;  // the nodes beyond the grid's ends
+    if (gx < B.gx_min || gx >= B.nx) continue;  // the nodes beyond the grid's ends
     const unsigned cb = div_small(cp, mP);
     const int part = (int)(cp - cb * P), c = (int)cb + B.c0;
     const int m = (part + 1) >> 1, im = (part > 0 && (part & 1) == 0) ? 1 : 0;
@@ -500,6 +508,12 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, const SpGrid &G, i64 base,
     wsm[1][threadIdx.x >> 5] = jsum;
   }
   __syncthreads();
+  if (A.ext_out && threadIdx.x == 0) {
+    // the block's live cells, absolute (x0 = xlo - win_k - 1 - D, x1 = xhi - win_k + 1 + D)
+    const int D = A.push ? (int)ceilf(A.dt * A.dx_inv) : 0;
+    A.ext_out[blockIdx.x] = bb[0] <= bb[1] ? make_int2(bb[0] + G.win_k + 1 + D, bb[1] + G.win_k - 1 - D)
+                                           : make_int2(INT_MAX, INT_MIN);
+  }
   BlockPlan P;
   float Bl = 0.0f, Bj = 0.0f;
   for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {  // fixed order
@@ -536,7 +550,7 @@ __device__ BlockPlan plan_block(const PushDepArgs &A, const SpGrid &G, i64 base,
 
 __device__ __forceinline__ BoxGeo make_geo(int *box, const BlockPlan &P, const PushDepArgs &A) {
   return BoxGeo{box, P.bx0, P.br0, P.bnx, P.bnr, P.c0, P.elJ, P.elR, P.eJ, P.eR, A.accJ, A.accR,
-                A.G.nx, A.G.nr, A.G.nm};
+                A.G.nx, A.G.nr, A.G.nm, A.gx_min};
 }
 
 // Generic push + deposit (any nm): one particle per thread and slot, each
@@ -749,6 +763,12 @@ __global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
     A.G.win_k = A.win->k;
     A.G.win_f = A.win->f;
   }
+  if (A.ext_in) {
+    // a block whose cells' nodes (at most one cell right of its live
+    // particles' cells) stay left of gx_min has nothing to write
+    const int2 e = A.ext_in[blockIdx.x];
+    if (e.x > e.y || e.y - A.G.win_k + 1 < A.gx_min) return;
+  }
   extern __shared__ __align__(16) int box[];
   __shared__ int bb[4];
   // slot indices: 32-bit in the rho-only kernel (measured faster there; the
@@ -809,6 +829,7 @@ __global__ void __launch_bounds__(kDepThreads, DJ ? 4 : kRhoMinBlocks)
         const Loc L = locate(u.ixn, u.fxn, u.yn, u.zn, A.G);
         const float ws[1] = {w * Pl.sR};
         deposit_at(L, ws, 1, 0, A.G, [&](int plane, int r, int x, float re, float im) {
+          if (x < A.gx_min) return;
           const i64 e = ((i64)plane * A.G.nr + r) * A.G.nx + x;
           const long long qr = f2ll(re), qi = f2ll(im);
           if (qr) atomicAdd(&A.accR[2 * e], (unsigned long long)qr);
@@ -1331,6 +1352,25 @@ struct EnvArgs {
   float kdx;          // kx0 dx
 };
 
+// Background density of a still species after a window move by a whole
+// number of cells ns: every node value moves ns columns left (the
+// particles' positions relative to the grid shift by exactly ns cells, so
+// their cells, weights, block plans and run sums are those of the previous
+// deposit), the ns columns entering at the right are left zero for the
+// masked deposit.  One block per row of the (nx, rows) {re, im} int64 grid.
+constexpr int kShiftThreads = 1024;
+constexpr int kShiftMaxNx = 14000;  // a row of 16-byte values in shared memory
+
+__global__ void __launch_bounds__(kShiftThreads) shift_acc_kernel(longlong2 *acc, int nx, int ns) {
+  extern __shared__ __align__(16) longlong2 srow[];
+  longlong2 *row = acc + (i64)blockIdx.x * nx;
+  for (int x = threadIdx.x; x < nx; x += kShiftThreads) srow[x] = row[x];
+  __syncthreads();  // the whole row read before any write
+  for (int x = threadIdx.x; x < nx; x += kShiftThreads)
+    row[x] = x + ns < nx ? srow[x + ns] : make_longlong2(0, 0);
+}
+
+
 __global__ void carrier_kernel(float2 *tab, int ntab, double kx0, double X0, double dx, int win_k,
                                const chm_sp_window *win) {
   const int k = win ? win->k : win_k;
@@ -1760,7 +1800,7 @@ int push_deposit(int32_t *ix, float *fx, float *y, float *z, float *px, float *p
   CHM_REQUIRE(ix && fx && y && z && px && py && pz && w, "sp_push_deposit: null particle array");
   CHM_REQUIRE(!accJ || scaleJ, "sp_push_deposit: J accumulator without scale");
   CHM_REQUIRE(!accR || scaleR, "sp_push_deposit: rho accumulator without scale");
-  PushDepArgs A;
+  PushDepArgs A{};
   A.P = SpParts{ix, fx, y, z, px, py, pz, w, n};
   A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
   A.dt = dt;
@@ -1818,7 +1858,7 @@ int gather_push(int32_t *ix, float *fx, float *y, float *z, float *px, float *py
   CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && nm >= 1, "sp_gather_push: bad dims");
   if (n == 0) return CHM_OK;
   CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && eb_c64, "sp_gather_push: null pointer");
-  GatherArgs A;
+  GatherArgs A{};
   A.P = SpParts{ix, fx, y, z, px, py, pz, w, n};
   A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
   A.eb = reinterpret_cast<const float2 *>(eb_c64);
@@ -1894,6 +1934,52 @@ int chm_sp_carrier(void *tab_c64, int64_t ntab, double kx0, double X0, double dx
   CHM_REQUIRE(tab_c64 && ntab > 0 && ntab < (1 << 30), "sp_carrier: bad args");
   carrier_kernel<<<grid_for(ntab, 128), 128, 0, as_stream(stream)>>>(
       reinterpret_cast<float2 *>(tab_c64), (int)ntab, kx0, X0, dx, win_k, win);
+  chm::count_launch();
+  CHM_CHECK_LAUNCH();
+  return CHM_OK;
+}
+
+int chm_sp_deposit_background(int32_t *ix, float *fx, float *y, float *z, float *px, float *py,
+                              float *pz, float *w, int64_t n, int win_k, float win_f, float dr_inv,
+                              int nx, int nr, int nm, uint64_t *accR, const double *scaleR,
+                              void *ext_int2, int64_t ext_len, int shift_cells, void *stream,
+                              const chm_sp_window *win) {
+  CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && nm >= 1 && nm <= 3 && n < (i64)INT32_MAX - kDepBlock,
+              "sp_deposit_background: bad dims (nm 1..3, n < 2^31)");
+  CHM_REQUIRE(shift_cells >= 0 && shift_cells < nx && nx <= kShiftMaxNx,
+              "sp_deposit_background: bad shift");
+  CHM_REQUIRE(accR && scaleR && ext_int2, "sp_deposit_background: null pointer");
+  const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
+  CHM_REQUIRE(ext_len >= (i64)blocks, "sp_deposit_background: block extent table too short");
+  cudaStream_t st = as_stream(stream);
+  if (shift_cells > 0) {
+    const int sm = nx * (int)sizeof(longlong2);
+    cudaFuncSetAttribute(shift_acc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    shift_acc_kernel<<<(unsigned)((i64)nr * nm), kShiftThreads, sm, st>>>(
+        reinterpret_cast<longlong2 *>(accR), nx, shift_cells);
+    chm::count_launch();
+  }
+  if (n == 0) return CHM_OK;
+  CHM_REQUIRE(ix && fx && y && z && px && py && pz && w, "sp_deposit_background: null particle array");
+  PushDepArgs A{};
+  A.P = SpParts{ix, fx, y, z, px, py, pz, w, n};
+  A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
+  A.dep_rho = 1;
+  A.accR = reinterpret_cast<unsigned long long *>(accR);
+  A.scaleR = scaleR;
+  A.win = win;
+  int2 *ext = reinterpret_cast<int2 *>(ext_int2);
+  if (shift_cells > 0) {
+    A.gx_min = nx - shift_cells;
+    A.ext_in = ext;
+  } else {
+    A.ext_out = ext;
+  }
+  void (*kern)(PushDepArgs) = nm == 1 ? push_deposit_run_kernel<1, false, false, true>
+                            : nm == 2 ? push_deposit_run_kernel<2, false, false, true>
+                                      : push_deposit_run_kernel<3, false, false, true>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kRhoBoxBytes);
+  kern<<<blocks, kDepThreads, kRhoBoxBytes, st>>>(A);
   chm::count_launch();
   CHM_CHECK_LAUNCH();
   return CHM_OK;

@@ -104,13 +104,20 @@ __global__ void window_kernel(chm_sp_window *w, int set, double leftX, double X0
     w->leftX = leftX;
     w->X0 = X0;
     w->dx = dx;
+    const double sv = (leftX - X0) / dx;
+    const double k = floor(sv);
+    w->k = (int32_t)k;
+    w->fd = sv - k;
   } else {
+    // the cell position advances by shift / dx from the previous one (a
+    // whole-cell move leaves the fraction exactly as it was)
     w->leftX = w->leftX + shift;
+    const double s = w->fd + shift / w->dx;
+    const double fl = floor(s);
+    w->k = w->k + (int32_t)fl;
+    w->fd = s - fl;
   }
-  const double sv = (w->leftX - w->X0) / w->dx;
-  const double k = floor(sv);
-  w->k = (int32_t)k;
-  w->f = (float)(sv - k);
+  w->f = (float)w->fd;
 }
 
 __device__ __forceinline__ float2 tw32(const float2 *tw, int t, int sign) {

@@ -313,9 +313,8 @@ class SplitRun:
         # the window origin on the device (chm_sp_window: leftX, X0, dx, k, f),
         # advanced on the stream at every window move, so the step's kernels
         # read the current origin also when the step replays as a CUDA graph
-        self.win = torch.zeros(32, dtype=torch.uint8, device=S.device)
-        _lib.call("chm_sp_window_set", self.win.data_ptr(), float(A["leftX"]), self.X0,
-                  float(A["dx"]), _stream())
+        self.win = torch.zeros(64, dtype=torch.uint8, device=S.device)
+        self._win_set(float(A["leftX"]))
         # operators (FP64 host build -> FP32 copy + split BF16)
         self._keep = []
         self.ops = {}
@@ -388,6 +387,9 @@ class SplitRun:
         # the background density is deposited on window moves
         # (chimera_main.py:277-284); it starts empty, as the reference's
         self.have_bg = False
+        self._bg_key = None  # still particles' layout at the last full background deposit
+        self._bg_ext = None  # per-block cell ranges of that deposit (device int2)
+        self.bg_shift = True  # move the background with whole-cell window moves
         self._inject_order = {}  # particle order of injected batches, per shape
         # the device error flags (a tensor-core CTA that gave up on a wait, a
         # deposit cell outside its block box) are read every this many steps
@@ -413,10 +415,35 @@ class SplitRun:
                 if "Still" in spc.Args["Features"]]
 
     def _win(self):
-        """Window origin leftX = X0 + (k + f) dx, in FP64 on the host."""
-        s = (float(self.solver.Args["leftX"]) - self.X0) / self.dx
-        k = int(np.floor(s))
-        return k, float(s - k)
+        """Window origin in cells from X0, k + f: the host mirror of the
+        device record (chm_sp_window), f rounded to FP32 as the kernels read it."""
+        return self._wk, float(np.float32(self._wfd))
+
+    def _win_set(self, leftX):
+        _lib.call("chm_sp_window_set", self.win.data_ptr(), float(leftX), self.X0, float(self.dx),
+                  _stream())
+        sv = (float(leftX) - self.X0) / float(self.dx)
+        k = np.floor(sv)
+        self._wk, self._wfd = int(k), float(sv - k)
+
+    def _win_restore(self, k, fd):
+        """Device record and host mirror with the cell position (k, fd)."""
+        import struct
+        raw = struct.pack("<ddddif", float(self.solver.Args["leftX"]), self.X0, float(self.dx),
+                          fd, k, float(np.float32(fd)))
+        buf = torch.frombuffer(bytearray(raw.ljust(self.win.numel(), b"\0")), dtype=torch.uint8)
+        self.win.copy_(buf.to(self.device))
+        self._wk, self._wfd = int(k), float(fd)
+
+    def _win_after(self, shift):
+        """(k, fd) after a move by shift, as chm_sp_window_advance computes them."""
+        s = self._wfd + float(shift) / float(self.dx)
+        fl = np.floor(s)
+        return self._wk + int(fl), float(s - fl)
+
+    def _win_advance(self, shift):
+        _lib.call("chm_sp_window_advance", self.win.data_ptr(), float(shift), _stream())
+        self._wk, self._wfd = self._win_after(shift)
 
     def _refresh_scales(self):
         """Global deposit scales from sum |w| (recomputed when particles change)."""
@@ -463,13 +490,66 @@ class SplitRun:
                   accR.data_ptr() if accR is not None else None,
                   scaleR.data_ptr() if scaleR is not None else None, _stream(), self.win.data_ptr())
 
-    def _deposit_background(self):
+    def _bg_shift(self, wind):
+        """Whole cells by which the background density can move with the
+        window at this move instead of a full deposit
+        (chm_sp_deposit_background): one still species whose particles are
+        unchanged since the last full deposit, no absorption or injection,
+        and a move of exactly n >= 1 cells that leaves the window's FP32
+        fraction as it was (the device window record advances the same
+        way); 0 for a full deposit.  Call before the move."""
+        still = self._still()
+        if (len(still) != 1 or self.nm > 3 or not self.have_bg or "AbsorbLayer" in wind
+                or "AddPlasma" in wind):
+            return 0
+        P = still[0][1]
+        if self._bg_key != (P.n, P.cap, *P.ptrs()):
+            return 0
+
+        k1, fd1 = self._win_after(wind["shiftX"])
+        n = k1 - self._wk
+        return n if (1 <= n < self.nx and np.float32(fd1) == np.float32(self._wfd)) else 0
+
+    def _bg_plan(self, istep):
+        """The background mode of step istep's window moves (for the graph key)."""
+        if not (self.space_charge and "BckGrndRho" in self.solver.Data):
+            return 0
+        fp = self.fp
+        out = 0
+        for wind in fp.MovingFrames:
+            if istep < wind["TimeActive"][0] or istep > wind["TimeActive"][1]:
+                continue
+            if np.mod(istep - wind["TimeActive"][0], wind["Steps"]) != 0:
+                continue
+            out = self._bg_shift(wind)
+        return out
+
+    def _deposit_background(self, shift_cells=0):
         if not self._scales_valid:
             self._refresh_scales()
-        self.accBG.zero_()
-        for spc, P in self._still():
-            self._deposit(P, False, None, self.accBG, None, self.scaleBG)
-        self.have_bg = bool(self._still())
+        still = self._still()
+        if len(still) != 1 or self.nm > 3 or still[0][1].n >= 2 ** 31 - 4096:
+            self.accBG.zero_()
+            for spc, P in still:
+                self._deposit(P, False, None, self.accBG, None, self.scaleBG)
+            self._bg_key = None
+        else:
+            # the run kernels' background pass: a full deposit that records each
+            # block's cell range, or (shift_cells > 0) the grid moved with the
+            # window and only the entering columns deposited
+            P = still[0][1]
+            if not shift_cells:
+                self.accBG.zero_()
+            nb = (P.cap + 2047) // 2048
+            if self._bg_ext is None or self._bg_ext.numel() < 2 * nb:
+                self._bg_ext = torch.empty(2 * nb, dtype=torch.int32, device=self.device)
+            k, f = self._win()
+            _lib.call("chm_sp_deposit_background", *P.ptrs(), P.n, k, f,
+                      float(self.solver.Args["dr_inv"]), self.nx, self.nr, self.nm,
+                      self.accBG.data_ptr(), self.scaleBG.data_ptr(), self._bg_ext.data_ptr(),
+                      self._bg_ext.numel() // 2, int(shift_cells), _stream(), self.win.data_ptr())
+            self._bg_key = (P.n, P.cap, *P.ptrs())
+        self.have_bg = bool(still)
 
     def _fb_in(self, out, acc, scale, acc2, scale2, ncomp):
         A = self.solver.Args
@@ -498,11 +578,13 @@ class SplitRun:
                 return False
         return self.sort_every != "auto"
 
-    def _layout_key(self):
-        # the particle arrays and counts, and which charge-gradient buffer
-        # holds the previous step's gradient (the step swaps the two)
+    def _layout_key(self, istep):
+        # the particle arrays and counts; which charge-gradient buffer holds
+        # the previous step's gradient (the step swaps the two) and whether
+        # the step's background deposit is full or a shift
         gp = self.gprv.data_ptr() if self.space_charge else 0
-        return tuple((P.n, P.cap, *P.ptrs()) for P in self.parts) + (gp,)
+        bg = self._bg_plan(istep) if self.bg_shift else 0
+        return tuple((P.n, P.cap, *P.ptrs()) for P in self.parts) + ((gp, bg),)
 
     def graph_step(self, istep):
         """make_step(istep) with the step's kernels replayed from a CUDA graph.
@@ -524,7 +606,7 @@ class SplitRun:
         self._maybe_sort(istep)
         if not self._scales_valid:
             self._refresh_scales()
-        key = self._layout_key()
+        key = self._layout_key(istep)
         graphs = getattr(self, "_graphs", None)
         if graphs is None or graphs[0] != key[:-1]:
             graphs = self._graphs = [key[:-1], {}]  # per gradient-buffer assignment
@@ -556,9 +638,12 @@ class SplitRun:
                 continue
             if np.mod(istep - wind["TimeActive"][0], wind["Steps"]) != 0:
                 continue
+            # (the device record advances inside the graph; the host mirror here)
             fp.move_frame(wind)
+            self._wk, self._wfd = self._win_after(wind["shiftX"])
             if "Staged" in wind["Features"]:
                 fp.move_frame(wind)
+                self._wk, self._wfd = self._win_after(wind["shiftX"])
 
     def _after_step(self):
         self._steps += 1
@@ -589,14 +674,15 @@ class SplitRun:
                 _lib.call("chm_sp_fb_filtr", self.EG.data_ptr(), float(A["leftX"]),
                           self.kx64.data_ptr(), prof.data_ptr(), prof.numel(), 0, self.nx,
                           self.nkr, self.nm, 6, ws, wsb, st, self.win.data_ptr())
+            bg_shift = self._bg_shift(wind) if self.bg_shift else 0
             fp.move_frame(wind)
-            _lib.call("chm_sp_window_advance", self.win.data_ptr(), float(wind["shiftX"]), st)
+            self._win_advance(wind["shiftX"])
             if "AddPlasma" in wind:
                 self._add_plasma(wind)
             if "AbsorbLayer" in wind:
                 self._absorb(wind)
             if self.space_charge and "BckGrndRho" in self.solver.Data:
-                self._deposit_background()
+                self._deposit_background(bg_shift)
             # the reference's dep_dens here (postframe_corr) is overwritten by
             # project_density before any use; it is not repeated
         if not self._scales_valid:
@@ -628,7 +714,7 @@ class SplitRun:
                 continue
             if "Staged" in wind["Features"]:
                 fp.move_frame(wind)
-                _lib.call("chm_sp_window_advance", self.win.data_ptr(), float(wind["shiftX"]), st)
+                self._win_advance(wind["shiftX"])
         # density
         if self.space_charge:
             if not fuse_rho:
@@ -846,6 +932,7 @@ class SplitRun:
         arrays["split/have_bg"] = np.asarray(self.have_bg)
         arrays["split/since_sort"] = np.asarray(self._since_sort)
         arrays["split/accBG"] = self.accBG.cpu().numpy()
+        arrays["split/win"] = np.array([self._wk, self._wfd], dtype=np.float64)
         return snapshot.write(snapshot.snap_name(fname), arrays)
 
     def read_snap(self, fname="./test.npz", verbose=False):
@@ -857,8 +944,11 @@ class SplitRun:
         with np.load(fname, allow_pickle=False) as f:
             snapshot.read_into(f, self.fp.Solvers, self.fp.Particles, verbose)
             D = self.solver.Data
-            _lib.call("chm_sp_window_set", self.win.data_ptr(), float(self.solver.Args["leftX"]),
-                      self.X0, float(self.dx), _stream())
+            self._win_set(float(self.solver.Args["leftX"]))
+            if "split/win" in f.files:
+                # the window's cell position as the writing run carried it
+                k, fd = f["split/win"]
+                self._win_restore(int(k), float(fd))
             self.EG.copy_(D["EG_fb"])
             if self.space_charge:
                 self.gprv.copy_(D["gradRho_fb_prv"])

@@ -419,15 +419,17 @@ int64_t chm_sp_capacity(int64_t n);
 int64_t chm_sp_slot(int64_t i);
 
 /* The moving window's origin in device memory, for the split-form entry
- * points below that take `win`: leftX = X0 + (k + f) dx with k = floor((leftX
- * - X0) / dx) and f = (leftX - X0) / dx - k, evaluated in FP64 on the device.
- * chm_sp_window_set writes it, chm_sp_window_advance adds a shift to leftX
- * (leftX + shift in FP64, as the window moves: chimera_main.py:286-290) and
- * re-evaluates k and f, so a step captured in a CUDA graph replays with the
- * current origin.  With win == NULL the entry points use their scalar
- * arguments (win_k, win_f, leftX). */
+ * points below that take `win`: the grid's left edge leftX (FP64, for the
+ * transforms' shift phases) and its position in cells from the particles'
+ * origin X0, k + fd (k whole cells, fd in [0, 1) in FP64, f = fd in FP32).
+ * chm_sp_window_set writes it from leftX (k = floor((leftX - X0) / dx));
+ * chm_sp_window_advance adds a shift (leftX + shift, as the window moves:
+ * chimera_main.py:286-290, and fd + shift / dx carried into k), so a move by
+ * a whole number of cells keeps f exact and a step captured in a CUDA graph
+ * replays with the current origin.  With win == NULL the entry points use
+ * their scalar arguments (win_k, win_f, leftX). */
 typedef struct {
-  double leftX, X0, dx;
+  double leftX, X0, dx, fd;
   int32_t k;
   float f;
 } chm_sp_window;
@@ -480,6 +482,23 @@ int chm_sp_gather_push_generic(int32_t *ix, float *fx, float *y, float *z,
                                const void *eb_c64, int nx, int nr, int nm,
                                float dtq, void *stream,
                         const chm_sp_window *win);
+
+/* Background density of a still species (the deposit of dep_bg,
+ * chimera_main.py:220-248, with the run kernels, nm <= 3, n < 2^31) into
+ * accR (nx,nr,nm) int64 {re, im} at the scale scaleR.  shift_cells = 0:
+ * the full deposit (accR zeroed by the caller), recording each block's
+ * cell range into ext (int2, at least ceil(n / 2048) entries).
+ * shift_cells = ns > 0, after a window move by exactly ns cells with the
+ * particles unchanged since the full deposit: the grid moves ns columns
+ * left and only the blocks whose cells reach the ns entering columns
+ * deposit there; bitwise the full deposit at the new window. */
+int chm_sp_deposit_background(int32_t *ix, float *fx, float *y, float *z,
+                              float *px, float *py, float *pz, float *w,
+                              int64_t n, int win_k, float win_f, float dr_inv,
+                              int nx, int nr, int nm, uint64_t *accR,
+                              const double *scaleR, void *ext_int2,
+                              int64_t ext_len, int shift_cells, void *stream,
+                              const chm_sp_window *win);
 
 /* Envelope (KxShift) solver, nm = 2K + 1 stored modes -K..K (K <= 2).
  * chm_sp_carrier fills tab (ntab >= nx + 4 complex64) with the carrier

@@ -592,3 +592,28 @@ def test_device_plasma_generation_matches_host(mods, spreads, with_profile):
     assert np.abs(dc[1:] - hc[1:]).max() <= 1e-14 * np.abs(hc[1:]).max()
     assert np.array_equal(dw, hw)
     assert np.array_equal(dp, hp)
+
+
+def test_background_moves_with_whole_cell_windows(mods):
+    """With a window moving one cell per step (dt = dx at c) the still
+    ions' background density is moved with the window and only the entering
+    column deposited (chm_sp_deposit_background shift mode): bitwise the full
+    re-deposit of every move, through re-sorts (a full deposit after each)
+    and graph replay."""
+    torch, _lib, fm, split = mods
+    from chimera_gb300 import workloads
+    runs = [split.SplitRun(workloads.components("cfg1", "none", seed=1001)) for _ in range(2)]
+    runs[1].bg_shift = False
+    for r in runs:
+        r.sort_every = 5
+    shifted = 0
+    for i in range(1, 13):
+        runs[0].graph_step(i)
+        runs[1].graph_step(i)
+        torch.cuda.synchronize()
+        shifted += runs[0]._bg_plan(i + 1) > 0
+        assert torch.equal(runs[0].accBG, runs[1].accBG), i
+    assert shifted >= 6
+    assert torch.equal(runs[0].EG, runs[1].EG) and torch.equal(runs[0].EB, runs[1].EB)
+    for r in runs:
+        r.check_status()
