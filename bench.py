@@ -198,8 +198,15 @@ def stage_roofline(form, prof, nprof, n_e, n_i, peaks, peak_kind):
                              "ms_per_step": t * 1e3})
             continue
         nb = None
+        bg_apart = "chm_sp_deposit_background" in prof  # (the still species' own pass)
         if name == "chm_sp_push_deposit":
-            nb = n_e * SPLIT_BYTES["push_electrons"] + n_i * SPLIT_BYTES["deposit_still"]
+            nb = n_e * SPLIT_BYTES["push_electrons"] + \
+                (0 if bg_apart else n_i * SPLIT_BYTES["deposit_still"])
+        elif name == "chm_sp_deposit_background":
+            # a whole-cell window move: the int64 {re, im} grid read and
+            # written once (the entering column's few ions aside)
+            W = workloads.SIZES[WORKLOAD_SIZE]
+            nb = 2 * 16 * W.nx * (W.nkr + 1) * W.modes
         elif name == "chm_sp_gather_push":
             nb = n_e * SPLIT_BYTES["gather_push"]
         elif name in ("chm_push_velocs", "chm_push_coords", "chm_proj_fld"):
@@ -219,7 +226,8 @@ def stage_roofline(form, prof, nprof, n_e, n_i, peaks, peak_kind):
     top["traffic"] = None
     tr = SPLIT_TRAFFIC.get(workloads.SIZES[WORKLOAD_SIZE].modes)
     if form == "split" and top.get("kernel") == "chm_sp_push_deposit" and tr:
-        top["traffic"] = n_e * tr["push_electrons"] + n_i * tr["deposit_still"]
+        top["traffic"] = n_e * tr["push_electrons"] + \
+            (0 if "chm_sp_deposit_background" in prof else n_i * tr["deposit_still"])
         top["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
                                  "quarter-radius case, scaled by particle count")
     top["peak_source"] = f"MEASURED_PEAKS.json ({peak_kind})" if top.get("bound") != "fp64" else \
