@@ -389,6 +389,9 @@ class SplitRun:
         self.have_bg = False
         self._bg_key = None  # still particles' layout at the last full background deposit
         self._bg_ext = None  # per-block cell ranges of that deposit (device int2)
+        for spc, P in self._still():  # (allocated here, outside any graph capture)
+            self._bg_ext = torch.empty(2 * ((P.cap + 2047) // 2048), dtype=torch.int32,
+                                       device=dev)
         self.bg_shift = True  # move the background with whole-cell window moves
         self._inject_order = {}  # particle order of injected batches, per shape
         # the device error flags (a tensor-core CTA that gave up on a wait, a
