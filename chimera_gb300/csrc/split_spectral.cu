@@ -420,7 +420,7 @@ struct Lines32 {
 // per-block twiddle table; 2: power of two >= 512, register radix-16 passes
 // in place (one buffer, blockDim = n / 16, twiddles from the global table)
 template <int MODE>
-__global__ void __launch_bounds__(MODE == 2 ? 256 : 512, MODE == 2 ? 3 : 1)
+__global__ void __launch_bounds__(MODE == 2 ? 256 : 512, MODE == 2 ? 4 : 1)
     lines32_kernel(Plan P, const float2 *__restrict__ tw, Lines32 L) {
   extern __shared__ __align__(16) float2 sm32[];
   constexpr bool POW2 = MODE == 1;
