@@ -232,6 +232,11 @@ def stage_roofline(form, prof, nprof, n_e, n_i, peaks, peak_kind):
                                  "quarter-radius case, scaled by particle count")
     top["peak_source"] = f"MEASURED_PEAKS.json ({peak_kind})" if top.get("bound") != "fp64" else \
         "FP64 FMA probe on this pool (1.20 TFLOP/s)"
+    if top.get("bound") == "tensor":
+        top["note"] = ("achieved counts the algorithmic 2 M N K flops of the FP32-accurate "
+                       "products; the split-BF16 form executes 6 times that on the tensor "
+                       "cores (executed_frac), and the stage includes its FP32 combines and "
+                       "splits; the particle kernels' rows are in stages")
     top["stages"] = rows
     return top
 
