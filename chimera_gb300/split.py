@@ -215,6 +215,23 @@ def _stream():
     return torch.cuda.current_stream().cuda_stream
 
 
+def window_cells(leftX, X0, dx):
+    """The window's position in cells from X0, (k, fd): k = floor((leftX -
+    X0) / dx) and the FP64 fraction fd, as chm_sp_window_set computes them."""
+    sv = (float(leftX) - float(X0)) / float(dx)
+    k = np.floor(sv)
+    return int(k), float(sv - k)
+
+
+def window_cells_after(k, fd, shift, dx):
+    """(k, fd) after a window move by shift, as chm_sp_window_advance computes
+    them: fd + shift / dx in FP64, its whole part carried into k (a move by a
+    whole number of cells leaves fd exactly as it was)."""
+    s = float(fd) + float(shift) / float(dx)
+    fl = np.floor(s)
+    return int(k) + int(fl), float(s - fl)
+
+
 # device functions of fimera the split form fuses into its gather + push
 # (chm_sp_gather_push_env und_kind)
 _UNDULATORS = {"undul_analytic": 1, "undul_analytic_taper": 2}
@@ -425,9 +442,7 @@ class SplitRun:
     def _win_set(self, leftX):
         _lib.call("chm_sp_window_set", self.win.data_ptr(), float(leftX), self.X0, float(self.dx),
                   _stream())
-        sv = (float(leftX) - self.X0) / float(self.dx)
-        k = np.floor(sv)
-        self._wk, self._wfd = int(k), float(sv - k)
+        self._wk, self._wfd = window_cells(leftX, self.X0, self.dx)
 
     def _win_restore(self, k, fd):
         """Device record and host mirror with the cell position (k, fd)."""
@@ -440,9 +455,7 @@ class SplitRun:
 
     def _win_after(self, shift):
         """(k, fd) after a move by shift, as chm_sp_window_advance computes them."""
-        s = self._wfd + float(shift) / float(self.dx)
-        fl = np.floor(s)
-        return self._wk + int(fl), float(s - fl)
+        return window_cells_after(self._wk, self._wfd, shift, self.dx)
 
     def _win_advance(self, shift):
         _lib.call("chm_sp_window_advance", self.win.data_ptr(), float(shift), _stream())

@@ -264,3 +264,28 @@ def test_diagnostics_dispatch_and_files_host(tmp_path, monkeypatch):
     assert p.shape == (2, 8)  # appended at steps 2 and 6
     (ret,) = D.nrg_out({"Type": "EnergyEM", "Step": 1, "Features": {"Return": True}})
     assert np.allclose(ret, e, rtol=1e-14, atol=0)
+
+
+def test_window_cells_advance_exactly():
+    """The split form's window position in cells: a move by a whole number
+    of cells keeps the FP64 fraction exactly (the still species' background
+    then moves with the window), fractional moves carry into the whole
+    cells, and the position tracks the accumulated leftX to rounding."""
+    from chimera_gb300.split import window_cells, window_cells_after
+    X0, dx = -81.92 + 0.04, 0.04
+    leftX = X0 + 0.37 * dx
+    k, fd = window_cells(leftX, X0, dx)
+    assert k == 0 and abs(fd - 0.37) < 1e-12
+    k1, fd1 = window_cells_after(k, fd, dx, dx)  # one cell
+    leftX += dx
+    assert k1 == 1 and abs(fd1 - fd) < 1e-15  # (fd + 1 - 1 in FP64)
+    f_first = fd1
+    for _ in range(500):
+        k1, fd1 = window_cells_after(k1, fd1, dx, dx)
+        leftX += dx
+    assert k1 == 501 and fd1 == f_first  # bitwise after the first move
+    kl, fl = window_cells(leftX, X0, dx)
+    assert abs((kl + fl) - (k1 + fd1)) < 1e-9  # the accumulated leftX agrees to rounding
+    # a staged half move carries after two halves
+    k2, f2 = window_cells_after(0, 0.75, 0.5 * 0.999 * dx, dx)
+    assert k2 == 1 and abs(f2 - (0.75 + 0.4995 - 1.0)) < 1e-12
