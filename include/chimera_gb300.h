@@ -386,8 +386,8 @@ int chm_align_data(double *dst, int64_t d_cs, int64_t d_ps, const double *src,
                    const int64_t *idx, int64_t n, void *stream);
 
 /* ======================================================================== */
-/* Split-precision form (spec precision pattern; no counterpart entry  */
-/* point in the reference): FP32 particles stored as int32 cell index +      */
+/* Split-precision form (a precision form of the same step; no counterpart  */
+/* entry point in the reference): FP32 particles stored as int32 cell index +*/
 /* FP32 offset, complex64 fields, DHT / coupling products on the tensor      */
 /* cores as 3-term split-BF16 with FP32 accumulation.  FP64 stays in the     */
 /* operator build and the window origin.                                     */
