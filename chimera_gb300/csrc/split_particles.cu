@@ -1998,12 +1998,13 @@ int chm_sp_push_deposit_env(int32_t *ix, float *fx, float *y, float *z, float *p
                             float *pz, float *w, int64_t n, int win_k, float win_f, float dx_inv,
                             float dr_inv, double dt, double dx, int nx, int nr, int nm,
                             uint64_t *accJ, const double *scaleJ, const void *carrier_c64,
-                            float kdx, void *stream, const chm_sp_window *win) {
+                            int64_t ntab, float kdx, void *stream, const chm_sp_window *win) {
   CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && (nm == 1 || nm == 3 || nm == 5) && dt > 0.0 && dx > 0.0,
               "sp_push_deposit_env: bad dims (the envelope modes -K..K, K <= 2)");
   if (n == 0) return CHM_OK;
   CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && accJ && scaleJ && carrier_c64,
               "sp_push_deposit_env: null pointer");
+  CHM_REQUIRE(ntab >= (int64_t)nx + 4, "sp_push_deposit_env: carrier table shorter than nx + 4");
   PushDepArgs A{};
   A.P = SpParts{ix, fx, y, z, px, py, pz, w, n};
   A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};
@@ -2036,7 +2037,8 @@ int chm_sp_push_deposit_env(int32_t *ix, float *fx, float *y, float *z, float *p
 int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z, float *px, float *py,
                            float *pz, float *w, int64_t n, int win_k, float win_f, float dr_inv,
                            const void *eb_c64, int nx, int nr, int nm, float dtq,
-                           const void *carrier_c64, float kdx, int und_kind, const double *und,
+                           const void *carrier_c64, int64_t ntab, float kdx, int und_kind,
+                           const double *und,
                            double X0, double dx, void *stream, const chm_sp_window *win) {
   CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && (nm == 1 || nm == 3 || nm == 5),
               "sp_gather_push_env: bad dims (the envelope modes -K..K, K <= 2)");
@@ -2044,6 +2046,7 @@ int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z, float *px
   if (n == 0) return CHM_OK;
   CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && eb_c64 && carrier_c64,
               "sp_gather_push_env: null pointer");
+  CHM_REQUIRE(ntab >= (int64_t)nx + 4, "sp_gather_push_env: carrier table shorter than nx + 4");
   GatherArgs A{};
   A.P = SpParts{ix, fx, y, z, px, py, pz, w, n};
   A.G = SpGrid{win_k, win_f, dr_inv, nx, nr, nm};

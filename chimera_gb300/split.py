@@ -497,7 +497,8 @@ class SplitRun:
                       float(self.solver.Args["dr_inv"]), float(self.dt), float(self.dx), self.nx,
                       self.nr, self.nm,
                       accJ.data_ptr(), scaleJ.data_ptr(), self.carrier.data_ptr(),
-                      float(self.kx0 * self.dx), _stream(), self.win.data_ptr())
+                      self.carrier.numel(), float(self.kx0 * self.dx), _stream(),
+                      self.win.data_ptr())
             return
         _lib.call("chm_sp_push_deposit", *P.ptrs(), P.n, k, f, 1.0 / self.dx,
                   float(self.solver.Args["dr_inv"]), float(self.dt), self.nx, self.nr, self.nm,
@@ -835,7 +836,7 @@ class SplitRun:
                 prm[:min(5, und[1].size)] = und[1][:5]
             _lib.call("chm_sp_gather_push_env", *P.ptrs(), P.n, k, f, float(A["dr_inv"]),
                       self.EB.data_ptr(), self.nx, self.nr, self.nm, float(dtq),
-                      self.carrier.data_ptr(), float(self.kx0 * self.dx),
+                      self.carrier.data_ptr(), self.carrier.numel(), float(self.kx0 * self.dx),
                       0 if und is None else und[0], prm.ctypes.data, self.X0, float(self.dx), st,
                       self.win.data_ptr())
 

@@ -504,7 +504,8 @@ int chm_sp_deposit_background(int32_t *ix, float *fx, float *y, float *z,
  * chm_sp_carrier fills tab (ntab >= nx + 4 complex64) with the carrier
  * e^{-i kx0 (X0 + (k + c - 2) dx)} of the window's cells c (k = the window
  * cell win->k, or win_k without a record), in FP64; the kernels below take
- * a particle's carrier as tab[ix - k + 2] e^{-i kdx fx}, kdx = kx0 dx. */
+ * a particle's carrier as tab[ix - k + 2] e^{-i kdx fx}, kdx = kx0 dx, and
+ * reject a table (ntab entries) shorter than nx + 4. */
 int chm_sp_carrier(void *tab_c64, int64_t ntab, double kx0, double X0, double dx,
                    int win_k, void *stream, const chm_sp_window *win);
 /* push_coords + dep_curr_env (particle_tools.f90:58-82,
@@ -519,8 +520,8 @@ int chm_sp_push_deposit_env(int32_t *ix, float *fx, float *y, float *z,
                             int win_k, float win_f, float dx_inv, float dr_inv,
                             double dt, double dx, int nx, int nr, int nm,
                             uint64_t *accJ, const double *scaleJ,
-                            const void *carrier_c64, float kdx, void *stream,
-                            const chm_sp_window *win);
+                            const void *carrier_c64, int64_t ntab, float kdx,
+                            void *stream, const chm_sp_window *win);
 /* proj_fld_env + an analytic undulator + push_velocs
  * (grid_deps_env.f90:164-238, devices.f90:117-203, particle_tools.f90:18-56):
  * gather with the carrier e^{+i kx0 x} and e^{+-i m theta} (1 on the axis),
@@ -532,7 +533,8 @@ int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z,
                            float *px, float *py, float *pz, float *w, int64_t n,
                            int win_k, float win_f, float dr_inv,
                            const void *eb_c64, int nx, int nr, int nm, float dtq,
-                           const void *carrier_c64, float kdx, int und_kind,
+                           const void *carrier_c64, int64_t ntab, float kdx,
+                           int und_kind,
                            const double *und, double X0, double dx,
                            void *stream, const chm_sp_window *win);
 

@@ -189,7 +189,8 @@ def test_envelope_particle_kernels_match_fp64(mods):
     prm[:und.size] = und
     dtq = spc.Args["push_fact"] * spc.Args["TimeStep"]
     _lib.call("chm_sp_gather_push_env", *P.ptrs(), P.n, k, f, float(A["dr_inv"]),
-              EB32.data_ptr(), nx, nr, nm, float(dtq), tab.data_ptr(), kdx, 1, prm.ctypes.data,
+              EB32.data_ptr(), nx, nr, nm, float(dtq), tab.data_ptr(), tab.numel(), kdx, 1,
+              prm.ctypes.data,
               X0, dx, st, None)
     spc.make_field()
     d["EB"] = fm.proj_fld_env(d["coords"], d["weights"], S.Data["EB"], d["EB"], A["leftX"],
@@ -216,7 +217,7 @@ def test_envelope_particle_kernels_match_fp64(mods):
     acc = torch.zeros(nx * nr * nm * 3 * 2, dtype=torch.int64, device=dev)
     _lib.call("chm_sp_push_deposit_env", *P.ptrs(), P.n, k, f, 1.0 / dx, float(A["dr_inv"]),
               float(spc.Args["TimeStep"]), dx, nx, nr, nm, acc.data_ptr(), scale.data_ptr(),
-              tab.data_ptr(), kdx, st, None)
+              tab.data_ptr(), tab.numel(), kdx, st, None)
     spc.push_coords()
     J = fm.fortran_zeros((nx, nr, nm, 3))
     J = fm.dep_curr_env(d["coords_halfstep"], d["momenta"], d["weights"], J, leftX_d,
