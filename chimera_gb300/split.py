@@ -976,6 +976,9 @@ class SplitRun:
                 P.counters.zero_()
                 d = spc.Data
                 P.append_f64(d["coords"], d["momenta"], d["weights"], self.X0, self.dx)
+            # (the background's block ranges belong to the particles before the
+            # read: the next window move deposits the background in full)
+            self._bg_key = None
             if "split/scaleJ" in f.files:
                 for t, k in ((self.scaleJ, "scaleJ"), (self.scaleR, "scaleR"),
                              (self.scaleBG, "scaleBG"), (self.accBG, "accBG")):
