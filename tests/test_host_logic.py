@@ -289,3 +289,33 @@ def test_window_cells_advance_exactly():
     # a staged half move carries after two halves
     k2, f2 = window_cells_after(0, 0.75, 0.5 * 0.999 * dx, dx)
     assert k2 == 1 and abs(f2 - (0.75 + 0.4995 - 1.0)) < 1e-12
+
+
+def test_background_shift_decision():
+    """When the split form may move the still species' background with the
+    window instead of re-depositing it (SplitRun._bg_shift): a whole-cell
+    move of one unchanged still species without absorption or injection."""
+    from types import SimpleNamespace
+
+    from chimera_gb300.split import SplitRun
+    dx = 0.04
+    P = SimpleNamespace(n=1000, cap=2048, ptrs=lambda: [11, 12, 13, 14, 15, 16, 17, 18])
+    run = SplitRun.__new__(SplitRun)
+    run.nm, run.nx, run.dx = 3, 4096, dx
+    run.have_bg = True
+    run._wk, run._wfd = 10, 0.25
+    run._bg_key = (P.n, P.cap, *P.ptrs())
+    run._still = lambda: [(None, P)]
+    assert run._bg_shift({"shiftX": dx}) == 1
+    assert run._bg_shift({"shiftX": 3 * dx}) == 3
+    assert run._bg_shift({"shiftX": 0.5 * dx}) == 0           # not a whole cell
+    assert run._bg_shift({"shiftX": dx, "AbsorbLayer": 64}) == 0
+    assert run._bg_shift({"shiftX": dx, "AddPlasma": None}) == 0
+    run._bg_key = None                                         # particles changed
+    assert run._bg_shift({"shiftX": dx}) == 0
+    run._bg_key = (P.n, P.cap, *P.ptrs())
+    run._still = lambda: [(None, P), (None, P)]               # two still species
+    assert run._bg_shift({"shiftX": dx}) == 0
+    run._still = lambda: [(None, P)]
+    run.have_bg = False
+    assert run._bg_shift({"shiftX": dx}) == 0
