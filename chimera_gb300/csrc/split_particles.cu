@@ -1511,18 +1511,47 @@ __global__ void __launch_bounds__(kDepThreads) push_deposit_env_kernel(PushDepAr
   flush();
 }
 
-// undul_analytic / undul_analytic_taper (devices.f90:117-203) on a
-// particle at x - X0u = xr: B_y += a s cosh(ku y), B_x += a c sinh(ku y),
-// (s, c) = sincos(ku xr), a = a0 ramp(xr) [taper]; ramps of one period at
-// both ends of the undulator
+// The undulators of devices.f90 on a particle at x (its cell ix, offset fx):
+//   undul_analytic[_taper] (devices.f90:117-203): with xr = x - X0u,
+//     B_y += a s cosh(ku y), B_x += a c sinh(ku y), (s, c) = sincos(ku xr),
+//     a = a0 ramp(xr) [taper], ramps of one period at both ends;
+//   undul_mapped[_tap] (devices.f90:18-115): the amplitudes a(2, nmap) of a
+//     field map of step mdx from Xleft, interpolated with quadratic weights
+//     at xm = x - Xleft (the reference's columns ix - 2 .. ix), B_y += amp
+//     s1 cosh(ku y), B_x += amp s2 sinh(ku y), amp the taper or 1.
+// Positions relative to the undulator are formed from FP64 cell offsets.
 struct UndArgs {
-  int kind;          // 0 none, 1 undul_analytic, 2 undul_analytic_taper
+  int kind;          // 0 none, 1 undul_analytic, 2 _taper, 3 undul_mapped, 4 _tap
   float a0, lam, ku, len, taper;
-  double xo, dx;     // particles' origin X0 - undulator start X0u; cell size
+  double xo, dx;     // X0 (particles' origin) - undulator start (X0u or Xleft); cell size
+  const float2 *map; // mapped: (a(0, col), a(1, col)) per column
+  int nmap;
+  float mdx, mdx_inv, x_shift;
 };
 
 __device__ __forceinline__ void undulator(float *F, int ix, float fx, float y, const UndArgs &U) {
   const float xr = (float)(U.xo + (double)ix * U.dx) + fx * (float)U.dx;
+  if (U.kind >= 3) {
+    if (xr < U.mdx || xr > U.nmap * U.mdx - U.mdx) return;
+    const float u = xr * U.mdx_inv;
+    const int im = (int)floorf(u + 0.5f);
+    const float d = u - (float)im;
+    const float S[3] = {0.5f * (0.5f - d) * (0.5f - d), 0.75f - d * d, 0.5f * (0.5f + d) * (0.5f + d)};
+    float s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int col = im - 2 + q;
+      if (col < 0 || col >= U.nmap) continue;
+      const float2 a = U.map[col];
+      s1 += S[q] * a.x;
+      s2 += S[q] * a.y;
+    }
+    const float amp =
+        U.kind == 4 ? 1.0f + U.taper * (xr - U.x_shift - 0.5f * U.len) / (0.5f * U.len) : 1.0f;
+    F[4] += amp * s1 * coshf(U.ku * y);
+    F[3] += amp * s2 * sinhf(U.ku * y);
+    return;
+  }
   float ampl;
   if (xr <= 0.0f || xr >= U.len) ampl = 0.0f;
   else if (xr < U.lam) ampl = xr / U.lam;
@@ -2038,11 +2067,13 @@ int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z, float *px
                            float *pz, float *w, int64_t n, int win_k, float win_f, float dr_inv,
                            const void *eb_c64, int nx, int nr, int nm, float dtq,
                            const void *carrier_c64, int64_t ntab, float kdx, int und_kind,
-                           const double *und,
+                           const double *und, const void *und_map, int64_t nmap,
                            double X0, double dx, void *stream, const chm_sp_window *win) {
   CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && (nm == 1 || nm == 3 || nm == 5),
               "sp_gather_push_env: bad dims (the envelope modes -K..K, K <= 2)");
-  CHM_REQUIRE(und_kind >= 0 && und_kind <= 2 && (und_kind == 0 || und), "sp_gather_push_env: bad undulator");
+  CHM_REQUIRE(und_kind >= 0 && und_kind <= 4 && (und_kind == 0 || und) &&
+                  (und_kind < 3 || (und_map && nmap > 0 && und[2] > 0.0)),
+              "sp_gather_push_env: bad undulator");
   if (n == 0) return CHM_OK;
   CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && eb_c64 && carrier_c64,
               "sp_gather_push_env: null pointer");
@@ -2056,7 +2087,7 @@ int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z, float *px
   const EnvArgs E{reinterpret_cast<const float2 *>(carrier_c64), kdx};
   UndArgs U{};
   U.kind = und_kind;
-  if (und_kind) {
+  if (und_kind == 1 || und_kind == 2) {
     // (a0, period, start, length[, taper]) as devices.f90 takes them
     U.a0 = (float)und[0];
     U.lam = (float)und[1];
@@ -2065,6 +2096,21 @@ int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z, float *px
     U.taper = und_kind == 2 ? (float)und[4] : 0.0f;
     U.xo = X0 - und[2];
     U.dx = dx;
+  } else if (und_kind >= 3) {
+    // (period, Xleft, map step[, length, taper]) and the map a(2, nmap)
+    U.lam = (float)und[0];
+    U.ku = (float)(2.0 * 3.14159265358979323846 / und[0]);
+    U.xo = X0 - und[1];
+    U.dx = dx;
+    U.mdx = (float)und[2];
+    U.mdx_inv = (float)(1.0 / und[2]);
+    U.map = reinterpret_cast<const float2 *>(und_map);
+    U.nmap = (int)nmap;
+    if (und_kind == 4) {
+      U.len = (float)und[3];
+      U.taper = (float)und[4];
+      U.x_shift = (float)(0.5 * ((double)nmap * und[2] - und[3]));
+    }
   }
   const unsigned blocks = (unsigned)((n + kDepBlock - 1) / kDepBlock);
   cudaStream_t st = as_stream(stream);

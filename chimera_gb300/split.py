@@ -234,7 +234,8 @@ def window_cells_after(k, fd, shift, dx):
 
 # device functions of fimera the split form fuses into its gather + push
 # (chm_sp_gather_push_env und_kind)
-_UNDULATORS = {"undul_analytic": 1, "undul_analytic_taper": 2}
+_UNDULATORS = {"undul_analytic": 1, "undul_analytic_taper": 2, "undul_mapped": 3,
+               "undul_mapped_tap": 4}
 
 
 class SortCadence:
@@ -306,18 +307,25 @@ class SplitRun:
         self.env = "KxShift" in A
         if self.env and ("SpaceCharge" in feats or "StillAsBackground" in feats):
             raise NotImplementedError("the envelope charge deposit is not in the split form")
-        # external fields: the analytic undulators, fused into the gather
+        # external fields: the undulators, fused into the gather; a mapped
+        # one carries its map a0(2, nmap) as FP32 column pairs on the device
         self.undulators = []
         for sp in self.fp.Particles:
             und = None
             for d in sp.Devices:
                 kind = _UNDULATORS.get(getattr(d[0], "__name__", ""))
-                if kind is None or und is not None or len(d) != 2:
+                if kind is None or und is not None or len(d) != (2 if kind <= 2 else 3):
                     raise NotImplementedError(
-                        "the split form fuses one analytic undulator (undul_analytic or "
-                        "undul_analytic_taper) per species into the push")
-                prm = np.asarray(d[1], dtype=np.float64).ravel()
-                und = (kind, prm)
+                        "the split form fuses one undulator (undul_analytic[_taper] or "
+                        "undul_mapped[_tap]) per species into the push")
+                prm = np.asarray(d[-1], dtype=np.float64).ravel()
+                amap = None
+                if kind >= 3:
+                    a = torch.as_tensor(d[1])
+                    if a.dim() != 2 or a.shape[0] != 2:
+                        raise ValueError("undul_mapped: the map is a0(2, nmap)")
+                    amap = a.t().to(device=S.device, dtype=torch.float32).contiguous()
+                und = (kind, prm, amap)
             self.undulators.append(und)
         if any(self.undulators) and not self.env:
             raise NotImplementedError("the split form fuses undulators into the envelope push only")
@@ -832,12 +840,16 @@ class SplitRun:
                 continue
             und = self.undulators[i]
             prm = np.zeros(5)
+            amap = None
             if und is not None:
                 prm[:min(5, und[1].size)] = und[1][:5]
+                amap = und[2]
             _lib.call("chm_sp_gather_push_env", *P.ptrs(), P.n, k, f, float(A["dr_inv"]),
                       self.EB.data_ptr(), self.nx, self.nr, self.nm, float(dtq),
                       self.carrier.data_ptr(), self.carrier.numel(), float(self.kx0 * self.dx),
-                      0 if und is None else und[0], prm.ctypes.data, self.X0, float(self.dx), st,
+                      0 if und is None else und[0], prm.ctypes.data,
+                      None if amap is None else amap.data_ptr(),
+                      0 if amap is None else amap.shape[0], self.X0, float(self.dx), st,
                       self.win.data_ptr())
 
     def _carrier(self):

@@ -522,21 +522,23 @@ int chm_sp_push_deposit_env(int32_t *ix, float *fx, float *y, float *z,
                             uint64_t *accJ, const double *scaleJ,
                             const void *carrier_c64, int64_t ntab, float kdx,
                             void *stream, const chm_sp_window *win);
-/* proj_fld_env + an analytic undulator + push_velocs
- * (grid_deps_env.f90:164-238, devices.f90:117-203, particle_tools.f90:18-56):
- * gather with the carrier e^{+i kx0 x} and e^{+-i m theta} (1 on the axis),
- * the undulator field of und_kind 1 (undul_analytic: und = a0, period,
- * start, length) or 2 (undul_analytic_taper: und = a0, period, start,
- * length, taper) at the particle's x = X0 + (ix + fx) dx, 0 for none, then
- * the Boris push. */
+/* proj_fld_env + an undulator + push_velocs (grid_deps_env.f90:164-238,
+ * devices.f90:18-203, particle_tools.f90:18-56): gather with the carrier
+ * e^{+i kx0 x} and e^{+-i m theta} (1 on the axis), the undulator field at
+ * the particle's x = X0 + (ix + fx) dx of und_kind 1 (undul_analytic: und =
+ * a0, period, start, length), 2 (undul_analytic_taper: und = a0, period,
+ * start, length, taper), 3 (undul_mapped: und = period, Xleft, map step;
+ * und_map the map's nmap columns as FP32 pairs (a(0, c), a(1, c))) or 4
+ * (undul_mapped_tap: und = period, Xleft, map step, length, taper), 0 for
+ * none, then the Boris push. */
 int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z,
                            float *px, float *py, float *pz, float *w, int64_t n,
                            int win_k, float win_f, float dr_inv,
                            const void *eb_c64, int nx, int nr, int nm, float dtq,
                            const void *carrier_c64, int64_t ntab, float kdx,
-                           int und_kind,
-                           const double *und, double X0, double dx,
-                           void *stream, const chm_sp_window *win);
+                           int und_kind, const double *und, const void *und_map,
+                           int64_t nmap, double X0, double dx, void *stream,
+                           const chm_sp_window *win);
 
 /* FP64 (3,n)/(n) particle arrays (particle order) <-> split layout; from_f64
  * writes particles offset .. offset+n-1 and clears their dead flags (dead

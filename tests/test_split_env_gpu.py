@@ -8,7 +8,8 @@ laser set-up of the reference (doc/tests/fel-testrun.py, workloads "fel4" and
   2048 x 128 x 3-mode operator sizes, within TOL_T relative L2;
 - the beam's carrier-phase current deposit and its gather + undulator +
   Boris push against the FP64 kernels (dep_curr_env, proj_fld_env,
-  undul_analytic, push_velocs) on the same particles;
+  undul_analytic, push_velocs) on the same particles, and the gather with
+  a mapped undulator (undul_mapped[_tap]) likewise;
 - split steps against the FP64 form from the same state: fields, beam
   momenta and the radiated energy (Diagnostics.nrg_out summed,
   diagnostics.py:109-122) within 1 %, and graph replay bitwise equal to
@@ -190,8 +191,7 @@ def test_envelope_particle_kernels_match_fp64(mods):
     dtq = spc.Args["push_fact"] * spc.Args["TimeStep"]
     _lib.call("chm_sp_gather_push_env", *P.ptrs(), P.n, k, f, float(A["dr_inv"]),
               EB32.data_ptr(), nx, nr, nm, float(dtq), tab.data_ptr(), tab.numel(), kdx, 1,
-              prm.ctypes.data,
-              X0, dx, st, None)
+              prm.ctypes.data, None, 0, X0, dx, st, None)
     spc.make_field()
     d["EB"] = fm.proj_fld_env(d["coords"], d["weights"], S.Data["EB"], d["EB"], A["leftX"],
                               *A["DepProj"])
@@ -234,6 +234,78 @@ def test_envelope_particle_kernels_match_fp64(mods):
           f" kick {err_dp:.2e} of |E| dt (|EB| gathered {gathered:.3g})")
     assert np.abs(J.cpu().numpy()).max() > 0 and gathered > 0 and np.abs(dp_64).max() > 0
     assert err_j < 1e-5 and err_x < 1e-6 and err_r < 1e-6 and err_dp < 1e-6
+
+
+@pytest.mark.parametrize("tap", [False, True])
+def test_envelope_gather_mapped_undulator_matches_fp64(mods, tap):
+    """The split gather + mapped undulator + Boris (und_kind 3, 4) against
+    proj_fld_env + undul_mapped[_tap] + push_velocs on the small FEL beam
+    after two steps: a map of step 0.35 periods (not a multiple of the grid's
+    cell) over the beam, with a 10 % taper for undul_mapped_tap."""
+    torch, _lib, fm, split = mods
+    from chimera_gb300 import ChimeraRun, workloads
+    run = ChimeraRun(workloads.fel_components("fel_small", seed=1004))
+    for i in range(1, 3):
+        run.make_step(i)
+    S, spc = run.Solvers[0], run.Particles[0]
+    A, d = S.Args, spc.Data
+    nx, nr, nm = A["Nx"], A["Nr"], A["Mtot"]
+    dev = torch.device("cuda")
+    n = spc.num_particles
+    dx = float(A["dx"])
+    X0 = float(A["Xgrid"][0]) - 3 * dx
+    st = _st(torch)
+    tab = torch.zeros(nx + 4, dtype=torch.complex64, device=dev)
+    s = (float(A["leftX"]) - X0) / dx
+    k = int(np.floor(s))
+    _lib.call("chm_sp_carrier", tab.data_ptr(), tab.numel(), float(A["kx0"]), X0, dx, k, st, None)
+    # the map: a wiggler field of 1-period wavelength sampled every 0.35
+    # periods, from 4 steps before the beam's head to 4 after its tail (the
+    # particles near both ends fall in the map's skipped edge columns)
+    xs = d["coords"][0]
+    mdx = 0.35
+    xleft = float(xs.min()) - 4 * mdx
+    nmap = int(np.ceil((float(xs.max()) - xleft) / mdx)) + 4
+    xc = xleft + mdx * np.arange(nmap)
+    K0 = workloads.FEL["fel_small"].K0
+    a0 = np.asfortranarray(np.stack([K0 * np.sin(2 * np.pi * xc), 0.7 * K0 * np.cos(2 * np.pi * xc)]))
+    prm = np.zeros(5)
+    if tap:
+        prm[:5] = (1.0, xleft, mdx, 0.8 * nmap * mdx, 0.1)
+    else:
+        prm[:3] = (1.0, xleft, mdx)
+    P = split._SpParticles(dev, n)
+    P.append_f64(d["coords"], d["momenta"], d["weights"], X0, dx)
+    EB32 = fm.fortran_empty(tuple(S.Data["EB"].shape), torch.complex64, dev)
+    EB32.copy_(S.Data["EB"])
+    p0 = d["momenta"].clone()
+    amap = torch.from_numpy(np.ascontiguousarray(a0.T)).to(dev, torch.float32)
+    dtq = spc.Args["push_fact"] * spc.Args["TimeStep"]
+    _lib.call("chm_sp_gather_push_env", *P.ptrs(), P.n, k, s - k, float(A["dr_inv"]),
+              EB32.data_ptr(), nx, nr, nm, float(dtq), tab.data_ptr(), tab.numel(),
+              float(A["kx0"] * dx), 4 if tap else 3, prm.ctypes.data, amap.data_ptr(), nmap,
+              X0, dx, st, None)
+    spc.make_field()
+    d["EB"] = fm.proj_fld_env(d["coords"], d["weights"], S.Data["EB"], d["EB"], A["leftX"],
+                              *A["DepProj"])
+    spc.Devices = ((fm.undul_mapped_tap if tap else fm.undul_mapped, a0, prm[:5 if tap else 3]),)
+    spc.make_device(3)
+    field = float(d["EB"].abs().max())
+    spc.push_velocs()
+    x64 = fm.fortran_zeros((3, n), torch.float64)
+    p64 = fm.fortran_zeros((3, n), torch.float64)
+    w64 = torch.zeros(n, dtype=torch.float64, device=dev)
+    _lib.call("chm_sp_to_f64", *P.ptrs(), P.n, x64.data_ptr(), x64.stride(0), x64.stride(1),
+              p64.data_ptr(), p64.stride(0), p64.stride(1), w64.data_ptr(), w64.stride(0), X0,
+              dx, st)
+    p0_32 = p0.to(torch.float32).to(torch.float64)
+    dp_sp = (p64 - p0_32)[1:].cpu().numpy()
+    dp_64 = (d["momenta"] - p0)[1:].cpu().numpy()
+    err_dp = float(np.abs(dp_sp - dp_64).max()) / (field * abs(dtq))
+    print(f"mapped undulator{' (tapered)' if tap else ''}: kick {err_dp:.2e} of |F| dt "
+          f"(|F| {field:.3g}, {nmap} map columns)")
+    assert field > 0 and np.abs(dp_64).max() > 0
+    assert err_dp < 1e-6
 
 
 def test_fel_split_steps_track_fp64(mods):
