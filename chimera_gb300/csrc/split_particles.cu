@@ -2072,8 +2072,10 @@ int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z, float *px
   CHM_REQUIRE(n >= 0 && nx > 1 && nr > 1 && (nm == 1 || nm == 3 || nm == 5),
               "sp_gather_push_env: bad dims (the envelope modes -K..K, K <= 2)");
   CHM_REQUIRE(und_kind >= 0 && und_kind <= 4 && (und_kind == 0 || und) &&
-                  (und_kind < 3 || (und_map && nmap > 0 && und[2] > 0.0)),
-              "sp_gather_push_env: bad undulator");
+                  (und_kind < 3 || (und_map && nmap > 0 && nmap < (1 << 30) && und[2] > 0.0 &&
+                                    (reinterpret_cast<uintptr_t>(und_map) & 7u) == 0)),
+              "sp_gather_push_env: bad undulator (a map needs nmap in [1, 2^30), a positive "
+              "step and 8-byte alignment)");
   if (n == 0) return CHM_OK;
   CHM_REQUIRE(ix && fx && y && z && px && py && pz && w && eb_c64 && carrier_c64,
               "sp_gather_push_env: null pointer");

@@ -51,6 +51,28 @@ def test_status_codes_without_gpu():
     assert lib.chm_dep_ws_bytes(16, 9, 2, 3, 10) >= 16 * 9 * 2 * 3 * 2 * 8
 
 
+def test_envelope_gather_rejects_bad_undulators_without_gpu():
+    """chm_sp_gather_push_env checks its undulator and carrier arguments on
+    the host: a mapped undulator without a map, with no columns or a
+    misaligned map, an unknown kind and a short carrier table."""
+    from chimera_gb300 import _lib
+    lib = _lib.load()
+    fake = C.c_void_p(256)
+    und = (C.c_double * 5)(1.0, 0.0, 0.35, 10.0, 0.1)
+
+    def call(kind, amap, nmap, ntab=20):
+        return lib.chm_sp_gather_push_env(*[fake] * 8, 100, 0, 0.0, 1.0, fake, 16, 9, 3, 0.1,
+                                          fake, ntab, 0.1, kind, und, amap, nmap, 0.0, 0.1,
+                                          None, None)
+
+    for kind, amap, nmap in ((3, None, 10), (4, fake, 0), (3, C.c_void_p(260), 10),
+                             (5, fake, 10)):
+        assert call(kind, amap, nmap) == 1, (kind, amap, nmap)  # CHM_ERR_ARG
+        assert b"undulator" in lib.chm_last_error()
+    assert call(3, fake, 10, ntab=19) == 1
+    assert b"carrier table" in lib.chm_last_error()
+
+
 def test_fimera_has_every_reference_kernel_name():
     """Every f2py routine the reference's Python calls exists in the shim."""
     from chimera_gb300 import fimera
