@@ -169,6 +169,43 @@ def test_undulator_closed_form(orc):
     assert np.allclose(F[3], a0 * np.cos(ku * (c[0] - X0)) * np.sinh(ku * c[1]), atol=1e-14)
 
 
+def test_mapped_undulator_known_answers(orc):
+    """devices.f90:18-115: the map column j (1-based) sits at Xleft + j dx
+    (the spline at ix reads a0(:, ix-1:ix+1)); the quadratic weights sum to
+    one, so a constant map returns the taper's amplitude exactly; particles
+    outside [Xleft + dx, Xright - dx] get nothing."""
+    rng = np.random.default_rng(11)
+    lam, xleft, mdx, nmap = 1.0, 0.3, 0.01, 700
+    xright = xleft + nmap * mdx
+    n = 400
+    x = rng.uniform(xleft + 2 * mdx, xright - 2 * mdx, n)
+    y = rng.uniform(-0.05, 0.05, n)
+    c = np.asfortranarray(np.vstack([x, y, np.zeros(n)]))
+    ku = 2 * np.pi / lam
+    xc = xleft + mdx * np.arange(1, nmap + 1)
+    # a sampled wiggler: the spline smooths sin(ku x) by about (ku dx)^2 / 8
+    a0 = np.asfortranarray(np.stack([np.sin(ku * xc), np.cos(ku * xc)]))
+    F = orc.undul_mapped(c, np.zeros((6, n), order="F"), 0.0, a0, np.array([lam, xleft, mdx]))
+    tol = (ku * mdx) ** 2 / 4
+    assert np.abs(F[4] - np.sin(ku * x) * np.cosh(ku * y)).max() < tol
+    assert np.abs(F[3] - np.cos(ku * x) * np.sinh(ku * y)).max() < tol
+    # the same samples one column along miss by about ku dx
+    a1 = np.asfortranarray(np.stack([np.sin(ku * (xc - mdx)), np.cos(ku * (xc - mdx))]))
+    F1 = orc.undul_mapped(c, np.zeros((6, n), order="F"), 0.0, a1, np.array([lam, xleft, mdx]))
+    assert np.abs(F1[4] - np.sin(ku * x) * np.cosh(ku * y)).max() > 10 * tol
+    # a constant map under the taper: amp = 1 + taper (x - x_shift - Xleft - Lx/2) / (Lx/2)
+    Lx, taper = 0.8 * nmap * mdx, 0.1
+    x_shift = 0.5 * (nmap * mdx - Lx)
+    ones = np.asfortranarray(np.stack([np.ones(nmap), np.zeros(nmap)]))
+    xe = np.concatenate([x, [xleft + 0.5 * mdx, xright - 0.5 * mdx]])
+    ce = np.asfortranarray(np.vstack([xe, np.zeros(n + 2), np.zeros(n + 2)]))
+    Ft = orc.undul_mapped_tap(ce, np.zeros((6, n + 2), order="F"), 0.0, ones,
+                              np.array([lam, xleft, mdx, Lx, taper]))
+    amp = 1 + taper * (x - x_shift - xleft - 0.5 * Lx) / (0.5 * Lx)
+    assert np.allclose(Ft[4, :n], amp, rtol=0, atol=1e-14)
+    assert np.all(Ft[:, n:] == 0) and np.all(Ft[3] == 0)
+
+
 def test_psatd_vacuum_matches_analytic(orc, golden):
     """maxwell_solvers.f90:62-96 with J = 0 rotates (E, G) by exp(i w dt):
     N steps equal one step of N dt."""
