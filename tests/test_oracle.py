@@ -206,6 +206,35 @@ def test_mapped_undulator_known_answers(orc):
     assert np.all(Ft[:, n:] == 0) and np.all(Ft[3] == 0)
 
 
+def test_planewave_and_gaussbeam_known_answers(orc):
+    """devices.f90:205-297: the plane wave's field (E_z, B_x, B_y) =
+    (1, sin theta, -cos theta) a0 ramp sin(k0 (x cos theta + y sin theta - t)
+    + phi0) with linear ramps of length `ramp` inside [X0, X0 + Lx]; the
+    Gaussian beam's E_z = a0 exp(-sum (x_i / L_i)^2) sin(2 pi x' / lambda)
+    with x' = x - x0 - axis t, and B_y = -axis E_z; nothing else is written."""
+    rng = np.random.default_rng(12)
+    n = 300
+    c = np.asfortranarray(rng.uniform(-1.0, 1.0, (3, n)) * np.array([[6.0], [1.0], [1.0]]))
+    x, y, z = c
+    a0, lam, X0, Lx, ramp, th, phi0, t = 0.7, 0.9, -4.0, 8.0, 1.5, 0.3, 0.2, 0.4
+    F = orc.planewave(c, np.zeros((6, n), order="F"), t,
+                      np.array([a0, lam, X0, Lx, ramp, th, phi0]))
+    env = np.clip(np.minimum(x - X0, X0 + Lx - x) / ramp, 0.0, 1.0)
+    e = a0 * env * np.sin(2 * np.pi / lam * (x * np.cos(th) + y * np.sin(th) - t) + phi0)
+    assert np.abs(F[2] - e).max() < 1e-14
+    assert np.abs(F[3] - e * np.sin(th)).max() < 1e-14
+    assert np.abs(F[4] + e * np.cos(th)).max() < 1e-14
+    assert np.all(F[[0, 1, 5]] == 0)
+    prm = np.array([0.8, 1.0, 0.5, 0.1, -0.2, 2.0, 0.7, 0.9])
+    G = orc.gaussbeam(c, np.zeros((6, n), order="F"), t, a0, prm)
+    xp = x - prm[2] - prm[1] * t
+    e = a0 * np.exp(-(xp / prm[5]) ** 2 - ((y - prm[3]) / prm[6]) ** 2
+                    - ((z - prm[4]) / prm[7]) ** 2) * np.sin(2 * np.pi / prm[0] * xp)
+    assert np.abs(G[2] - e).max() < 1e-14
+    assert np.abs(G[4] + prm[1] * e).max() < 1e-14
+    assert np.all(G[[0, 1, 3, 5]] == 0)
+
+
 def test_psatd_vacuum_matches_analytic(orc, golden):
     """maxwell_solvers.f90:62-96 with J = 0 rotates (E, G) by exp(i w dt):
     N steps equal one step of N dt."""
