@@ -528,7 +528,8 @@ int chm_sp_push_deposit_env(int32_t *ix, float *fx, float *y, float *z,
  * the particle's x = X0 + (ix + fx) dx of und_kind 1 (undul_analytic: und =
  * a0, period, start, length), 2 (undul_analytic_taper: und = a0, period,
  * start, length, taper), 3 (undul_mapped: und = period, Xleft, map step;
- * und_map the map's nmap columns as FP32 pairs (a(0, c), a(1, c))) or 4
+ * und_map the map's nmap columns as FP32 pairs (a(0, c), a(1, c)), 8-byte
+ * aligned device memory) or 4
  * (undul_mapped_tap: und = period, Xleft, map step, length, taper), 0 for
  * none, then the Boris push. */
 int chm_sp_gather_push_env(int32_t *ix, float *fx, float *y, float *z,
