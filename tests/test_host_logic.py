@@ -319,3 +319,54 @@ def test_background_shift_decision():
     run._still = lambda: [(None, P)]
     run.have_bg = False
     assert run._bg_shift({"shiftX": dx}) == 0
+
+
+def test_sort_cadence_rule(monkeypatch):
+    """SortCadence (the re-sort autotuner) on fake step and sort timings: the
+    cadence is sqrt(2 S / g) with S the sort time and g the per-step time a
+    sort recovered over the interval before it, clamped to [lo, hi]; a sort
+    that recovers nothing sends it to hi."""
+    import torch
+
+    from chimera_gb300.split import SortCadence
+
+    class Ev:
+        def __init__(self, enable_timing=True):
+            self.t = 0.0
+
+        def query(self):
+            return True
+
+        def elapsed_time(self, other):
+            return other.t - self.t
+
+    monkeypatch.setattr(torch.cuda, "Event", Ev)
+    sc = SortCadence(start=32, lo=8, hi=512)
+
+    def interval(nsteps, base, slope, sort_ms):
+        for s in range(nsteps):
+            a, b = sc.step_events(s)
+            b.t = base + slope * s
+        a, b = sc.sort_events()
+        b.t = sort_ms
+
+    interval(32, 1.0, 0.01, 8.0)
+    sc.update(32)
+    assert sc.cadence == 32 and sc.history[-1] == (32, 32, 8.0, None)  # no earlier sort
+    interval(32, 1.0, 0.01, 8.0)
+    sc.update(64)
+    g = 0.01 * (29.5 - 1.5) / 32  # last four minus first four steps, per step
+    assert abs(sc.history[-1][3] - g) < 1e-12
+    assert sc.cadence == int(np.sqrt(2 * 8.0 / g)) == 42
+    interval(42, 1.0, 1.0, 8.0)      # slower after the sort than before it: hi
+    sc.update(106)
+    assert sc.history[-1][3] < 0 and sc.cadence == 512
+    interval(8, 1.0, 0.0, 8.0)       # the sort recovered 39.5 ms over 42 steps: lo
+    sc.update(114)
+    assert abs(sc.history[-1][3] - 39.5 / 42) < 1e-12 and sc.cadence == 8
+    interval(3, 1.0, 0.5, 8.0)       # too few steps to judge: unchanged
+    sc.update(117)
+    assert sc.history[-1][3] is None and sc.cadence == 8
+    interval(8, 1.0, 0.0, 8.0)       # nothing recovered: hi
+    sc.update(125)
+    assert sc.history[-1][3] == 0 and sc.cadence == 512 and len(sc.history) == 6
