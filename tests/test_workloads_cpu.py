@@ -47,3 +47,20 @@ def test_fel_resonance(size):
     gz = W.gamma / np.sqrt(1 + W.K0 ** 2 / 2)
     vb = np.sqrt(1 - gz ** -2)
     assert abs((1 - vb) * 2 * gz ** 2 - 1) < 1e-3
+
+
+def test_batched_draws_cover_the_ragged_configuration():
+    """The batched workload's 64 instances (seed 1005): Nx 256-2048, Nr
+    32-256, 2 or 3 stored modes, uneven particle counts; the draw is
+    reproducible from its seed."""
+    from chimera_gb300.batched import draw_instances
+    P = draw_instances(64, 1005)
+    assert P == draw_instances(64, 1005) and P != draw_instances(64, 1006)
+    nx = {p["nx"] for p in P}
+    nr = {p["nr"] for p in P}
+    assert min(nx) >= 256 and max(nx) <= 2048 and len(nx) > 8
+    assert min(nr) >= 32 and max(nr) <= 256 and len(nr) > 4
+    assert {p["max_mode"] + 1 for p in P} == {2, 3}
+    cells = [p["nx"] * p["nr"] * p["ppc_theta"] for p in P]
+    assert max(cells) > 20 * min(cells)  # ragged: the particle counts differ widely
+    assert len({p["seed"] for p in P}) == 64
