@@ -236,6 +236,35 @@ def window_cells_after(k, fd, shift, dx):
 # (chm_sp_gather_push_env und_kind)
 _UNDULATORS = {"undul_analytic": 1, "undul_analytic_taper": 2, "undul_mapped": 3,
                "undul_mapped_tap": 4}
+_UND_PARAMS = {1: 4, 2: 5, 3: 3, 4: 5}  # params(n) of devices.f90 per kind
+
+
+def fused_undulator(devices, device):
+    """The undulator of a species' Devices as the split push takes it:
+    None, or (und_kind, params, map) with the map a0(2, nmap) as nmap FP32
+    column pairs on `device` (None for the analytic kinds).  Raises for a
+    device the split form does not fuse, for more than one device, and for
+    a parameter array of the wrong length (f2py's dimension check,
+    devices.f90:18-203)."""
+    und = None
+    for d in devices:
+        kind = _UNDULATORS.get(getattr(d[0], "__name__", ""))
+        if kind is None or und is not None or len(d) != (2 if kind <= 2 else 3):
+            raise NotImplementedError(
+                "the split form fuses one undulator (undul_analytic[_taper] or "
+                "undul_mapped[_tap]) per species into the push")
+        prm = np.asarray(d[-1], dtype=np.float64).ravel()
+        if prm.size != _UND_PARAMS[kind]:
+            raise ValueError(f"{d[0].__name__}: params has {prm.size} values, "
+                             f"expected {_UND_PARAMS[kind]}")
+        amap = None
+        if kind >= 3:
+            a = torch.as_tensor(d[1])
+            if a.dim() != 2 or a.shape[0] != 2 or a.shape[1] < 1:
+                raise ValueError(f"{d[0].__name__}: the map is a0(2, nmap)")
+            amap = a.t().to(device=device, dtype=torch.float32).contiguous()
+        und = (kind, prm, amap)
+    return und
 
 
 class SortCadence:
@@ -309,24 +338,7 @@ class SplitRun:
             raise NotImplementedError("the envelope charge deposit is not in the split form")
         # external fields: the undulators, fused into the gather; a mapped
         # one carries its map a0(2, nmap) as FP32 column pairs on the device
-        self.undulators = []
-        for sp in self.fp.Particles:
-            und = None
-            for d in sp.Devices:
-                kind = _UNDULATORS.get(getattr(d[0], "__name__", ""))
-                if kind is None or und is not None or len(d) != (2 if kind <= 2 else 3):
-                    raise NotImplementedError(
-                        "the split form fuses one undulator (undul_analytic[_taper] or "
-                        "undul_mapped[_tap]) per species into the push")
-                prm = np.asarray(d[-1], dtype=np.float64).ravel()
-                amap = None
-                if kind >= 3:
-                    a = torch.as_tensor(d[1])
-                    if a.dim() != 2 or a.shape[0] != 2:
-                        raise ValueError("undul_mapped: the map is a0(2, nmap)")
-                    amap = a.t().to(device=S.device, dtype=torch.float32).contiguous()
-                und = (kind, prm, amap)
-            self.undulators.append(und)
+        self.undulators = [fused_undulator(sp.Devices, S.device) for sp in self.fp.Particles]
         if any(self.undulators) and not self.env:
             raise NotImplementedError("the split form fuses undulators into the envelope push only")
         dev = self.device = S.device

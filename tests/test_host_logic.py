@@ -370,3 +370,37 @@ def test_sort_cadence_rule(monkeypatch):
     interval(8, 1.0, 0.0, 8.0)       # nothing recovered: hi
     sc.update(125)
     assert sc.history[-1][3] == 0 and sc.cadence == 512 and len(sc.history) == 6
+
+
+def test_fused_undulator_parsing():
+    """The devices the split push fuses (split.fused_undulator): the
+    analytic and mapped undulators with their parameter counts, the map
+    as FP32 column pairs; other devices, two devices and wrong parameter
+    counts raise."""
+    import torch
+
+    from chimera_gb300 import fimera
+    from chimera_gb300.split import fused_undulator
+    cpu = torch.device("cpu")
+    assert fused_undulator((), cpu) is None
+    k, prm, amap = fused_undulator(([fimera.undul_analytic, np.array([2.0, 1.0, 1.0, 80.0])],), cpu)
+    assert k == 1 and prm.tolist() == [2.0, 1.0, 1.0, 80.0] and amap is None
+    k, _, _ = fused_undulator(([fimera.undul_analytic_taper, np.arange(5.0)],), cpu)
+    assert k == 2
+    a0 = np.asfortranarray(np.arange(14.0).reshape(2, 7))
+    k, prm, amap = fused_undulator(([fimera.undul_mapped, a0, np.array([1.0, 0.3, 0.01])],), cpu)
+    assert k == 3 and amap.dtype == torch.float32 and tuple(amap.shape) == (7, 2)
+    assert amap.is_contiguous() and np.array_equal(amap.numpy(), a0.T)  # (a(0, c), a(1, c))
+    k, _, amap = fused_undulator(([fimera.undul_mapped_tap, torch.from_numpy(a0),
+                                   np.arange(5.0)],), cpu)
+    assert k == 4 and np.array_equal(amap.numpy().ravel(), a0.T.ravel())
+    with pytest.raises(NotImplementedError):
+        fused_undulator(([fimera.planewave, np.zeros(7)],), cpu)
+    with pytest.raises(NotImplementedError):
+        fused_undulator(([fimera.undul_analytic, np.zeros(4)],) * 2, cpu)
+    with pytest.raises(NotImplementedError):
+        fused_undulator(([fimera.undul_mapped, np.zeros(3)],), cpu)  # no map
+    with pytest.raises(ValueError):
+        fused_undulator(([fimera.undul_analytic, np.zeros(3)],), cpu)
+    with pytest.raises(ValueError):
+        fused_undulator(([fimera.undul_mapped, np.zeros((3, 7)), np.zeros(3)],), cpu)
