@@ -139,6 +139,46 @@ def test_dep_dens_conserves_charge(orc):
     assert abs(dens[:, :, 0].sum() - w.sum()) < 1e-12 * w.sum()
 
 
+def test_envelope_deposits_single_particle(orc):
+    """grid_deps_env.f90:18-162 for one particle: the current's J_z (the only
+    component deposited) is w v_z / gamma S_x S_r e^{-i kx0 x} e^{-+i m theta}
+    in modes +-m; the density takes the complex weight w e^{-i kx0 x} twice,
+    w^2 e^{-2 i kx0 x}; a particle on the ghost row (r < dr / 2) is folded
+    into row 1 with the sign flipped and row 0 cleared."""
+    nx, nr, K = 16, 6, 2
+    nm = 2 * K + 1
+    dx, dr, leftX, kx0 = 0.1, 0.25, -0.8, 37.0
+    rg = dr * (np.arange(nr) - 0.5)
+    for r, th in ((0.61, 0.7), (0.07, 2.1)):
+        x = leftX + 6.3 * dx
+        c = np.asfortranarray([[x], [r * np.cos(th)], [r * np.sin(th)]])
+        p = np.asfortranarray([[0.3], [-0.4], [1.7]])
+        w = np.array([0.8])
+        J = orc.dep_curr_env(c, p, w, np.zeros((nx, nr, nm, 3), complex, order="F"), leftX, rg,
+                             1 / dx, 1 / dr, kx0)
+        D = orc.dep_dens_env(c, w, np.zeros((nx, nr, nm), complex, order="F"), leftX, rg,
+                             1 / dx, 1 / dr, kx0)
+        ix = int(np.floor((x - leftX) / dx))
+        ir = int(np.floor((r - rg[0]) / dr))
+        sx = (x - leftX) / dx - ix
+        sr = (r - rg[ir]) / dr
+        S = np.outer([1 - sx, sx], [1 - sr, sr])
+        car = np.exp(-1j * kx0 * x)
+        vz = p[2, 0] / np.sqrt(1 + (p[:, 0] ** 2).sum())
+        Jz = np.zeros((nx, nr, nm), complex)
+        Dn = np.zeros((nx, nr, nm), complex)
+        for m in range(-K, K + 1):
+            ph = np.exp(-1j * m * th)
+            Jz[ix:ix + 2, ir:ir + 2, m + K] = w[0] * vz * S * car * ph
+            Dn[ix:ix + 2, ir:ir + 2, m + K] = (w[0] * car) ** 2 * S * ph
+        for G in (Jz, Dn):
+            G[:, 1] -= G[:, 0]
+            G[:, 0] = 0
+        assert (ir == 0) == (r < 0.5 * dr)
+        assert np.abs(J[..., 2] - Jz).max() < 1e-14 and np.all(J[..., :2] == 0)
+        assert np.abs(D - Dn).max() < 1e-14
+
+
 def test_chunked_deposit_matches_serial(orc):
     """grid_deps_chnk.f90: same grid as the serial deposit when chunk 0 holds
     no particle next to x-node 0."""
