@@ -179,6 +179,41 @@ def test_envelope_deposits_single_particle(orc):
         assert np.abs(D - Dn).max() < 1e-14
 
 
+def test_envelope_gather_and_correction_single_particle(orc):
+    """grid_deps_env.f90:164-283: the gather of one particle is
+    sum over m = -K..K and the 2 x 2 nodes of Re(S_x S_r e^{+i kx0 x}
+    e^{+i m theta} F_m), with theta's phase 1 on the axis;
+    eb_correction_env scales every mode by 1/pi and writes row 0 as -row 1
+    (+row 1 with a single mode)."""
+    rng = np.random.default_rng(13)
+    nx, nr, K = 12, 5, 2
+    nm = 2 * K + 1
+    dx, dr, leftX, kx0 = 0.2, 0.3, -1.0, 21.0
+    rg = dr * (np.arange(nr) - 0.5)
+    F = np.asfortranarray(rng.standard_normal((nx, nr, nm, 6))
+                          + 1j * rng.standard_normal((nx, nr, nm, 6)))
+    for r, th in ((0.52, -1.1), (0.0, 0.0)):
+        x = leftX + 4.7 * dx
+        c = np.asfortranarray([[x], [r * np.cos(th)], [r * np.sin(th)]])
+        got = orc.proj_fld_env(c, np.array([1.3]), F, np.zeros((6, 1), order="F"), leftX, rg,
+                               1 / dx, 1 / dr, kx0)
+        ix = int(np.floor((x - leftX) / dx))
+        ir = int(np.floor((r - rg[0]) / dr))
+        sx, sr = (x - leftX) / dx - ix, (r - rg[ir]) / dr
+        S = np.outer([1 - sx, sx], [1 - sr, sr]) * np.exp(1j * kx0 * x)
+        want = np.zeros(6)
+        for m in range(-K, K + 1):
+            ph = np.exp(1j * m * th)  # th = 0 on the axis: phase 1
+            for l in range(6):
+                want[l] += np.real(S * ph * F[ix:ix + 2, ir:ir + 2, m + K, l]).sum()
+        assert np.abs(got[:, 0] - want).max() < 1e-13 * np.abs(F).max()
+    for modes, sign in ((nm, -1.0), (1, 1.0)):
+        G = np.asfortranarray(F[:, :, :modes].copy())
+        out = orc.eb_correction_env(G.copy(order="F"))
+        assert np.allclose(out[:, 1:], G[:, 1:] / np.pi, rtol=1e-15, atol=0)
+        assert np.array_equal(out[:, 0], sign * out[:, 1])
+
+
 def test_chunked_deposit_matches_serial(orc):
     """grid_deps_chnk.f90: same grid as the serial deposit when chunk 0 holds
     no particle next to x-node 0."""
