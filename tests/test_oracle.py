@@ -230,6 +230,48 @@ def test_chunked_deposit_matches_serial(orc):
     assert rel_l2(chk, ser) < 1e-13
 
 
+def test_bookkeeping_known_answers(orc):
+    """particle_tools.f90:130-208, 270-324: sortpartsout keeps the 0-based
+    indices of particles with lims(1) <= x <= lims(2) and lims(3) <= r^2 <=
+    lims(4); chunk_coords_boundaries labels each kept particle with
+    floor((x - Xgrid(0)) / L), L = Xgrid(len / nchnk) - Xgrid(0), the others
+    with -2, returns the chunk offsets and the count outside (a kept
+    particle past the last chunk is counted in none); align_data
+    gathers the first len(idx) particles by index and keeps the rest."""
+    rng = np.random.default_rng(14)
+    n = 3000
+    c = np.asfortranarray(np.vstack([rng.uniform(-3.0, 4.0, n), rng.uniform(-1.5, 1.5, n),
+                                     rng.uniform(-1.5, 1.5, n)]))
+    c[0, :5] = [-2.0, 3.0, 0.0, 1.0, -1.0]  # on the x limits and on chunk edges
+    xg = -2.0 + 0.05 * np.arange(101)
+    lims = np.array([-2.0, 3.0, 0.01, 1.44])
+    x, r2 = c[0], c[1] ** 2 + c[2] ** 2
+    keep = (x >= lims[0]) & (x <= lims[1]) & (r2 >= lims[2]) & (r2 <= lims[3])
+    idx, num = orc.sortpartsout(c, lims)
+    assert num == keep.sum() and np.array_equal(idx[:num], np.flatnonzero(keep))
+    assert np.all(idx[num:] == 0)
+    nch = 4
+    ids, ind, go = orc.chunk_coords_boundaries(c, lims, xg, nch)
+    L = xg[xg.size // nch] - xg[0]
+    want = np.where(keep, np.floor((x - xg[0]) * (1.0 / L)), -2).astype(np.int8)
+    assert np.array_equal(ids, want) and go == n - keep.sum()
+    # x = lims(2) at the grid's right edge falls in chunk nchnk, one past the
+    # last: labelled so, counted in no chunk (the Fortran's count array
+    # would be written one past its end there)
+    assert ids[1] == nch
+    counts = np.bincount(want[keep & (want < nch)], minlength=nch)
+    assert np.array_equal(ind, np.concatenate([[0], np.cumsum(counts)]))
+    order = np.argsort(ids, kind="stable")[go:].astype(np.int64)
+    d = np.asfortranarray(rng.standard_normal((3, n)))
+    got = orc.align_data_vec(d.copy(order="F"), order)
+    assert np.array_equal(got[:, :order.size], d[:, order])
+    assert np.array_equal(got[:, order.size:], d[:, order.size:])
+    s = rng.standard_normal(n)
+    got = orc.align_data_scl(s.copy(), order)
+    assert np.array_equal(got[:order.size], s[order]) and np.array_equal(got[order.size:],
+                                                                          s[order.size:])
+
+
 def test_undulator_closed_form(orc):
     """devices.f90:162-203 inside the flat part of the undulator."""
     n = 200
