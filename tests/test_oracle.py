@@ -352,6 +352,36 @@ def test_planewave_and_gaussbeam_known_answers(orc):
     assert np.all(G[[0, 1, 3, 5]] == 0)
 
 
+def test_spectral_elementwise_known_answers(orc):
+    """maxwell_solvers.f90:18-60, 131-164, 228-318 restated in numpy:
+    PSATD with space charge (E' = C1 . [E, G, J, grad rho_n, grad rho_n+1],
+    G' = C2 . [the same, from the old E and G]), the Poisson correction
+    J += (grad div J + (grad rho_n+1 - grad rho_n) / dt) / w^2, and the
+    real multiply / complex add of the vector and scalar helpers."""
+    rng = np.random.default_rng(15)
+    sh = (10, 7, 2)
+    eg = _rand_fb(sh + (6,), 1)
+    j, gn, gp, gd = (_rand_fb(sh + (3,), s) for s in (2, 3, 4, 5))
+    C1 = np.asfortranarray(rng.standard_normal(sh + (5,)))
+    C2 = np.asfortranarray(rng.standard_normal(sh + (5,)))
+    terms = [eg[..., :3], eg[..., 3:], j, gn, gp]
+    e_new = sum(C1[..., i, None] * t for i, t in enumerate(terms))
+    g_new = sum(C2[..., i, None] * t for i, t in enumerate(terms))
+    out = orc.maxwell_push_with_spchrg(eg.copy(order="F"), j, gn, gp, C1, C2)
+    assert np.abs(out[..., :3] - e_new).max() < 1e-13
+    assert np.abs(out[..., 3:] - g_new).max() < 1e-13
+    w2_inv = np.asfortranarray(rng.uniform(0.1, 2.0, sh))
+    dt_inv = 7.0
+    out = orc.poiss_corr(j.copy(order="F"), gd, gn, gp, dt_inv, w2_inv)
+    assert np.abs(out - (j + (gd + (gp - gn) * dt_inv) * w2_inv[..., None])).max() < 1e-13
+    A = np.asfortranarray(rng.standard_normal(sh))
+    assert np.array_equal(orc.omp_mult_vec(j.copy(order="F"), A), j * A[..., None])
+    assert np.array_equal(orc.omp_mult_scl(gd[..., 0].copy(order="F"), A), gd[..., 0] * A)
+    assert np.array_equal(orc.omp_add_vec(j.copy(order="F"), gd), j + gd)
+    assert np.array_equal(orc.omp_add_scl(gn[..., 1].copy(order="F"), gp[..., 2].copy(order="F")),
+                          gn[..., 1] + gp[..., 2])
+
+
 def test_psatd_vacuum_matches_analytic(orc, golden):
     """maxwell_solvers.f90:62-96 with J = 0 rotates (E, G) by exp(i w dt):
     N steps equal one step of N dt."""
