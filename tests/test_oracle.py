@@ -76,6 +76,77 @@ def test_fb_grad_vs_numpy(orc, golden, name, env):
     assert rel_l2(got, ref) < 1e-13
 
 
+def _np_rot(v, Dp, Dm, kx, env):
+    """numpy restatement of fb_rot (fb_math.f90:18-94) and fb_rot_env
+    (fb_math_env.f90:106-162, whose lower-neighbour term of the first
+    component is computed and discarded, :146-151)."""
+    nx, nk, nm, _ = v.shape
+    nkl = Dp.shape[1]
+    out = np.zeros((nx, nkl, nm, 3), complex)
+    ext = -np.conj(v[(-np.arange(nx)) % nx, :, 1]) if nm > 1 else None
+    for mi in range(nm):
+        md = mi + 1 if env else mi
+        out[:, :, mi, 1] -= 1j * kx[:, None] * v[:, :nkl, mi, 2]
+        out[:, :, mi, 2] += 1j * kx[:, None] * v[:, :nkl, mi, 1]
+        if mi < nm - 1:
+            up = v[:, :, mi + 1]
+            out[:, :, mi, 0] -= (1j * up[..., 1] - up[..., 2]) @ Dp[:, :, md]
+            sl = up[..., 0] @ Dp[:, :, md]
+            out[:, :, mi, 1] += 1j * sl
+            out[:, :, mi, 2] -= sl
+        lo = v[:, :, mi - 1] if mi > 0 else (None if env else ext)
+        if lo is not None:
+            if not env:
+                out[:, :, mi, 0] -= (1j * lo[..., 1] + lo[..., 2]) @ Dm[:, :, md]
+            sl = lo[..., 0] @ Dm[:, :, md]
+            out[:, :, mi, 1] += 1j * sl
+            out[:, :, mi, 2] += sl
+    return out
+
+
+@pytest.mark.parametrize("name,env", [("lpa_m2", False), ("lpa_m3_chunked", False),
+                                      ("fel_env_k1", True)])
+def test_fb_rot_vs_numpy(orc, golden, name, env):
+    g = _ops(golden, name)
+    nx, nk, nm = int(g["Nx"]), int(g["Nkr"]), int(g["Mtot"])
+    v = _rand_fb((nx, nk, nm, 3), 3)
+    out = np.zeros((nx, nk, nm, 3), complex, order="F")
+    f = orc.fb_rot_env if env else orc.fb_rot
+    got = f(out, v, g["DpS2S"], g["DmS2S"], g["kx"])
+    assert rel_l2(got, _np_rot(v, g["DpS2S"], g["DmS2S"], g["kx"], env)) < 1e-13
+
+
+def _np_div(v, Dp, Dm, kx, env):
+    """numpy restatement of fb_div (fb_math.f90:150-199) and fb_div_env
+    (fb_math_env.f90:62-104)."""
+    nx, nk, nm, _ = v.shape
+    nkl = Dp.shape[1]
+    out = np.zeros((nx, nkl, nm), complex)
+    ext = -np.conj(v[(-np.arange(nx)) % nx, :, 1]) if nm > 1 else None
+    for mi in range(nm):
+        md = mi + 1 if env else mi
+        out[:, :, mi] += 1j * kx[:, None] * v[:, :nkl, mi, 0]
+        lo = v[:, :, mi - 1] if mi > 0 else (None if env else ext)
+        if lo is not None:
+            out[:, :, mi] += (1j * lo[..., 2] - lo[..., 1]) @ Dm[:, :, md]
+        if mi < nm - 1:
+            up = v[:, :, mi + 1]
+            out[:, :, mi] += (1j * up[..., 2] + up[..., 1]) @ Dp[:, :, md]
+    return out
+
+
+@pytest.mark.parametrize("name,env", [("lpa_m2", False), ("lpa_m3_chunked", False),
+                                      ("fel_env_k1", True)])
+def test_fb_div_vs_numpy(orc, golden, name, env):
+    g = _ops(golden, name)
+    nx, nk, nm = int(g["Nx"]), int(g["Nkr"]), int(g["Mtot"])
+    v = _rand_fb((nx, nk, nm, 3), 4)
+    out = np.zeros((nx, nk, nm), complex, order="F")
+    f = orc.fb_div_env if env else orc.fb_div
+    got = f(out, v, g["DpS2S"], g["DmS2S"], g["kx"])
+    assert rel_l2(got, _np_div(v, g["DpS2S"], g["DmS2S"], g["kx"], env)) < 1e-13
+
+
 def test_graddiv_equals_grad_of_div_interior(orc, golden):
     """fb_graddiv builds the divergence on one extra mode; for the m=0..M-2
     outputs it equals grad(div v) formed with fb_div and fb_grad."""
