@@ -147,6 +147,60 @@ def test_fb_div_vs_numpy(orc, golden, name, env):
     assert rel_l2(got, _np_div(v, g["DpS2S"], g["DmS2S"], g["kx"], env)) < 1e-13
 
 
+def _np_graddiv(v, Dp, Dm, kx, env):
+    """numpy restatement of fb_graddiv (fb_math.f90:201-293) and
+    fb_graddiv_env (fb_math_env.f90:164-233): the divergence on one extra
+    mode above (and, for the envelope, one below) the stored ones, then its
+    gradient back on the stored modes."""
+    nx, nk, nm, _ = v.shape
+    lo0 = 1 if env else 0          # slot of the first stored mode in S
+    ns = nm + 1 + lo0              # slots of the divergence
+    S = np.zeros((nx, nk, ns), complex)
+    refl = (-np.arange(nx)) % nx
+    for j in range(ns):
+        mi = j - lo0               # stored mode index (may be -1 or nm)
+        if 0 <= mi < nm:
+            S[:, :, j] += 1j * kx[:, None] * v[:, :, mi, 0]
+        if mi >= 1:
+            lo = v[:, :, mi - 1]
+        elif not env and mi == 0 and nm > 1:
+            lo = -np.conj(v[refl, :, 1])
+        else:
+            lo = None
+        if lo is not None:
+            S[:, :, j] += (1j * lo[..., 2] - lo[..., 1]) @ Dm[:, :, j]
+        if mi < nm - 1:
+            up = v[:, :, mi + 1]
+            S[:, :, j] += (1j * up[..., 2] + up[..., 1]) @ Dp[:, :, j]
+    out = np.zeros((nx, nk, nm, 3), complex)
+    for mi in range(nm):
+        j = mi + lo0
+        out[:, :, mi, 0] = 1j * kx[:, None] * S[:, :, j]
+        if j > 0:
+            sl = S[:, :, j - 1] @ Dm[:, :, j]
+        elif nm > 1:
+            sl = -np.conj(S[refl, :, 1]) @ Dm[:, :, j]
+        else:
+            sl = 0
+        out[:, :, mi, 1] -= sl
+        out[:, :, mi, 2] += 1j * sl
+        sl = S[:, :, j + 1] @ Dp[:, :, j]
+        out[:, :, mi, 1] += sl
+        out[:, :, mi, 2] += 1j * sl
+    return out
+
+
+@pytest.mark.parametrize("name,env", [("lpa_m2", False), ("lpa_m3_chunked", False),
+                                      ("fel_env_k1", True)])
+def test_fb_graddiv_vs_numpy(orc, golden, name, env):
+    g = _ops(golden, name)
+    nx, nk, nm = int(g["Nx"]), int(g["Nkr"]), int(g["Mtot"])
+    v = _rand_fb((nx, nk, nm, 3), 5)
+    f = orc.fb_graddiv_env if env else orc.fb_graddiv
+    got = f(v.copy(order="F"), g["DpS2S"], g["DmS2S"], g["kx"])
+    assert rel_l2(got, _np_graddiv(v, g["DpS2S"], g["DmS2S"], g["kx"], env)) < 1e-13
+
+
 def test_graddiv_equals_grad_of_div_interior(orc, golden):
     """fb_graddiv builds the divergence on one extra mode; for the m=0..M-2
     outputs it equals grad(div v) formed with fb_div and fb_grad."""
