@@ -33,6 +33,58 @@ def test_fb_round_trip(orc, golden):
     assert rel_l2(back[:, 1:], nx * v[:, 1:]) < 1e-12
 
 
+def test_fb_transforms_vs_numpy(orc, golden):
+    """fb_io.f90:18-228 restated with numpy's FFT (FFTW_FORWARD = fft,
+    FFTW_BACKWARD = n ifft): fb_vec_in sums In(r, k, m) over rows 1..Nr-1
+    (the ghost row skipped), transforms along x and multiplies by
+    e^{-i kx leftX}; fb_vec_out multiplies the Out sum by e^{+i kx leftX}
+    and transforms back unnormalised into rows 1..Nr-1 (row 0 zero);
+    fb_eb_out does that for E (e_fb's first three components) and B into
+    the six components of a zeroed grid."""
+    g = _ops(golden, "lpa_m2")
+    nx, nr, nk, nm = int(g["Nx"]), int(g["Nr"]), int(g["Nkr"]), int(g["Mtot"])
+    leftX, kx, In, Out = float(g["leftX"]) + 0.37, g["kx"], g["In"], g["Out"]
+    v = _rand_fb((nx, nr, nm, 3), 6)
+    got = orc.fb_vec_in(np.zeros((nx, nk, nm, 3), complex, order="F"), v, leftX, kx, In)
+    A = np.einsum("rkm,xrml->xkml", In, v[:, 1:])
+    want = np.fft.fft(A, axis=0) * np.exp(-1j * kx * leftX)[:, None, None, None]
+    assert rel_l2(got, want) < 1e-13
+    vf = _rand_fb((nx, nk, nm, 3), 7)
+    got = orc.fb_vec_out(vf, leftX, kx, Out)
+    B = np.einsum("krm,xkml->xrml", Out, vf) * np.exp(1j * kx * leftX)[:, None, None, None]
+    want = np.zeros((nx, nr, nm, 3), complex)
+    want[:, 1:] = nx * np.fft.ifft(B, axis=0)
+    assert rel_l2(got, want) < 1e-13 and np.all(got[:, 0] == 0)
+    e_fb = _rand_fb((nx, nk, nm, 6), 8)
+    eb = orc.fb_eb_out(_rand_fb((nx, nr, nm, 6), 9), e_fb, vf, leftX, kx, Out)
+    want6 = np.concatenate([orc.fb_vec_out(np.asfortranarray(e_fb[..., :3]), leftX, kx, Out),
+                            orc.fb_vec_out(vf, leftX, kx, Out)], axis=-1)
+    assert np.array_equal(eb, want6)
+
+
+@pytest.mark.parametrize("modefilt", [0, 1, 2])
+def test_fb_filtr_vs_numpy(orc, golden, modefilt):
+    """fb_io.f90:230-308: back to x (unnormalised, with e^{+i kx leftX}),
+    the first nxfilt cells times the profile (mode 0), the last nxfilt times
+    the reversed profile (mode 1), both (mode 2), forward again and divided
+    by nx e^{+i kx leftX}."""
+    g = _ops(golden, "lpa_m2")
+    nx, nk, nm = int(g["Nx"]), int(g["Nkr"]), int(g["Mtot"])
+    leftX, kx = float(g["leftX"]) - 0.21, g["kx"]
+    prof = np.linspace(0.0, 1.0, 9)[1:]
+    nf = prof.size
+    v = _rand_fb((nx, nk, nm, 3), 10)
+    sh = np.exp(1j * kx * leftX)[:, None, None, None]
+    a = nx * np.fft.ifft(v * sh, axis=0)
+    if modefilt in (0, 2):
+        a[:nf] *= prof[:, None, None, None]
+    if modefilt in (1, 2):
+        a[nx - nf:] *= prof[::-1, None, None, None]
+    want = np.fft.fft(a, axis=0) / (nx * sh)
+    got = orc.fb_filtr(v.copy(order="F"), leftX, kx, prof, modefilt)
+    assert rel_l2(got, want) < 1e-13
+
+
 def _rand_fb(shape, seed):
     rng = np.random.default_rng(seed)
     return np.asfortranarray(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
