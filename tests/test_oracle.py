@@ -391,6 +391,57 @@ def test_envelope_gather_and_correction_single_particle(orc):
         assert np.array_equal(out[:, 0], sign * out[:, 1])
 
 
+def test_plain_deposit_gather_correction_single_particle(orc):
+    """grid_deps.f90:18-266 for one particle: J_l = w v_l / gamma S_x S_r
+    e^{-i m theta} on modes m = 0..M-1 and rho = w S_x S_r e^{-i m theta},
+    both folded at the ghost row; the gather sums Re(S_x S_r e^{+i m theta}
+    F_m) with theta's phase 0 on the axis (only m = 0 there); eb_correction
+    scales m = 0 by 1/(2 pi) and m > 0 by 1/pi, row 0 = +row 1 for m = 0
+    and -row 1 for m > 0.  A particle at rest deposits no current."""
+    rng = np.random.default_rng(16)
+    nx, nr, nm = 12, 6, 3
+    dx, dr, leftX = 0.15, 0.2, -0.9
+    rg = dr * (np.arange(nr) - 0.5)
+    F = np.asfortranarray(rng.standard_normal((nx, nr, nm, 6))
+                          + 1j * rng.standard_normal((nx, nr, nm, 6)))
+    for r, th, p in ((0.47, 0.9, (0.2, -0.6, 1.1)), (0.05, -2.0, (1.0, 0.5, -0.3)),
+                     (0.0, 0.0, (0.3, 0.0, 0.0)), (0.33, 1.3, (0.0, 0.0, 0.0))):
+        x = leftX + 5.4 * dx
+        c = np.asfortranarray([[x], [r * np.cos(th)], [r * np.sin(th)]])
+        pp = np.asfortranarray(np.array(p, float)[:, None])
+        w = np.array([0.7])
+        J = orc.dep_curr(c, pp, w, np.zeros((nx, nr, nm, 3), complex, order="F"), leftX, rg,
+                         1 / dx, 1 / dr)
+        D = orc.dep_dens(c, w, np.zeros((nx, nr, nm), complex, order="F"), leftX, rg,
+                         1 / dx, 1 / dr)
+        E = orc.proj_fld(c, w, F, np.zeros((6, 1), order="F"), leftX, rg, 1 / dx, 1 / dr)
+        ix = int(np.floor((x - leftX) / dx))
+        ir = int(np.floor((r - rg[0]) / dr))
+        sx, sr = (x - leftX) / dx - ix, (r - rg[ir]) / dr
+        S = np.outer([1 - sx, sx], [1 - sr, sr])
+        ph = np.array([np.exp(-1j * m * th) if (r > 0 or m == 0) else 0 for m in range(nm)])
+        v = np.array(p) / np.sqrt(1 + np.sum(np.square(p)))
+        Jw = np.zeros((nx, nr, nm, 3), complex)
+        Dw = np.zeros((nx, nr, nm), complex)
+        for m in range(nm):
+            Dw[ix:ix + 2, ir:ir + 2, m] = w[0] * S * ph[m]
+            if any(p):
+                for l in range(3):
+                    Jw[ix:ix + 2, ir:ir + 2, m, l] = w[0] * v[l] * S * ph[m]
+        for G in (Jw, Dw):
+            G[:, 1] -= G[:, 0]
+            G[:, 0] = 0
+        assert np.abs(J - Jw).max() < 1e-14 and np.abs(D - Dw).max() < 1e-14
+        want = [sum(np.real(S * np.conj(ph[m]) * F[ix:ix + 2, ir:ir + 2, m, l]).sum()
+                    for m in range(nm)) for l in range(6)]
+        assert np.abs(E[:, 0] - want).max() < 1e-13
+    out = orc.eb_correction(F.copy(order="F"))
+    scale = np.array([0.5, 1.0, 1.0]) / np.pi
+    assert np.allclose(out[:, 1:], F[:, 1:] * scale[None, None, :, None], rtol=1e-15, atol=0)
+    assert np.array_equal(out[:, 0, 0], out[:, 1, 0])
+    assert np.array_equal(out[:, 0, 1:], -out[:, 1, 1:])
+
+
 def test_chunked_deposit_matches_serial(orc):
     """grid_deps_chnk.f90: same grid as the serial deposit when chunk 0 holds
     no particle next to x-node 0."""
