@@ -284,6 +284,27 @@ def test_boris_uniform_b_gyration(orc):
     assert np.allclose(-ang, 2 * np.arctan(dt * B / (2 * g)), rtol=1e-12)
 
 
+def test_boris_vs_numpy(orc):
+    """particle_tools.f90:18-56 restated in numpy (half E kick, rotation by
+    t = dt/2 B / gamma and s = 2 t / (1 + t^2), half E kick) on random
+    momenta and fields, including strong fields."""
+    rng = np.random.default_rng(18)
+    n = 500
+    p = np.asfortranarray(rng.standard_normal((3, n)) * 3)
+    F = np.asfortranarray(rng.standard_normal((6, n)) * np.r_[[1.0] * 3, [5.0] * 3][:, None])
+    dt = 0.3
+    h = 0.5 * dt
+    um = p + h * F[:3]
+    g = np.sqrt(1.0 + (um * um).sum(0))
+    t = h * F[3:] / g
+    sv = 2 * t / (1 + (t * t).sum(0))
+    u0 = um + np.cross(um, t, axis=0)
+    up = um + np.cross(u0, sv, axis=0)
+    want = up + h * F[:3]
+    got = orc.push_velocs(p.copy(order="F"), F, dt)
+    assert np.abs(got - want).max() < 1e-13 * np.abs(want).max()
+
+
 def test_push_coords_half_step(orc):
     x = np.asfortranarray(np.random.default_rng(4).standard_normal((3, 10)))
     p = np.asfortranarray(np.random.default_rng(5).standard_normal((3, 10)))
@@ -608,6 +629,31 @@ def test_spectral_elementwise_known_answers(orc):
     assert np.array_equal(orc.omp_add_vec(j.copy(order="F"), gd), j + gd)
     assert np.array_equal(orc.omp_add_scl(gn[..., 1].copy(order="F"), gp[..., 2].copy(order="F")),
                           gn[..., 1] + gp[..., 2])
+
+
+def test_static_field_routines_known_answers(orc):
+    """maxwell_solvers.f90:98-129, 166-226 restated in numpy:
+    maxwell_init_push adds C1 . [J, grad rho] to E and C2 . [J, grad rho]
+    to G (complex coefficients), poiss_corr_stat adds (grad div J + DT(kx)
+    grad rho) / w^2 to J, and field_drift multiplies every component by
+    exp(-i dt beta0 kx / 2)."""
+    rng = np.random.default_rng(17)
+    sh = (9, 5, 2)
+    eg = _rand_fb(sh + (6,), 11)
+    j, gr, gd = (_rand_fb(sh + (3,), s) for s in (12, 13, 14))
+    C1, C2 = _rand_fb(sh + (2,), 15), _rand_fb(sh + (2,), 16)
+    out = orc.maxwell_init_push(eg.copy(order="F"), j, gr, C1, C2)
+    assert np.abs(out[..., :3] - (eg[..., :3] + C1[..., :1] * j + C1[..., 1:] * gr)).max() < 1e-13
+    assert np.abs(out[..., 3:] - (eg[..., 3:] + C2[..., :1] * j + C2[..., 1:] * gr)).max() < 1e-13
+    DT = rng.standard_normal(sh[0]) + 1j * rng.standard_normal(sh[0])
+    w2_inv = np.asfortranarray(rng.uniform(0.1, 2.0, sh))
+    out = orc.poiss_corr_stat(j.copy(order="F"), gd, gr, DT, w2_inv)
+    want = j + (gd + DT[:, None, None, None] * gr) * w2_inv[..., None]
+    assert np.abs(out - want).max() < 1e-13
+    kx = rng.uniform(-30.0, 30.0, sh[0])
+    out = orc.field_drift(eg.copy(order="F"), kx, 0.99, 0.4)
+    want = eg * np.exp(-0.5j * 0.4 * 0.99 * kx)[:, None, None, None]
+    assert np.abs(out - want).max() < 1e-13
 
 
 def test_psatd_vacuum_matches_analytic(orc, golden):
