@@ -521,6 +521,27 @@ def test_bookkeeping_known_answers(orc):
                                                                           s[order.size:])
 
 
+def test_chunked_envelope_deposits_match_serial(orc):
+    """grid_deps_env_chnk.f90: the chunked envelope current and density equal
+    the serial ones when chunk 0 holds no particle next to x-node 0."""
+    c, p, w = _particles(3000, 17, -2.3, 3.5)
+    rg = 0.25 * (np.arange(13) - 0.5)
+    leftX, nx, nch, nm, kx0 = -2.5, 64, 4, 3, 11.0
+    xg = leftX + 0.1 * np.arange(nx)
+    ids, ind, go = orc.chunk_coords_boundaries(c, np.array([leftX, xg[-1], 0, 100.0]), xg, nch)
+    order = np.argsort(ids, kind="stable")[go:]
+    c2, p2, w2 = (np.asfortranarray(a[..., order]) for a in (c, p, w))
+    zJ = np.zeros((nx, 13, nm, 3), complex, order="F")
+    zD = np.zeros((nx, 13, nm), complex, order="F")
+    ser = orc.dep_curr_env(c2, p2, w2, zJ.copy(order="F"), leftX, rg, 10.0, 4.0, kx0)
+    chk = orc.dep_curr_env_chnk(c2, p2, w2, zJ.copy(order="F"), ind, 3, leftX, rg, 10.0, 4.0,
+                                kx0)
+    assert np.abs(ser).max() > 0 and rel_l2(chk, ser) < 1e-13
+    ser = orc.dep_dens_env(c2, w2, zD.copy(order="F"), leftX, rg, 10.0, 4.0, kx0)
+    chk = orc.dep_dens_env_chnk(c2, w2, zD.copy(order="F"), ind, 3, leftX, rg, 10.0, 4.0, kx0)
+    assert rel_l2(chk, ser) < 1e-13
+
+
 def test_undulator_closed_form(orc):
     """devices.f90:162-203 inside the flat part of the undulator."""
     n = 200
