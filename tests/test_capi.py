@@ -97,3 +97,26 @@ def test_fimera_rejects_cpu_tensors():
     with pytest.raises(fimera.ChimeraError):
         fimera.push_velocs(torch.zeros(3, 4, dtype=torch.float64),
                            torch.zeros(6, 4, dtype=torch.float64), 0.1)
+
+
+def test_empty_species_without_gpu():
+    """A species with no particles (n = 0) is a no-op for the particle entry
+    points of both forms: status 0 with null particle arrays, before any
+    device work (the Fortran loops run zero times)."""
+    from chimera_gb300 import _lib
+    lib = _lib.load()
+    N = None
+    und = (C.c_double * 5)(1.0, 0.0, 0.35, 10.0, 0.1)
+    calls = {
+        "chm_push_velocs": (N, 1, 3, N, 1, 6, 0.1, 0, N),
+        "chm_push_coords": (N, 1, 3, N, 1, 3, N, 1, 3, 0.1, 0, N),
+        "chm_sp_push_deposit": (*[N] * 8, 0, 0, 0.0, 1.0, 1.0, 0.1, 16, 9, 3, 1,
+                                *[N] * 6),
+        "chm_sp_gather_push": (*[N] * 8, 0, 0, 0.0, 1.0, N, 16, 9, 3, 0.1, N, N),
+        "chm_sp_push_deposit_env": (*[N] * 8, 0, 0, 0.0, 1.0, 1.0, 0.1, 0.1, 16, 9, 3, N, N, N,
+                                    20, 0.1, N, N),
+        "chm_sp_gather_push_env": (*[N] * 8, 0, 0, 0.0, 1.0, N, 16, 9, 3, 0.1, N, 20, 0.1, 0,
+                                   und, N, 0, 0.0, 0.1, N, N),
+    }
+    for name, args in calls.items():
+        assert getattr(lib, name)(*args) == 0, (name, lib.chm_last_error())
